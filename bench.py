@@ -1,0 +1,320 @@
+"""Benchmark of the visibility-buffer pass (the headline metric).
+
+Workload: the 512-object scene (clusters per axis uniform in [2,16], value-
+noise bits with period 64 voxels thresholded at 0.5, seed 1, uniform random
+rotations, translations uniform in a 2048^3 box), one 1920x1080 view from the
+box centre, 60 degree vFOV, far 4096.  A step is one visibility frame
+(tgx_vis_render): cluster setup, tile binning, DDA and resolve, with the
+scene resident on the device.  Seeded synthetic data.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  With --impl reference it times the CPU
+implementation of the same pass (the oracle's transcription of
+visibility.frag, OpenMP over all host cores) on a bounded sample of rows.
+Under torchrun with N>1 every rank renders its own replica of the frame
+(the pass does not shard: replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+W, H = 1920, 1080
+METRIC = "1080p vis-buffer Grays/s"
+CONFIG = {
+    "workload": "vis-buffer, 512-object value-noise scene (clusters/axis U[2,16], period 64, seed 1), "
+                "1920x1080, 60deg vFOV, camera at box centre, far 4096",
+    "objects": 512, "width": W, "height": H, "seed": 1,
+    "l2": "L2 flushed between timed steps (256 MiB write)",
+}
+
+
+def make_scene():
+    import tg_gb300 as tg
+    return tg.generate_scene(1, 512, 2, 16, seed=1, noise_period=64.0, noise_threshold=0.5,
+                             box_min=(-1024.0, -1024.0, -1024.0), box_max=(1024.0, 1024.0, 1024.0), n_luts=32)
+
+
+def make_view():
+    import tg_gb300 as tg
+    return tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), W, H, 0.1, 4096.0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(budget_s: float = 12.0, rows_per_chunk: int = 32):
+    """The oracle (CPU transcription of visibility.frag) on bands of rows of the
+    same frame, all host threads, until about budget_s seconds are spent."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import Oracle
+
+    scene, view = make_scene(), make_view()
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    rows = 0
+    y = 0
+    # spread the sampled bands over the frame so the sample sees the same mix of sky and geometry
+    order = list(range(0, H, rows_per_chunk))
+    rng = np.random.default_rng(0)
+    rng.shuffle(order)
+    for y in order:
+        o.vis_render(scene, view, mode=1, rows=(y, min(H, y + rows_per_chunk)), threads=cores)
+        rows += min(H, y + rows_per_chunk) - y
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    value = rows * W / dt / 1e9
+    return {"value": value, "unit": "Grays/s", "cores": cores, "kind": "port",
+            "sample": f"{rows} of {H} rows of the 1920x1080 frame ({rows * W} primary rays) in {dt:.1f} s"}
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    steps = []
+    cb = None
+    per_step = max(2.0, min(10.0, 150.0 / (args.warmup + args.steps)))
+    for i in range(args.warmup + args.steps):
+        r = cpu_reference(budget_s=per_step / 2 if i < args.warmup else per_step)
+        if i >= args.warmup:
+            steps.append(r)
+        cb = r
+    value = statistics.mean(s["value"] for s in steps)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": W * H / (value * 1e9) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": CONFIG,
+        "impl": "reference",
+        "cpu_baseline": {**cb, "value": value},
+        "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import tg_gb300 as tg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    scene = make_scene()
+    view = make_view()
+    ctx = tg.Context(local)
+    sc = ctx.upload(scene)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    out = torch.empty(W * H, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.vis_render(sc, view, [out])
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        ctx.sync()
+        err = ctx.device_error()
+        if err.code:
+            raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
+
+        # ---- timed region: K steps, per-step CUDA events on the launching stream ----
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        launches0 = ctx.launches()
+        barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clocks:
+            t_wall = time.perf_counter()
+            for i in range(args.steps):
+                flush.fill_(i & 0xFF)          # L2 flush, outside the event pair
+                starts[i].record(stream)
+                step()
+                ends[i].record(stream)
+            ctx.sync()
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall
+        barrier()
+        launches = ctx.launches() - launches0
+        ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        ms = statistics.mean(ms_steps)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+
+        # ---- per-kernel times (trace events) for the roofline ----
+        ctx.trace_reset()
+        ctx.trace(True)
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            step()
+        trace = ctx.trace_read()
+        ctx.trace(False)
+
+        # ---- end to end through the host-buffer entry point ----
+        host_out = np.empty(W * H, np.uint64)
+        try:
+            import ctypes
+            pinned = torch.empty(W * H, dtype=torch.int64, pin_memory=True)
+            host_out = pinned.numpy().view(np.uint64)
+        except Exception:
+            pass
+        for _ in range(2):
+            ctx.vis_render_host(sc, view, [host_out])
+        e2e_ms = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.vis_render_host(sc, view, [host_out])
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e = statistics.mean(e2e_ms)
+        err = ctx.device_error()
+        if err.code:
+            raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
+
+    hits = int((out.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)).sum())
+    rays = W * H
+    value = rays * world / (ms * 1e-3) / 1e9
+
+    # roofline of the dominant kernel: algorithmic bytes per launch / its mean event time
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    top = max(trace.items(), key=lambda kv: kv[1][0]) if trace else ("k_vis_tiles", (ms * args.steps, args.steps))
+    top_name, (top_ms_sum, top_n) = top
+    top_ms = top_ms_sum / max(top_n, 1)
+    stats = ctx.vis_stats()
+    n_vis = int(stats.visible_clusters)
+    algo_bytes = 8 * rays + 72 * n_vis + 96 * len(scene.objects)
+    achieved = algo_bytes / (top_ms * 1e-3) / 1e9
+
+    traffic = None
+    tf = ROOT / "profiles" / "vis_tiles_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {**CONFIG, "parallelism": "replicas" if world > 1 else "single-gpu"},
+        "e2e": {"value": rays * world / (e2e * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
+                "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e,
+                "path": "tgx_vis_render_host (views from host, visibility buffer back to pinned host memory)"},
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in trace.items()},
+        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "algorithmic_bytes": algo_bytes,
+                     "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback"},
+        "clocks": clocks.summary(),
+        "hit_pixels": hits,
+        "vis_stats": {"visible_clusters": n_vis, "bin_entries": int(stats.bin_entries), "tiles": int(stats.tiles),
+                      "dda_overruns": int(stats.dda_overruns)},
+        "wall_s_timed": t_wall,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference(budget_s=12.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sc.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,312 @@
+/*
+ * tgx.h -- C ABI of the GB300 voxel ray-tracing passes for tg's data model.
+ *
+ * Plain C99, no CUDA or C++ types in any signature.  The engine's C host code
+ * calls these where tg's Vulkan raytracer sat:
+ *
+ *   tg_raytracer_create            (tgvk_raytracer.c:662)   -> tgx_create
+ *   tg_raytracer_destroy           (tgvk_raytracer.c:791)   -> tgx_destroy
+ *   tg_raytracer_create_object     (tgvk_raytracer.c:805)   -> tgx_scene_upload (whole scene store)
+ *   tg_raytracer_color_lut_set     (tgvk_raytracer.c:1122)  -> tgx_scene_desc.luts
+ *   tg_raytracer_clear             (tgvk_raytracer.c:1556)  -> fused into tgx_vis_render
+ *   tg_raytracer_render            (tgvk_raytracer.c:1144)  -> tgx_svo_build + tgx_vis_render (+ tgx_gi_render)
+ *   tg_raytracer_get_hovered_voxel (tgvk_raytracer.c:1605)  -> tgx_pick
+ *   tg_svo_create                  (tg_sparse_voxel_octree.c:466) -> tgx_svo_build
+ *   tg_svo_traverse                (tg_sparse_voxel_octree.c:558; GPU form svo_functions.inc:1-329) -> tgx_svo_trace
+ *
+ * Data model (unchanged from tg):
+ *   - an object carries its clusters per axis, its first cluster pointer, a
+ *     translation and a rotation (tg_object_data_ssbo, tgvk_raytracer.c:35-42);
+ *   - cluster pointers map to 31-bit cluster indices (tgvk_raytracer.h:98-100);
+ *   - a cluster is 8^3 one-bit voxels, 16 u32 words, bit 64z+8y+x
+ *     (visibility.frag:143-148), voxel indices are 9 bits;
+ *   - materials are 8-bit indices (512 B per cluster, byte v of cluster c at
+ *     offset 512c+v, shading.frag:128-131) into 256-entry LUTs.
+ *
+ * Errors: every call returns a tgx_status and never aborts.  Device-side
+ * failures (step budget exhausted, capacity exceeded, bad index) are recorded
+ * in a device status word read by tgx_last_device_error after tgx_sync.
+ *
+ * Threading: one context per host thread; calls are ordered on the context's
+ * stream and are asynchronous until tgx_sync unless stated otherwise.
+ */
+#ifndef TGX_H
+#define TGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TGX_ABI_VERSION                 1u
+
+#define TGX_CLUSTER_SIDE                8u      /* TG_N_PRIMITIVES_PER_CLUSTER_CUBE_ROOT, cluster.inc:3 */
+#define TGX_VOXELS_PER_CLUSTER          512u    /* TG_N_PRIMITIVES_PER_CLUSTER, cluster.inc:2 */
+#define TGX_CLUSTER_WORDS               16u     /* 512 bits as u32 */
+#define TGX_CLUSTER_MATERIAL_BYTES      512u    /* TG_CLUSTER_SIZE(8) */
+#define TGX_CLUSTER_IDX_BITS            31u     /* TG_CLUSTERS_IDX_N_BITS, cluster.inc:4 */
+#define TGX_LUT_ENTRIES                 256u
+#define TGX_SVO_BLOCK_SIDE              32u     /* TG_SVO_BLOCK_SIDE_LENGTH, svo.inc:2 */
+#define TGX_SVO_BLOCK_WORDS             1024u   /* 32^3 bits as u32, bit 1024z+32y+x */
+
+/* Empty visibility-buffer word: depth field 2^24-1 means "no hit"
+ * (shading.frag:118-122; clear.comp:19 intends all ones). */
+#define TGX_VIS_EMPTY                   UINT64_MAX
+
+typedef enum tgx_status
+{
+    TGX_OK                      = 0,
+    TGX_ERR_INVALID_ARGUMENT    = 1,
+    TGX_ERR_OUT_OF_MEMORY       = 2,
+    TGX_ERR_CUDA                = 3,   /* a CUDA runtime call failed; see tgx_last_error_string */
+    TGX_ERR_CAPACITY            = 4,   /* a fixed capacity would be exceeded */
+    TGX_ERR_TIMEOUT             = 5,   /* a device loop ran out of its step budget */
+    TGX_ERR_NOT_SUPPORTED       = 6,
+    TGX_ERR_NO_DEVICE           = 7,
+    TGX_ERR_DEVICE_FAULT        = 8    /* a kernel recorded a bounds or consistency error */
+} tgx_status;
+
+/* Object record, 96 bytes, identical to tg_object_data_ssbo
+ * (tgvk_raytracer.c:35-42, buffers.inc:6-13, std430). */
+typedef struct tgx_object
+{
+    uint32_t n_cluster_pointers_per_dim[3];
+    uint32_t first_cluster_pointer;
+    float    translation[3];
+    uint32_t lut_idx;          /* the reference's `pad` word; the reference always
+                                  writes 0 and has one global LUT (tgvk_raytracer.c:1124) */
+    float    rotation[16];     /* column-major 4x4, as tg's m4 (tg_math.h:240-275) */
+} tgx_object;
+
+/* Camera of one view: tg_camera_ubo (tgvk_raytracer.c:65-74) plus the
+ * visibility-buffer size header (tgvk_raytracer.c:76-81).  Corner rays are
+ * the normalised directions tg_camera_make_corner_ray_directions computes on
+ * the host (tgvk_core.c:435-444); the fourth component is ignored. */
+typedef struct tgx_view
+{
+    float    camera[4];
+    float    ray_bl[4];
+    float    ray_br[4];
+    float    ray_tr[4];
+    float    ray_tl[4];
+    float    near_plane;
+    float    far_plane;
+    uint32_t width;
+    uint32_t height;
+} tgx_view;
+
+/* One LUT entry: linear albedo and roughness (16 bytes). */
+typedef struct tgx_material
+{
+    float albedo[3];
+    float roughness;
+} tgx_material;
+
+/* Host-side scene store, the arrays of tg_scene (tgvk_raytracer.h:90-108)
+ * plus the material grid and LUTs.  tgx_scene_upload copies everything; the
+ * caller keeps ownership of its host memory. */
+typedef struct tgx_scene_desc
+{
+    uint32_t             n_objects;
+    const tgx_object*    objects;                    /* [n_objects] */
+    uint32_t             n_cluster_pointers;
+    const uint32_t*      cluster_pointers;           /* [n_cluster_pointers] -> cluster idx */
+    uint32_t             n_clusters;
+    const uint32_t*      cluster_idx_to_object_idx;  /* [n_clusters] */
+    const uint32_t*      voxel_bits;                 /* [n_clusters * 16] */
+    const uint8_t*       material_idx;               /* [n_clusters * 512] or NULL */
+    uint32_t             n_luts;
+    const tgx_material*  luts;                       /* [n_luts * 256] or NULL */
+} tgx_scene_desc;
+
+typedef struct tgx_config
+{
+    int      device;           /* CUDA device ordinal */
+    void*    stream;           /* cudaStream_t to run on, or NULL for a context-owned stream */
+    uint32_t tile_w;           /* visibility tile width in pixels (0 = default 16) */
+    uint32_t tile_h;           /* visibility tile height in pixels (0 = default 16) */
+    uint32_t flags;            /* reserved, must be 0 */
+} tgx_config;
+
+typedef struct tgx_device_error
+{
+    uint32_t code;             /* tgx_status of the first device-side error, 0 if none */
+    uint32_t where;            /* kernel-specific location code */
+    uint64_t detail;           /* offending index or value */
+} tgx_device_error;
+
+typedef struct tgx_ctx   tgx_ctx;
+typedef struct tgx_scene tgx_scene;
+typedef struct tgx_svo   tgx_svo;
+
+/* ---- context ---- */
+
+uint32_t    tgx_abi_version(void);
+const char* tgx_status_string(tgx_status status);
+/* Text of the last host-side error of this thread (CUDA message, argument name). */
+const char* tgx_last_error_string(void);
+
+tgx_status  tgx_create(const tgx_config* config, tgx_ctx** out_ctx);
+void        tgx_destroy(tgx_ctx* ctx);
+/* The cudaStream_t the context launches on (as void*). */
+void*       tgx_stream(tgx_ctx* ctx);
+tgx_status  tgx_sync(tgx_ctx* ctx);
+/* Reads and clears the device status word (synchronises the stream). */
+tgx_status  tgx_last_device_error(tgx_ctx* ctx, tgx_device_error* out_error);
+/* Number of kernels this context has launched so far. */
+uint64_t    tgx_launch_count(tgx_ctx* ctx);
+
+/*
+ * Per-kernel device timing (tracing).  While enabled, every kernel the context
+ * launches is bracketed by CUDA events on its stream.  tgx_trace_get
+ * synchronises and returns, for kernel slot `slot` (0 .. tgx_trace_slots()-1),
+ * its name, summed device milliseconds and launch count since the last reset.
+ * Stands in for tg's QPC frame timer (tg_platform_win32.c:520-570), which has
+ * no per-pass GPU timestamps.
+ */
+tgx_status  tgx_trace_enable(tgx_ctx* ctx, int enable);
+tgx_status  tgx_trace_reset(tgx_ctx* ctx);
+uint32_t    tgx_trace_slots(void);
+tgx_status  tgx_trace_get(tgx_ctx* ctx, uint32_t slot, const char** out_name, double* out_ms,
+                          uint64_t* out_launches);
+
+/* ---- scene ---- */
+
+/* Copies a host scene store to the device (blocking).  Replaces the
+ * per-object staging uploads of tg_raytracer_create_object
+ * (tgvk_raytracer.c:849-978). */
+tgx_status  tgx_scene_upload(tgx_ctx* ctx, const tgx_scene_desc* desc, tgx_scene** out_scene);
+void        tgx_scene_destroy(tgx_ctx* ctx, tgx_scene* scene);
+
+/* ---- visibility buffer (visibility.vert/.frag + clear.comp) ---- */
+
+/*
+ * Renders the visibility buffer of each view: every pixel gets the minimum
+ * over all clusters of depth(24)|cluster pointer(31)|voxel(9), exactly as
+ * visibility.frag:22-207 computes it per fragment, or TGX_VIS_EMPTY.
+ * d_visbuf[i] is a DEVICE pointer to views[i].width*views[i].height u64.
+ * The clear of clear.comp is fused in.  Asynchronous on the context stream.
+ */
+tgx_status  tgx_vis_render(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
+                           uint64_t* const* d_visbuf);
+
+/* Same as tgx_vis_render but h_visbuf[i] are HOST pointers; the call copies
+ * the views in and the buffers out and returns when they are on the host. */
+tgx_status  tgx_vis_render_host(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
+                                uint64_t* const* h_visbuf);
+
+/* Counters of the last tgx_vis_render on this context (blocking). */
+typedef struct tgx_vis_stats
+{
+    uint32_t visible_clusters;    /* non-empty clusters inside some view's frustum */
+    uint32_t bin_entries;         /* (tile, cluster) pairs binned */
+    uint32_t tiles;               /* screen tiles over all views */
+    uint32_t dda_overruns;        /* DDAs that exceeded their step bound (always 0 unless a bug) */
+} tgx_vis_stats;
+
+tgx_status  tgx_vis_get_stats(tgx_ctx* ctx, tgx_vis_stats* out_stats);
+
+/* Decodes one visibility-buffer word like tg_raytracer_get_hovered_voxel
+ * (tgvk_raytracer.c:1639-1653): returns 1 on hit.  Host-only, no device work. */
+int         tgx_vis_decode(uint64_t packed, float* out_depth, uint32_t* out_cluster_pointer, uint32_t* out_voxel_idx);
+
+/* Reads pixel (x, y) of a device visibility buffer of width w and decodes it
+ * (tg_raytracer_get_hovered_voxel, tgvk_raytracer.c:1605-1655).  Blocking. */
+tgx_status  tgx_pick(tgx_ctx* ctx, const uint64_t* d_visbuf, uint32_t w, uint32_t h, uint32_t x, uint32_t y,
+                     float* out_depth, uint32_t* out_cluster_pointer, uint32_t* out_voxel_idx, int* out_hit);
+
+/* ---- one-bit SVO (tg_sparse_voxel_octree.c) ---- */
+
+/*
+ * Builds the one-bit voxel set tg_svo_create (tg_sparse_voxel_octree.c:466-542)
+ * defines over the cube [min, min + 2^extent_log2)^3 (extent_log2 in 6..14;
+ * the reference fixes it at 10): a world voxel is set iff some cluster that
+ * passes the reference's recursive OBB/AABB test for every node on the path to
+ * the voxel's 32^3 block samples a set bit at the voxel centre.  The result is
+ * stored as a dense block table, a pool of 32^3-bit blocks and an occupancy
+ * pyramid (see tgx_svo_info).  Asynchronous; the pool capacity is sized from
+ * the scene and grown (blocking) when exceeded.
+ */
+tgx_status  tgx_svo_build(tgx_ctx* ctx, const tgx_scene* scene, const float min[3], uint32_t extent_log2,
+                          tgx_svo** out_svo);
+void        tgx_svo_destroy(tgx_ctx* ctx, tgx_svo* svo);
+
+typedef struct tgx_svo_info
+{
+    float    min[3];
+    uint32_t extent_log2;
+    uint32_t blocks_per_axis;     /* 2^(extent_log2-5) */
+    uint32_t n_blocks;            /* allocated 32^3 blocks (candidates) */
+    uint32_t n_nonempty_blocks;   /* blocks with at least one voxel set */
+    uint32_t n_pairs;             /* (cluster, block) voxelisation pairs */
+    uint64_t device_bytes;        /* table + pool + pyramid */
+} tgx_svo_info;
+
+tgx_status  tgx_svo_get_info(tgx_ctx* ctx, const tgx_svo* svo, tgx_svo_info* out_info);
+
+/*
+ * Copies the non-empty blocks to the host, sorted by block index
+ * (bz*B*B + by*B + bx): out_block_xyz[3i..3i+2] = world min corner of block i,
+ * out_words[1024i..] its bits (1024z+32y+x).  Returns the block count in
+ * *out_n (blocks beyond capacity are counted, not written).  Blocking.
+ */
+tgx_status  tgx_svo_download(tgx_ctx* ctx, const tgx_svo* svo, int32_t* out_block_xyz, uint32_t* out_words,
+                             uint32_t capacity, uint32_t* out_n);
+
+/*
+ * Traces n rays (device arrays of float3 origin and direction, world space)
+ * through the SVO and writes, per ray, the hit distance t (FLT_MAX on miss)
+ * and the world voxel coordinate (int3; undefined on miss).  At most
+ * max_steps voxel/node steps per ray; a ray that exhausts them is reported as
+ * a miss and counted in the device status word.  Asynchronous.
+ */
+tgx_status  tgx_svo_trace(tgx_ctx* ctx, const tgx_svo* svo, uint32_t n, const float* d_origins,
+                          const float* d_dirs, uint32_t max_steps, float* d_t, int32_t* d_voxel);
+
+/* ---- synthetic scenes (the reference's CPU noise loop, tgvk_raytracer.c:870-978) ---- */
+
+typedef struct tgx_gen_params
+{
+    uint32_t kind;               /* 0: one object, Bernoulli bits; 1: many objects, value-noise bits */
+    uint32_t n_objects;
+    uint32_t min_clusters_per_axis;
+    uint32_t max_clusters_per_axis;
+    float    bernoulli_p;        /* kind 0 */
+    float    noise_period;       /* kind 1, lattice spacing in voxels */
+    float    noise_threshold;    /* kind 1 */
+    uint64_t seed;
+    float    box_min[3];         /* translations uniform in [box_min, box_max) (kind 1) */
+    float    box_max[3];
+    float    fixed_translation[3]; /* kind 0 */
+    uint32_t n_luts;
+    uint32_t threads;            /* host threads, 0 = all */
+} tgx_gen_params;
+
+typedef struct tgx_gen_scene
+{
+    tgx_scene_desc desc;         /* points into the arrays below */
+    tgx_object*    objects;
+    uint32_t*      cluster_pointers;
+    uint32_t*      cluster_idx_to_object_idx;
+    uint32_t*      voxel_bits;
+    uint8_t*       material_idx;
+    tgx_material*  luts;
+} tgx_gen_scene;
+
+tgx_status  tgx_generate_scene(const tgx_gen_params* params, tgx_gen_scene* out_scene);
+void        tgx_free_generated_scene(tgx_gen_scene* scene);
+
+/* Pinhole view from a position, yaw/pitch (radians) and vertical field of
+ * view, with tg's corner-ray construction (tgvk_core.c:382-444): view
+ * rotation inverse(euler(pitch, yaw, 0)), projection tgm_m4_perspective,
+ * corners inverse(P*R) * (+-1, +-1, 1, 1), normalised. */
+tgx_status  tgx_make_view(const float position[3], float pitch, float yaw, float fov_y, uint32_t width,
+                          uint32_t height, float near_plane, float far_plane, tgx_view* out_view);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TGX_H */

@@ -1,0 +1,136 @@
+"""GPU parity of the visibility pass: the CUDA kernels through the C ABI
+against the CPU oracle's transcription of visibility.frag, bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import tg_gb300 as tg
+from scenes import cfg1_scene, cfg1_view, fuzz_scene, permute_clusters, single_cluster_scene
+
+pytestmark = pytest.mark.gpu
+EMPTY = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def render(ctx, scene, views):
+    import torch
+    sc = ctx.upload(scene)
+    outs = [torch.empty(int(v["width"]) * int(v["height"]), dtype=torch.int64, device="cuda") for v in views]
+    ctx.vis_render(sc, views, outs)
+    ctx.sync()
+    err = ctx.device_error()
+    assert err.code == 0, (err.code, err.where, err.detail)
+    res = [o.cpu().numpy().view(np.uint64) for o in outs]
+    sc.close()
+    return res
+
+
+def assert_same(gpu, ref):
+    bad = np.nonzero(gpu != ref)[0]
+    assert len(bad) == 0, f"{len(bad)} pixels differ, first {bad[:5]}: gpu {gpu[bad[:5]]} oracle {ref[bad[:5]]}"
+
+
+def test_cfg1_bit_exact(ctx, oracle):
+    s, v = cfg1_scene(), cfg1_view()
+    (g,) = render(ctx, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=1))
+    assert (g != EMPTY).sum() > 10000
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_fuzz_scenes_bit_exact(ctx, oracle, seed):
+    s = permute_clusters(fuzz_scene(seed, n_objects=6, box=40.0, max_cpa=4), seed)
+    rng = np.random.default_rng(100 + seed)
+    pos = rng.uniform(-10, 10, 3)
+    v = tg.make_view(pos, rng.uniform(-0.5, 0.5), rng.uniform(-3, 3), rng.uniform(0.6, 1.6),
+                     int(rng.integers(40, 200)), int(rng.integers(30, 150)), 0.1, float(rng.uniform(40, 200)))
+    (g,) = render(ctx, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=0))
+
+
+def test_camera_inside_and_near_clusters(ctx, oracle):
+    # camera inside an object: clusters straddle the camera plane (full-screen bins)
+    s = fuzz_scene(11, n_objects=3, box=3.0, max_cpa=3, density=0.05)
+    v = tg.make_view((0.5, 0.25, -0.75), 0.3, 1.0, 1.2, 96, 64, 0.1, 64.0)
+    (g,) = render(ctx, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=0))
+
+
+def test_axis_aligned_rays_and_zero_direction_components(ctx, oracle):
+    # identity rotation, camera on the axis: many ray components are exactly 0
+    s = single_cluster_scene(range(0, 512, 3), translation=(0.0, 0.0, 12.0))
+    v = cfg1_view(33, 33)
+    (g,) = render(ctx, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=0))
+
+
+def test_multi_view_batch_equals_single_views(ctx, oracle):
+    s = fuzz_scene(21, n_objects=5, box=40.0)
+    views = np.concatenate([
+        tg.make_view((0, 0, -60), 0.0, float(np.pi), 1.0, 64, 48, 0.1, 200.0),
+        tg.make_view((5, 3, 70), 0.2, 0.1, 0.9, 37, 53, 0.1, 200.0),
+        tg.make_view((-60, 0, 0), 0.0, float(np.pi / 2), 1.3, 128, 16, 0.1, 200.0),
+    ])
+    outs = render(ctx, s, views)
+    for i in range(len(views)):
+        assert_same(outs[i], oracle.vis_render(s, views[i:i + 1], mode=1))
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (32, 8), (32, 32)])
+def test_tile_shapes_agree(oracle, tile):
+    s, v = cfg1_scene(), cfg1_view(100, 70)
+    with tg.Context(0, tile=tile) as c:
+        (g,) = render(c, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=1))
+
+
+def test_host_buffers_and_pick(ctx, oracle):
+    s, v = cfg1_scene(), cfg1_view(64, 64)
+    sc = ctx.upload(s)
+    out = np.zeros(64 * 64, np.uint64)
+    ctx.vis_render_host(sc, v, [out])
+    ref = oracle.vis_render(s, v, mode=1)
+    assert_same(out, ref)
+    import torch
+    d = torch.from_numpy(out.view(np.int64)).cuda()
+    for (x, y) in [(32, 32), (0, 0), (40, 20)]:
+        hit, depth, ptr, vox = ctx.pick(d, 64, 64, x, y)
+        assert (hit, ptr if hit else None, vox if hit else None) == (
+            tg.decode(int(ref[y * 64 + x]))[0],
+            tg.decode(int(ref[y * 64 + x]))[2] if hit else None,
+            tg.decode(int(ref[y * 64 + x]))[3] if hit else None)
+    sc.close()
+
+
+def test_empty_clusters_give_empty_buffer(ctx):
+    s = single_cluster_scene([], translation=(0.0, 0.0, 10.0))
+    (g,) = render(ctx, s, cfg1_view(40, 30))
+    assert (g == EMPTY).all()
+
+
+def test_rejects_bad_arguments(ctx):
+    s = cfg1_scene()
+    bad = tg.HostScene(s.objects, s.cluster_pointers + np.uint32(1000), s.cluster_idx_to_object_idx, s.voxel_bits)
+    with pytest.raises(tg.TgxError) as e:
+        ctx.upload(bad)
+    assert e.value.status == 1
+    sc = ctx.upload(s)
+    v = cfg1_view(16, 16)
+    v["width"] = 0
+    import torch
+    with pytest.raises(tg.TgxError):
+        ctx.vis_render(sc, v, [torch.empty(1, dtype=torch.int64, device="cuda")])
+    sc.close()
+
+
+def test_cfg2_scale_rows_bit_exact(ctx, oracle):
+    """512 noise objects at 1080p: a band of rows checked against the oracle."""
+    s = tg.generate_scene(1, 512, 2, 16, seed=1, noise_period=64.0, noise_threshold=0.5,
+                          box_min=(-1024, -1024, -1024), box_max=(1024, 1024, 1024), n_luts=32)
+    v = tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), 1920, 1080, 0.1, 4096.0)
+    (g,) = render(ctx, s, v)
+    rows = (500, 520)
+    ref = oracle.vis_render(s, v, mode=1, rows=rows)
+    sl = slice(rows[0] * 1920, rows[1] * 1920)
+    assert_same(g[sl], ref[sl])
+    assert (g != EMPTY).mean() > 0.05

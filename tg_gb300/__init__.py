@@ -1,0 +1,367 @@
+"""tg_gb300 -- Python mirror of the tgx C ABI (include/tgx.h).
+
+The compute path is libtgx.so (CUDA for sm_103a behind an ``extern "C"``
+boundary).  This module only binds it with ctypes and converts numpy / torch
+buffers to plain pointers, the way tg's C host code would call it:
+
+    tg_raytracer_create / create_object / render / clear / get_hovered_voxel
+        -> Context, Scene (tgx_scene_upload), Context.vis_render, Context.pick
+
+There is no fallback: if the library is missing, importing raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libtgx.so"
+
+TGX_OK = 0
+STATUS_NAMES = {
+    0: "TGX_OK", 1: "TGX_ERR_INVALID_ARGUMENT", 2: "TGX_ERR_OUT_OF_MEMORY", 3: "TGX_ERR_CUDA",
+    4: "TGX_ERR_CAPACITY", 5: "TGX_ERR_TIMEOUT", 6: "TGX_ERR_NOT_SUPPORTED", 7: "TGX_ERR_NO_DEVICE",
+    8: "TGX_ERR_DEVICE_FAULT",
+}
+VIS_EMPTY = 0xFFFFFFFFFFFFFFFF
+
+# numpy views of the C structs -------------------------------------------------
+
+OBJECT_DTYPE = np.dtype([
+    ("n_cluster_pointers_per_dim", np.uint32, 3),
+    ("first_cluster_pointer", np.uint32),
+    ("translation", np.float32, 3),
+    ("lut_idx", np.uint32),
+    ("rotation", np.float32, 16),
+])
+assert OBJECT_DTYPE.itemsize == 96
+
+VIEW_DTYPE = np.dtype([
+    ("camera", np.float32, 4), ("ray_bl", np.float32, 4), ("ray_br", np.float32, 4),
+    ("ray_tr", np.float32, 4), ("ray_tl", np.float32, 4), ("near_plane", np.float32),
+    ("far_plane", np.float32), ("width", np.uint32), ("height", np.uint32),
+])
+assert VIEW_DTYPE.itemsize == 96
+
+MATERIAL_DTYPE = np.dtype([("albedo", np.float32, 3), ("roughness", np.float32)])
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("n_objects", C.c_uint32), ("objects", C.c_void_p),
+        ("n_cluster_pointers", C.c_uint32), ("cluster_pointers", C.c_void_p),
+        ("n_clusters", C.c_uint32), ("cluster_idx_to_object_idx", C.c_void_p),
+        ("voxel_bits", C.c_void_p), ("material_idx", C.c_void_p),
+        ("n_luts", C.c_uint32), ("luts", C.c_void_p),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("tile_w", C.c_uint32),
+                ("tile_h", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class DeviceError(C.Structure):
+    _fields_ = [("code", C.c_uint32), ("where", C.c_uint32), ("detail", C.c_uint64)]
+
+
+class GenParams(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint32), ("n_objects", C.c_uint32), ("min_clusters_per_axis", C.c_uint32),
+        ("max_clusters_per_axis", C.c_uint32), ("bernoulli_p", C.c_float), ("noise_period", C.c_float),
+        ("noise_threshold", C.c_float), ("seed", C.c_uint64), ("box_min", C.c_float * 3),
+        ("box_max", C.c_float * 3), ("fixed_translation", C.c_float * 3), ("n_luts", C.c_uint32),
+        ("threads", C.c_uint32),
+    ]
+
+
+class GenScene(C.Structure):
+    _fields_ = [
+        ("desc", SceneDesc), ("objects", C.c_void_p), ("cluster_pointers", C.c_void_p),
+        ("cluster_idx_to_object_idx", C.c_void_p), ("voxel_bits", C.c_void_p),
+        ("material_idx", C.c_void_p), ("luts", C.c_void_p),
+    ]
+
+
+class VisStats(C.Structure):
+    _fields_ = [("visible_clusters", C.c_uint32), ("bin_entries", C.c_uint32), ("tiles", C.c_uint32),
+                ("dda_overruns", C.c_uint32)]
+
+
+class SvoInfo(C.Structure):
+    _fields_ = [("min", C.c_float * 3), ("extent_log2", C.c_uint32), ("blocks_per_axis", C.c_uint32),
+                ("n_blocks", C.c_uint32), ("n_nonempty_blocks", C.c_uint32), ("n_pairs", C.c_uint32),
+                ("device_bytes", C.c_uint64)]
+
+
+# library --------------------------------------------------------------------
+
+EXPORTS = [
+    "tgx_abi_version", "tgx_status_string", "tgx_last_error_string", "tgx_create", "tgx_destroy",
+    "tgx_stream", "tgx_sync", "tgx_last_device_error", "tgx_launch_count", "tgx_scene_upload",
+    "tgx_scene_destroy", "tgx_vis_render", "tgx_vis_render_host", "tgx_vis_decode", "tgx_pick",
+    "tgx_svo_build", "tgx_svo_destroy", "tgx_svo_get_info", "tgx_svo_download", "tgx_svo_trace",
+    "tgx_generate_scene", "tgx_free_generated_scene", "tgx_make_view", "tgx_trace_enable", "tgx_trace_reset",
+    "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats",
+]
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(LIB_PATH))
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    sig = {
+        "tgx_abi_version": (u32, []),
+        "tgx_status_string": (C.c_char_p, [i32]),
+        "tgx_last_error_string": (C.c_char_p, []),
+        "tgx_create": (i32, [C.POINTER(Config), C.POINTER(vp)]),
+        "tgx_destroy": (None, [vp]),
+        "tgx_stream": (vp, [vp]),
+        "tgx_sync": (i32, [vp]),
+        "tgx_last_device_error": (i32, [vp, C.POINTER(DeviceError)]),
+        "tgx_launch_count": (u64, [vp]),
+        "tgx_scene_upload": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(vp)]),
+        "tgx_scene_destroy": (None, [vp, vp]),
+        "tgx_vis_render": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_vis_render_host": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_vis_decode": (i32, [u64, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32)]),
+        "tgx_pick": (i32, [vp, vp, u32, u32, u32, u32, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32), C.POINTER(i32)]),
+        "tgx_svo_build": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_svo_destroy": (None, [vp, vp]),
+        "tgx_svo_get_info": (i32, [vp, vp, C.POINTER(SvoInfo)]),
+        "tgx_svo_download": (i32, [vp, vp, vp, vp, u32, C.POINTER(u32)]),
+        "tgx_svo_trace": (i32, [vp, vp, u32, vp, vp, u32, vp, vp]),
+        "tgx_generate_scene": (i32, [C.POINTER(GenParams), C.POINTER(GenScene)]),
+        "tgx_free_generated_scene": (None, [C.POINTER(GenScene)]),
+        "tgx_make_view": (i32, [vp, C.c_float, C.c_float, C.c_float, u32, u32, C.c_float, C.c_float, vp]),
+        "tgx_trace_enable": (i32, [vp, i32]),
+        "tgx_vis_get_stats": (i32, [vp, C.POINTER(VisStats)]),
+        "tgx_trace_reset": (i32, [vp]),
+        "tgx_trace_slots": (u32, []),
+        "tgx_trace_get": (i32, [vp, u32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(u64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+class TgxError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        msg = lib.tgx_last_error_string().decode(errors="replace")
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(status: int, where: str) -> None:
+    if status != TGX_OK:
+        raise TgxError(status, where)
+
+
+def _ptr(a) -> int:
+    """Address of a numpy array or torch tensor (host or device)."""
+    if a is None:
+        return 0
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+# scenes -----------------------------------------------------------------------
+
+class HostScene:
+    """A tg scene store held in numpy arrays (tg_scene, tgvk_raytracer.h:90-108)."""
+
+    def __init__(self, objects, cluster_pointers, cluster_idx_to_object_idx, voxel_bits,
+                 material_idx=None, luts=None):
+        self.objects = np.ascontiguousarray(objects, dtype=OBJECT_DTYPE)
+        self.cluster_pointers = np.ascontiguousarray(cluster_pointers, dtype=np.uint32)
+        self.cluster_idx_to_object_idx = np.ascontiguousarray(cluster_idx_to_object_idx, dtype=np.uint32)
+        self.voxel_bits = np.ascontiguousarray(voxel_bits, dtype=np.uint32).reshape(-1, 16)
+        self.material_idx = None if material_idx is None else np.ascontiguousarray(material_idx, dtype=np.uint8).reshape(-1, 512)
+        self.luts = None if luts is None else np.ascontiguousarray(luts, dtype=MATERIAL_DTYPE)
+
+    @property
+    def n_clusters(self) -> int:
+        return self.voxel_bits.shape[0]
+
+    def desc(self) -> SceneDesc:
+        d = SceneDesc()
+        d.n_objects = len(self.objects)
+        d.objects = _ptr(self.objects)
+        d.n_cluster_pointers = len(self.cluster_pointers)
+        d.cluster_pointers = _ptr(self.cluster_pointers)
+        d.n_clusters = self.n_clusters
+        d.cluster_idx_to_object_idx = _ptr(self.cluster_idx_to_object_idx)
+        d.voxel_bits = _ptr(self.voxel_bits)
+        d.material_idx = _ptr(self.material_idx)
+        d.n_luts = 0 if self.luts is None else len(self.luts) // 256
+        d.luts = _ptr(self.luts)
+        return d
+
+
+def generate_scene(kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, *,
+                   bernoulli_p: float = 0.3, noise_period: float = 64.0, noise_threshold: float = 0.5,
+                   box_min=(0.0, 0.0, 0.0), box_max=(0.0, 0.0, 0.0), translation=(0.0, 0.0, 0.0),
+                   n_luts: int = 1, threads: int = 0) -> HostScene:
+    """Seeded synthetic scene (tgx_generate_scene); arrays are copied into numpy."""
+    p = GenParams(kind=kind, n_objects=n_objects, min_clusters_per_axis=min_cpa, max_clusters_per_axis=max_cpa,
+                  bernoulli_p=bernoulli_p, noise_period=noise_period, noise_threshold=noise_threshold, seed=seed,
+                  n_luts=n_luts, threads=threads)
+    p.box_min[:] = box_min
+    p.box_max[:] = box_max
+    p.fixed_translation[:] = translation
+    g = GenScene()
+    check(lib.tgx_generate_scene(C.byref(p), C.byref(g)), "tgx_generate_scene")
+    try:
+        d = g.desc
+        n_cl = d.n_clusters
+
+        def arr(ptr, dtype, count):
+            buf = (C.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype=dtype, count=count).copy()
+
+        scene = HostScene(
+            arr(g.objects, OBJECT_DTYPE, d.n_objects),
+            arr(g.cluster_pointers, np.uint32, d.n_cluster_pointers),
+            arr(g.cluster_idx_to_object_idx, np.uint32, n_cl),
+            arr(g.voxel_bits, np.uint32, n_cl * 16),
+            arr(g.material_idx, np.uint8, n_cl * 512),
+            arr(g.luts, MATERIAL_DTYPE, d.n_luts * 256),
+        )
+    finally:
+        lib.tgx_free_generated_scene(C.byref(g))
+    return scene
+
+
+def make_view(position, pitch: float, yaw: float, fov_y: float, width: int, height: int,
+              near: float = 0.1, far: float = 256.0) -> np.ndarray:
+    """One tgx_view (tg camera corner rays, tgvk_core.c:382-444) as a numpy record."""
+    v = np.zeros(1, dtype=VIEW_DTYPE)
+    pos = np.asarray(position, dtype=np.float32)
+    check(lib.tgx_make_view(_ptr(pos), pitch, yaw, fov_y, width, height, near, far, _ptr(v)), "tgx_make_view")
+    return v
+
+
+def decode(packed: int):
+    """tgx_vis_decode: (hit, depth, cluster_pointer, voxel_idx)."""
+    d, cp, vx = C.c_float(), C.c_uint32(), C.c_uint32()
+    hit = lib.tgx_vis_decode(C.c_uint64(packed), C.byref(d), C.byref(cp), C.byref(vx))
+    return bool(hit), d.value, cp.value, vx.value
+
+
+# context ----------------------------------------------------------------------
+
+class Context:
+    """tgx_ctx: one device, one stream."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, tile: tuple[int, int] = (16, 16)):
+        cfg = Config(device=device, stream=stream or 0, tile_w=tile[0], tile_h=tile[1], flags=0)
+        h = C.c_void_p()
+        check(lib.tgx_create(C.byref(cfg), C.byref(h)), "tgx_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            lib.tgx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib.tgx_stream(self.handle) or 0
+
+    def sync(self) -> None:
+        check(lib.tgx_sync(self.handle), "tgx_sync")
+
+    def launches(self) -> int:
+        return int(lib.tgx_launch_count(self.handle))
+
+    def device_error(self) -> DeviceError:
+        e = DeviceError()
+        lib.tgx_last_device_error(self.handle, C.byref(e))
+        return e
+
+    def trace(self, enable: bool) -> None:
+        check(lib.tgx_trace_enable(self.handle, int(enable)), "tgx_trace_enable")
+
+    def trace_reset(self) -> None:
+        check(lib.tgx_trace_reset(self.handle), "tgx_trace_reset")
+
+    def trace_read(self) -> dict[str, tuple[float, int]]:
+        """{kernel name: (summed device ms, launches)} for kernels launched since the last reset."""
+        out = {}
+        for i in range(lib.tgx_trace_slots()):
+            name, ms, n = C.c_char_p(), C.c_double(), C.c_uint64()
+            check(lib.tgx_trace_get(self.handle, i, C.byref(name), C.byref(ms), C.byref(n)), "tgx_trace_get")
+            if n.value:
+                out[name.value.decode()] = (ms.value, int(n.value))
+        return out
+
+    def upload(self, scene: HostScene) -> "Scene":
+        d = scene.desc()
+        h = C.c_void_p()
+        check(lib.tgx_scene_upload(self.handle, C.byref(d), C.byref(h)), "tgx_scene_upload")
+        return Scene(self, h)
+
+    def vis_render(self, scene: "Scene", views: np.ndarray, outs) -> None:
+        """Device outputs: `outs` is a list of device tensors (int64/uint64, W*H each)."""
+        views = np.ascontiguousarray(views, dtype=VIEW_DTYPE)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(o) for o in outs])
+        check(lib.tgx_vis_render(self.handle, scene.handle, _ptr(views), len(views), ptrs), "tgx_vis_render")
+
+    def vis_render_host(self, scene: "Scene", views: np.ndarray, outs) -> None:
+        """Host outputs: `outs` is a list of uint64 numpy arrays (W*H each); blocking."""
+        views = np.ascontiguousarray(views, dtype=VIEW_DTYPE)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(o) for o in outs])
+        check(lib.tgx_vis_render_host(self.handle, scene.handle, _ptr(views), len(views), ptrs),
+              "tgx_vis_render_host")
+
+    def vis_stats(self) -> VisStats:
+        st = VisStats()
+        check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
+        return st
+
+    def pick(self, d_visbuf, w: int, h: int, x: int, y: int):
+        d, cp, vx, hit = C.c_float(), C.c_uint32(), C.c_uint32(), C.c_int()
+        check(lib.tgx_pick(self.handle, _ptr(d_visbuf), w, h, x, y, C.byref(d), C.byref(cp), C.byref(vx),
+                           C.byref(hit)), "tgx_pick")
+        return bool(hit.value), d.value, cp.value, vx.value
+
+
+class Scene:
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def close(self) -> None:
+        if self.handle and self.ctx.handle:
+            lib.tgx_scene_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,568 @@
+// vis.cu -- visibility-buffer pass.
+//
+// Replaces tg's instanced cluster-box raster (visibility.vert:19-26 with
+// cluster_functions.inc:1-38), its fragment-shader DDA (visibility.frag:22-207)
+// and the clear pass (clear.comp:15-21) with a binned compute pass:
+//
+//   1. k_vis_cluster_setup  one thread per (view, cluster pointer): drops
+//      empty clusters, computes a conservative screen-tile rectangle of the
+//      cluster box, and for kept clusters the ws2ms matrix and the camera
+//      position in cluster space exactly as the shader does; appends a
+//      32-byte record and counts the tiles it covers.
+//   2. k_vis_scan           exclusive scan of the per-tile counts.
+//   3. k_vis_bin_fill       scatters record indices into per-tile bins.
+//   4. k_vis_tiles          one CTA per screen tile, one thread per pixel:
+//      stages batches of records and their 64-byte bitmasks in shared
+//      memory, runs the shader's ray/box test and DDA for every
+//      (pixel, binned cluster) pair and keeps the minimum packed
+//      depth|pointer|voxel word; writes every pixel once (fused clear).
+//
+// Every pair evaluates the same binary32 operations in the same order as the
+// CPU oracle's transcription of visibility.frag, so the buffer is bit-exact.
+
+#include "tgx_internal.cuh"
+
+#include <climits>
+#include <cmath>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t kCluster = 8;
+constexpr uint32_t kBatch = 64;            // records staged per shared-memory batch
+constexpr uint32_t kMaxDdaSteps = 64;      // the 8^3 DDA needs at most 22
+
+struct alignas(16) VisRecord
+{
+    float    ox, oy, oz;        // camera position in cluster space (visibility.frag:66)
+    uint32_t cluster_idx;
+    uint32_t cluster_pointer;
+    uint32_t object_idx;
+    uint32_t rect_lo;           // tile x0 | y0 << 12 | view bits 0..7 << 24
+    uint32_t rect_hi;           // tile x1 | y1 << 12 | view bits 8..15 << 24 (inclusive)
+};
+static_assert(sizeof(VisRecord) == 32, "record layout");
+
+enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_COUNT = 4 };
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
+{
+    const uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// 1. per-cluster setup
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_vis_cluster_setup(
+    const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
+    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp,
+    const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
+    uint32_t record_capacity, uint32_t* __restrict__ counters, uint32_t* __restrict__ tile_cnt,
+    tgx_dev_status* __restrict__ status)
+{
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t v = (uint32_t)(gid / n_cp);
+    const uint32_t cp = (uint32_t)(gid % n_cp);
+    bool keep = false;
+    VisRecord rec = {};
+    uint32_t tx0 = 0, ty0 = 0, tx1 = 0, ty1 = 0;
+    if (v < n_views) {
+        const ViewConst& vc = views[v];
+        const uint32_t ci = cluster_pointers[cp];
+        const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
+        const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
+        const uint32_t any = a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w;
+        if (any) {
+            const uint32_t oi = c2o[ci];
+            const tgx_object& od = objects[oi];
+            const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
+            const uint32_t rel = cp - od.first_cluster_pointer;
+            const uint32_t rx = rel % nx, ry = (rel / nx) % ny, rz = rel / (nx * ny);
+            const float offx = (float)(rx * kCluster), offy = (float)(ry * kCluster), offz = (float)(rz * kCluster);
+            const float half = xmul((float)kCluster, 0.5f);
+            const float ohx = xmul(half, (float)od.n_cluster_pointers_per_dim[0]);
+            const float ohy = xmul(half, (float)od.n_cluster_pointers_per_dim[1]);
+            const float ohz = xmul(half, (float)od.n_cluster_pointers_per_dim[2]);
+            float rot[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
+
+            // ---- conservative screen rectangle (only culls; widened by a margin) ----
+            float fxmin = 1e30f, fxmax = -1e30f, fymin = 1e30f, fymax = -1e30f;
+            bool full = false, any_front = false;
+            bool inside0 = false, inside1 = false, inside2 = false, inside3 = false;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const float lx = offx + ((k & 1) ? 8.0f : 0.0f) - ohx;
+                const float ly = offy + ((k & 2) ? 8.0f : 0.0f) - ohy;
+                const float lz = offz + ((k & 4) ? 8.0f : 0.0f) - ohz;
+                float p[3];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+                    p[r] = DM(rot, r, 0) * lx + DM(rot, r, 1) * ly + DM(rot, r, 2) * lz + od.translation[r] - vc.cam[r];
+                const float depth = p[0] * vc.fwd[0] + p[1] * vc.fwd[1] + p[2] * vc.fwd[2];
+                if (depth > -0.5f) any_front = true;
+                const float slack = -(0.05f + 1e-5f * (fabsf(p[0]) + fabsf(p[1]) + fabsf(p[2])));
+                inside0 |= vc.planes[0] * p[0] + vc.planes[1] * p[1] + vc.planes[2] * p[2] > slack;
+                inside1 |= vc.planes[3] * p[0] + vc.planes[4] * p[1] + vc.planes[5] * p[2] > slack;
+                inside2 |= vc.planes[6] * p[0] + vc.planes[7] * p[1] + vc.planes[8] * p[2] > slack;
+                inside3 |= vc.planes[9] * p[0] + vc.planes[10] * p[1] + vc.planes[11] * p[2] > slack;
+                const float s = vc.inv_basis[0] * p[0] + vc.inv_basis[1] * p[1] + vc.inv_basis[2] * p[2];
+                if (depth < 0.5f || s <= 0.0f) { full = true; continue; }
+                const float fa = (vc.inv_basis[3] * p[0] + vc.inv_basis[4] * p[1] + vc.inv_basis[5] * p[2]) / s;
+                const float fb = (vc.inv_basis[6] * p[0] + vc.inv_basis[7] * p[1] + vc.inv_basis[8] * p[2]) / s;
+                fxmin = fminf(fxmin, fa); fxmax = fmaxf(fxmax, fa);
+                fymin = fminf(fymin, fb); fymax = fmaxf(fymax, fb);
+            }
+            if (any_front && inside0 && inside1 && inside2 && inside3) {
+                const float W = (float)vc.width, H = (float)vc.height;
+                float x0, x1, y0, y1;
+                if (full) {
+                    x0 = 0.0f; y0 = 0.0f; x1 = W - 1.0f; y1 = H - 1.0f;
+                } else {
+                    const float m = 2.0f;   // pixels of slack for the float projection
+                    x0 = fxmin * W - 0.5f - m; x1 = fxmax * W - 0.5f + m;
+                    y0 = (1.0f - fymax) * H - 0.5f - m; y1 = (1.0f - fymin) * H - 0.5f + m;
+                }
+                if (!(x1 < 0.0f || y1 < 0.0f || x0 > W - 1.0f || y0 > H - 1.0f)) {
+                    const int ix0 = max(0, (int)floorf(x0)), iy0 = max(0, (int)floorf(y0));
+                    const int ix1 = min((int)vc.width - 1, (int)ceilf(x1));
+                    const int iy1 = min((int)vc.height - 1, (int)ceilf(y1));
+                    if (ix0 <= ix1 && iy0 <= iy1) {
+                        keep = true;
+                        tx0 = (uint32_t)ix0 / vc.tile_w; ty0 = (uint32_t)iy0 / vc.tile_h;
+                        tx1 = (uint32_t)ix1 / vc.tile_w; ty1 = (uint32_t)iy1 / vc.tile_h;
+                    }
+                }
+            }
+            if (keep) {
+                // ---- exact ws2ms and ray origin (visibility.frag:57-66) ----
+                float m0[16], m1[16], m2[16], m3[16], ws2ms[16];
+                dm4_translate(-od.translation[0], -od.translation[1], -od.translation[2], m0);
+                dm4_inverse(rot, m1);
+                dm4_translate(ohx, ohy, ohz, m2);
+                dm4_translate(-offx, -offy, -offz, m3);
+                dm4_mul(m3, m2, ws2ms);
+                dm4_mul(ws2ms, m1, ws2ms);
+                dm4_mul(ws2ms, m0, ws2ms);
+                float o[3];
+                dm4_mulv4(ws2ms, vc.cam[0], vc.cam[1], vc.cam[2], 1.0f, o);
+                rec.ox = o[0]; rec.oy = o[1]; rec.oz = o[2];
+                rec.cluster_idx = ci;
+                rec.cluster_pointer = cp;
+                rec.object_idx = oi;
+                rec.rect_lo = tx0 | (ty0 << 12) | ((v & 0xffu) << 24);
+                rec.rect_hi = tx1 | (ty1 << 12) | ((v >> 8) << 24);
+            }
+        }
+    }
+    const uint32_t slot = warp_append(&counters[C_RECORDS], keep);
+    if (!keep) return;
+    if (slot >= record_capacity) {
+        dev_error(status, TGX_ERR_CAPACITY, 1, slot);
+        return;
+    }
+    records[slot] = rec;
+    const ViewConst& vc = views[v];
+    for (uint32_t ty = ty0; ty <= ty1; ty++)
+        for (uint32_t tx = tx0; tx <= tx1; tx++)
+            atomicAdd(&tile_cnt[vc.tile_base + ty * vc.tiles_x + tx], 1u);
+}
+
+// ---------------------------------------------------------------------------
+// 2. exclusive scan of tile counts (single CTA; n_tiles is a few 10^4)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ tile_off,
+                                                   uint32_t n_tiles, uint32_t* __restrict__ counters)
+{
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < n_tiles; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t x = i < n_tiles ? tile_cnt[i] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t s = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if ((int)lane >= o) s += y;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        const uint32_t warp_prefix = wid ? warp_sums[wid - 1] : 0u;
+        if (i < n_tiles) {
+            tile_off[i] = carry + warp_prefix + incl - x;
+            tile_cnt[i] = 0;   // becomes the fill cursor
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sums[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        tile_off[n_tiles] = carry;
+        counters[C_ENTRIES] = carry;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. bin fill
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restrict__ records,
+                                                     const uint32_t* __restrict__ counters,
+                                                     const ViewConst* __restrict__ views,
+                                                     const uint32_t* __restrict__ tile_off,
+                                                     uint32_t* __restrict__ cursor, uint32_t* __restrict__ bins,
+                                                     uint32_t bin_capacity, tgx_dev_status* __restrict__ status)
+{
+    const uint32_t n = counters[C_RECORDS];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const VisRecord r = records[i];
+        const uint32_t v = (r.rect_lo >> 24) | ((r.rect_hi >> 24) << 8);
+        const ViewConst& vc = views[v];
+        const uint32_t tx0 = r.rect_lo & 0xfffu, ty0 = (r.rect_lo >> 12) & 0xfffu;
+        const uint32_t tx1 = r.rect_hi & 0xfffu, ty1 = (r.rect_hi >> 12) & 0xfffu;
+        for (uint32_t ty = ty0; ty <= ty1; ty++)
+            for (uint32_t tx = tx0; tx <= tx1; tx++) {
+                const uint32_t t = vc.tile_base + ty * vc.tiles_x + tx;
+                const uint32_t pos = tile_off[t] + atomicAdd(&cursor[t], 1u);
+                if (pos < bin_capacity) bins[pos] = i;
+                else dev_error(status, TGX_ERR_CAPACITY, 3, pos);
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. per-tile ray/cluster evaluation
+// ---------------------------------------------------------------------------
+
+// One (pixel, cluster) fragment of visibility.frag:78-207 given the cluster-space
+// ray (o, d) and the cluster's 16 bit words.  Returns the packed word or ~0.
+__device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float oz, float dx, float dy, float dz,
+                                                       const uint32_t* __restrict__ w, uint32_t cluster_pointer,
+                                                       float far_plane, uint32_t* overrun)
+{
+    float enter, exit_;
+    if (!ray_aabb(ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f, enter, exit_)) return ULLONG_MAX;
+    const bool ent = enter > 0.0f;
+    const float hx = ent ? xadd(ox, xmul(enter, dx)) : ox;
+    const float hy = ent ? xadd(oy, xmul(enter, dy)) : oy;
+    const float hz = ent ? xadd(oz, xmul(enter, dz)) : oz;
+    int x = (int)gmin(gmax(floorf(hx), 0.0f), 7.0f);
+    int y = (int)gmin(gmax(floorf(hy), 0.0f), 7.0f);
+    int z = (int)gmin(gmax(floorf(hz), 0.0f), 7.0f);
+    int sx = 0, sy = 0, sz = 0;
+    float tmx = F32_MAX_TG, tmy = F32_MAX_TG, tmz = F32_MAX_TG;
+    float tdx = F32_MAX_TG, tdy = F32_MAX_TG, tdz = F32_MAX_TG;
+    if (dx > 0.0f) { sx = 1; tmx = xadd(enter, xdiv(xsub((float)(x + 1), hx), dx)); tdx = xdiv(1.0f, dx); }
+    else if (dx < 0.0f) { sx = -1; tmx = xadd(enter, xdiv(xsub(hx, (float)x), -dx)); tdx = xdiv(1.0f, -dx); }
+    if (dy > 0.0f) { sy = 1; tmy = xadd(enter, xdiv(xsub((float)(y + 1), hy), dy)); tdy = xdiv(1.0f, dy); }
+    else if (dy < 0.0f) { sy = -1; tmy = xadd(enter, xdiv(xsub(hy, (float)y), -dy)); tdy = xdiv(1.0f, -dy); }
+    if (dz > 0.0f) { sz = 1; tmz = xadd(enter, xdiv(xsub((float)(z + 1), hz), dz)); tdz = xdiv(1.0f, dz); }
+    else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = xdiv(1.0f, -dz); }
+    for (uint32_t step = 0; step < kMaxDdaSteps; step++) {
+        const uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
+        if (w[rvi >> 5] & (1u << (rvi & 31u))) {
+            float ve, vx;
+            ray_aabb(ox, oy, oz, dx, dy, dz, (float)x, (float)y, (float)z, (float)(x + 1), (float)(y + 1),
+                     (float)(z + 1), ve, vx);
+            const float depth = gmax(0.0f, xdiv(ve, far_plane));
+            if (!(depth <= 1.0f)) return ULLONG_MAX;
+            const unsigned long long d24 = __float2ull_rz(xmul(depth, 16777215.0f));
+            return (d24 << 40) | ((unsigned long long)cluster_pointer << 9) | (unsigned long long)rvi;
+        }
+        if (tmx < tmy) {
+            if (tmx < tmz) { tmx = xadd(tmx, tdx); x += sx; if (x < 0 || x >= 8) return ULLONG_MAX; }
+            else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
+        } else {
+            if (tmy < tmz) { tmy = xadd(tmy, tdy); y += sy; if (y < 0 || y >= 8) return ULLONG_MAX; }
+            else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
+        }
+    }
+    atomicAdd(overrun, 1u);
+    return ULLONG_MAX;
+}
+
+__global__ void __launch_bounds__(1024) k_vis_tiles(const VisRecord* __restrict__ records,
+                                                   const uint32_t* __restrict__ bins,
+                                                   const uint32_t* __restrict__ tile_off,
+                                                   const ViewConst* __restrict__ views, uint32_t n_views,
+                                                   const uint32_t* __restrict__ bits,
+                                                   const float* __restrict__ inv_rot,
+                                                   unsigned long long* const* __restrict__ outs,
+                                                   uint32_t* __restrict__ counters)
+{
+    __shared__ VisRecord s_rec[kBatch];
+    __shared__ __align__(16) uint32_t s_bits[kBatch * 16];
+    __shared__ uint32_t s_view;
+
+    const uint32_t tile = blockIdx.x;
+    if (threadIdx.x == 0) {
+        uint32_t v = 0;
+        while (v + 1 < n_views && views[v + 1].tile_base <= tile) v++;
+        s_view = v;
+    }
+    __syncthreads();
+    const ViewConst& vc = views[s_view];
+    const uint32_t lt = tile - vc.tile_base;
+    const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
+    const uint32_t px = tx * vc.tile_w + threadIdx.x % vc.tile_w;
+    const uint32_t py = ty * vc.tile_h + threadIdx.x / vc.tile_w;
+    const bool valid = px < vc.width && py < vc.height;
+
+    // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
+    const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
+    const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)vc.height));
+    float dws[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float a = xadd(xmul(vc.bl[i], xsub(1.0f, fy)), xmul(vc.tl[i], fy));
+        const float b = xadd(xmul(vc.br[i], xsub(1.0f, fy)), xmul(vc.tr[i], fy));
+        dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
+    }
+
+    unsigned long long best = ULLONG_MAX;
+    uint32_t cur_obj = 0xffffffffu;
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    const uint32_t begin = tile_off[tile], end = tile_off[tile + 1];
+    for (uint32_t base = begin; base < end; base += kBatch) {
+        const uint32_t n = min(kBatch, end - base);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s_rec[k] = records[bins[base + k]];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n * 4; k += blockDim.x) {
+            const uint32_t r = k >> 2, q = k & 3u;
+            reinterpret_cast<uint4*>(s_bits)[k] =
+                reinterpret_cast<const uint4*>(bits + (uint64_t)s_rec[r].cluster_idx * 16u)[q];
+        }
+        __syncthreads();
+        if (!valid) continue;
+        for (uint32_t k = 0; k < n; k++) {
+            const VisRecord& r = s_rec[k];
+            if (r.object_idx != cur_obj) {
+                // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
+                // object's shared linear part (see k_object_setup)
+                cur_obj = r.object_idx;
+                const float* L = inv_rot + 9u * cur_obj;
+                const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
+                const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
+                const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
+                const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
+                dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
+            }
+            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, &s_bits[k * 16], r.cluster_pointer,
+                                                  vc.far_plane, &counters[C_DDA_OVERRUN]);
+            best = p < best ? p : best;
+        }
+    }
+    if (valid) outs[s_view][(size_t)py * vc.width + px] = best;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static void make_view_const(const tgx_view& v, uint32_t tile_w, uint32_t tile_h, uint32_t tile_base, ViewConst& c)
+{
+    memset(&c, 0, sizeof(c));
+    for (int i = 0; i < 3; i++) {
+        c.cam[i] = v.camera[i];
+        c.bl[i] = v.ray_bl[i]; c.br[i] = v.ray_br[i]; c.tr[i] = v.ray_tr[i]; c.tl[i] = v.ray_tl[i];
+    }
+    c.far_plane = v.far_plane;
+    c.width = v.width;
+    c.height = v.height;
+    c.tile_w = tile_w;
+    c.tile_h = tile_h;
+    c.tiles_x = (v.width + tile_w - 1) / tile_w;
+    c.tiles_y = (v.height + tile_h - 1) / tile_h;
+    c.tile_base = tile_base;
+    // affine corner-ray model d(fx, fy) = bl + fx (br - bl) + fy (tl - bl):
+    // p = s * d  <=>  (s, s fx, s fy) = B^-1 p with B = [bl | br-bl | tl-bl]
+    double B[3][3];
+    for (int i = 0; i < 3; i++) {
+        B[i][0] = v.ray_bl[i];
+        B[i][1] = (double)v.ray_br[i] - v.ray_bl[i];
+        B[i][2] = (double)v.ray_tl[i] - v.ray_bl[i];
+    }
+    const double det = B[0][0] * (B[1][1] * B[2][2] - B[1][2] * B[2][1]) - B[0][1] * (B[1][0] * B[2][2] - B[1][2] * B[2][0]) +
+                       B[0][2] * (B[1][0] * B[2][1] - B[1][1] * B[2][0]);
+    const double inv[9] = {
+        (B[1][1] * B[2][2] - B[1][2] * B[2][1]) / det, (B[0][2] * B[2][1] - B[0][1] * B[2][2]) / det,
+        (B[0][1] * B[1][2] - B[0][2] * B[1][1]) / det, (B[1][2] * B[2][0] - B[1][0] * B[2][2]) / det,
+        (B[0][0] * B[2][2] - B[0][2] * B[2][0]) / det, (B[0][2] * B[1][0] - B[0][0] * B[1][2]) / det,
+        (B[1][0] * B[2][1] - B[1][1] * B[2][0]) / det, (B[0][1] * B[2][0] - B[0][0] * B[2][1]) / det,
+        (B[0][0] * B[1][1] - B[0][1] * B[1][0]) / det};
+    for (int i = 0; i < 9; i++) c.inv_basis[i] = (float)inv[i];
+    double f[3], fl = 0.0;
+    for (int i = 0; i < 3; i++) {
+        f[i] = 0.25 * ((double)v.ray_bl[i] + v.ray_br[i] + v.ray_tr[i] + v.ray_tl[i]);
+        fl += f[i] * f[i];
+    }
+    fl = sqrt(fl);
+    for (int i = 0; i < 3; i++) c.fwd[i] = (float)(f[i] / fl);
+    // side planes through the camera, spanned by adjacent corner rays, normals pointing inward
+    const float* cr[4] = {v.ray_bl, v.ray_br, v.ray_tr, v.ray_tl};
+    for (int k = 0; k < 4; k++) {
+        const float* a = cr[k];
+        const float* b = cr[(k + 1) % 4];
+        double n[3] = {(double)a[1] * b[2] - (double)a[2] * b[1], (double)a[2] * b[0] - (double)a[0] * b[2],
+                       (double)a[0] * b[1] - (double)a[1] * b[0]};
+        const double sgn = n[0] * f[0] + n[1] * f[1] + n[2] * f[2] < 0 ? -1.0 : 1.0;
+        const double l = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int i = 0; i < 3; i++) c.planes[3 * k + i] = (float)(sgn * n[i] / l);
+    }
+}
+
+static tgx_status check_views(const tgx_view* views, uint32_t n_views, uint32_t tile_w, uint32_t tile_h)
+{
+    if (!views || n_views == 0 || n_views > 65535) { tgx_set_error("views: NULL or count %u out of range", n_views); return TGX_ERR_INVALID_ARGUMENT; }
+    for (uint32_t i = 0; i < n_views; i++) {
+        const tgx_view& v = views[i];
+        if (v.width == 0 || v.height == 0 || (v.width + tile_w - 1) / tile_w > 4095 || (v.height + tile_h - 1) / tile_h > 4095) {
+            tgx_set_error("view %u: size %ux%u out of range", i, v.width, v.height);
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+        if (!(v.far_plane > 0.0f)) { tgx_set_error("view %u: far plane must be > 0", i); return TGX_ERR_INVALID_ARGUMENT; }
+    }
+    return TGX_OK;
+}
+
+tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
+                             uint64_t* const* d_visbuf)
+{
+    if (!c || !s || !d_visbuf) { tgx_set_error("tgx_vis_render: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
+    for (uint32_t i = 0; i < n_views; i++)
+        if (!d_visbuf[i]) { tgx_set_error("tgx_vis_render: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
+    TGX_CUDA(cudaSetDevice(c->device));
+
+    // view constants + output pointer table in one pinned staging block
+    std::vector<ViewConst> vcs(n_views);
+    uint32_t n_tiles = 0;
+    for (uint32_t i = 0; i < n_views; i++) {
+        make_view_const(views[i], c->tile_w, c->tile_h, n_tiles, vcs[i]);
+        n_tiles += vcs[i].tiles_x * vcs[i].tiles_y;
+    }
+    const size_t vc_bytes = n_views * sizeof(ViewConst);
+    const size_t ptr_off = (vc_bytes + 15) & ~(size_t)15;
+    const size_t stage_bytes = ptr_off + n_views * sizeof(void*);
+    if (c->h_pinned_bytes < stage_bytes) {
+        if (c->h_pinned) cudaFreeHost(c->h_pinned);
+        c->h_pinned = nullptr;
+        c->h_pinned_bytes = 0;
+        TGX_CUDA(cudaStreamSynchronize(c->stream));
+        TGX_CUDA(cudaMallocHost(&c->h_pinned, stage_bytes));
+        c->h_pinned_bytes = stage_bytes;
+    }
+    // the previous call's copy out of the staging block must be complete
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    memcpy(c->h_pinned, vcs.data(), vc_bytes);
+    memcpy((char*)c->h_pinned + ptr_off, d_visbuf, n_views * sizeof(void*));
+    TGX_TRY(devbuf_reserve(c->vis_views, stage_bytes));
+    TGX_CUDA(cudaMemcpyAsync(c->vis_views.ptr, c->h_pinned, stage_bytes, cudaMemcpyHostToDevice, c->stream));
+    const ViewConst* d_vc = (const ViewConst*)c->vis_views.ptr;
+    unsigned long long* const* d_outs = (unsigned long long* const*)((char*)c->vis_views.ptr + ptr_off);
+
+    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
+    if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
+    const uint32_t rec_cap = (uint32_t)n_pairs;
+    TGX_TRY(devbuf_reserve(c->vis_records, (size_t)rec_cap * sizeof(VisRecord)));
+    TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
+    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * 4));
+    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4));
+    uint32_t* counters = (uint32_t*)c->vis_counters.ptr;
+    uint32_t* tile_cnt = (uint32_t*)c->vis_tile_cnt.ptr;
+    uint32_t* tile_off = (uint32_t*)c->vis_tile_off.ptr;
+    TGX_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
+    TGX_CUDA(cudaMemsetAsync(tile_cnt, 0, (size_t)n_tiles * 4, c->stream));
+
+    const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
+    TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
+               s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
+               (VisRecord*)c->vis_records.ptr, rec_cap, counters, tile_cnt, c->d_status);
+    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, tile_cnt, tile_off, n_tiles, counters);
+    // bin storage is sized from the scan result
+    TGX_CUDA(cudaMemcpyAsync(c->h_counter, counters + C_ENTRIES, 4, cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    const uint32_t entries = *(uint32_t*)c->h_counter;
+    TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)(entries ? entries : 1) * 4));
+    const uint32_t fill_blocks = (uint32_t)std::min<uint64_t>((n_pairs + 255) / 256, (uint64_t)c->num_sms * 16);
+    TGX_LAUNCH(c, TR_VIS_BIN, fill_blocks ? fill_blocks : 1, 256, 0, k_vis_bin_fill,
+               (const VisRecord*)c->vis_records.ptr, counters, d_vc, tile_off, tile_cnt, (uint32_t*)c->vis_bins.ptr,
+               (uint32_t)(c->vis_bins.bytes / 4), c->d_status);
+    c->vis_last_tiles = n_tiles;
+    TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, c->tile_w * c->tile_h, 0, k_vis_tiles,
+               (const VisRecord*)c->vis_records.ptr, (const uint32_t*)c->vis_bins.ptr, tile_off, d_vc, n_views,
+               s->d_bits, s->d_inv_rot, d_outs, counters);
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_vis_render(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
+                                     uint64_t* const* d_visbuf)
+{
+    return vis_render_device(c, s, views, n_views, d_visbuf);
+}
+
+extern "C" tgx_status tgx_vis_render_host(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
+                                          uint64_t* const* h_visbuf)
+{
+    if (!c || !s || !h_visbuf) { tgx_set_error("tgx_vis_render_host: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
+    size_t total = 0;
+    std::vector<size_t> offs(n_views);
+    for (uint32_t i = 0; i < n_views; i++) {
+        if (!h_visbuf[i]) { tgx_set_error("tgx_vis_render_host: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
+        offs[i] = total;
+        total += (size_t)views[i].width * views[i].height;
+    }
+    TGX_TRY(devbuf_reserve(c->host_stage, total * 8));
+    std::vector<uint64_t*> dptr(n_views);
+    for (uint32_t i = 0; i < n_views; i++) dptr[i] = (uint64_t*)c->host_stage.ptr + offs[i];
+    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data()));
+    for (uint32_t i = 0; i < n_views; i++)
+        TGX_CUDA(cudaMemcpyAsync(h_visbuf[i], dptr[i], (size_t)views[i].width * views[i].height * 8,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_vis_get_stats(tgx_ctx* c, tgx_vis_stats* out)
+{
+    if (!c || !out) return TGX_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    if (!c->vis_counters.ptr) return TGX_OK;
+    uint32_t h[C_COUNT];
+    TGX_CUDA(cudaMemcpyAsync(c->h_counter, c->vis_counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    memcpy(h, c->h_counter, sizeof(h));
+    out->visible_clusters = h[C_RECORDS];
+    out->bin_entries = h[C_ENTRIES];
+    out->dda_overruns = h[C_DDA_OVERRUN];
+    out->tiles = c->vis_last_tiles;
+    return TGX_OK;
+}
