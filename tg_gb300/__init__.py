@@ -338,6 +338,12 @@ class Context:
         check(lib.tgx_vis_render_host(self.handle, scene.handle, _ptr(views), len(views), ptrs),
               "tgx_vis_render_host")
 
+    def svo_build(self, scene: "Scene", mn, extent_log2: int) -> Svo:
+        m = np.asarray(mn, dtype=np.float32)
+        h = C.c_void_p()
+        check(lib.tgx_svo_build(self.handle, scene.handle, _ptr(m), extent_log2, C.byref(h)), "tgx_svo_build")
+        return Svo(self, h)
+
     def vis_stats(self) -> VisStats:
         st = VisStats()
         check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
@@ -348,6 +354,46 @@ class Context:
         check(lib.tgx_pick(self.handle, _ptr(d_visbuf), w, h, x, y, C.byref(d), C.byref(cp), C.byref(vx),
                            C.byref(hit)), "tgx_pick")
         return bool(hit.value), d.value, cp.value, vx.value
+
+
+class Svo:
+    """tgx_svo: the one-bit voxel set of tg_svo_create on the device."""
+
+    def __init__(self, ctx: "Context", handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def info(self) -> SvoInfo:
+        i = SvoInfo()
+        check(lib.tgx_svo_get_info(self.ctx.handle, self.handle, C.byref(i)), "tgx_svo_get_info")
+        return i
+
+    def download(self):
+        """(block_xyz int32[n,3], words uint32[n,1024]) of the non-empty blocks, sorted by block index."""
+        n = C.c_uint32()
+        check(lib.tgx_svo_download(self.ctx.handle, self.handle, None, None, 0, C.byref(n)), "tgx_svo_download")
+        xyz = np.zeros((n.value, 3), np.int32)
+        words = np.zeros((n.value, 1024), np.uint32)
+        check(lib.tgx_svo_download(self.ctx.handle, self.handle, _ptr(xyz), _ptr(words), n.value, C.byref(n)),
+              "tgx_svo_download")
+        return xyz, words
+
+    def trace(self, origins, dirs, t_out, voxel_out, max_steps: int = 4096) -> None:
+        """Device arrays: origins/dirs float32[n,3], t_out float32[n], voxel_out int32[n,3]."""
+        n = origins.shape[0]
+        check(lib.tgx_svo_trace(self.ctx.handle, self.handle, n, _ptr(origins), _ptr(dirs), max_steps, _ptr(t_out),
+                                _ptr(voxel_out)), "tgx_svo_trace")
+
+    def close(self) -> None:
+        if self.handle and self.ctx.handle:
+            lib.tgx_svo_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Scene:

@@ -1,13 +1,594 @@
-// svo.cu -- one-bit SVO build and traversal (placeholder entry points).
+// svo.cu -- one-bit SVO build on the GPU.
+//
+// Replaces tg's recursive single-threaded CPU builder tg_svo_create
+// (tg_sparse_voxel_octree.c:466-542) with four data-parallel passes that set
+// exactly the same world voxels:
+//
+//   1. k_svo_candidates  one thread per cluster pointer: drops empty clusters
+//      (:515-531), finds the 32^3 blocks its box can touch, and for each runs
+//      the reference's OBB/AABB test (tg_physics.c:226-392) on every node on
+//      the path from the root's children down to the block, with the node
+//      boxes and ws2ms matrix of tg__construct_inner_node (:319-397).  A block
+//      whose whole path passes becomes a (cluster, block) pair; the block is
+//      marked in the dense block table.
+//   2. k_svo_alloc       gives every marked block a slot in the block pool.
+//   3. k_svo_voxelize    one warp per pair: the leaf voxelisation of
+//      tg__construct_leaf_node (:102-317) -- corner lerp, [0,8)^3 test, bit
+//      fetch -- into a warp-private 4 KiB block image in shared memory, then
+//      coalesced atomicOr of its non-zero words into the pool.
+//   4. k_svo_pyramid     bottom-up occupancy: one bit per non-empty block and
+//      per non-empty node of every coarser level.
+//
+// The node encoding of the reference (u16 relative child pointers, 64-entry
+// leaf lists) is not kept; the voxel set is.  Side length 2^6 .. 2^14.
+
 #include "tgx_internal.cuh"
 
-extern "C" tgx_status tgx_svo_build(tgx_ctx*, const tgx_scene*, const float*, uint32_t, tgx_svo** out)
+#include <algorithm>
+#include <vector>
+
+struct tgx_svo
 {
-    if (out) *out = nullptr;
-    tgx_set_error("tgx_svo_build: not built yet");
+    float     mn[3] = {0, 0, 0};
+    uint32_t  L = 0;              // extent_log2
+    uint32_t  B = 0;              // blocks per axis
+    uint32_t  n_blocks = 0;       // allocated (candidate) blocks
+    uint32_t  n_pairs = 0;
+    uint32_t* d_table = nullptr;  // B^3 entries: 0 = no block, else slot + 1
+    uint32_t* d_pool = nullptr;   // n_blocks * 1024 words
+    uint32_t* d_occ = nullptr;    // occupancy pyramid, level 0 = blocks
+    uint64_t  occ_words = 0;
+    uint64_t  occ_off[10] = {};   // word offset of each level
+    uint32_t  n_levels = 0;       // L - 5 + 1 levels (blocks .. root)
+    uint32_t* d_nonempty = nullptr;  // per slot: 1 if any bit set
+    uint64_t  device_bytes = 0;
+};
+
+namespace {
+
+constexpr uint32_t kBlockSide = 32;
+constexpr uint32_t kBlockWords = 1024;
+constexpr uint32_t kMark = 0xffffffffu;
+constexpr uint32_t kWarpsPerVoxCta = 4;
+
+struct SvoPair
+{
+    uint32_t cluster_pointer;
+    uint32_t block;
+};
+
+enum SvoCounter { S_PAIRS = 0, S_MARKED = 1, S_SLOTS = 2, S_NONEMPTY = 3, S_COUNT = 4 };
+
+struct dv3 { float x, y, z; };
+
+__device__ __forceinline__ void cluster_offsets(const tgx_object& od, uint32_t rel, float off[3], float ohe[3])
+{
+    const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
+    off[0] = (float)((rel % nx) * 8u);
+    off[1] = (float)(((rel / nx) % ny) * 8u);
+    off[2] = (float)((rel / (nx * ny)) * 8u);
+    const float h = 4.0f;   // (f32)(TG_N_PRIMITIVES_PER_CLUSTER_CUBE_ROOT / 2)
+    ohe[0] = xmul((float)od.n_cluster_pointers_per_dim[0], h);
+    ohe[1] = xmul((float)od.n_cluster_pointers_per_dim[1], h);
+    ohe[2] = xmul((float)od.n_cluster_pointers_per_dim[2], h);
+}
+
+// tg_world_space_to_cluster_model_space (tg_sparse_voxel_octree.c:23-60)
+__device__ __forceinline__ void svo_ws2ms(const tgx_object& od, uint32_t rel, float* out)
+{
+    float off[3], ohe[3], rot[16], m1[16], m2[16], m3[16], m4[16];
+    cluster_offsets(od, rel, off, ohe);
+#pragma unroll
+    for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
+    dm4_translate(-od.translation[0], -od.translation[1], -od.translation[2], m1);
+    dm4_inverse(rot, m2);
+    dm4_translate(ohe[0], ohe[1], ohe[2], m3);
+    dm4_translate(-off[0], -off[1], -off[2], m4);
+    dm4_mul(m4, m3, out);
+    dm4_mul(out, m2, out);
+    dm4_mul(out, m1, out);
+}
+
+// tg_cluster_model_space_to_world_space (tg_sparse_voxel_octree.c:62-100)
+__device__ __forceinline__ void svo_cs2ws(const tgx_object& od, uint32_t rel, float* out)
+{
+    float off[3], ohe[3], rot[16], m1[16], m2[16], m4[16];
+    cluster_offsets(od, rel, off, ohe);
+#pragma unroll
+    for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
+    dm4_translate(off[0], off[1], off[2], m1);
+    dm4_translate(-ohe[0], -ohe[1], -ohe[2], m2);
+    dm4_translate(od.translation[0], od.translation[1], od.translation[2], m4);
+    dm4_mul(m4, rot, out);
+    dm4_mul(out, m2, out);
+    dm4_mul(out, m1, out);
+}
+
+__device__ __forceinline__ dv3 mulv4p(const float* m, float x, float y, float z)
+{
+    float r[3];
+    dm4_mulv4(m, x, y, z, 1.0f, r);
+    return dv3{r[0], r[1], r[2]};
+}
+
+__device__ __forceinline__ float dot3(dv3 a, dv3 b) { return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z)); }
+__device__ __forceinline__ float mag3(dv3 a) { return xsqrt(dot3(a, a)); }
+__device__ __forceinline__ dv3 sub3(dv3 a, dv3 b) { return dv3{xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)}; }
+__device__ __forceinline__ dv3 normalized3(dv3 a)
+{
+    const float m = mag3(a);
+    return dv3{xdiv(a.x, m), xdiv(a.y, m), xdiv(a.z, m)};
+}
+
+// tg_intersect_aabb_obb_ignore_contact (tg_physics.c:226-392) with the AABB
+// [0,8]^3 (the cluster) and the OBB given by its 8 corners (a block).
+__device__ __forceinline__ bool aabb_obb(const dv3* c)
+{
+    const float mx = 8.0f;
+    bool sep;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].x <= 0.0f;
+    if (sep) return false;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].x >= mx;
+    if (sep) return false;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].y <= 0.0f;
+    if (sep) return false;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].y >= mx;
+    if (sep) return false;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].z <= 0.0f;
+    if (sep) return false;
+    sep = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) sep &= c[i].z >= mx;
+    if (sep) return false;
+
+    const dv3 nxp = normalized3(sub3(c[1], c[0]));
+    const dv3 nyp = normalized3(sub3(c[2], c[0]));
+    const dv3 nzp = normalized3(sub3(c[4], c[0]));
+    const dv3 nrm[6] = {dv3{-nxp.x, -nxp.y, -nxp.z}, nxp, dv3{-nyp.x, -nyp.y, -nyp.z}, nyp,
+                        dv3{-nzp.x, -nzp.y, -nzp.z}, nzp};
+    const float l0 = mag3(c[0]);
+    const float l1 = mag3(c[7]);
+    const dv3 n0 = l0 == 0.0f ? dv3{0.0f, 0.0f, 0.0f} : dv3{xdiv(c[0].x, l0), xdiv(c[0].y, l0), xdiv(c[0].z, l0)};
+    const dv3 n1 = l1 == 0.0f ? dv3{0.0f, 0.0f, 0.0f} : dv3{xdiv(c[7].x, l1), xdiv(c[7].y, l1), xdiv(c[7].z, l1)};
+    float dist[6];
+    dist[0] = xmul(l0, dot3(n0, nrm[0]));
+    dist[1] = xmul(l1, dot3(n1, nrm[1]));
+    dist[2] = xmul(l0, dot3(n0, nrm[2]));
+    dist[3] = xmul(l1, dot3(n1, nrm[3]));
+    dist[4] = xmul(l0, dot3(n0, nrm[4]));
+    dist[5] = xmul(l1, dot3(n1, nrm[5]));
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+        sep = true;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const dv3 pt = dv3{(k & 1) ? mx : 0.0f, (k & 2) ? mx : 0.0f, (k & 4) ? mx : 0.0f};
+            sep &= xsub(dot3(nrm[p], pt), dist[p]) >= 0.0f;
+        }
+        if (sep) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// 1. candidates
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_svo_candidates(
+    const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
+    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp, float mnx, float mny,
+    float mnz, uint32_t L, uint32_t B, uint32_t* __restrict__ table, SvoPair* __restrict__ pairs,
+    uint32_t pair_capacity, uint32_t* __restrict__ counters, tgx_dev_status* __restrict__ status)
+{
+    const uint32_t cp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cp >= n_cp) return;
+    const uint32_t ci = cluster_pointers[cp];
+    const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
+    const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
+    if (!(a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w)) return;
+    const tgx_object& od = objects[c2o[ci]];
+    const uint32_t rel = cp - od.first_cluster_pointer;
+
+    // conservative world box of the cluster (only selects blocks to test)
+    float off[3], ohe[3];
+    cluster_offsets(od, rel, off, ohe);
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float lx = off[0] + ((k & 1) ? 8.0f : 0.0f) - ohe[0];
+        const float ly = off[1] + ((k & 2) ? 8.0f : 0.0f) - ohe[1];
+        const float lz = off[2] + ((k & 4) ? 8.0f : 0.0f) - ohe[2];
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const float p = DM(od.rotation, r, 0) * lx + DM(od.rotation, r, 1) * ly + DM(od.rotation, r, 2) * lz +
+                            od.translation[r];
+            lo[r] = fminf(lo[r], p);
+            hi[r] = fmaxf(hi[r], p);
+        }
+    }
+    const float mn[3] = {mnx, mny, mnz};
+    int b0[3], b1[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const float slack = 0.5f + 1e-5f * fabsf(lo[r]) + 1e-5f * fabsf(hi[r]);
+        b0[r] = (int)floorf((lo[r] - slack - mn[r]) / 32.0f);
+        b1[r] = (int)floorf((hi[r] + slack - mn[r]) / 32.0f);
+        b0[r] = max(b0[r], 0);
+        b1[r] = min(b1[r], (int)B - 1);
+        if (b0[r] > b1[r]) return;
+    }
+    float ws2ms[16];
+    svo_ws2ms(od, rel, ws2ms);
+    const float ext = (float)(1u << L);
+    for (int bz = b0[2]; bz <= b1[2]; bz++)
+        for (int by = b0[1]; by <= b1[1]; by++)
+            for (int bx = b0[0]; bx <= b1[0]; bx++) {
+                // walk the reference's recursion from the root to this block
+                dv3 pmin = dv3{mnx, mny, mnz};
+                dv3 pmax = dv3{xadd(mnx, ext), xadd(mny, ext), xadd(mnz, ext)};
+                bool pass = true;
+                for (int lev = (int)L - 1; lev >= 5; lev--) {
+                    const dv3 ce = dv3{xmul(xsub(pmax.x, pmin.x), 0.5f), xmul(xsub(pmax.y, pmin.y), 0.5f),
+                                       xmul(xsub(pmax.z, pmin.z), 0.5f)};
+                    const uint32_t sh = (uint32_t)lev - 5;
+                    const uint32_t cx = ((uint32_t)bx >> sh) & 1u, cy = ((uint32_t)by >> sh) & 1u,
+                                   cz = ((uint32_t)bz >> sh) & 1u;
+                    const dv3 cmin = dv3{xadd(pmin.x, xmul((float)cx, ce.x)), xadd(pmin.y, xmul((float)cy, ce.y)),
+                                         xadd(pmin.z, xmul((float)cz, ce.z))};
+                    const dv3 cmax = dv3{xadd(cmin.x, ce.x), xadd(cmin.y, ce.y), xadd(cmin.z, ce.z)};
+                    dv3 bc[8];
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        bc[k] = mulv4p(ws2ms, (k & 1) ? cmax.x : cmin.x, (k & 2) ? cmax.y : cmin.y,
+                                       (k & 4) ? cmax.z : cmin.z);
+                    if (!aabb_obb(bc)) { pass = false; break; }
+                    pmin = cmin;
+                    pmax = cmax;
+                }
+                if (!pass) continue;
+                const uint32_t blk = ((uint32_t)bz * B + (uint32_t)by) * B + (uint32_t)bx;
+                const uint32_t slot = atomicAdd(&counters[S_PAIRS], 1u);
+                if (slot < pair_capacity) pairs[slot] = SvoPair{cp, blk};
+                else dev_error(status, TGX_ERR_CAPACITY, 11, slot);
+                if (atomicCAS(&table[blk], 0u, kMark) == 0u) atomicAdd(&counters[S_MARKED], 1u);
+            }
+}
+
+// ---------------------------------------------------------------------------
+// 2. slot allocation
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_svo_alloc(uint32_t* __restrict__ table, uint64_t n_table,
+                                                  uint32_t* __restrict__ counters, uint32_t pool_blocks,
+                                                  tgx_dev_status* __restrict__ status)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_table;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (table[i] == kMark) {
+            const uint32_t s = atomicAdd(&counters[S_SLOTS], 1u);
+            if (s < pool_blocks) table[i] = s + 1u;
+            else { table[i] = 0u; dev_error(status, TGX_ERR_CAPACITY, 12, s); }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. voxelisation: one warp per (cluster, block) pair
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t trim_u32(float v) { return v > 0.0f ? (uint32_t)v : 0u; }
+
+__global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
+    const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
+    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, const SvoPair* __restrict__ pairs,
+    const uint32_t* __restrict__ counters, uint32_t pair_capacity, const uint32_t* __restrict__ table,
+    uint32_t* __restrict__ pool, float mnx, float mny, float mnz, uint32_t B)
+{
+    __shared__ uint32_t s_img[kWarpsPerVoxCta][kBlockWords];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    uint32_t* img = s_img[wid];
+    const uint32_t n_pairs = min(counters[S_PAIRS], pair_capacity);
+    for (uint32_t pi = blockIdx.x * kWarpsPerVoxCta + wid; pi < n_pairs; pi += gridDim.x * kWarpsPerVoxCta) {
+        const SvoPair pr = pairs[pi];
+        const uint32_t tv = table[pr.block];
+        if (tv == 0u) continue;   // allocation failed (recorded in the status word)
+        const uint32_t slot = tv - 1u;
+        const uint32_t cp = pr.cluster_pointer;
+        const uint32_t ci = cluster_pointers[cp];
+        const tgx_object& od = objects[c2o[ci]];
+        const uint32_t rel = cp - od.first_cluster_pointer;
+        const uint32_t bx = pr.block % B, by = (pr.block / B) % B, bz = pr.block / (B * B);
+        // block box: same values the recursion produces (exact powers of two)
+        const dv3 pmin = dv3{xadd(mnx, (float)(bx * kBlockSide)), xadd(mny, (float)(by * kBlockSide)),
+                             xadd(mnz, (float)(bz * kBlockSide))};
+        const dv3 pmax = dv3{xadd(pmin.x, 32.0f), xadd(pmin.y, 32.0f), xadd(pmin.z, 32.0f)};
+        const dv3 pext = sub3(pmax, pmin);
+
+        float cs2ws[16], ws2cs[16];
+        svo_cs2ws(od, rel, cs2ws);
+        dv3 cw[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            cw[k] = mulv4p(cs2ws, (k & 1) ? 8.0f : 0.0f, (k & 2) ? 8.0f : 0.0f, (k & 4) ? 8.0f : 0.0f);
+        // :180-194 -- note corner 2 twice, corner 3 never
+        auto vmin = [](dv3 p, dv3 q) { return dv3{p.x < q.x ? p.x : q.x, p.y < q.y ? p.y : q.y, p.z < q.z ? p.z : q.z}; };
+        auto vmax = [](dv3 p, dv3 q) { return dv3{p.x > q.x ? p.x : q.x, p.y > q.y ? p.y : q.y, p.z > q.z ? p.z : q.z}; };
+        const dv3 min_c = vmin(vmin(vmin(cw[0], cw[1]), vmin(cw[2], cw[2])), vmin(vmin(cw[4], cw[6]), vmin(cw[5], cw[7])));
+        const dv3 max_c = vmax(vmax(vmax(cw[0], cw[1]), vmax(cw[2], cw[2])), vmax(vmax(cw[4], cw[6]), vmax(cw[5], cw[7])));
+        const dv3 fmin_c = dv3{floorf(min_c.x), floorf(min_c.y), floorf(min_c.z)};
+        const dv3 cmax_c = dv3{ceilf(max_c.x), ceilf(max_c.y), ceilf(max_c.z)};
+        dm4_inverse(cs2ws, ws2cs);
+        dv3 bc[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            bc[k] = mulv4p(ws2cs, (k & 1) ? pmax.x : pmin.x, (k & 2) ? pmax.y : pmin.y, (k & 4) ? pmax.z : pmin.z);
+        const dv3 tmin = vmax(pmin, fmin_c);
+        const dv3 tmax = vmin(pmax, cmax_c);
+        const uint32_t x0 = trim_u32(xsub(tmin.x, pmin.x)), y0 = trim_u32(xsub(tmin.y, pmin.y)), z0 = trim_u32(xsub(tmin.z, pmin.z));
+        const uint32_t x1 = trim_u32(xsub(tmax.x, pmin.x)), y1 = trim_u32(xsub(tmax.y, pmin.y)), z1 = trim_u32(xsub(tmax.z, pmin.z));
+        if (x0 >= x1 || y0 >= y1 || z0 >= z1) continue;
+
+        for (uint32_t k = lane; k < kBlockWords; k += 32) img[k] = 0u;
+        __syncwarp();
+        const uint32_t nx = x1 - x0, ny = y1 - y0, nz = z1 - z0;
+        const uint32_t total = nx * ny * nz;
+        const uint32_t* cb = bits + (uint64_t)ci * 16u;
+        uint32_t cw16[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) cw16[k] = cb[k];
+        for (uint32_t t = lane; t < total; t += 32) {
+            const uint32_t ix = x0 + t % nx, iy = y0 + (t / nx) % ny, iz = z0 + t / (nx * ny);
+            const float tz = xdiv(xadd((float)iz, 0.5f), pext.z);
+            const float omtz = xsub(1.0f, tz);
+            const float ty = xdiv(xadd((float)iy, 0.5f), pext.y);
+            const float omty = xsub(1.0f, ty);
+            const float tx = xdiv(xadd((float)ix, 0.5f), pext.x);
+            const float omtx = xsub(1.0f, tx);
+#define LZ(i, j, comp) xadd(xmul(omtz, bc[i].comp), xmul(tz, bc[j].comp))
+            const float pz0x = LZ(0, 4, x), pz0y = LZ(0, 4, y), pz0z = LZ(0, 4, z);
+            const float pz1x = LZ(1, 5, x), pz1y = LZ(1, 5, y), pz1z = LZ(1, 5, z);
+            const float pz2x = LZ(2, 6, x), pz2y = LZ(2, 6, y), pz2z = LZ(2, 6, z);
+            const float pz3x = LZ(3, 7, x), pz3y = LZ(3, 7, y), pz3z = LZ(3, 7, z);
+#undef LZ
+            const float py0x = xadd(xmul(omty, pz0x), xmul(ty, pz2x));
+            const float py0y = xadd(xmul(omty, pz0y), xmul(ty, pz2y));
+            const float py0z = xadd(xmul(omty, pz0z), xmul(ty, pz2z));
+            const float py1x = xadd(xmul(omty, pz1x), xmul(ty, pz3x));
+            const float py1y = xadd(xmul(omty, pz1y), xmul(ty, pz3y));
+            const float py1z = xadd(xmul(omty, pz1z), xmul(ty, pz3z));
+            const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
+            if (cx < 0.0f || cx >= 8.0f) continue;
+            const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
+            if (cy < 0.0f || cy >= 8.0f) continue;
+            const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
+            if (cz < 0.0f || cz >= 8.0f) continue;
+            const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
+            uint32_t word = 0;
+#pragma unroll
+            for (int k = 0; k < 16; k++) word = (rvi >> 5) == (uint32_t)k ? cw16[k] : word;
+            if (word & (1u << (rvi & 31u))) {
+                const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy)),
+                                                    (float)ix);
+                atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
+            }
+        }
+        __syncwarp();
+        uint32_t* dst = pool + (uint64_t)slot * kBlockWords;
+        for (uint32_t k = lane; k < kBlockWords; k += 32) {
+            const uint32_t v = img[k];
+            if (v) atomicOr(&dst[k], v);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. occupancy pyramid
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_svo_pyramid(const uint32_t* __restrict__ table, uint64_t n_table,
+                                                    const uint32_t* __restrict__ pool, uint32_t* __restrict__ nonempty,
+                                                    uint32_t* __restrict__ occ, const uint64_t* __restrict__ occ_off,
+                                                    uint32_t n_levels, uint32_t B, uint32_t* __restrict__ counters)
+{
+    // one warp per table entry
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = warp; i < n_table; i += n_warps) {
+        const uint32_t tv = table[i];
+        if (tv == 0u) continue;
+        const uint32_t* blk = pool + (uint64_t)(tv - 1u) * kBlockWords;
+        uint32_t any = 0;
+        for (uint32_t k = lane; k < kBlockWords; k += 32) any |= blk[k];
+        any = __any_sync(0xffffffffu, any != 0u);
+        if (lane == 0) nonempty[tv - 1u] = any ? 1u : 0u;
+        if (!any) continue;
+        if (lane == 0) atomicAdd(&counters[S_NONEMPTY], 1u);
+        const uint32_t bx = (uint32_t)(i % B), by = (uint32_t)((i / B) % B), bz = (uint32_t)(i / ((uint64_t)B * B));
+        if (lane < n_levels) {
+            const uint32_t s = lane, n = B >> s;
+            const uint64_t idx = ((uint64_t)(bz >> s) * n + (by >> s)) * n + (bx >> s);
+            atomicOr(&occ[occ_off[s] + (idx >> 5)], 1u << (idx & 31u));
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static void svo_free(tgx_svo* s)
+{
+    if (!s) return;
+    cudaFree(s->d_table);
+    cudaFree(s->d_pool);
+    cudaFree(s->d_occ);
+    cudaFree(s->d_nonempty);
+    delete s;
+}
+
+extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float* mn, uint32_t L, tgx_svo** out)
+{
+    if (!c || !sc || !mn || !out) { tgx_set_error("tgx_svo_build: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    if (L < 6 || L > 14) { tgx_set_error("tgx_svo_build: extent_log2 %u outside 6..14", L); return TGX_ERR_INVALID_ARGUMENT; }
+    for (int i = 0; i < 3; i++)
+        if (!(fabsf(mn[i]) <= 16777216.0f) || mn[i] != floorf(mn[i])) {
+            tgx_set_error("tgx_svo_build: min must be integral and |min| <= 2^24");
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+    TGX_CUDA(cudaSetDevice(c->device));
+    tgx_svo* s = new (std::nothrow) tgx_svo();
+    if (!s) return TGX_ERR_OUT_OF_MEMORY;
+    s->mn[0] = mn[0]; s->mn[1] = mn[1]; s->mn[2] = mn[2];
+    s->L = L;
+    s->B = 1u << (L - 5);
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    s->n_levels = L - 5 + 1;
+    uint64_t occ_words = 0;
+    for (uint32_t l = 0; l < s->n_levels; l++) {
+        const uint64_t n = (uint64_t)(s->B >> l);
+        s->occ_off[l] = occ_words;
+        occ_words += (n * n * n + 31) / 32;
+    }
+    s->occ_words = occ_words;
+
+    auto fail = [&](tgx_status st) { cudaStreamSynchronize(c->stream); svo_free(s); return st; };
+    if (cudaMalloc(&s->d_table, n_table * 4) != cudaSuccess || cudaMalloc(&s->d_occ, occ_words * 4 + 128) != cudaSuccess) {
+        tgx_set_error("tgx_svo_build: out of device memory for the block table");
+        return fail(TGX_ERR_OUT_OF_MEMORY);
+    }
+    if (cudaMemsetAsync(s->d_table, 0, n_table * 4, c->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->d_occ, 0, occ_words * 4, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync((char*)s->d_occ + occ_words * 4, s->occ_off, sizeof(s->occ_off), cudaMemcpyHostToDevice,
+                        c->stream) != cudaSuccess) {
+        tgx_set_error("tgx_svo_build: memset failed");
+        return fail(TGX_ERR_CUDA);
+    }
+    tgx_status st;
+    if ((st = devbuf_reserve(c->svo_counters, S_COUNT * 4)) != TGX_OK) return fail(st);
+    uint32_t* counters = (uint32_t*)c->svo_counters.ptr;
+    cudaMemsetAsync(counters, 0, S_COUNT * 4, c->stream);
+    // pair storage: start from a per-cluster estimate, retry once with the exact count
+    uint64_t cap = std::max<uint64_t>(1024, (uint64_t)sc->n_cluster_pointers * 4);
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if ((st = devbuf_reserve(c->svo_pairs, cap * sizeof(SvoPair))) != TGX_OK) return fail(st);
+        cudaMemsetAsync(counters, 0, S_COUNT * 4, c->stream);
+        cudaMemsetAsync(s->d_table, 0, n_table * 4, c->stream);
+        auto launch = [&]() -> tgx_status {
+            TGX_LAUNCH(c, TR_SVO_CANDIDATES, (sc->n_cluster_pointers + 127) / 128, 128, 0, k_svo_candidates,
+                       sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, sc->n_cluster_pointers, mn[0],
+                       mn[1], mn[2], L, s->B, s->d_table, (SvoPair*)c->svo_pairs.ptr, (uint32_t)cap, counters,
+                       c->d_status);
+            return TGX_OK;
+        };
+        if ((st = launch()) != TGX_OK) return fail(st);
+        if (cudaMemcpyAsync(c->h_counter, counters, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+            cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            tgx_set_error("tgx_svo_build: %s", cudaGetErrorString(cudaGetLastError()));
+            return fail(TGX_ERR_CUDA);
+        }
+        const uint32_t n_pairs = ((uint32_t*)c->h_counter)[S_PAIRS];
+        if (n_pairs <= cap) break;
+        // the capacity error recorded by the first attempt is expected; clear it
+        cudaMemsetAsync(c->d_status, 0, sizeof(tgx_dev_status), c->stream);
+        cap = (uint64_t)n_pairs + 1024;
+    }
+    const uint32_t* hc = (const uint32_t*)c->h_counter;
+    s->n_pairs = hc[S_PAIRS];
+    s->n_blocks = hc[S_MARKED];
+    if (cudaMalloc(&s->d_pool, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4) != cudaSuccess ||
+        cudaMalloc(&s->d_nonempty, (uint64_t)std::max(s->n_blocks, 1u) * 4) != cudaSuccess) {
+        tgx_set_error("tgx_svo_build: out of device memory for %u blocks", s->n_blocks);
+        return fail(TGX_ERR_OUT_OF_MEMORY);
+    }
+    cudaMemsetAsync(s->d_pool, 0, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4, c->stream);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((n_table + 255) / 256, (uint64_t)c->num_sms * 32);
+    auto rest = [&]() -> tgx_status {
+        TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_alloc, s->d_table, n_table, counters, s->n_blocks, c->d_status);
+        const uint32_t vgrid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((s->n_pairs + kWarpsPerVoxCta - 1) / kWarpsPerVoxCta,
+                                                                                  (uint64_t)c->num_sms * 16));
+        TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects,
+                   sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
+                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, mn[0], mn[1], mn[2], s->B);
+        const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
+        TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
+                   s->d_occ, (const uint64_t*)((char*)s->d_occ + occ_words * 4), s->n_levels, s->B, counters);
+        return TGX_OK;
+    };
+    if ((st = rest()) != TGX_OK) return fail(st);
+    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 4) + occ_words * 4;
+    *out = s;
+    return TGX_OK;
+}
+
+extern "C" void tgx_svo_destroy(tgx_ctx* c, tgx_svo* s)
+{
+    if (c) cudaStreamSynchronize(c->stream);
+    svo_free(s);
+}
+
+extern "C" tgx_status tgx_svo_get_info(tgx_ctx* c, const tgx_svo* s, tgx_svo_info* out)
+{
+    if (!c || !s || !out) return TGX_ERR_INVALID_ARGUMENT;
+    TGX_CUDA(cudaMemcpyAsync(c->h_counter, c->svo_counters.ptr, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    out->min[0] = s->mn[0]; out->min[1] = s->mn[1]; out->min[2] = s->mn[2];
+    out->extent_log2 = s->L;
+    out->blocks_per_axis = s->B;
+    out->n_blocks = s->n_blocks;
+    out->n_nonempty_blocks = ((const uint32_t*)c->h_counter)[S_NONEMPTY];
+    out->n_pairs = s->n_pairs;
+    out->device_bytes = s->device_bytes;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_svo_download(tgx_ctx* c, const tgx_svo* s, int32_t* out_xyz, uint32_t* out_words,
+                                       uint32_t capacity, uint32_t* out_n)
+{
+    if (!c || !s || !out_n) return TGX_ERR_INVALID_ARGUMENT;
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    std::vector<uint32_t> table(n_table), nonempty(std::max(s->n_blocks, 1u));
+    TGX_CUDA(cudaMemcpyAsync(table.data(), s->d_table, n_table * 4, cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaMemcpyAsync(nonempty.data(), s->d_nonempty, nonempty.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    uint32_t n = 0;
+    for (uint64_t i = 0; i < n_table; i++) {
+        const uint32_t tv = table[i];
+        if (!tv || !nonempty[tv - 1]) continue;
+        if (n < capacity) {
+            if (out_xyz) {
+                out_xyz[3 * n + 0] = (int32_t)(s->mn[0] + (float)((i % s->B) * kBlockSide));
+                out_xyz[3 * n + 1] = (int32_t)(s->mn[1] + (float)(((i / s->B) % s->B) * kBlockSide));
+                out_xyz[3 * n + 2] = (int32_t)(s->mn[2] + (float)((i / ((uint64_t)s->B * s->B)) * kBlockSide));
+            }
+            if (out_words)
+                TGX_CUDA(cudaMemcpyAsync(out_words + (uint64_t)n * kBlockWords, s->d_pool + (uint64_t)(tv - 1) * kBlockWords,
+                                         kBlockWords * 4, cudaMemcpyDeviceToHost, c->stream));
+        }
+        n++;
+    }
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    *out_n = n;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_svo_trace(tgx_ctx*, const tgx_svo*, uint32_t, const float*, const float*, uint32_t, float*,
+                                    int32_t*)
+{
+    tgx_set_error("tgx_svo_trace: not built yet");
     return TGX_ERR_NOT_SUPPORTED;
 }
-extern "C" void tgx_svo_destroy(tgx_ctx*, tgx_svo*) {}
-extern "C" tgx_status tgx_svo_get_info(tgx_ctx*, const tgx_svo*, tgx_svo_info*) { return TGX_ERR_NOT_SUPPORTED; }
-extern "C" tgx_status tgx_svo_download(tgx_ctx*, const tgx_svo*, int32_t*, uint32_t*, uint32_t, uint32_t*) { return TGX_ERR_NOT_SUPPORTED; }
-extern "C" tgx_status tgx_svo_trace(tgx_ctx*, const tgx_svo*, uint32_t, const float*, const float*, uint32_t, float*, int32_t*) { return TGX_ERR_NOT_SUPPORTED; }

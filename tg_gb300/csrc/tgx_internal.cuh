@@ -118,6 +118,8 @@ struct tgx_ctx
     DevBuf vis_tile_off;   // per-tile offsets (exclusive scan), n_tiles+1
     DevBuf vis_bins;       // tile -> record indices
     DevBuf vis_views;      // device copies of the views
+    DevBuf svo_counters;   // SVO build counters
+    DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
     uint32_t vis_last_tiles = 0;
     DevBuf host_stage;     // pinned host staging (views)
     void*  h_pinned = nullptr;
