@@ -165,6 +165,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -190,7 +191,13 @@ def main() -> None:
 
     scene = make_scene()
     view = make_view()
-    ctx = tg.Context(local)
+    if args.tile == "auto":
+        from tg_gb300.autotune import tune_visibility
+        tile, tuning = tune_visibility(scene, view, device=local, use_cache=False)
+    else:
+        tile = tuple(int(x) for x in args.tile.lower().split("x"))
+        tuning = {}
+    ctx = tg.Context(local, tile=tile)
     sc = ctx.upload(scene)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = torch.empty(W * H, dtype=torch.int64, device="cuda")
@@ -290,7 +297,9 @@ def main() -> None:
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": {**CONFIG, "parallelism": "replicas" if world > 1 else "single-gpu"},
+        "config": {**CONFIG, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "tile": f"{tile[0]}x{tile[1]}",
+                   "autotune_ms": {f"{t[0]}x{t[1]}": round(v, 4) for t, v in tuning.items()}},
         "e2e": {"value": rays * world / (e2e * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
                 "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e,
                 "path": "tgx_vis_render_host (views from host, visibility buffer back to pinned host memory)"},

@@ -127,8 +127,12 @@ typedef struct tgx_config
     void*    stream;           /* cudaStream_t to run on, or NULL for a context-owned stream */
     uint32_t tile_w;           /* visibility tile width in pixels (0 = default 16) */
     uint32_t tile_h;           /* visibility tile height in pixels (0 = default 16) */
-    uint32_t flags;            /* reserved, must be 0 */
+    uint32_t flags;            /* TGX_FLAG_* bits, 0 for defaults */
 } tgx_config;
+
+/* Keeps the visibility bin storage at its minimum (64 entries) so frames
+ * overflow it and take the exact record-scan path; for testing that path. */
+#define TGX_FLAG_MIN_BIN_CAPACITY       1u
 
 typedef struct tgx_device_error
 {

@@ -123,4 +123,23 @@ static inline int or_ray_aabb(const float o[3], const float d[3], const float mn
     return *exit_ > 0.0f && *enter <= *exit_;
 }
 
+/*
+ * The cluster-box test of visibility.frag:78 as the raster pipeline applies
+ * it: the shader only runs for pixels the box's rasterised faces cover
+ * (tgvk_raytracer.c:1293, cluster_functions.inc:1-38), i.e. pixels whose ray
+ * crosses the box.  collide.inc:5-10 substitutes -/+F32_MAX for an axis with a
+ * zero direction component without checking that the origin lies inside that
+ * slab, so on its own it would accept rays parallel to a slab they never
+ * cross -- fragments the rasteriser never generates.  Those pairs are misses
+ * here.  Everything else is or_ray_aabb, operation for operation.
+ */
+static inline int or_ray_cluster(const float o[3], const float d[3], const float mn[3], const float mx[3],
+                                 float* enter, float* exit_)
+{
+    const int hit = or_ray_aabb(o, d, mn, mx, enter, exit_);
+    for (int i = 0; i < 3; i++)
+        if (d[i] == 0.0f && (o[i] < mn[i] || o[i] > mx[i])) return 0;
+    return hit;
+}
+
 #endif

@@ -1,0 +1,527 @@
+/*
+ * oracle_gi.c -- CPU oracle of SVO ray traversal and of plain GI.
+ *
+ * TEST INFRASTRUCTURE.  Neither exists in the reference as a runnable pass:
+ * its GPU traversal (svo_functions.inc:1-329) only feeds a debug view and
+ * shading.frag:285-316 does direct light only; secondary rays exist only in a
+ * disabled CPU probe (tgvk_raytracer.c:1390-1434).  This file therefore
+ * DEFINES the semantics the CUDA path must reproduce, using only exactly
+ * rounded binary32 operations (+ - * / sqrt floor) so that both sides give
+ * the same bits:
+ *
+ *  - traversal: a hierarchical DDA over the one-bit voxel set (the same set
+ *    tg_svo_create builds): occupancy levels of 2^k voxels for k = L-1 .. 5,
+ *    then single voxels; descend into occupied cells, step out of empty ones
+ *    through the nearest face, ascend when the step leaves the parent; one
+ *    loop iteration is one step.  The hit is the first set voxel along the
+ *    ray, its distance is the entry distance, its normal the face crossed.
+ *  - primary hits come from the visibility buffer, decoded as shading.frag
+ *    does (:116-135), with the hit point and face normal of shading.frag:
+ *    177-228 in cluster space and rotated to world space.
+ *  - bounce lighting: Lambertian albedo from the material LUT, a directional
+ *    sun with an SVO shadow ray, a constant sky, cosine-weighted secondary
+ *    directions (Malley's method, rejection-sampled unit disk) in the
+ *    orthonormal basis of Duff et al. 2017, random numbers from
+ *    Philox4x32-10 (Salmon et al. 2011) keyed by the seed and counted by
+ *    (pixel, sample, bounce|frame, draw).
+ */
+#include "oracle_common.h"
+
+#include <stdlib.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* SVO in the oracle: dense block table over the non-empty blocks.     */
+/* ------------------------------------------------------------------ */
+
+typedef struct
+{
+    float     mn[3];
+    uint32_t  L, B, NL;          /* side 2^L, blocks per axis, traversal levels */
+    uint32_t* table;             /* B^3, 0 = empty, else block + 1 */
+    uint32_t* words;             /* n * 1024 */
+    uint16_t* mats;              /* n * 32768 or NULL */
+    uint32_t* occ;               /* pyramid bits, level 0 = blocks */
+    uint64_t  occ_off[16];
+} osvo;
+
+void* oracle_svo_open(const int32_t* block_xyz, const uint32_t* words, const uint16_t* mats, uint32_t n,
+                      const float mn[3], uint32_t L)
+{
+    osvo* s = (osvo*)calloc(1, sizeof(osvo));
+    memcpy(s->mn, mn, sizeof(s->mn));
+    s->L = L;
+    s->B = 1u << (L - 5);
+    s->NL = 1 + (L - 5);
+    const uint64_t nt = (uint64_t)s->B * s->B * s->B;
+    s->table = (uint32_t*)calloc(nt, 4);
+    s->words = (uint32_t*)malloc((size_t)(n ? n : 1) * 4096);
+    memcpy(s->words, words, (size_t)n * 4096);
+    if (mats)
+    {
+        s->mats = (uint16_t*)malloc((size_t)(n ? n : 1) * 65536);
+        memcpy(s->mats, mats, (size_t)n * 65536);
+    }
+    uint64_t off = 0;
+    for (uint32_t k = 0; k + 1 <= s->NL - 1 + 1 && k < 16; k++)
+    {
+        const uint64_t m = (uint64_t)(s->B >> k);
+        if (m == 0) break;
+        s->occ_off[k] = off;
+        off += (m * m * m + 31) / 32;
+    }
+    s->occ = (uint32_t*)calloc(off + 1, 4);
+    for (uint32_t i = 0; i < n; i++)
+    {
+        const uint32_t bx = (uint32_t)((float)block_xyz[3 * i] - mn[0]) / 32u;
+        const uint32_t by = (uint32_t)((float)block_xyz[3 * i + 1] - mn[1]) / 32u;
+        const uint32_t bz = (uint32_t)((float)block_xyz[3 * i + 2] - mn[2]) / 32u;
+        s->table[((uint64_t)bz * s->B + by) * s->B + bx] = i + 1;
+        for (uint32_t k = 0; (s->B >> k) >= 1 && k < 16; k++)
+        {
+            const uint64_t m = s->B >> k;
+            const uint64_t idx = ((uint64_t)(bz >> k) * m + (by >> k)) * m + (bx >> k);
+            s->occ[s->occ_off[k] + idx / 32] |= 1u << (idx % 32);
+            if (m == 1) break;
+        }
+    }
+    return s;
+}
+
+void oracle_svo_close(void* h)
+{
+    osvo* s = (osvo*)h;
+    if (!s) return;
+    free(s->table); free(s->words); free(s->mats); free(s->occ); free(s);
+}
+
+static inline float level_size(uint32_t li) { return li == 0 ? 1.0f : (float)(1u << (li + 4)); }
+static inline int32_t level_cells(const osvo* s, uint32_t li) { return li == 0 ? (int32_t)(s->B << 5) : (int32_t)(s->B >> (li - 1)); }
+
+static int occupied(const osvo* s, uint32_t li, const int32_t c[3])
+{
+    if (li == 0)
+    {
+        const uint32_t bx = (uint32_t)c[0] >> 5, by = (uint32_t)c[1] >> 5, bz = (uint32_t)c[2] >> 5;
+        const uint32_t tv = s->table[((uint64_t)bz * s->B + by) * s->B + bx];
+        if (!tv) return 0;
+        const uint32_t v = ((uint32_t)c[2] & 31u) * 1024u + ((uint32_t)c[1] & 31u) * 32u + ((uint32_t)c[0] & 31u);
+        return (s->words[(uint64_t)(tv - 1) * 1024u + v / 32u] >> (v % 32u)) & 1u;
+    }
+    const uint32_t k = li - 1;
+    const uint64_t m = s->B >> k;
+    const uint64_t idx = ((uint64_t)c[2] * m + (uint64_t)c[1]) * m + (uint64_t)c[0];
+    return (s->occ[s->occ_off[k] + idx / 32] >> (idx % 32)) & 1u;
+}
+
+static uint16_t material_at(const osvo* s, const int32_t c[3])
+{
+    if (!s->mats) return 0;
+    const uint32_t bx = (uint32_t)c[0] >> 5, by = (uint32_t)c[1] >> 5, bz = (uint32_t)c[2] >> 5;
+    const uint32_t tv = s->table[((uint64_t)bz * s->B + by) * s->B + bx];
+    if (!tv) return 0;
+    const uint32_t v = ((uint32_t)c[2] & 31u) * 1024u + ((uint32_t)c[1] & 31u) * 32u + ((uint32_t)c[0] & 31u);
+    return s->mats[(uint64_t)(tv - 1) * 32768u + v];
+}
+
+/* cell index of coordinate p at a level: floor(p / size), a point exactly on
+ * a cell face belongs to the cell the ray moves into, clamped to [lo, hi] */
+static inline int32_t cell_at(float p, float inv_size, int32_t step, int32_t lo, int32_t hi)
+{
+    const float x = p * inv_size;
+    float f = floorf(x);
+    if (step < 0 && x == f) f = f - 1.0f;
+    int32_t c = (int32_t)f;
+    if (f < (float)lo) c = lo;
+    if (f > (float)hi) c = hi;
+    return c;
+}
+
+/*
+ * Traverses one ray (world origin o, direction d).  Returns 1 on hit (t =
+ * entry distance in units of |d|, c = grid voxel, *axis = face axis crossed
+ * or -1 when the origin is inside the voxel), 0 on a miss, -1 when the step
+ * budget ran out (treated as a miss by callers).  *steps = steps used.
+ */
+int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max_steps, float* out_t,
+                 int32_t out_c[3], int32_t* out_axis, uint32_t* out_steps)
+{
+    const osvo* s = (const osvo*)h;
+    const float E = (float)(1u << s->L);
+    float og[3], inv[3];
+    int32_t st[3];
+    for (int a = 0; a < 3; a++)
+    {
+        og[a] = o[a] - s->mn[a];
+        st[a] = d[a] > 0.0f ? 1 : d[a] < 0.0f ? -1 : 0;
+        inv[a] = st[a] ? 1.0f / d[a] : 0.0f;
+    }
+    *out_steps = 0;
+    if (!st[0] && !st[1] && !st[2]) return 0;
+    /* slab test against the SVO cube [0, E]^3 */
+    float t0 = OR_F32_MIN, t1 = OR_F32_MAX;
+    int32_t entry_axis = -1;
+    for (int a = 0; a < 3; a++)
+    {
+        if (!st[a])
+        {
+            if (og[a] < 0.0f || og[a] >= E) return 0;
+            continue;
+        }
+        const float ta = (0.0f - og[a]) * inv[a];
+        const float tb = (E - og[a]) * inv[a];
+        const float tn = ta < tb ? ta : tb;
+        const float tf = ta < tb ? tb : ta;
+        if (tn > t0) { t0 = tn; entry_axis = a; }
+        if (tf < t1) t1 = tf;
+    }
+    float t = t0 > 0.0f ? t0 : 0.0f;
+    if (!(t < t1)) return 0;
+    int32_t last_axis = t0 > 0.0f ? entry_axis : -1;
+
+    uint32_t li = s->NL - 1;
+    int32_t c[3];
+    {
+        const float isz = 1.0f / level_size(li);
+        const int32_t hi = level_cells(s, li) - 1;
+        for (int a = 0; a < 3; a++) c[a] = cell_at(og[a] + t * d[a], isz, st[a], 0, hi);
+    }
+    uint32_t steps = 0;
+    while (steps < max_steps)
+    {
+        steps++;
+        if (occupied(s, li, c))
+        {
+            if (li == 0)
+            {
+                *out_t = t;
+                out_c[0] = c[0]; out_c[1] = c[1]; out_c[2] = c[2];
+                *out_axis = last_axis;
+                *out_steps = steps;
+                return 1;
+            }
+            const uint32_t shift = li == 1 ? 5u : 1u;
+            li--;
+            const float isz = 1.0f / level_size(li);
+            for (int a = 0; a < 3; a++)
+            {
+                const int32_t lo = c[a] << shift, hi = lo + (1 << shift) - 1;
+                c[a] = cell_at(og[a] + t * d[a], isz, st[a], lo, hi);
+            }
+            continue;
+        }
+        const float size = level_size(li);
+        float tn[3];
+        for (int a = 0; a < 3; a++)
+            tn[a] = st[a] > 0 ? ((float)(c[a] + 1) * size - og[a]) * inv[a]
+                  : st[a] < 0 ? ((float)c[a] * size - og[a]) * inv[a] : OR_F32_MAX;
+        int32_t am = 0;
+        if (tn[1] < tn[am]) am = 1;
+        if (tn[2] < tn[am]) am = 2;
+        if (tn[am] > t) t = tn[am];
+        last_axis = am;
+        int32_t prev = c[am];
+        c[am] += st[am];
+        if (c[am] < 0 || c[am] >= level_cells(s, li)) { *out_steps = steps; return 0; }
+        int32_t cur = c[am];
+        while (li < s->NL - 1)
+        {
+            const uint32_t shift = li == 0 ? 5u : 1u;
+            if ((prev >> shift) == (cur >> shift)) break;
+            prev >>= shift; cur >>= shift;
+            c[0] >>= shift; c[1] >>= shift; c[2] >>= shift;
+            li++;
+        }
+    }
+    *out_steps = steps;
+    return -1;
+}
+
+/* batch form for tests: out_t = FLT max on miss */
+void oracle_trace_batch(const void* h, uint32_t n, const float* o, const float* d, uint32_t max_steps, float* out_t,
+                        int32_t* out_voxel, int32_t* out_axis, uint32_t* out_steps)
+{
+    const osvo* s = (const osvo*)h;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; i++)
+    {
+        float t;
+        int32_t c[3], ax;
+        uint32_t stp;
+        const int r = oracle_trace(h, &o[3 * i], &d[3 * i], max_steps, &t, c, &ax, &stp);
+        out_steps[i] = stp;
+        if (r == 1)
+        {
+            out_t[i] = t;
+            for (int a = 0; a < 3; a++) out_voxel[3 * i + a] = c[a] + (int32_t)s->mn[a];
+            out_axis[i] = ax;
+        }
+        else
+        {
+            out_t[i] = OR_F32_MAX;
+            out_voxel[3 * i] = out_voxel[3 * i + 1] = out_voxel[3 * i + 2] = 0;
+            out_axis[i] = r == -1 ? -2 : -1;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10                                                       */
+/* ------------------------------------------------------------------ */
+
+static inline void philox(uint32_t ctr[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; r++)
+    {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * ctr[0];
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * ctr[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ ctr[1] ^ k0;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ ctr[3] ^ k1;
+        ctr[1] = (uint32_t)p1;
+        ctr[3] = (uint32_t)p0;
+        ctr[0] = n0;
+        ctr[2] = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+void oracle_philox(const uint32_t in[4], uint32_t k0, uint32_t k1, uint32_t out[4])
+{
+    uint32_t c[4] = { in[0], in[1], in[2], in[3] };
+    philox(c, k0, k1);
+    memcpy(out, c, sizeof(c));
+}
+
+static inline float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+/* ------------------------------------------------------------------ */
+/* GI                                                                  */
+/* ------------------------------------------------------------------ */
+
+typedef struct
+{
+    uint32_t spp, bounces, max_steps, frame;
+    uint64_t seed;
+    float    sun_dir[3];      /* unit vector toward the sun */
+    float    sun_radiance[3];
+    float    sky_radiance[3];
+    float    offset;          /* ray origin offset along the normal, voxels */
+} ogi_params;
+
+#define OR_INV_PI 0.318309886f
+
+/* cosine-weighted direction about unit n (Malley; Duff et al. basis) */
+static void sample_cosine(const float n[3], uint32_t pixel, uint32_t sample, uint32_t bounce, const ogi_params* p,
+                          float out[3])
+{
+    const float sign = n[2] >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sign + n[2]);
+    const float b = n[0] * n[1] * a;
+    const float t1[3] = { 1.0f + sign * n[0] * n[0] * a, sign * b, -sign * n[0] };
+    const float t2[3] = { b, sign + n[1] * n[1] * a, -n[1] };
+    for (uint32_t draw = 0; draw < 8; draw++)
+    {
+        uint32_t c[4] = { pixel, sample, bounce | (p->frame << 8), draw };
+        philox(c, (uint32_t)p->seed, (uint32_t)(p->seed >> 32));
+        for (int k = 0; k < 2; k++)
+        {
+            const float u = 2.0f * u01(c[2 * k]) - 1.0f;
+            const float v = 2.0f * u01(c[2 * k + 1]) - 1.0f;
+            const float r2 = u * u + v * v;
+            if (r2 < 1.0f)
+            {
+                const float z = sqrtf(1.0f - r2);
+                for (int i = 0; i < 3; i++) out[i] = u * t1[i] + v * t2[i] + z * n[i];
+                return;
+            }
+        }
+    }
+    out[0] = n[0]; out[1] = n[1]; out[2] = n[2];
+}
+
+static void svo_albedo(const osvo* s, const int32_t c[3], const tgx_material* luts, float out[3])
+{
+    const uint16_t code = material_at(s, c);
+    if (!code || !luts) { out[0] = out[1] = out[2] = 0.5f; return; }
+    const tgx_material* m = &luts[code - 1u];
+    out[0] = m->albedo[0]; out[1] = m->albedo[1]; out[2] = m->albedo[2];
+}
+
+/* sun light arriving at a surface point (origin already offset) with normal n and albedo a */
+static void direct_sun(const osvo* s, const float o2[3], const float n[3], const float a[3], const ogi_params* p,
+                       float out[3])
+{
+    out[0] = out[1] = out[2] = 0.0f;
+    const float ndl = n[0] * p->sun_dir[0] + n[1] * p->sun_dir[1] + n[2] * p->sun_dir[2];
+    if (!(ndl > 0.0f)) return;
+    float t; int32_t c[3], ax; uint32_t stp;
+    if (oracle_trace(s, o2, p->sun_dir, p->max_steps, &t, c, &ax, &stp) == 1) return;
+    for (int i = 0; i < 3; i++) out[i] = a[i] * OR_INV_PI * p->sun_radiance[i] * ndl;
+}
+
+/* radiance arriving along a secondary ray from o2 in direction w (after `depth` bounces so far) */
+static void incoming(const osvo* s, const float o2[3], const float w[3], uint32_t pixel, uint32_t sample,
+                     uint32_t bounce, const tgx_material* luts, const ogi_params* p, float out[3])
+{
+    float t; int32_t c[3], ax; uint32_t stp;
+    if (oracle_trace(s, o2, w, p->max_steps, &t, c, &ax, &stp) != 1)
+    {
+        out[0] = p->sky_radiance[0]; out[1] = p->sky_radiance[1]; out[2] = p->sky_radiance[2];
+        return;
+    }
+    float n2[3] = { 0.0f, 0.0f, 0.0f };
+    if (ax >= 0) n2[ax] = w[ax] > 0.0f ? -1.0f : 1.0f;
+    else
+    {
+        int m = 0;
+        if (fabsf(w[1]) > fabsf(w[m])) m = 1;
+        if (fabsf(w[2]) > fabsf(w[m])) m = 2;
+        n2[m] = w[m] > 0.0f ? -1.0f : 1.0f;
+    }
+    float a2[3];
+    svo_albedo(s, c, luts, a2);
+    float o3[3];
+    for (int i = 0; i < 3; i++) o3[i] = (o2[i] + t * w[i]) + n2[i] * p->offset;
+    direct_sun(s, o3, n2, a2, p, out);
+    if (bounce + 1 < p->bounces)
+    {
+        float w2[3], l2[3];
+        sample_cosine(n2, pixel, sample, bounce + 1, p, w2);
+        incoming(s, o3, w2, pixel, sample, bounce + 1, luts, p, l2);
+        for (int i = 0; i < 3; i++) out[i] = out[i] + a2[i] * l2[i];
+    }
+}
+
+/*
+ * One pixel of plain GI.  The primary hit comes from the visibility word (as
+ * shading.frag:116-228 decodes it); world hit point = camera + enter * the
+ * normalised pixel ray.  Writes RGB.
+ */
+void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t* cluster_pointers,
+                     const uint32_t* c2o, const uint8_t* material, const tgx_material* luts, const tgx_view* cam,
+                     const ogi_params* p, uint64_t word, uint32_t px, uint32_t py, float out[3])
+{
+    const osvo* s = (const osvo*)svo;
+    const float fx = ((float)px + 0.5f) / (float)cam->width;
+    const float fy = 1.0f - ((float)py + 0.5f) / (float)cam->height;
+    const float depth = (float)(word >> 40) / 16777215.0f;
+    if (!(depth < 1.0f))
+    {
+        out[0] = p->sky_radiance[0]; out[1] = p->sky_radiance[1]; out[2] = p->sky_radiance[2];
+        return;
+    }
+    const uint32_t ptr = (uint32_t)(word >> 9) & 2147483647u;
+    const uint32_t voxel = (uint32_t)word & 511u;
+    const uint32_t ci = cluster_pointers[ptr];
+    const tgx_object* od = &objects[c2o[ci]];
+    /* shading.frag:147-181: the same ws2ms, origin and direction as the visibility pass */
+    const uint32_t nx = od->n_cluster_pointers_per_dim[0], ny = od->n_cluster_pointers_per_dim[1];
+    const uint32_t rel = ptr - od->first_cluster_pointer;
+    const float offx = (float)((rel % nx) * 8u), offy = (float)(((rel / nx) % ny) * 8u), offz = (float)((rel / (nx * ny)) * 8u);
+    const float half = 8.0f * 0.5f;
+    float m0[16], m1[16], m2[16], m3[16], ws2ms[16];
+    or_m4_translate(-od->translation[0], -od->translation[1], -od->translation[2], m0);
+    or_m4_inverse(od->rotation, m1);
+    or_m4_translate(half * (float)od->n_cluster_pointers_per_dim[0], half * (float)od->n_cluster_pointers_per_dim[1],
+                    half * (float)od->n_cluster_pointers_per_dim[2], m2);
+    or_m4_translate(-offx, -offy, -offz, m3);
+    or_m4_mul(m3, m2, ws2ms);
+    or_m4_mul(ws2ms, m1, ws2ms);
+    or_m4_mul(ws2ms, m0, ws2ms);
+    const float ow[4] = { cam->camera[0], cam->camera[1], cam->camera[2], 1.0f };
+    float o4[4];
+    or_m4_mulv4(ws2ms, ow, o4);
+    float dws[4];
+    for (int i = 0; i < 3; i++)
+    {
+        const float a = cam->ray_bl[i] * (1.0f - fy) + cam->ray_tl[i] * fy;
+        const float b = cam->ray_br[i] * (1.0f - fy) + cam->ray_tr[i] * fy;
+        dws[i] = a * (1.0f - fx) + b * fx;
+    }
+    dws[3] = 0.0f;
+    float d4[4];
+    or_m4_mulv4(ws2ms, dws, d4);
+    const float mag = sqrtf(d4[0] * d4[0] + d4[1] * d4[1] + d4[2] * d4[2]);
+    const float dm[3] = { d4[0] / mag, d4[1] / mag, d4[2] / mag };
+    const float vmin[3] = { (float)(voxel % 8u), (float)((voxel / 8u) % 8u), (float)(voxel / 64u) };
+    const float vmax[3] = { vmin[0] + 1.0f, vmin[1] + 1.0f, vmin[2] + 1.0f };
+    float enter, exit_;
+    float nw[3] = { 0.0f, 0.0f, 0.0f };
+    const int hit = or_ray_aabb(o4, dm, vmin, vmax, &enter, &exit_);
+    if (hit)
+    {
+        /* shading.frag:195-228 */
+        float hm[3], nm[3];
+        for (int i = 0; i < 3; i++) hm[i] = enter > 0.0f ? o4[i] + enter * dm[i] : o4[i];
+        for (int i = 0; i < 3; i++) nm[i] = hm[i] - (vmin[i] + 0.5f);
+#define SGN(v) ((v) > 0.0f ? 1.0f : (v) < 0.0f ? -1.0f : 0.0f)
+        if (fabsf(nm[0]) > fabsf(nm[1]))
+        {
+            nm[1] = 0.0f;
+            if (fabsf(nm[0]) > fabsf(nm[2])) { nm[0] = SGN(nm[0]); nm[2] = 0.0f; }
+            else { nm[2] = SGN(nm[2]); nm[0] = 0.0f; }
+        }
+        else
+        {
+            nm[0] = 0.0f;
+            if (fabsf(nm[1]) > fabsf(nm[2])) { nm[1] = SGN(nm[1]); nm[2] = 0.0f; }
+            else { nm[2] = SGN(nm[2]); nm[1] = 0.0f; }
+        }
+#undef SGN
+        const float n4[4] = { nm[0], nm[1], nm[2], 0.0f };
+        float r4[4];
+        or_m4_mulv4(od->rotation, n4, r4);
+        const float rl = sqrtf(r4[0] * r4[0] + r4[1] * r4[1] + r4[2] * r4[2]);
+        if (rl > 0.0f) { nw[0] = r4[0] / rl; nw[1] = r4[1] / rl; nw[2] = r4[2] / rl; }
+    }
+    const float dl = sqrtf(dws[0] * dws[0] + dws[1] * dws[1] + dws[2] * dws[2]);
+    const float dn[3] = { dws[0] / dl, dws[1] / dl, dws[2] / dl };
+    if (nw[0] == 0.0f && nw[1] == 0.0f && nw[2] == 0.0f) { nw[0] = -dn[0]; nw[1] = -dn[1]; nw[2] = -dn[2]; }
+    const float te = hit && enter > 0.0f ? enter : 0.0f;
+    float a[3] = { 0.5f, 0.5f, 0.5f };
+    if (material && luts)
+    {
+        const tgx_material* m = &luts[od->lut_idx * 256u + material[(uint64_t)ci * 512u + voxel]];
+        a[0] = m->albedo[0]; a[1] = m->albedo[1]; a[2] = m->albedo[2];
+    }
+    float o2[3];
+    for (int i = 0; i < 3; i++) o2[i] = (cam->camera[i] + te * dn[i]) + nw[i] * p->offset;
+    float L[3];
+    direct_sun(s, o2, nw, a, p, L);
+    const uint32_t pixel = py * cam->width + px;
+    float acc[3] = { 0.0f, 0.0f, 0.0f };
+    for (uint32_t smp = 0; smp < p->spp; smp++)
+    {
+        float w[3], li[3];
+        sample_cosine(nw, pixel, smp, 0, p, w);
+        incoming(s, o2, w, pixel, smp, 0, luts, p, li);
+        for (int i = 0; i < 3; i++) acc[i] = acc[i] + li[i];
+    }
+    const float inv_spp = 1.0f / (float)(p->spp ? p->spp : 1);
+    for (int i = 0; i < 3; i++) out[i] = L[i] + a[i] * (acc[i] * inv_spp);
+}
+
+/* whole frame (rows [row0, row1)); out = W*H*3 floats */
+void oracle_gi_render(const void* svo, const tgx_object* objects, const uint32_t* cluster_pointers, const uint32_t* c2o,
+                      const uint8_t* material, const tgx_material* luts, const tgx_view* cam, const ogi_params* p,
+                      const uint64_t* visbuf, float* out, uint32_t row0, uint32_t row1, int n_threads)
+{
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    const uint32_t W = cam->width;
+    if (row1 > cam->height) row1 = cam->height;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t y = row0; y < (int64_t)row1; y++)
+        for (uint32_t x = 0; x < W; x++)
+        {
+            const uint64_t i = (uint64_t)y * W + x;
+            oracle_gi_pixel(svo, objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[i], x, (uint32_t)y,
+                            &out[3 * i]);
+        }
+}

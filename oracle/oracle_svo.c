@@ -11,6 +11,11 @@
  * uses corner 2 twice and never corner 3) are kept operation for operation.
  * The object rotation is the m4 the reference builds with tgm_m4_angle_axis
  * (:25); callers pass it precomputed in tgx_object.rotation.
+ *
+ * New with respect to the reference (which keeps no per-voxel material in its
+ * SVO): each set voxel also gets the material code (lut << 8 | byte) + 1 of
+ * the largest code among the cluster samples that set it, for the bounce
+ * lighting's albedo lookup.
  */
 #include "oracle_common.h"
 
@@ -129,10 +134,12 @@ typedef struct
     const uint32_t*   cluster_pointers;
     const uint32_t*   c2o;
     const uint32_t*   bits;
+    const uint8_t*    material;   /* 512 per cluster, or NULL */
     /* output blocks */
     uint32_t  n, cap;
     uint64_t* keys;     /* block index */
     uint32_t* words;    /* 1024 per block */
+    uint16_t* mats;     /* 32768 per block: (lut << 8 | byte) + 1 of the max contributor, 0 = none */
     float     mn[3];
     uint32_t  bpa;      /* blocks per axis */
     uint64_t  samples;  /* voxel-centre samples evaluated */
@@ -142,7 +149,9 @@ typedef struct
 static void leaf(svo_state* st, ov3 pmin, ov3 pmax, uint32_t n, const uint32_t* cps)
 {
     uint32_t words[BLOCK * BLOCK * BLOCK / 32];
+    static _Thread_local uint16_t mats[BLOCK * BLOCK * BLOCK];
     memset(words, 0, sizeof(words));
+    if (st->material) memset(mats, 0, sizeof(mats));
     int any = 0;
     const ov3 pext = v3_sub(pmax, pmin);
     const float ws[8][3] = {
@@ -209,6 +218,11 @@ static void leaf(svo_state* st, ov3 pmin, ov3 pmax, uint32_t n, const uint32_t* 
                         const uint32_t bvi = (uint32_t)(pext.x * pext.y * (float)bz + pext.x * (float)by + (float)bx);
                         words[bvi / 32u] |= 1u << (bvi % 32u);
                         any = 1;
+                        if (st->material)
+                        {
+                            const uint16_t code = (uint16_t)(((od->lut_idx << 8) | st->material[(uint64_t)cidx * 512u + rvi]) + 1u);
+                            if (code > mats[bvi]) mats[bvi] = code;
+                        }
                     }
                 }
             }
@@ -220,12 +234,14 @@ static void leaf(svo_state* st, ov3 pmin, ov3 pmax, uint32_t n, const uint32_t* 
         st->cap = st->cap ? 2 * st->cap : 64;
         st->keys = realloc(st->keys, (size_t)st->cap * sizeof(uint64_t));
         st->words = realloc(st->words, (size_t)st->cap * 4096);
+        if (st->material) st->mats = realloc(st->mats, (size_t)st->cap * 65536);
     }
     const uint64_t bx = (uint64_t)((pmin.x - st->mn[0]) / (float)BLOCK);
     const uint64_t by = (uint64_t)((pmin.y - st->mn[1]) / (float)BLOCK);
     const uint64_t bz = (uint64_t)((pmin.z - st->mn[2]) / (float)BLOCK);
     st->keys[st->n] = (bz * st->bpa + by) * st->bpa + bx;
     memcpy(&st->words[(size_t)st->n * 1024], words, 4096);
+    if (st->material) memcpy(&st->mats[(size_t)st->n * 32768], mats, 65536);
     st->n++;
 }
 
@@ -287,14 +303,16 @@ static int cmp_idx(const void* a, const void* b)
  * world min corner, out_words = 1024 words each.  Returns the number of
  * non-empty blocks; *out_samples = voxel-centre samples evaluated.
  */
-int64_t oracle_svo_build(const tgx_object* objects, uint32_t n_objects, uint32_t n_cluster_pointers,
-                         const uint32_t* cluster_pointers, const uint32_t* c2o, const uint32_t* bits,
-                         const float mn[3], uint32_t extent_log2,
-                         int32_t* out_block_xyz, uint32_t* out_words, uint32_t capacity, uint64_t* out_samples)
+int64_t oracle_svo_build_mat(const tgx_object* objects, uint32_t n_objects, uint32_t n_cluster_pointers,
+                             const uint32_t* cluster_pointers, const uint32_t* c2o, const uint32_t* bits,
+                             const uint8_t* material, const float mn[3], uint32_t extent_log2,
+                             int32_t* out_block_xyz, uint32_t* out_words, uint16_t* out_mats, uint32_t capacity,
+                             uint64_t* out_samples)
 {
     svo_state st;
     memset(&st, 0, sizeof(st));
     st.objects = objects; st.cluster_pointers = cluster_pointers; st.c2o = c2o; st.bits = bits;
+    st.material = out_mats ? material : NULL;
     memcpy(st.mn, mn, sizeof(st.mn));
     st.bpa = 1u << (extent_log2 - 5);
 
@@ -335,12 +353,23 @@ int64_t oracle_svo_build(const tgx_object* objects, uint32_t n_objects, uint32_t
         out_block_xyz[3 * i + 1] = (int32_t)(mn[1] + (float)(by * BLOCK));
         out_block_xyz[3 * i + 2] = (int32_t)(mn[2] + (float)(bz * BLOCK));
         memcpy(&out_words[(size_t)i * 1024], &st.words[(size_t)order[i] * 1024], 4096);
+        if (st.material) memcpy(&out_mats[(size_t)i * 32768], &st.mats[(size_t)order[i] * 32768], 65536);
     }
     free(order);
     free(st.keys);
     free(st.words);
+    free(st.mats);
     if (out_samples) *out_samples = st.samples;
     return (int64_t)st.n;
+}
+
+int64_t oracle_svo_build(const tgx_object* objects, uint32_t n_objects, uint32_t n_cluster_pointers,
+                         const uint32_t* cluster_pointers, const uint32_t* c2o, const uint32_t* bits,
+                         const float mn[3], uint32_t extent_log2,
+                         int32_t* out_block_xyz, uint32_t* out_words, uint32_t capacity, uint64_t* out_samples)
+{
+    return oracle_svo_build_mat(objects, n_objects, n_cluster_pointers, cluster_pointers, c2o, bits, NULL, mn,
+                                extent_log2, out_block_xyz, out_words, NULL, capacity, out_samples);
 }
 
 int oracle_aabb_obb_flat(const float mn[3], const float mx[3], const float corners[24])

@@ -7,7 +7,9 @@
  * FMA contraction.  The rasteriser's job (which fragments run) is replaced by
  * "every pixel against every cluster" (mode 0) or by a conservative
  * per-cluster screen rectangle computed in double precision (mode 1); the
- * shader's own ray/box test (visibility.frag:78) is the only arbiter in both.
+ * shader's own ray/box test (visibility.frag:78) is the only arbiter in both,
+ * applied as the raster pipeline applies it (or_ray_cluster: a ray parallel
+ * to a slab it does not cross produces no fragment).
  *
  * GLSL leaves the rounding of inverse(), normalize(), mix() and matrix
  * products to the driver, so the oracle pins them to tg's C math, which the
@@ -101,7 +103,7 @@ int oracle_vis_pair(const tgx_object* objects, const uint32_t* cluster_pointers,
     float depth = OR_F32_MAX;
     uint32_t voxel_idx = 0;
     float enter, exit_;
-    if (or_ray_aabb(o, d, cmin, cmax, &enter, &exit_))
+    if (or_ray_cluster(o, d, cmin, cmax, &enter, &exit_))
     {
         /* :83-84 */
         float hit[3], xyz[3];
@@ -339,7 +341,7 @@ int oracle_cluster_dda(const float o[3], const float d[3], const uint32_t* words
     const float cmin[3] = { 0.0f, 0.0f, 0.0f }, cmax[3] = { 8.0f, 8.0f, 8.0f };
     float enter, exit_;
     out_xyz[0] = out_xyz[1] = out_xyz[2] = -1;
-    if (!or_ray_aabb(o, d, cmin, cmax, &enter, &exit_)) return 0;
+    if (!or_ray_cluster(o, d, cmin, cmax, &enter, &exit_)) return 0;
     float hit[3], xyz[3];
     for (int i = 0; i < 3; i++)
     {

@@ -274,7 +274,8 @@ void tgref_svo_stats(uint32_t out[3])
 }
 
 /*
- * Traverses the last-built SVO for n rays.  out_hit[i] = 1 on hit,
+ * Traverses the last-built SVO for n rays.  out_hit[i] = 1 on hit, -1 when
+ * one of the reference's assertions fails for the ray,
  * out_distance = the reference distance, out_world_voxel = world integer
  * coordinate of the hit voxel (from the leaf block origin + voxel index).
  */
@@ -290,7 +291,18 @@ void tgref_svo_traverse(uint32_t n, const float* origins, const float* dirs,
          * (tg_sparse_voxel_octree.c:574) while testing against svo.min/max;
          * callers pass world origins exactly as the reference's probe does
          * (tgvk_raytracer.c:1400). */
+        g_assert_armed = 1;
+        if (setjmp(g_assert_jmp))
+        {
+            /* one of the reference's assertions failed for this ray */
+            g_assert_armed = 0;
+            out_hit[i] = -1;
+            out_distance[i] = 0.0f;
+            out_world_voxel[3 * i] = out_world_voxel[3 * i + 1] = out_world_voxel[3 * i + 2] = 0;
+            continue;
+        }
         const b32 hit = tg_svo_traverse(&g_scene.svo, o, d, &dist, &node, &vox);
+        g_assert_armed = 0;
         out_hit[i] = hit;
         out_distance[i] = dist;
         out_world_voxel[3 * i] = out_world_voxel[3 * i + 1] = out_world_voxel[3 * i + 2] = 0;

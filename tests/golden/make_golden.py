@@ -11,6 +11,8 @@ Fixtures:
   ref_svo_<name>.npz   tg_svo_create over [-512, 512)^3 on seeded scenes:
                        the scene arrays and the non-empty 32^3 blocks
                        (world min corner + 1024 bit words), sorted by index
+  ref_trace_<name>.npz tg_svo_traverse on that SVO for seeded rays: hit flag,
+                       distance and the world voxel of the hit
 """
 from __future__ import annotations
 
@@ -159,8 +161,21 @@ def svo_scene(ref, rng, yonly: bool):
     objs["first_cluster_pointer"] = firsts
     objs["translation"] = trans
     objs["rotation"] = rot
-    return dict(objects=objs.view(np.uint8), cluster_pointers=cp, c2o=c2o, voxel_bits=words, mn=mn,
-                angles=angles, axes=axes, block_xyz=rb[:n][o], block_words=rw[:n][o])
+    sc = dict(objects=objs.view(np.uint8), cluster_pointers=cp, c2o=c2o, voxel_bits=words, mn=mn,
+              angles=angles, axes=axes, block_xyz=rb[:n][o], block_words=rw[:n][o])
+    # rays through the region of the scene, traversed by the reference's own tg_svo_traverse
+    m = 4000
+    lo = sc["block_xyz"].min(0) - 40
+    hi = sc["block_xyz"].max(0) + 72
+    orig = rng.uniform(lo, hi, (m, 3)).astype(np.float32)
+    d = rng.normal(size=(m, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    hit = np.zeros(m, np.int32)
+    dist = np.zeros(m, np.float32)
+    vox = np.zeros((m, 3), np.int32)
+    ref.tgref_svo_traverse(C.c_uint32(m), P(orig), P(d), P(hit), P(dist), P(vox))
+    trace = dict(origin=orig, dir=d, hit=hit, distance=dist, voxel=vox)
+    return sc, trace
 
 
 def main():
@@ -174,11 +189,13 @@ def main():
         k = 0
         seed = 0
         while k < 3:
-            sc = svo_scene(ref, np.random.default_rng(1000 * (1 + yonly) + seed), yonly)
+            res = svo_scene(ref, np.random.default_rng(1000 * (1 + yonly) + seed), yonly)
             seed += 1
-            if sc is None:
+            if res is None:
                 continue
+            sc, trace = res
             np.savez_compressed(HERE / f"ref_svo_{name}_{k}.npz", **sc)
+            np.savez_compressed(HERE / f"ref_trace_{name}_{k}.npz", **trace)
             k += 1
             made += 1
     print(f"wrote ref_primitives.npz and {made} SVO fixtures")

@@ -70,3 +70,85 @@ class Oracle:
                                       capacity, _p(samples))
         assert n <= capacity, "capacity too small"
         return blocks[:n].copy(), words[:n].copy(), int(samples[0])
+
+
+GI_PARAMS_DTYPE = np.dtype([
+    ("spp", np.uint32), ("bounces", np.uint32), ("max_steps", np.uint32), ("frame", np.uint32),
+    ("seed", np.uint64), ("sun_dir", np.float32, 3), ("sun_radiance", np.float32, 3),
+    ("sky_radiance", np.float32, 3), ("offset", np.float32),
+])
+assert GI_PARAMS_DTYPE.itemsize == 64
+
+
+class OracleSvo:
+    """The oracle's view of an SVO (non-empty blocks + optional materials)."""
+
+    def __init__(self, oracle: "Oracle", block_xyz, words, mats, mn, L):
+        lib = oracle.lib
+        vp, u32 = C.c_void_p, C.c_uint32
+        lib.oracle_svo_open.restype = vp
+        lib.oracle_svo_open.argtypes = [vp, vp, vp, u32, vp, u32]
+        lib.oracle_svo_close.argtypes = [vp]
+        lib.oracle_trace_batch.argtypes = [vp, u32, vp, vp, u32, vp, vp, vp, vp]
+        self.lib = lib
+        self._keep = (np.ascontiguousarray(block_xyz, np.int32), np.ascontiguousarray(words, np.uint32),
+                      None if mats is None else np.ascontiguousarray(mats, np.uint16), np.asarray(mn, np.float32))
+        b, w, m, mnv = self._keep
+        self.h = lib.oracle_svo_open(_p(b), _p(w), _p(m), len(b), _p(mnv), L)
+        self.mn = mnv
+        self.L = L
+
+    def trace(self, o, d, max_steps: int = 1 << 20):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = len(o)
+        t = np.zeros(n, np.float32)
+        vox = np.zeros((n, 3), np.int32)
+        ax = np.zeros(n, np.int32)
+        steps = np.zeros(n, np.uint32)
+        self.lib.oracle_trace_batch(self.h, n, _p(o), _p(d), max_steps, _p(t), _p(vox), _p(ax), _p(steps))
+        return t, vox, ax, steps
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_svo_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def svo_build_with_materials(oracle: "Oracle", scene, mn, L, capacity: int = 1 << 14):
+    lib = oracle.lib
+    vp, u32 = C.c_void_p, C.c_uint32
+    lib.oracle_svo_build_mat.restype = C.c_int64
+    lib.oracle_svo_build_mat.argtypes = [vp, u32, u32, vp, vp, vp, vp, vp, u32, vp, vp, vp, u32, vp]
+    mnv = np.asarray(mn, np.float32)
+    blocks = np.zeros((capacity, 3), np.int32)
+    words = np.zeros((capacity, 1024), np.uint32)
+    mats = np.zeros((capacity, 32768), np.uint16)
+    samples = np.zeros(1, np.uint64)
+    n = lib.oracle_svo_build_mat(_p(scene.objects), len(scene.objects), len(scene.cluster_pointers),
+                                 _p(scene.cluster_pointers), _p(scene.cluster_idx_to_object_idx),
+                                 _p(scene.voxel_bits), _p(scene.material_idx), _p(mnv), L, _p(blocks), _p(words),
+                                 _p(mats), capacity, _p(samples))
+    assert n <= capacity
+    return blocks[:n].copy(), words[:n].copy(), mats[:n].copy()
+
+
+def gi_render(oracle: "Oracle", osvo: OracleSvo, scene, view, params, visbuf, rows=None, threads: int = 0):
+    lib = oracle.lib
+    vp, u32 = C.c_void_p, C.c_uint32
+    lib.oracle_gi_render.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, u32, C.c_int]
+    v = np.ascontiguousarray(view).reshape(1)
+    W, H = int(v["width"][0]), int(v["height"][0])
+    out = np.zeros((H * W, 3), np.float32)
+    r0, r1 = (0, H) if rows is None else rows
+    p = np.ascontiguousarray(params, GI_PARAMS_DTYPE).reshape(1)
+    lib.oracle_gi_render(osvo.h, _p(scene.objects), _p(scene.cluster_pointers), _p(scene.cluster_idx_to_object_idx),
+                         _p(scene.material_idx), _p(scene.luts), _p(v), _p(p),
+                         _p(np.ascontiguousarray(visbuf, np.uint64)), _p(out), r0, r1, threads)
+    return out

@@ -76,7 +76,7 @@ def test_multi_view_batch_equals_single_views(ctx, oracle):
         assert_same(outs[i], oracle.vis_render(s, views[i:i + 1], mode=1))
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (32, 8), (32, 32)])
+@pytest.mark.parametrize("tile", [(8, 4), (8, 8), (32, 8), (32, 32)])
 def test_tile_shapes_agree(oracle, tile):
     s, v = cfg1_scene(), cfg1_view(100, 70)
     with tg.Context(0, tile=tile) as c:
@@ -134,3 +134,32 @@ def test_cfg2_scale_rows_bit_exact(ctx, oracle):
     sl = slice(rows[0] * 1920, rows[1] * 1920)
     assert_same(g[sl], ref[sl])
     assert (g != EMPTY).mean() > 0.05
+
+
+def test_bin_overflow_takes_exact_record_scan(oracle):
+    """With the bin storage pinned at its minimum the frame overflows it; the
+    tile kernel then walks every record and must give the same buffer."""
+    s = fuzz_scene(31, n_objects=8, box=30.0, max_cpa=4)
+    v = tg.make_view((0.0, 0.0, -70.0), 0.0, float(np.pi), 1.2, 160, 120, 0.1, 256.0)
+    with tg.Context(0, flags=tg.FLAG_MIN_BIN_CAPACITY) as c:
+        (g,) = render(c, s, v)
+        st = c.vis_stats()
+    assert st.bin_entries > 64
+    assert_same(g, oracle.vis_render(s, v, mode=1))
+
+
+def test_repeated_frames_reuse_scratch(ctx, oracle):
+    """Many frames in a row on one context (capacity grown from earlier frames)."""
+    import torch
+    s = fuzz_scene(41, n_objects=6, box=40.0)
+    sc = ctx.upload(s)
+    views = [tg.make_view((0.0, 0.0, -80.0 + 10 * i), 0.05 * i, float(np.pi) + 0.1 * i, 1.0, 96, 72, 0.1, 256.0)
+             for i in range(6)]
+    outs = [torch.empty(96 * 72, dtype=torch.int64, device="cuda") for _ in views]
+    for v, o in zip(views, outs):
+        ctx.vis_render(sc, v, [o])
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    for v, o in zip(views, outs):
+        assert_same(o.cpu().numpy().view(np.uint64), oracle.vis_render(s, v, mode=1))
+    sc.close()

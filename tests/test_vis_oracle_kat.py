@@ -83,3 +83,16 @@ def test_cfg1_has_hits(oracle):
     img = oracle.vis_render(cfg1_scene(), cfg1_view(), mode=1)
     n = int((img != EMPTY).sum())
     assert 10000 < n < 40000
+
+
+def test_ray_parallel_to_a_slab_it_misses_is_no_fragment(oracle):
+    """Identity rotation and a yaw-0 view of odd width give the centre column
+    rays an exactly-zero x component.  A cluster displaced in x is crossed by
+    no such ray, so the rasterised reference never shades it there; the
+    shader's slab test alone (collide.inc:5-10) would accept it."""
+    s = single_cluster_scene(range(512), translation=(20.0, 0.0, -40.0))
+    v = tg.make_view((0.0, 0.0, 0.0), 0.0, 0.0, 1.0, 33, 17, 0.1, 256.0)
+    assert v["ray_bl"][0][0] == -v["ray_br"][0][0]
+    a = oracle.vis_render(s, v, mode=0).reshape(17, 33)
+    assert (a[:, 16] == EMPTY).all()
+    assert np.array_equal(a.reshape(-1), oracle.vis_render(s, v, mode=1))

@@ -27,6 +27,7 @@ STATUS_NAMES = {
     8: "TGX_ERR_DEVICE_FAULT",
 }
 VIS_EMPTY = 0xFFFFFFFFFFFFFFFF
+FLAG_MIN_BIN_CAPACITY = 1
 
 # numpy views of the C structs -------------------------------------------------
 
@@ -265,8 +266,8 @@ def decode(packed: int):
 class Context:
     """tgx_ctx: one device, one stream."""
 
-    def __init__(self, device: int = 0, stream: int | None = None, tile: tuple[int, int] = (16, 16)):
-        cfg = Config(device=device, stream=stream or 0, tile_w=tile[0], tile_h=tile[1], flags=0)
+    def __init__(self, device: int = 0, stream: int | None = None, tile: tuple[int, int] = (16, 16), flags: int = 0):
+        cfg = Config(device=device, stream=stream or 0, tile_w=tile[0], tile_h=tile[1], flags=flags)
         h = C.c_void_p()
         check(lib.tgx_create(C.byref(cfg), C.byref(h)), "tgx_create")
         self.handle = h

@@ -22,27 +22,12 @@
 // The node encoding of the reference (u16 relative child pointers, 64-entry
 // leaf lists) is not kept; the voxel set is.  Side length 2^6 .. 2^14.
 
-#include "tgx_internal.cuh"
+#include "svo_trace.cuh"
 
 #include <algorithm>
 #include <vector>
 
-struct tgx_svo
-{
-    float     mn[3] = {0, 0, 0};
-    uint32_t  L = 0;              // extent_log2
-    uint32_t  B = 0;              // blocks per axis
-    uint32_t  n_blocks = 0;       // allocated (candidate) blocks
-    uint32_t  n_pairs = 0;
-    uint32_t* d_table = nullptr;  // B^3 entries: 0 = no block, else slot + 1
-    uint32_t* d_pool = nullptr;   // n_blocks * 1024 words
-    uint32_t* d_occ = nullptr;    // occupancy pyramid, level 0 = blocks
-    uint64_t  occ_words = 0;
-    uint64_t  occ_off[10] = {};   // word offset of each level
-    uint32_t  n_levels = 0;       // L - 5 + 1 levels (blocks .. root)
-    uint32_t* d_nonempty = nullptr;  // per slot: 1 if any bit set
-    uint64_t  device_bytes = 0;
-};
+
 
 namespace {
 
@@ -288,11 +273,27 @@ __global__ void __launch_bounds__(256) k_svo_alloc(uint32_t* __restrict__ table,
 
 __device__ __forceinline__ uint32_t trim_u32(float v) { return v > 0.0f ? (uint32_t)v : 0u; }
 
+// max of a 16-bit code in place (CAS on the containing aligned word)
+__device__ __forceinline__ void atomic_max_u16(uint16_t* addr, uint32_t val)
+{
+    uint32_t* base = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(addr) & ~(uintptr_t)3);
+    const uint32_t shift = (reinterpret_cast<uintptr_t>(addr) & 2) ? 16u : 0u;
+    uint32_t old = *base;
+    for (int guard = 0; guard < 1 << 20; guard++) {
+        if (((old >> shift) & 0xffffu) >= val) return;
+        const uint32_t nv = (old & ~(0xffffu << shift)) | (val << shift);
+        const uint32_t prev = atomicCAS(base, old, nv);
+        if (prev == old) return;
+        old = prev;
+    }
+}
+
 __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
     const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, const SvoPair* __restrict__ pairs,
     const uint32_t* __restrict__ counters, uint32_t pair_capacity, const uint32_t* __restrict__ table,
-    uint32_t* __restrict__ pool, float mnx, float mny, float mnz, uint32_t B)
+    uint32_t* __restrict__ pool, const uint8_t* __restrict__ material, uint16_t* __restrict__ mat_pool,
+    float mnx, float mny, float mnz, uint32_t B)
 {
     __shared__ uint32_t s_img[kWarpsPerVoxCta][kBlockWords];
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
@@ -380,6 +381,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
                 const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy)),
                                                     (float)ix);
                 atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
+                if (mat_pool)
+                    atomic_max_u16(mat_pool + (uint64_t)slot * 32768u + bvi,
+                                   ((od.lut_idx << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
             }
         }
         __syncwarp();
@@ -437,6 +441,7 @@ static void svo_free(tgx_svo* s)
     cudaFree(s->d_pool);
     cudaFree(s->d_occ);
     cudaFree(s->d_nonempty);
+    cudaFree(s->d_mat);
     delete s;
 }
 
@@ -516,6 +521,14 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
         return fail(TGX_ERR_OUT_OF_MEMORY);
     }
     cudaMemsetAsync(s->d_pool, 0, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4, c->stream);
+    if (sc->d_material && sc->d_luts) {
+        const uint64_t mb = (uint64_t)std::max(s->n_blocks, 1u) * 32768u * 2u;
+        if (cudaMalloc(&s->d_mat, mb) != cudaSuccess) {
+            tgx_set_error("tgx_svo_build: out of device memory for the material grid");
+            return fail(TGX_ERR_OUT_OF_MEMORY);
+        }
+        cudaMemsetAsync(s->d_mat, 0, mb, c->stream);
+    }
     const uint32_t grid = (uint32_t)std::min<uint64_t>((n_table + 255) / 256, (uint64_t)c->num_sms * 32);
     auto rest = [&]() -> tgx_status {
         TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_alloc, s->d_table, n_table, counters, s->n_blocks, c->d_status);
@@ -523,14 +536,15 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
                                                                                   (uint64_t)c->num_sms * 16));
         TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects,
                    sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
-                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, mn[0], mn[1], mn[2], s->B);
+                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, sc->d_material, s->d_mat,
+                   mn[0], mn[1], mn[2], s->B);
         const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
         TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
                    s->d_occ, (const uint64_t*)((char*)s->d_occ + occ_words * 4), s->n_levels, s->B, counters);
         return TGX_OK;
     };
     if ((st = rest()) != TGX_OK) return fail(st);
-    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 4) + occ_words * 4;
+    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 4 + (s->d_mat ? 65536 : 0)) + occ_words * 4;
     *out = s;
     return TGX_OK;
 }
@@ -586,9 +600,46 @@ extern "C" tgx_status tgx_svo_download(tgx_ctx* c, const tgx_svo* s, int32_t* ou
     return TGX_OK;
 }
 
-extern "C" tgx_status tgx_svo_trace(tgx_ctx*, const tgx_svo*, uint32_t, const float*, const float*, uint32_t, float*,
-                                    int32_t*)
+namespace {
+
+__global__ void __launch_bounds__(128) k_svo_trace(SvoDev s, uint32_t n, const float* __restrict__ o,
+                                                  const float* __restrict__ d, uint32_t max_steps,
+                                                  float* __restrict__ out_t, int32_t* __restrict__ out_voxel,
+                                                  uint32_t* __restrict__ n_exhausted)
 {
-    tgx_set_error("tgx_svo_trace: not built yet");
-    return TGX_ERR_NOT_SUPPORTED;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float oi[3] = {o[3 * i], o[3 * i + 1], o[3 * i + 2]};
+    const float di[3] = {d[3 * i], d[3 * i + 1], d[3 * i + 2]};
+    float t;
+    int32_t c[3], ax;
+    uint32_t steps;
+    const int r = svo_trace(s, oi, di, max_steps, t, c, ax, steps);
+    if (r == 1) {
+        out_t[i] = t;
+        out_voxel[3 * i] = c[0] + (int32_t)s.mn[0];
+        out_voxel[3 * i + 1] = c[1] + (int32_t)s.mn[1];
+        out_voxel[3 * i + 2] = c[2] + (int32_t)s.mn[2];
+    } else {
+        out_t[i] = F32_MAX_TG;
+        out_voxel[3 * i] = out_voxel[3 * i + 1] = out_voxel[3 * i + 2] = 0;
+        if (r < 0) atomicAdd(n_exhausted, 1u);
+    }
+}
+
+}  // namespace
+
+extern "C" tgx_status tgx_svo_trace(tgx_ctx* c, const tgx_svo* s, uint32_t n, const float* d_o, const float* d_d,
+                                    uint32_t max_steps, float* d_t, int32_t* d_voxel)
+{
+    if (!c || !s || (n && (!d_o || !d_d || !d_t || !d_voxel))) {
+        tgx_set_error("tgx_svo_trace: NULL argument");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return TGX_OK;
+    TGX_TRY(devbuf_reserve(c->svo_counters, S_COUNT * 4 + 64));
+    uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + S_COUNT;
+    TGX_LAUNCH(c, TR_SVO_TRACE, (n + 127) / 128, 128, 0, k_svo_trace, svo_dev(s), n, d_o, d_d, max_steps, d_t, d_voxel,
+               exhausted);
+    return TGX_OK;
 }

@@ -71,7 +71,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     }
     tgx_config def = {};
     if (!cfg) cfg = &def;
-    if (cfg->device < 0 || cfg->device >= n || cfg->flags != 0) {
+    if (cfg->device < 0 || cfg->device >= n || (cfg->flags & ~TGX_FLAG_MIN_BIN_CAPACITY) != 0) {
         tgx_set_error("tgx_create: bad device %d or flags %u", cfg->device, cfg->flags);
         return TGX_ERR_INVALID_ARGUMENT;
     }
@@ -86,6 +86,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     c->device = cfg->device;
     c->tile_w = tw;
     c->tile_h = th;
+    c->flags = cfg->flags;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
     if (cfg->stream) {
         c->stream = (cudaStream_t)cfg->stream;
@@ -99,7 +100,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     }
     if (cudaMalloc(&c->d_status, sizeof(tgx_dev_status)) != cudaSuccess ||
         cudaMemset(c->d_status, 0, sizeof(tgx_dev_status)) != cudaSuccess ||
-        cudaMallocHost(&c->h_counter, 64) != cudaSuccess) {
+        cudaMallocHost(&c->h_counter, 64) != cudaSuccess || cudaMallocHost(&c->h_vis_counters, 64) != cudaSuccess) {
         tgx_set_error("tgx_create: allocation failed");
         tgx_destroy(c);
         return TGX_ERR_OUT_OF_MEMORY;
@@ -125,6 +126,8 @@ extern "C" void tgx_destroy(tgx_ctx* c)
     devbuf_free(c->host_stage);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->h_counter) cudaFreeHost(c->h_counter);
+    if (c->h_vis_counters) cudaFreeHost(c->h_vis_counters);
+    if (c->vis_done) cudaEventDestroy(c->vis_done);
     if (c->d_status) cudaFree(c->d_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -133,7 +136,7 @@ extern "C" void tgx_destroy(tgx_ctx* c)
 // ---- tracing ----
 
 static const char* kTraceNames[TR_COUNT] = {
-    "k_object_setup", "k_vis_cluster_setup", "k_vis_scan", "k_vis_bin_fill", "k_vis_tiles",
+    "k_object_setup", "k_vis_cluster_setup", "k_vis_count", "k_vis_prefix", "k_vis_scan", "k_vis_bin_fill", "k_vis_tiles",
     "k_svo_candidates", "k_svo_alloc", "k_svo_voxelize", "k_svo_pyramid", "k_svo_trace", "k_gi", "k_mlp"};
 
 static cudaEvent_t trace_event(tgx_ctx* c)

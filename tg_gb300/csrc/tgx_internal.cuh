@@ -75,6 +75,8 @@ enum TraceSlot
 {
     TR_OBJECT_SETUP = 0,
     TR_VIS_SETUP,
+    TR_VIS_COUNT,
+    TR_VIS_PREFIX,
     TR_VIS_SCAN,
     TR_VIS_BIN,
     TR_VIS_TILES,
@@ -107,6 +109,7 @@ struct tgx_ctx
     cudaStream_t   stream = nullptr;
     bool           own_stream = false;
     uint32_t       tile_w = 16, tile_h = 16;
+    uint32_t       flags = 0;
     uint64_t       launches = 0;
     int            num_sms = 0;
     tgx_dev_status* d_status = nullptr;
@@ -121,6 +124,8 @@ struct tgx_ctx
     DevBuf svo_counters;   // SVO build counters
     DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
     uint32_t vis_last_tiles = 0;
+    void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters
+    cudaEvent_t vis_done = nullptr;    // recorded after that copy
     DevBuf host_stage;     // pinned host staging (views)
     void*  h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
@@ -137,6 +142,25 @@ struct tgx_scene
     uint32_t*   d_bits = nullptr;
     uint8_t*    d_material = nullptr;
     tgx_material* d_luts = nullptr;
+};
+
+// One-bit SVO on the device (built by tgx_svo_build, svo.cu).
+struct tgx_svo
+{
+    float     mn[3] = {0, 0, 0};
+    uint32_t  L = 0;              // extent_log2
+    uint32_t  B = 0;              // blocks per axis
+    uint32_t  n_blocks = 0;       // allocated (candidate) blocks
+    uint32_t  n_pairs = 0;
+    uint32_t* d_table = nullptr;  // B^3 entries: 0 = no block, else slot + 1
+    uint32_t* d_pool = nullptr;   // n_blocks * 1024 words
+    uint32_t* d_occ = nullptr;    // occupancy pyramid, level 0 = blocks
+    uint64_t  occ_words = 0;
+    uint64_t  occ_off[10] = {};   // word offset of each level
+    uint32_t  n_levels = 0;       // L - 5 + 1 levels (blocks .. root)
+    uint32_t* d_nonempty = nullptr;  // per slot: 1 if any bit set
+    uint16_t* d_mat = nullptr;    // n_blocks * 32768 material codes ((lut << 8 | byte) + 1, 0 = none) or null
+    uint64_t  device_bytes = 0;
 };
 
 // ---------------------------------------------------------------------------

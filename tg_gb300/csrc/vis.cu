@@ -5,17 +5,26 @@
 // and the clear pass (clear.comp:15-21) with a binned compute pass:
 //
 //   1. k_vis_cluster_setup  one thread per (view, cluster pointer): drops
-//      empty clusters, computes a conservative screen-tile rectangle of the
-//      cluster box, and for kept clusters the ws2ms matrix and the camera
-//      position in cluster space exactly as the shader does; appends a
-//      32-byte record and counts the tiles it covers.
-//   2. k_vis_scan           exclusive scan of the per-tile counts.
-//   3. k_vis_bin_fill       scatters record indices into per-tile bins.
-//   4. k_vis_tiles          one CTA per screen tile, one thread per pixel:
-//      stages batches of records and their 64-byte bitmasks in shared
-//      memory, runs the shader's ray/box test and DDA for every
-//      (pixel, binned cluster) pair and keeps the minimum packed
-//      depth|pointer|voxel word; writes every pixel once (fused clear).
+//      clusters outside the frustum or beyond the far plane (bounding
+//      sphere, then box corners) and empty clusters, computes a conservative
+//      screen-tile rectangle and a lower bound of the packed depth, and for
+//      kept clusters the ws2ms matrix and the camera position in cluster
+//      space exactly as the shader does; appends a 32-byte record.
+//   2. k_vis_count          one warp per record: counts it per (tile, depth bucket).
+//   3. k_vis_prefix         per tile: offsets of its 16 depth buckets.
+//   4. k_vis_scan           exclusive scan of the tile totals; tile launch
+//                           order, heaviest first.
+//   5. k_vis_bin_fill       one warp per record: scatters it into the
+//                           (tile, bucket) bins, so every tile's list runs
+//                           near to far.
+//   6. k_vis_tiles          one CTA per screen tile, one thread per pixel:
+//      stages batches of records in shared memory and their 64-byte
+//      bitmasks with cp.async.bulk (TMA) on an mbarrier; per pixel skips
+//      clusters whose depth bound cannot beat its current word, rejects clear
+//      misses with a conservative reciprocal slab test, runs the shader's
+//      exact ray/box test and DDA for the rest and keeps the minimum packed
+//      depth|pointer|voxel word; stops when every pixel of the tile is closer
+//      than the next depth bucket; writes every pixel once (fused clear).
 //
 // Every pair evaluates the same binary32 operations in the same order as the
 // CPU oracle's transcription of visibility.frag, so the buffer is bit-exact.
@@ -31,6 +40,8 @@ namespace {
 constexpr uint32_t kCluster = 8;
 constexpr uint32_t kBatch = 64;            // records staged per shared-memory batch
 constexpr uint32_t kMaxDdaSteps = 64;      // the 8^3 DDA needs at most 22
+constexpr uint32_t kBuckets = 16;          // depth buckets per tile
+constexpr uint32_t kWaitLimit = 1u << 20;  // mbarrier polls before a copy is declared lost
 
 struct alignas(16) VisRecord
 {
@@ -38,12 +49,20 @@ struct alignas(16) VisRecord
     uint32_t cluster_idx;
     uint32_t cluster_pointer;
     uint32_t object_idx;
-    uint32_t rect_lo;           // tile x0 | y0 << 12 | view bits 0..7 << 24
-    uint32_t rect_hi;           // tile x1 | y1 << 12 | view bits 8..15 << 24 (inclusive)
+    uint32_t d24_lb;            // lower bound of the 24-bit depth field any pixel can get from it
+    uint32_t view;
 };
 static_assert(sizeof(VisRecord) == 32, "record layout");
 
-enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_COUNT = 4 };
+enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_COUNT = 8 };
+constexpr uint32_t kOrderClasses = 32;     // tiles are launched heaviest class (log2 of bin count) first
+
+// bucket of a depth key: one per power of two of the 24-bit depth, keys < 512 share bucket 0
+__device__ __forceinline__ uint32_t depth_bucket(uint32_t key)
+{
+    return key < 512u ? 0u : min(kBuckets - 1u, (31u - (uint32_t)__clz(key)) - 8u);
+}
+__device__ __forceinline__ uint32_t bucket_lo(uint32_t b) { return b == 0u ? 0u : (1u << (b + 8u)); }
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
 {
@@ -66,7 +85,7 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
     const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp,
     const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
-    uint32_t record_capacity, uint32_t* __restrict__ counters, uint32_t* __restrict__ tile_cnt,
+    uint2* __restrict__ rects, uint32_t record_capacity, uint32_t* __restrict__ counters,
     tgx_dev_status* __restrict__ status)
 {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -78,10 +97,8 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
     if (v < n_views) {
         const ViewConst& vc = views[v];
         const uint32_t ci = cluster_pointers[cp];
-        const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
-        const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
-        const uint32_t any = a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w;
-        if (any) {
+        {
+            bool oi_cull = false;
             const uint32_t oi = c2o[ci];
             const tgx_object& od = objects[oi];
             const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
@@ -96,10 +113,34 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
 #pragma unroll
             for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
 
-            // ---- conservative screen rectangle (only culls; widened by a margin) ----
+            // ---- bounding-sphere cull against the side planes and the far plane ----
+            {
+                const float lx = offx + 4.0f - ohx, ly = offy + 4.0f - ohy, lz = offz + 4.0f - ohz;
+                float q[3];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+                    q[r] = DM(rot, r, 0) * lx + DM(rot, r, 1) * ly + DM(rot, r, 2) * lz + od.translation[r] - vc.cam[r];
+                const float rad = 6.9283f + 0.05f + 1e-5f * (fabsf(q[0]) + fabsf(q[1]) + fabsf(q[2]));
+                const float dist = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+                bool out = dist - rad > vc.far_plane * 1.0001f;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    out |= vc.planes[3 * k] * q[0] + vc.planes[3 * k + 1] * q[1] + vc.planes[3 * k + 2] * q[2] < -rad;
+                if (out) oi_cull = true;
+            }
+
+            if (!oi_cull) {
+                // a cluster without set bits never writes (its DDA finds nothing)
+                const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
+                const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
+                oi_cull = !(a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w);
+            }
+            if (!oi_cull) {
+            // ---- culling and conservative screen rectangle (never exact-critical: widened) ----
             float fxmin = 1e30f, fxmax = -1e30f, fymin = 1e30f, fymax = -1e30f;
             bool full = false, any_front = false;
             bool inside0 = false, inside1 = false, inside2 = false, inside3 = false;
+            float cxw = 0.0f, cyw = 0.0f, czw = 0.0f;
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 const float lx = offx + ((k & 1) ? 8.0f : 0.0f) - ohx;
@@ -109,6 +150,7 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
 #pragma unroll
                 for (int r = 0; r < 3; r++)
                     p[r] = DM(rot, r, 0) * lx + DM(rot, r, 1) * ly + DM(rot, r, 2) * lz + od.translation[r] - vc.cam[r];
+                cxw += p[0]; cyw += p[1]; czw += p[2];
                 const float depth = p[0] * vc.fwd[0] + p[1] * vc.fwd[1] + p[2] * vc.fwd[2];
                 if (depth > -0.5f) any_front = true;
                 const float slack = -(0.05f + 1e-5f * (fabsf(p[0]) + fabsf(p[1]) + fabsf(p[2])));
@@ -123,7 +165,11 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
                 fxmin = fminf(fxmin, fa); fxmax = fmaxf(fxmax, fa);
                 fymin = fminf(fymin, fb); fymax = fmaxf(fymax, fb);
             }
-            if (any_front && inside0 && inside1 && inside2 && inside3) {
+            // lower bound of the distance from the camera to any point of the box
+            const float cdist = sqrtf(cxw * cxw + cyw * cyw + czw * czw) * 0.125f;
+            const float lb = fmaxf(0.0f, cdist * (1.0f - 1e-5f) - 6.9283f - 0.01f);
+            const float lbq = lb / vc.far_plane;
+            if (any_front && inside0 && inside1 && inside2 && inside3 && lbq <= 1.0001f) {
                 const float W = (float)vc.width, H = (float)vc.height;
                 float x0, x1, y0, y1;
                 if (full) {
@@ -160,8 +206,10 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
                 rec.cluster_idx = ci;
                 rec.cluster_pointer = cp;
                 rec.object_idx = oi;
-                rec.rect_lo = tx0 | (ty0 << 12) | ((v & 0xffu) << 24);
-                rec.rect_hi = tx1 | (ty1 << 12) | ((v >> 8) << 24);
+                const float k24 = fminf(lbq, 1.0f) * 16777215.0f;
+                rec.d24_lb = k24 >= 2.0f ? (uint32_t)k24 - 1u : 0u;
+                rec.view = v;
+            }
             }
         }
     }
@@ -172,27 +220,74 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
         return;
     }
     records[slot] = rec;
-    const ViewConst& vc = views[v];
-    for (uint32_t ty = ty0; ty <= ty1; ty++)
-        for (uint32_t tx = tx0; tx <= tx1; tx++)
-            atomicAdd(&tile_cnt[vc.tile_base + ty * vc.tiles_x + tx], 1u);
+    rects[slot] = make_uint2(tx0 | (ty0 << 16), tx1 | (ty1 << 16));
 }
 
 // ---------------------------------------------------------------------------
-// 2. exclusive scan of tile counts (single CTA; n_tiles is a few 10^4)
+// 2. per-(tile, bucket) counts: one warp per record, lanes over its tiles
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ tile_off,
-                                                   uint32_t n_tiles, uint32_t* __restrict__ counters)
+__global__ void __launch_bounds__(256) k_vis_count(const VisRecord* __restrict__ records, const uint2* __restrict__ rects,
+                                                  const uint32_t* __restrict__ counters,
+                                                  const ViewConst* __restrict__ views,
+                                                  uint32_t* __restrict__ bucket_cnt, uint32_t n_tiles)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n = counters[C_RECORDS];
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const uint2 r = rects[i];
+        const VisRecord& rec = records[i];
+        const ViewConst& vc = views[rec.view];
+        const uint32_t b = depth_bucket(rec.d24_lb);
+        const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
+        const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
+        for (uint32_t k = lane; k < cnt; k += 32) {
+            const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
+            atomicAdd(&bucket_cnt[b * n_tiles + t], 1u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. per-tile bucket offsets (one thread per tile, bucket-major = coalesced)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_vis_prefix(uint32_t* __restrict__ bucket_cnt, uint32_t* __restrict__ bucket_off,
+                                                   uint32_t* __restrict__ tile_total, uint32_t n_tiles)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    uint32_t run = 0;
+#pragma unroll
+    for (uint32_t b = 0; b < kBuckets; b++) {
+        const uint32_t c = bucket_cnt[b * n_tiles + t];
+        bucket_off[b * n_tiles + t] = run;
+        bucket_cnt[b * n_tiles + t] = 0;   // becomes the fill cursor
+        run += c;
+    }
+    tile_total[t] = run;
+}
+
+// ---------------------------------------------------------------------------
+// 4. exclusive scan of tile totals and the launch order of the tiles
+//    (single CTA; n_tiles is a few 10^4).
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(1024) k_vis_scan(const uint32_t* __restrict__ tile_total, uint32_t* __restrict__ tile_off,
+                                                   uint32_t* __restrict__ tile_order, uint32_t n_tiles,
+                                                   uint32_t bin_capacity, uint32_t* __restrict__ counters)
 {
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t carry;
+    __shared__ uint32_t cls_cnt[kOrderClasses];
     if (threadIdx.x == 0) carry = 0;
+    if (threadIdx.x < kOrderClasses) cls_cnt[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     for (uint32_t base = 0; base < n_tiles; base += 1024) {
         const uint32_t i = base + threadIdx.x;
-        const uint32_t x = i < n_tiles ? tile_cnt[i] : 0u;
+        const uint32_t x = i < n_tiles ? tile_total[i] : 0u;
+        if (i < n_tiles) atomicAdd(&cls_cnt[x ? 32u - __clz(x) : 0u], 1u);
         uint32_t incl = x;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -212,10 +307,7 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ tile_c
         }
         __syncthreads();
         const uint32_t warp_prefix = wid ? warp_sums[wid - 1] : 0u;
-        if (i < n_tiles) {
-            tile_off[i] = carry + warp_prefix + incl - x;
-            tile_cnt[i] = 0;   // becomes the fill cursor
-        }
+        if (i < n_tiles) tile_off[i] = carry + warp_prefix + incl - x;
         __syncthreads();
         if (threadIdx.x == 0) carry += warp_sums[31];
         __syncthreads();
@@ -223,39 +315,57 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ tile_c
     if (threadIdx.x == 0) {
         tile_off[n_tiles] = carry;
         counters[C_ENTRIES] = carry;
+        counters[C_OVERFLOW] = carry > bin_capacity ? 1u : 0u;
+        // class cursors, heaviest class first
+        uint32_t run = 0;
+        for (int c = (int)kOrderClasses - 1; c >= 0; c--) {
+            const uint32_t n = cls_cnt[c];
+            cls_cnt[c] = run;
+            run += n;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_tiles; i += blockDim.x) {
+        const uint32_t x = tile_total[i];
+        tile_order[atomicAdd(&cls_cnt[x ? 32u - __clz(x) : 0u], 1u)] = i;
     }
 }
 
 // ---------------------------------------------------------------------------
-// 3. bin fill
+// 5. bin fill: one warp per record, lanes over its tiles
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restrict__ records,
+                                                     const uint2* __restrict__ rects,
                                                      const uint32_t* __restrict__ counters,
                                                      const ViewConst* __restrict__ views,
                                                      const uint32_t* __restrict__ tile_off,
+                                                     const uint32_t* __restrict__ bucket_off,
                                                      uint32_t* __restrict__ cursor, uint32_t* __restrict__ bins,
-                                                     uint32_t bin_capacity, tgx_dev_status* __restrict__ status)
+                                                     uint32_t n_tiles, uint32_t bin_capacity,
+                                                     tgx_dev_status* __restrict__ status)
 {
+    if (counters[C_OVERFLOW]) return;   // the tile kernel scans all records instead
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = counters[C_RECORDS];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const VisRecord r = records[i];
-        const uint32_t v = (r.rect_lo >> 24) | ((r.rect_hi >> 24) << 8);
-        const ViewConst& vc = views[v];
-        const uint32_t tx0 = r.rect_lo & 0xfffu, ty0 = (r.rect_lo >> 12) & 0xfffu;
-        const uint32_t tx1 = r.rect_hi & 0xfffu, ty1 = (r.rect_hi >> 12) & 0xfffu;
-        for (uint32_t ty = ty0; ty <= ty1; ty++)
-            for (uint32_t tx = tx0; tx <= tx1; tx++) {
-                const uint32_t t = vc.tile_base + ty * vc.tiles_x + tx;
-                const uint32_t pos = tile_off[t] + atomicAdd(&cursor[t], 1u);
-                if (pos < bin_capacity) bins[pos] = i;
-                else dev_error(status, TGX_ERR_CAPACITY, 3, pos);
-            }
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const uint2 r = rects[i];
+        const VisRecord& rec = records[i];
+        const ViewConst& vc = views[rec.view];
+        const uint32_t b = depth_bucket(rec.d24_lb);
+        const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
+        const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
+        for (uint32_t k = lane; k < cnt; k += 32) {
+            const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
+            const uint32_t pos = tile_off[t] + bucket_off[b * n_tiles + t] + atomicAdd(&cursor[b * n_tiles + t], 1u);
+            if (pos < bin_capacity) bins[pos] = i;
+            else dev_error(status, TGX_ERR_DEVICE_FAULT, 3, pos);
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
-// 4. per-tile ray/cluster evaluation
+// 6. per-tile ray/cluster evaluation
 // ---------------------------------------------------------------------------
 
 // One (pixel, cluster) fragment of visibility.frag:78-207 given the cluster-space
@@ -266,6 +376,10 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
 {
     float enter, exit_;
     if (!ray_aabb(ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f, enter, exit_)) return ULLONG_MAX;
+    // a ray parallel to a slab it does not cross is never rasterised
+    if ((dx == 0.0f && (ox < 0.0f || ox > 8.0f)) || (dy == 0.0f && (oy < 0.0f || oy > 8.0f)) ||
+        (dz == 0.0f && (oz < 0.0f || oz > 8.0f)))
+        return ULLONG_MAX;
     const bool ent = enter > 0.0f;
     const float hx = ent ? xadd(ox, xmul(enter, dx)) : ox;
     const float hy = ent ? xadd(oy, xmul(enter, dy)) : oy;
@@ -285,12 +399,15 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     for (uint32_t step = 0; step < kMaxDdaSteps; step++) {
         const uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
         if (w[rvi >> 5] & (1u << (rvi & 31u))) {
-            float ve, vx;
-            ray_aabb(ox, oy, oz, dx, dy, dz, (float)x, (float)y, (float)z, (float)(x + 1), (float)(y + 1),
-                     (float)(z + 1), ve, vx);
+            // entry distance of the voxel box (visibility.frag:155): only the near-plane
+            // quotient of each axis can be the maximum, since (vmin-o)/d <= (vmax-o)/d for d>0
+            const float nx = dx > 0.0f ? xdiv(xsub((float)x, ox), dx) : dx < 0.0f ? xdiv(xsub((float)(x + 1), ox), dx) : F32_MIN_TG;
+            const float ny = dy > 0.0f ? xdiv(xsub((float)y, oy), dy) : dy < 0.0f ? xdiv(xsub((float)(y + 1), oy), dy) : F32_MIN_TG;
+            const float nz = dz > 0.0f ? xdiv(xsub((float)z, oz), dz) : dz < 0.0f ? xdiv(xsub((float)(z + 1), oz), dz) : F32_MIN_TG;
+            const float ve = gmax(gmax(nx, ny), nz);
             const float depth = gmax(0.0f, xdiv(ve, far_plane));
             if (!(depth <= 1.0f)) return ULLONG_MAX;
-            const unsigned long long d24 = __float2ull_rz(xmul(depth, 16777215.0f));
+            const unsigned long long d24 = __float2uint_rz(xmul(depth, 16777215.0f));   // < 2^24
             return (d24 << 40) | ((unsigned long long)cluster_pointer << 9) | (unsigned long long)rvi;
         }
         if (tmx < tmy) {
@@ -305,24 +422,55 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     return ULLONG_MAX;
 }
 
-__global__ void __launch_bounds__(1024) k_vis_tiles(const VisRecord* __restrict__ records,
+// Conservative reject: true only if the exact test of vis_pair surely misses.
+// Slab distances use a correctly rounded reciprocal (error < 2 ulp against
+// the exact quotient); a miss is declared only with a 1e-5 relative margin.
+__device__ __forceinline__ bool surely_misses(float ox, float oy, float oz, float dx, float dy, float dz, float ix,
+                                              float iy, float iz)
+{
+    float en = -3.0e38f, ex = 3.0e38f;
+    if (dx == 0.0f) { if (ox < 0.0f || ox > 8.0f) return true; }
+    else { const float a = -ox * ix, b = (8.0f - ox) * ix; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
+    if (dy == 0.0f) { if (oy < 0.0f || oy > 8.0f) return true; }
+    else { const float a = -oy * iy, b = (8.0f - oy) * iy; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
+    if (dz == 0.0f) { if (oz < 0.0f || oz > 8.0f) return true; }
+    else { const float a = -oz * iz, b = (8.0f - oz) * iz; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
+    if (!(fabsf(en) < 1e37f) || !(fabsf(ex) < 1e37f)) return false;
+    const float tol = 1e-5f * (fabsf(en) + fabsf(ex)) + 1e-30f;
+    return ex < -tol || en > ex + 2.0f * tol;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Instantiated per block size (= tile pixels) so the register budget can be
+// bounded for the occupancy each size needs.
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRecord* __restrict__ records,
+                                                   const uint2* __restrict__ rects,
                                                    const uint32_t* __restrict__ bins,
                                                    const uint32_t* __restrict__ tile_off,
+                                                   const uint32_t* __restrict__ tile_order,
                                                    const ViewConst* __restrict__ views, uint32_t n_views,
                                                    const uint32_t* __restrict__ bits,
                                                    const float* __restrict__ inv_rot,
                                                    unsigned long long* const* __restrict__ outs,
-                                                   uint32_t* __restrict__ counters)
+                                                   uint32_t* __restrict__ counters, tgx_dev_status* __restrict__ status)
 {
     __shared__ VisRecord s_rec[kBatch];
-    __shared__ __align__(16) uint32_t s_bits[kBatch * 16];
+    __shared__ __align__(128) uint32_t s_bits[kBatch * 16];
+    __shared__ __align__(8) unsigned long long s_bar;
     __shared__ uint32_t s_view;
+    __shared__ uint32_t s_n;
 
-    const uint32_t tile = blockIdx.x;
+    const uint32_t tile = tile_order[blockIdx.x];
+    // bins overflowed this frame: walk every record and test its rectangle (slow, exact)
+    const bool scan_all = counters[C_OVERFLOW] != 0u;
     if (threadIdx.x == 0) {
         uint32_t v = 0;
         while (v + 1 < n_views && views[v + 1].tile_base <= tile) v++;
         s_view = v;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&s_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const ViewConst& vc = views[s_view];
@@ -344,23 +492,63 @@ __global__ void __launch_bounds__(1024) k_vis_tiles(const VisRecord* __restrict_
     }
 
     unsigned long long best = ULLONG_MAX;
+    uint32_t best_d24 = 0xffffffu;
     uint32_t cur_obj = 0xffffffffu;
-    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    const uint32_t begin = tile_off[tile], end = tile_off[tile + 1];
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
+    const uint32_t begin = scan_all ? 0u : tile_off[tile];
+    const uint32_t end = scan_all ? counters[C_RECORDS] : tile_off[tile + 1];
+    uint32_t phase = 0;
     for (uint32_t base = begin; base < end; base += kBatch) {
-        const uint32_t n = min(kBatch, end - base);
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s_rec[k] = records[bins[base + k]];
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < n * 4; k += blockDim.x) {
-            const uint32_t r = k >> 2, q = k & 3u;
-            reinterpret_cast<uint4*>(s_bits)[k] =
-                reinterpret_cast<const uint4*>(bits + (uint64_t)s_rec[r].cluster_idx * 16u)[q];
+        uint32_t n = min(kBatch, end - base);
+        __syncthreads();   // the previous batch is fully consumed
+        if (!scan_all) {
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s_rec[k] = records[bins[base + k]];
+            __syncthreads();
+            // every pixel already closer than the nearest bucket left: the tile is done
+            const uint32_t lo = bucket_lo(depth_bucket(s_rec[0].d24_lb));
+            if (__syncthreads_and(!valid || best_d24 < lo)) break;
+        } else {
+            // keep the records of this view whose tile rectangle holds this tile
+            if (threadIdx.x == 0) s_n = 0;
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+                const VisRecord r = records[base + k];
+                const uint2 q = rects[base + k];
+                if (r.view == s_view && tx >= (q.x & 0xffffu) && tx <= (q.y & 0xffffu) && ty >= (q.x >> 16) &&
+                    ty <= (q.y >> 16))
+                    s_rec[atomicAdd(&s_n, 1u)] = r;
+            }
+            __syncthreads();
+            n = s_n;
+            if (n == 0) continue;
         }
-        __syncthreads();
+        // stage the n bitmasks (64 B each) with bulk async copies completing on the mbarrier
+        if (threadIdx.x == 0)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&s_bar)), "r"(n * 64u) : "memory");
+        // order this thread's earlier generic reads of s_bits before the async-proxy writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+            const uint32_t* src = bits + (uint64_t)s_rec[k].cluster_idx * 16u;
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];"
+                         :: "r"(smem_addr(&s_bits[k * 16])), "l"(src), "r"(smem_addr(&s_bar)) : "memory");
+        }
+        // bounded wait on the barrier phase
+        {
+            uint32_t done = 0, polls = 0;
+            while (!done) {
+                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                             : "=r"(done) : "r"(smem_addr(&s_bar)), "r"(phase) : "memory");
+                if (++polls >= kWaitLimit && !done) {
+                    dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
+                    break;
+                }
+            }
+        }
+        phase ^= 1u;
         if (!valid) continue;
         for (uint32_t k = 0; k < n; k++) {
             const VisRecord& r = s_rec[k];
+            if (best_d24 < r.d24_lb) continue;   // cannot produce a smaller word
             if (r.object_idx != cur_obj) {
                 // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
                 // object's shared linear part (see k_object_setup)
@@ -371,10 +559,14 @@ __global__ void __launch_bounds__(1024) k_vis_tiles(const VisRecord* __restrict_
                 const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
                 const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
                 dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
+                ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
+                iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
+                iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
             }
+            if (surely_misses(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz)) continue;
             const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, &s_bits[k * 16], r.cluster_pointer,
                                                   vc.far_plane, &counters[C_DDA_OVERRUN]);
-            best = p < best ? p : best;
+            if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
         }
     }
     if (valid) outs[s_view][(size_t)py * vc.width + px] = best;
@@ -461,7 +653,7 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
         if (!d_visbuf[i]) { tgx_set_error("tgx_vis_render: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
     TGX_CUDA(cudaSetDevice(c->device));
 
-    // view constants + output pointer table in one pinned staging block
+    // view constants + output pointer table, copied from pageable memory (staged by the driver, no sync)
     std::vector<ViewConst> vcs(n_views);
     uint32_t n_tiles = 0;
     for (uint32_t i = 0; i < n_views; i++) {
@@ -471,54 +663,78 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     const size_t vc_bytes = n_views * sizeof(ViewConst);
     const size_t ptr_off = (vc_bytes + 15) & ~(size_t)15;
     const size_t stage_bytes = ptr_off + n_views * sizeof(void*);
-    if (c->h_pinned_bytes < stage_bytes) {
-        if (c->h_pinned) cudaFreeHost(c->h_pinned);
-        c->h_pinned = nullptr;
-        c->h_pinned_bytes = 0;
-        TGX_CUDA(cudaStreamSynchronize(c->stream));
-        TGX_CUDA(cudaMallocHost(&c->h_pinned, stage_bytes));
-        c->h_pinned_bytes = stage_bytes;
-    }
-    // the previous call's copy out of the staging block must be complete
-    TGX_CUDA(cudaStreamSynchronize(c->stream));
-    memcpy(c->h_pinned, vcs.data(), vc_bytes);
-    memcpy((char*)c->h_pinned + ptr_off, d_visbuf, n_views * sizeof(void*));
+    std::vector<unsigned char> stage(stage_bytes);
+    memcpy(stage.data(), vcs.data(), vc_bytes);
+    memcpy(stage.data() + ptr_off, d_visbuf, n_views * sizeof(void*));
     TGX_TRY(devbuf_reserve(c->vis_views, stage_bytes));
-    TGX_CUDA(cudaMemcpyAsync(c->vis_views.ptr, c->h_pinned, stage_bytes, cudaMemcpyHostToDevice, c->stream));
+    TGX_CUDA(cudaMemcpyAsync(c->vis_views.ptr, stage.data(), stage_bytes, cudaMemcpyHostToDevice, c->stream));
     const ViewConst* d_vc = (const ViewConst*)c->vis_views.ptr;
     unsigned long long* const* d_outs = (unsigned long long* const*)((char*)c->vis_views.ptr + ptr_off);
+
+    // bin capacity: grown from earlier frames' totals (read back without waiting); a frame
+    // that still overflows is rendered correctly by the tile kernel's record scan
+    uint32_t bin_capacity;
+    if (c->flags & TGX_FLAG_MIN_BIN_CAPACITY) {
+        TGX_TRY(devbuf_reserve(c->vis_bins, 64 * 4));
+        bin_capacity = 64;
+    } else {
+        if (c->vis_done && cudaEventQuery(c->vis_done) == cudaSuccess) {
+            const uint32_t prev = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
+            if ((size_t)prev * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)prev * 2 * 4));
+        }
+        cudaGetLastError();
+        TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 64, (size_t)1 << 20) * 4));
+        bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
+    }
 
     const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
     if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
     const uint32_t rec_cap = (uint32_t)n_pairs;
-    TGX_TRY(devbuf_reserve(c->vis_records, (size_t)rec_cap * sizeof(VisRecord)));
+    TGX_TRY(devbuf_reserve(c->vis_records, (size_t)rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
     TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
-    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * 4));
-    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4));
+    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4));
+    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4 * 2));
+    VisRecord* records = (VisRecord*)c->vis_records.ptr;
+    uint2* rects = (uint2*)(records + rec_cap);
     uint32_t* counters = (uint32_t*)c->vis_counters.ptr;
-    uint32_t* tile_cnt = (uint32_t*)c->vis_tile_cnt.ptr;
+    uint32_t* bucket_cnt = (uint32_t*)c->vis_tile_cnt.ptr;
+    uint32_t* bucket_off = bucket_cnt + (size_t)n_tiles * kBuckets;
+    uint32_t* tile_total = bucket_off + (size_t)n_tiles * kBuckets;
     uint32_t* tile_off = (uint32_t*)c->vis_tile_off.ptr;
+    uint32_t* tile_order = tile_off + (n_tiles + 1);
     TGX_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
-    TGX_CUDA(cudaMemsetAsync(tile_cnt, 0, (size_t)n_tiles * 4, c->stream));
+    TGX_CUDA(cudaMemsetAsync(bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
 
     const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
     TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
                s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-               (VisRecord*)c->vis_records.ptr, rec_cap, counters, tile_cnt, c->d_status);
-    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, tile_cnt, tile_off, n_tiles, counters);
-    // bin storage is sized from the scan result
-    TGX_CUDA(cudaMemcpyAsync(c->h_counter, counters + C_ENTRIES, 4, cudaMemcpyDeviceToHost, c->stream));
-    TGX_CUDA(cudaStreamSynchronize(c->stream));
-    const uint32_t entries = *(uint32_t*)c->h_counter;
-    TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)(entries ? entries : 1) * 4));
-    const uint32_t fill_blocks = (uint32_t)std::min<uint64_t>((n_pairs + 255) / 256, (uint64_t)c->num_sms * 16);
-    TGX_LAUNCH(c, TR_VIS_BIN, fill_blocks ? fill_blocks : 1, 256, 0, k_vis_bin_fill,
-               (const VisRecord*)c->vis_records.ptr, counters, d_vc, tile_off, tile_cnt, (uint32_t*)c->vis_bins.ptr,
-               (uint32_t)(c->vis_bins.bytes / 4), c->d_status);
+               records, rects, rec_cap, counters, c->d_status);
+    const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
+    TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
+    TGX_LAUNCH(c, TR_VIS_PREFIX, (n_tiles + 255) / 256, 256, 0, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles);
+    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, tile_total, tile_off, tile_order, n_tiles, bin_capacity,
+               counters);
+    TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
+               records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, (uint32_t*)c->vis_bins.ptr,
+               n_tiles, bin_capacity, c->d_status);
     c->vis_last_tiles = n_tiles;
-    TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, c->tile_w * c->tile_h, 0, k_vis_tiles,
-               (const VisRecord*)c->vis_records.ptr, (const uint32_t*)c->vis_bins.ptr, tile_off, d_vc, n_views,
-               s->d_bits, s->d_inv_rot, d_outs, counters);
+    const uint32_t threads = c->tile_w * c->tile_h;
+#define VIS_TILES_ARGS records, rects, (const uint32_t*)c->vis_bins.ptr, tile_off, tile_order, d_vc, n_views, \
+                       s->d_bits, s->d_inv_rot, d_outs, counters, c->d_status
+    if (threads == 64) {
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 16>), VIS_TILES_ARGS);
+    } else if (threads == 128) {
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), VIS_TILES_ARGS);
+    } else if (threads == 256) {
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), VIS_TILES_ARGS);
+    } else {
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), VIS_TILES_ARGS);
+    }
+#undef VIS_TILES_ARGS
+    // counters of this frame to pinned memory, read by the next call without waiting
+    TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    if (!c->vis_done) TGX_CUDA(cudaEventCreateWithFlags(&c->vis_done, cudaEventDisableTiming));
+    TGX_CUDA(cudaEventRecord(c->vis_done, c->stream));
     return TGX_OK;
 }
 
