@@ -201,6 +201,35 @@ tgx_status  tgx_vis_render(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view*
 tgx_status  tgx_vis_render_host(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                                 uint64_t* const* h_visbuf);
 
+/*
+ * Visibility render that allocates nothing.  No counterpart in the reference:
+ * tg always owns its Vulkan buffers.  It exists for callers that cannot call
+ * cudaMalloc -- an engine or plugin host that owns every device allocation
+ * through its own allocator or a fixed memory budget, or code that must not
+ * risk the device-wide synchronisation cudaMalloc/cudaFree can cause.  Needs
+ * no tgx_ctx (tgx_create allocates).
+ *
+ * The caller passes the scene as DEVICE arrays with the tgx_scene_desc layout
+ * (objects, cluster pointers, cluster->object map, voxel bits; indices are
+ * trusted, not validated), the view on the host, and a DEVICE output of
+ * width*height u64.  The result equals tgx_vis_render's bit for bit.  All
+ * scratch lives in one fixed device array of about 31 MiB inside the library,
+ * which every GPU that loads the library holds until the process exits.
+ * Limits: at most 65,536 objects, 524,288 cluster pointers and 32,768 screen
+ * tiles of 16x16 pixels (3840x2160 fits); larger inputs are rejected with
+ * TGX_ERR_CAPACITY and a message.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream capture.
+ * Every call shares the one array and reuses what the previous call left in
+ * it, so calls whose work overlaps on the GPU (other streams, other host
+ * threads) race; serialise them.  Runs on `stream` (a cudaStream_t, or NULL
+ * for the legacy default stream) and returns without waiting, unless
+ * out_error is non-NULL: then it waits and reports the device status word.
+ */
+tgx_status  tgx_vis_render_noalloc(void* stream, const tgx_object* d_objects, uint32_t n_objects,
+                                   const uint32_t* d_cluster_pointers, uint32_t n_cluster_pointers,
+                                   const uint32_t* d_cluster_idx_to_object_idx, const uint32_t* d_voxel_bits,
+                                   const tgx_view* view, uint64_t* d_visbuf, tgx_device_error* out_error);
+
 /* Counters of the last tgx_vis_render on this context (blocking). */
 typedef struct tgx_vis_stats
 {

@@ -33,6 +33,7 @@
 
 #include <climits>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -782,3 +783,182 @@ extern "C" tgx_status tgx_vis_get_stats(tgx_ctx* c, tgx_vis_stats* out)
     out->tiles = c->vis_last_tiles;
     return TGX_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Visibility render without any allocation (tgx_vis_render_noalloc).
+//
+// For callers that cannot allocate device memory at all: code running under an
+// allocator they do not own (a host application with a fixed memory budget, or
+// a plugin whose host forbids cudaMalloc), or code that must not trigger the
+// implicit device synchronisation a cudaMalloc/cudaFree can cause.  All the
+// scratch of the pass lives in one file-scope device array of fixed size,
+// created when the library is loaded on a device and kept until the process
+// exits.  The caller passes the scene arrays and the output buffer, both in
+// device memory.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr uint32_t kNaMaxObjects = 65536;
+constexpr uint32_t kNaMaxClusterPointers = 1u << 19;
+constexpr uint32_t kNaMaxTiles = 32768;      // 16x16 tiles: up to 3840x2160
+constexpr uint32_t kNaBins = 1u << 20;       // more entries take the exact record-scan path
+constexpr uint32_t kNaTile = 16;
+
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNaCounters = 0;
+constexpr size_t kNaStatus = kNaCounters + 256;
+constexpr size_t kNaViews = kNaStatus + 256;
+constexpr size_t kNaInvRot = kNaViews + na_align(sizeof(ViewConst) + 16);
+constexpr size_t kNaRecords = kNaInvRot + na_align((size_t)kNaMaxObjects * 9 * 4);
+constexpr size_t kNaRects = kNaRecords + na_align((size_t)kNaMaxClusterPointers * sizeof(VisRecord));
+constexpr size_t kNaBucketCnt = kNaRects + na_align((size_t)kNaMaxClusterPointers * 8);
+constexpr size_t kNaBucketOff = kNaBucketCnt + na_align((size_t)kNaMaxTiles * kBuckets * 4);
+constexpr size_t kNaTileTotal = kNaBucketOff + na_align((size_t)kNaMaxTiles * kBuckets * 4);
+constexpr size_t kNaTileOff = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
+constexpr size_t kNaTileOrder = kNaTileOff + na_align(((size_t)kNaMaxTiles + 1) * 4);
+constexpr size_t kNaBinsOff = kNaTileOrder + na_align((size_t)kNaMaxTiles * 4);
+constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * 4);   // about 31 MiB
+
+// The scratch.  In host code this name is only a host-side stand-in: its
+// device address is taken with cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_vis_noalloc_scratch[kNaBytes];
+
+// per-object 3x3 of inverse(rotation), as k_object_setup computes it at upload
+__global__ void __launch_bounds__(128) k_vis_noalloc_inv_rot(const tgx_object* __restrict__ objs, uint32_t n,
+                                                            float* __restrict__ inv_rot)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float rot[16], inv[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) rot[k] = objs[i].rotation[k];
+    dm4_inverse(rot, inv);
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) inv_rot[9 * i + 3 * r + c] = DM(inv, r, c);
+}
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mutex;
+void* g_na_ptr[kNaMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per device.
+tgx_status na_scratch(int device, unsigned char** out)
+{
+    if (device < 0 || device >= kNaMaxDevices) {
+        tgx_set_error("tgx_vis_render_noalloc: device %d out of range", device);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_vis_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            tgx_set_error("tgx_vis_render_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return TGX_ERR_CUDA;
+        }
+        g_na_ptr[device] = p;
+    }
+    *out = (unsigned char*)g_na_ptr[device];
+    return TGX_OK;
+}
+
+#define NA_LAUNCH(grid, block, kernel, ...)                                                        \
+    do {                                                                                           \
+        kernel<<<(grid), (block), 0, st>>>(__VA_ARGS__);                                           \
+        const cudaError_t le_ = cudaGetLastError();                                                \
+        if (le_ != cudaSuccess) {                                                                  \
+            tgx_set_error("tgx_vis_render_noalloc: launch of %s failed: %s", #kernel,              \
+                          cudaGetErrorString(le_));                                                \
+            return TGX_ERR_CUDA;                                                                   \
+        }                                                                                          \
+    } while (0)
+
+}  // namespace
+
+extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_objects, uint32_t n_objects,
+                                             const uint32_t* d_cluster_pointers, uint32_t n_cluster_pointers,
+                                             const uint32_t* d_cluster_idx_to_object_idx,
+                                             const uint32_t* d_voxel_bits, const tgx_view* view, uint64_t* d_visbuf,
+                                             tgx_device_error* out_error)
+{
+    if (!d_objects || !d_cluster_pointers || !d_cluster_idx_to_object_idx || !d_voxel_bits || !view || !d_visbuf) {
+        tgx_set_error("tgx_vis_render_noalloc: NULL argument");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    if (n_objects == 0 || n_objects > kNaMaxObjects) {
+        tgx_set_error("tgx_vis_render_noalloc: %u objects, the fixed scratch holds 1..%u", n_objects, kNaMaxObjects);
+        return TGX_ERR_CAPACITY;
+    }
+    if (n_cluster_pointers == 0 || n_cluster_pointers > kNaMaxClusterPointers) {
+        tgx_set_error("tgx_vis_render_noalloc: %u cluster pointers, the fixed scratch holds 1..%u", n_cluster_pointers,
+                      kNaMaxClusterPointers);
+        return TGX_ERR_CAPACITY;
+    }
+    TGX_TRY(check_views(view, 1, kNaTile, kNaTile));
+    ViewConst vc;
+    make_view_const(*view, kNaTile, kNaTile, 0, vc);
+    const uint32_t n_tiles = vc.tiles_x * vc.tiles_y;
+    if (n_tiles > kNaMaxTiles) {
+        tgx_set_error("tgx_vis_render_noalloc: %ux%u needs %u tiles of 16x16, the fixed scratch holds %u", view->width,
+                      view->height, n_tiles, kNaMaxTiles);
+        return TGX_ERR_CAPACITY;
+    }
+    int device = 0;
+    TGX_CUDA(cudaGetDevice(&device));
+    unsigned char* base = nullptr;
+    TGX_TRY(na_scratch(device, &base));
+    cudaStream_t st = (cudaStream_t)stream;
+
+    uint32_t* counters = (uint32_t*)(base + kNaCounters);
+    tgx_dev_status* status = (tgx_dev_status*)(base + kNaStatus);
+    ViewConst* d_vc = (ViewConst*)(base + kNaViews);
+    unsigned long long** d_outs = (unsigned long long**)(base + kNaViews + ((sizeof(ViewConst) + 15) & ~(size_t)15));
+    float* inv_rot = (float*)(base + kNaInvRot);
+    VisRecord* records = (VisRecord*)(base + kNaRecords);
+    uint2* rects = (uint2*)(base + kNaRects);
+    uint32_t* bucket_cnt = (uint32_t*)(base + kNaBucketCnt);
+    uint32_t* bucket_off = (uint32_t*)(base + kNaBucketOff);
+    uint32_t* tile_total = (uint32_t*)(base + kNaTileTotal);
+    uint32_t* tile_off = (uint32_t*)(base + kNaTileOff);
+    uint32_t* tile_order = (uint32_t*)(base + kNaTileOrder);
+    uint32_t* bins = (uint32_t*)(base + kNaBinsOff);
+
+    // what must start at zero; everything else is written before it is read
+    TGX_CUDA(cudaMemsetAsync(counters, 0, 256, st));
+    TGX_CUDA(cudaMemsetAsync(status, 0, sizeof(tgx_dev_status), st));
+    TGX_CUDA(cudaMemsetAsync(bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, st));
+    unsigned char stage[sizeof(ViewConst) + 32];
+    const size_t ptr_off = (sizeof(ViewConst) + 15) & ~(size_t)15;
+    memcpy(stage, &vc, sizeof(ViewConst));
+    memcpy(stage + ptr_off, &d_visbuf, sizeof(void*));
+    TGX_CUDA(cudaMemcpyAsync(d_vc, stage, ptr_off + sizeof(void*), cudaMemcpyHostToDevice, st));
+
+    int sms = 0;
+    TGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const uint32_t warp_grid = (uint32_t)sms * 8;
+    NA_LAUNCH((n_objects + 127) / 128, 128, k_vis_noalloc_inv_rot, d_objects, n_objects, inv_rot);
+    NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
+              d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
+              kNaMaxClusterPointers, counters, status);
+    NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
+    NA_LAUNCH((n_tiles + 255) / 256, 256, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles);
+    NA_LAUNCH(1, 1024, k_vis_scan, tile_total, tile_off, tile_order, n_tiles, kNaBins, counters);
+    NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, bins,
+              n_tiles, kNaBins, status);
+    NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), records, rects, bins, tile_off, tile_order, d_vc, 1u,
+              d_voxel_bits, inv_rot, d_outs, counters, status);
+    if (out_error) {
+        tgx_dev_status hs;
+        TGX_CUDA(cudaMemcpyAsync(&hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        TGX_CUDA(cudaStreamSynchronize(st));
+        out_error->code = hs.code;
+        out_error->where = hs.where;
+        out_error->detail = hs.detail;
+        if (hs.code) return (tgx_status)hs.code;
+    }
+    return TGX_OK;
+}
+#undef NA_LAUNCH
