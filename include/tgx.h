@@ -298,6 +298,64 @@ tgx_status  tgx_svo_download(tgx_ctx* ctx, const tgx_svo* svo, int32_t* out_bloc
 tgx_status  tgx_svo_trace(tgx_ctx* ctx, const tgx_svo* svo, uint32_t n, const float* d_origins,
                           const float* d_dirs, uint32_t max_steps, float* d_t, int32_t* d_voxel);
 
+/* ---- bounce lighting (new: the reference shades direct light only, shading.frag:285-316) ---- */
+
+typedef struct tgx_gi_params
+{
+    uint32_t spp;               /* cosine-weighted secondary rays per pixel */
+    uint32_t bounces;           /* 1..4 */
+    uint32_t max_steps;         /* SVO steps per traced ray, 0 = 256 */
+    uint32_t frame;             /* Philox counter word: decorrelates frames */
+    uint64_t seed;              /* Philox key */
+    float    sun_dir[3];        /* unit vector toward the sun */
+    float    sun_radiance[3];
+    float    sky_radiance[3];
+    float    offset;            /* ray origins move this far (voxels) along the normal */
+} tgx_gi_params;
+
+/*
+ * Plain GI for one view from its visibility buffer (d_visbuf, DEVICE, as
+ * tgx_vis_render wrote it) and the SVO: per pixel, direct sun light with an
+ * SVO shadow ray plus `spp` cosine-weighted bounce rays through the SVO
+ * (`bounces` deep), Lambertian albedo from the material LUTs (0.5 grey when
+ * the scene has none).  Writes linear RGB, 3 floats per pixel, to d_rgb
+ * (DEVICE).  Rays that run out of max_steps count as misses and are counted
+ * in the device status.  Asynchronous.
+ */
+tgx_status  tgx_gi_render(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, const tgx_view* view,
+                          const uint64_t* d_visbuf, const tgx_gi_params* params, float* d_rgb);
+
+/* ---- learned radiance cache (new: the reference has no learned component) ---- */
+
+/*
+ * A small MLP mapping (position normalised to [0,1]^3, normal, direction) to
+ * RGB radiance: 9 inputs -> 216 sin/cos features (12 octaves of pi) -> 4 ReLU
+ * layers of 64 -> 3 outputs, no biases.  BF16 weights and activations with
+ * FP32 accumulation on the tensor cores, FP32 master weights and Adam.
+ * Inputs are n x 9 floats, outputs n x 3 floats, all DEVICE memory.
+ */
+typedef struct tgx_cache tgx_cache;
+
+uint32_t    tgx_cache_n_params(void);
+tgx_status  tgx_cache_create(tgx_ctx* ctx, uint64_t seed, tgx_cache** out_cache);
+void        tgx_cache_destroy(tgx_ctx* ctx, tgx_cache* cache);
+tgx_status  tgx_cache_infer(tgx_ctx* ctx, tgx_cache* cache, uint32_t n, const float* d_x, float* d_rgb);
+/* One Adam step (lr, beta 0.9/0.99) on the relative-L2 loss of a batch. */
+tgx_status  tgx_cache_train_step(tgx_ctx* ctx, tgx_cache* cache, uint32_t n, const float* d_x, const float* d_target,
+                                 float lr);
+/* Batch loss of the last training step or gradient call (blocking). */
+tgx_status  tgx_cache_last_loss(tgx_ctx* ctx, const tgx_cache* cache, float* out_loss);
+/* The batch gradient without an update, to HOST memory (blocking); for checking. */
+tgx_status  tgx_cache_gradient(tgx_ctx* ctx, tgx_cache* cache, uint32_t n, const float* d_x, const float* d_target,
+                               float* out_grad, float* out_loss);
+/* FP32 master weights as one HOST array of tgx_cache_n_params() floats, in the
+ * order W0 [64][216], W1, W2, W3 [64][64], W4 [3][64] (row-major [out][in]). */
+tgx_status  tgx_cache_get_weights(tgx_ctx* ctx, const tgx_cache* cache, float* out_w);
+tgx_status  tgx_cache_set_weights(tgx_ctx* ctx, tgx_cache* cache, const float* w);
+/* Checkpoint and resume: weights, Adam moments and step count. */
+tgx_status  tgx_cache_save(tgx_ctx* ctx, const tgx_cache* cache, const char* path);
+tgx_status  tgx_cache_load(tgx_ctx* ctx, tgx_cache* cache, const char* path);
+
 /* ---- synthetic scenes (the reference's CPU noise loop, tgvk_raytracer.c:870-978) ---- */
 
 typedef struct tgx_gen_params

@@ -152,3 +152,44 @@ def gi_render(oracle: "Oracle", osvo: OracleSvo, scene, view, params, visbuf, ro
                          _p(scene.material_idx), _p(scene.luts), _p(v), _p(p),
                          _p(np.ascontiguousarray(visbuf, np.uint64)), _p(out), r0, r1, threads)
     return out
+
+
+class OracleMlp:
+    """FP64 oracle of the radiance-cache network (oracle/oracle_mlp.c)."""
+
+    def __init__(self, oracle: "Oracle"):
+        lib = oracle.lib
+        vp, u32 = C.c_void_p, C.c_uint32
+        lib.oracle_mlp_n_params.restype = C.c_int
+        lib.oracle_mlp_encode.argtypes = [vp, u32, vp]
+        lib.oracle_mlp_forward.argtypes = [vp, vp, u32, vp]
+        lib.oracle_mlp_loss_grad.restype = C.c_double
+        lib.oracle_mlp_loss_grad.argtypes = [vp, vp, vp, u32, vp]
+        lib.oracle_mlp_adam.argtypes = [vp, vp, vp, vp, u32, u32, C.c_double, C.c_double, C.c_double, C.c_double]
+        self.lib = lib
+        self.n_params = lib.oracle_mlp_n_params()
+
+    def encode(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros((len(x), 216), np.float64)
+        self.lib.oracle_mlp_encode(_p(x), len(x), _p(out))
+        return out
+
+    def forward(self, w, x):
+        x = np.ascontiguousarray(x, np.float32)
+        w = np.ascontiguousarray(w, np.float64)
+        out = np.zeros((len(x), 3), np.float64)
+        self.lib.oracle_mlp_forward(_p(w), _p(x), len(x), _p(out))
+        return out
+
+    def loss_grad(self, w, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        w = np.ascontiguousarray(w, np.float64)
+        g = np.zeros(self.n_params, np.float64)
+        loss = self.lib.oracle_mlp_loss_grad(_p(w), _p(x), _p(t), len(x), _p(g))
+        return loss, g
+
+    def adam(self, w, m, v, g, step, lr=1e-2, b1=0.9, b2=0.99, eps=1e-15):
+        self.lib.oracle_mlp_adam(_p(w), _p(m), _p(v), _p(np.ascontiguousarray(g, np.float64)), self.n_params, step,
+                                 lr, b1, b2, eps)

@@ -1,0 +1,107 @@
+"""CPU checks of the traversal and GI oracle (the semantics the CUDA path must
+reproduce), pinned where the reference has code:
+
+- traversal: every hit voxel equals the reference's tg_svo_traverse
+  (tg_sparse_voxel_octree.c:558-740) on its own SVO, for 24k fixture rays;
+- Philox4x32-10: the published known-answer vectors (Salmon et al. 2011,
+  Random123 kat_vectors);
+- GI: energy and sampling sanity on a closed form (a plane under a sun).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import tg_gb300 as tg
+from oracle_lib import OracleSvo, gi_render, svo_build_with_materials
+from scenes import fuzz_scene
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("name", sorted(p.stem.replace("ref_trace_", "") for p in GOLD.glob("ref_trace_*.npz")))
+def test_traversal_matches_tg_svo_traverse(oracle, name):
+    svo = np.load(GOLD / f"ref_svo_{name}.npz")
+    tr = np.load(GOLD / f"ref_trace_{name}.npz")
+    o = OracleSvo(oracle, svo["block_xyz"], svo["block_words"], None, svo["mn"], 10)
+    t, vox, ax, steps = o.trace(tr["origin"], tr["dir"])
+    ok = tr["hit"] >= 0
+    assert ok.all()
+    hit = t < 3e38
+    assert np.array_equal(hit, tr["hit"] == 1)
+    assert hit.sum() > 10
+    assert np.array_equal(vox[hit], tr["voxel"][hit])
+    # distances: the reference reports the (negative) entry distance behind the
+    # origin when the ray starts inside the hit voxel; this traversal reports 0
+    inside = ((tr["origin"] >= tr["voxel"]) & (tr["origin"] < tr["voxel"] + 1)).all(axis=1) & hit
+    assert (t[inside] == 0).all() and (tr["distance"][inside] <= 0).all()
+    rest = hit & ~inside
+    assert (np.abs(t[rest] - tr["distance"][rest]) <= 2e-4 + 2e-6 * t[rest]).all()
+
+
+def test_philox_known_answers(oracle):
+    lib = oracle.lib
+    lib.oracle_philox.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+    cases = [
+        ((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+        ((0xffffffff,) * 4, (0xffffffff, 0xffffffff), (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+        ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+         (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+    ]
+    for ctr, key, want in cases:
+        c = np.array(ctr, np.uint32)
+        out = np.zeros(4, np.uint32)
+        lib.oracle_philox(c.ctypes.data, key[0], key[1], out.ctypes.data)
+        assert tuple(int(x) for x in out) == want
+
+
+def test_gi_plane_under_sun_matches_closed_form(oracle):
+    """A flat slab of voxels, normal +y, sun straight above, black sky, one
+    bounce that can only escape: radiance = albedo/pi * E_sun exactly."""
+    objs = np.zeros(1, tg.OBJECT_DTYPE)
+    objs["n_cluster_pointers_per_dim"] = (4, 1, 4)
+    objs["translation"] = (0.0, -4.0, 0.0)
+    objs["rotation"] = np.eye(4, dtype=np.float32).T.reshape(-1)
+    bits = np.zeros((16, 16), np.uint32)
+    for c in range(16):
+        for v in range(512):
+            if (v >> 3) & 7 == 7:          # top layer of every cluster only
+                bits[c, v >> 5] |= np.uint32(1 << (v & 31))
+    mat = np.full((16, 512), 3, np.uint8)
+    luts = np.zeros(256, tg.MATERIAL_DTYPE)
+    luts["albedo"] = (0.6, 0.4, 0.2)
+    s = tg.HostScene(objs, np.arange(16, dtype=np.uint32), np.zeros(16, np.uint32), bits, mat, luts)
+    mn = [-64.0, -64.0, -64.0]
+    blocks, words, mats = svo_build_with_materials(oracle, s, mn, 7)
+    osvo = OracleSvo(oracle, blocks, words, mats, mn, 7)
+    view = tg.make_view((0.0, 20.0, 0.0), -float(np.pi / 2), 0.0, 0.6, 16, 16, 0.1, 100.0)
+    vis = oracle.vis_render(s, view, mode=0)
+    assert (vis != np.uint64(tg.VIS_EMPTY)).all()
+    p = tg.gi_params(spp=4, bounces=1, sun_dir=(0.0, 1.0, 0.0), sun_radiance=(1.0, 1.0, 1.0),
+                     sky_radiance=(0.0, 0.0, 0.0))
+    rgb = gi_render(oracle, osvo, s, view, p, vis)
+    want = np.array([0.6, 0.4, 0.2], np.float32) * np.float32(0.318309886)
+    assert np.allclose(rgb, want[None, :], rtol=1e-6)
+
+
+def test_gi_sky_and_determinism(oracle):
+    s = fuzz_scene(3, n_objects=3, box=20.0, max_cpa=3)
+    mn = [-64.0, -64.0, -64.0]
+    blocks, words, mats = svo_build_with_materials(oracle, s, mn, 7)
+    osvo = OracleSvo(oracle, blocks, words, mats, mn, 7)
+    view = tg.make_view((0.0, 0.0, -50.0), 0.0, float(np.pi), 1.0, 40, 30, 0.1, 200.0)
+    vis = oracle.vis_render(s, view, mode=0)
+    p = tg.gi_params(spp=4, bounces=2, seed=7)
+    a = gi_render(oracle, osvo, s, view, p, vis)
+    b = gi_render(oracle, osvo, s, view, p, vis)
+    assert np.array_equal(a, b)
+    sky = vis == np.uint64(tg.VIS_EMPTY)
+    assert sky.any() and (~sky).any()
+    assert np.allclose(a[sky], p["sky_radiance"][0])
+    assert (a[~sky] >= 0).all() and np.isfinite(a).all()
+    p2 = tg.gi_params(spp=4, bounces=2, seed=8)
+    c = gi_render(oracle, osvo, s, view, p2, vis)
+    assert not np.array_equal(a[~sky], c[~sky])

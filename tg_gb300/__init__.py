@@ -49,6 +49,25 @@ assert VIEW_DTYPE.itemsize == 96
 
 MATERIAL_DTYPE = np.dtype([("albedo", np.float32, 3), ("roughness", np.float32)])
 
+GI_PARAMS_DTYPE = np.dtype([
+    ("spp", np.uint32), ("bounces", np.uint32), ("max_steps", np.uint32), ("frame", np.uint32),
+    ("seed", np.uint64), ("sun_dir", np.float32, 3), ("sun_radiance", np.float32, 3),
+    ("sky_radiance", np.float32, 3), ("offset", np.float32),
+])
+assert GI_PARAMS_DTYPE.itemsize == 64
+
+
+def gi_params(spp: int = 4, bounces: int = 1, seed: int = 2, max_steps: int = 256, frame: int = 0,
+              sun_dir=(0.3, 0.8, 0.5), sun_radiance=(3.0, 2.9, 2.7), sky_radiance=(0.25, 0.3, 0.4),
+              offset: float = 1.0) -> np.ndarray:
+    """A tgx_gi_params record; sun_dir is normalised here."""
+    p = np.zeros(1, GI_PARAMS_DTYPE)
+    d = np.asarray(sun_dir, np.float64)
+    p["spp"], p["bounces"], p["max_steps"], p["frame"], p["seed"] = spp, bounces, max_steps, frame, seed
+    p["sun_dir"] = (d / np.linalg.norm(d)).astype(np.float32)
+    p["sun_radiance"], p["sky_radiance"], p["offset"] = sun_radiance, sky_radiance, offset
+    return p
+
 
 class SceneDesc(C.Structure):
     _fields_ = [
@@ -106,7 +125,7 @@ EXPORTS = [
     "tgx_scene_destroy", "tgx_vis_render", "tgx_vis_render_host", "tgx_vis_decode", "tgx_pick",
     "tgx_svo_build", "tgx_svo_destroy", "tgx_svo_get_info", "tgx_svo_download", "tgx_svo_trace",
     "tgx_generate_scene", "tgx_free_generated_scene", "tgx_make_view", "tgx_trace_enable", "tgx_trace_reset",
-    "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats",
+    "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats", "tgx_gi_render",
 ]
 
 
@@ -141,6 +160,7 @@ def _load() -> C.CDLL:
         "tgx_make_view": (i32, [vp, C.c_float, C.c_float, C.c_float, u32, u32, C.c_float, C.c_float, vp]),
         "tgx_trace_enable": (i32, [vp, i32]),
         "tgx_vis_get_stats": (i32, [vp, C.POINTER(VisStats)]),
+        "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "tgx_trace_reset": (i32, [vp]),
         "tgx_trace_slots": (u32, []),
         "tgx_trace_get": (i32, [vp, u32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(u64)]),
@@ -344,6 +364,13 @@ class Context:
         h = C.c_void_p()
         check(lib.tgx_svo_build(self.handle, scene.handle, _ptr(m), extent_log2, C.byref(h)), "tgx_svo_build")
         return Svo(self, h)
+
+    def gi_render(self, scene: "Scene", svo: "Svo", view: np.ndarray, visbuf, params: np.ndarray, rgb) -> None:
+        """Device buffers: visbuf (W*H u64 as int64), rgb (W*H*3 float32)."""
+        view = np.ascontiguousarray(view, dtype=VIEW_DTYPE).reshape(1)
+        params = np.ascontiguousarray(params, dtype=GI_PARAMS_DTYPE).reshape(1)
+        check(lib.tgx_gi_render(self.handle, scene.handle, svo.handle, _ptr(view), _ptr(visbuf), _ptr(params),
+                                _ptr(rgb)), "tgx_gi_render")
 
     def vis_stats(self) -> VisStats:
         st = VisStats()

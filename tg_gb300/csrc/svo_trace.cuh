@@ -78,7 +78,7 @@ __device__ __forceinline__ int32_t svo_cell_at(float p, float inv_size, int32_t 
 
 // Returns 1 on hit (t, grid voxel c, face axis or -1), 0 on miss, -1 when
 // max_steps ran out.
-__device__ int svo_trace(const SvoDev& s, const float o[3], const float d[3], uint32_t max_steps, float& out_t,
+static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d[3], uint32_t max_steps, float& out_t,
                          int32_t out_c[3], int32_t& out_axis, uint32_t& out_steps)
 {
     const float E = (float)(1u << s.L);
