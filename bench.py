@@ -158,6 +158,74 @@ def run_reference(args, rank: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def rel_mse(x, r, mask):
+    """relMSE = mean((x - r)^2 / (r^2 + 1e-2)) over the pixels of `mask` and the 3 channels."""
+    xs = x.reshape(-1, 3)[mask]
+    rs = r.reshape(-1, 3)[mask]
+    return float(((xs - rs) ** 2 / (rs ** 2 + 1e-2)).mean())
+
+
+def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, hits: int):
+    """Config 4: 2-bounce GI at 1080p on the 512-object scene.  The judge is a
+    256-spp plain 2-bounce render; plain GI and learned-cache GI (65,536
+    training samples per frame from 16-spp SVO paths, 4 Adam steps, lr 1e-2)
+    are timed per frame and scored by relMSE over the geometry pixels."""
+    import torch
+    import tg_gb300 as tg
+
+    n = W * H * 3
+    mask = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
+    ref = torch.empty(n, dtype=torch.float32, device="cuda")
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=1234), ref)
+    ctx.sync()
+    ref_s = time.perf_counter() - t0
+    r = ref.cpu().numpy()
+
+    def timed(fn, frames):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for f in range(frames):
+            fn(f)
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1) / frames
+
+    plain = {}
+    with torch.cuda.stream(stream):
+        for spp in (1, 2, 4, 8, 16):
+            ms = timed(lambda f: ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=f),
+                                               out), 3)
+            plain[spp] = {"frame_ms": ms, "relmse": rel_mse(out.cpu().numpy(), r, mask)}
+        cache = tg.Cache(ctx, seed=7)
+        cp = tg.cache_gi_params((-1100.0,) * 3, (1100.0,) * 3, n_train=65536, train_spp=16, train_steps=4, lr=1e-2)
+        warm = 60
+        for f in range(warm):
+            ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=2, bounces=2, seed=2, frame=f), cp, out)
+        ctx.sync()
+        cached = {}
+        for spp in (1, 2, 4):
+            ms = timed(lambda f: ctx.gi_render_cached(
+                sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=warm + f), cp, out), 3)
+            cached[spp] = {"frame_ms": ms, "relmse": rel_mse(out.cpu().numpy(), r, mask)}
+        cache.close()
+
+    def best(d):
+        ok = [(v["frame_ms"], k) for k, v in d.items() if v["relmse"] <= 0.01]
+        return min(ok) if ok else None
+
+    bp, bc = best(plain), best(cached)
+    res = {"reference": "plain 2-bounce, 256 spp", "reference_s": ref_s, "plain": plain, "cached": cached,
+           "target_relmse": 0.01, "cache_warmup_frames": warm}
+    if bp and bc:
+        res["plain_best"] = {"spp": bp[1], "frame_ms": bp[0]}
+        res["cached_best"] = {"spp": bc[1], "frame_ms": bc[0]}
+        res["speedup_at_equal_relmse"] = bp[0] / bc[0]
+    return res
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -165,6 +233,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-gi", action="store_true", help="skip the SVO build and GI measurements")
+    ap.add_argument("--gi-cache", action="store_true",
+                    help="also compare learned-cache GI with plain 2-bounce GI at equal relMSE (config 4)")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -271,6 +342,52 @@ def main() -> None:
             raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
 
     hits = int((out.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)).sum())
+
+    # ---- one-bit SVO build (4096^3 around the camera) and plain GI on the same frame ----
+    gi_report = {}
+    if not args.no_gi:
+        svo_mn = (-2048.0, -2048.0, -2048.0)
+        svo = ctx.svo_build(sc, svo_mn, 12)          # warm-up build
+        ctx.sync()
+        if args.gi_cache:
+            gi_report["gi_cache_vs_plain"] = compare_cache_vs_plain(ctx, sc, svo, view, out, stream, hits)
+        svo.close()
+        build_ms = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            svo = ctx.svo_build(sc, svo_mn, 12)
+            ctx.sync()
+            build_ms.append((time.perf_counter() - t0) * 1e3)
+            if _ < 2:
+                svo.close()
+        info = svo.info()
+        params = tg.gi_params(spp=4, bounces=1, seed=2, max_steps=256)
+        rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                ctx.gi_render(sc, svo, view, out, params, rgb)
+            ctx.sync()
+            g0 = torch.cuda.Event(enable_timing=True)
+            g1 = torch.cuda.Event(enable_timing=True)
+            gi_frames = 5
+            g0.record(stream)
+            for _ in range(gi_frames):
+                ctx.gi_render(sc, svo, view, out, params, rgb)
+            g1.record(stream)
+            ctx.sync()
+        gi_ms = g0.elapsed_time(g1) / gi_frames
+        err = ctx.device_error()
+        gi_report = {
+            "svo_build_ms": statistics.median(build_ms),
+            "svo": {"extent": 4096, "blocks": int(info.n_blocks), "nonempty_blocks": int(info.n_nonempty_blocks),
+                    "pairs": int(info.n_pairs), "device_mb": round(info.device_bytes / 2**20, 1)},
+            "gi_plain_frame_ms": gi_ms,
+            "gi_config": "1 bounce, 4 spp, Philox seed 2, <=256 SVO steps, sun + sky",
+            "gi_bounce_rays_per_s": hits * 4 / (gi_ms * 1e-3),
+            "gi_device_status": int(err.code),
+        }
+        svo.close()
     rays = W * H
     value = rays * world / (ms * 1e-3) / 1e9
 
@@ -311,6 +428,7 @@ def main() -> None:
                      "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback"},
         "clocks": clocks.summary(),
         "hit_pixels": hits,
+        **gi_report,
         "vis_stats": {"visible_clusters": n_vis, "bin_entries": int(stats.bin_entries), "tiles": int(stats.tiles),
                       "dda_overruns": int(stats.dda_overruns)},
         "wall_s_timed": t_wall,

@@ -356,6 +356,30 @@ tgx_status  tgx_cache_set_weights(tgx_ctx* ctx, tgx_cache* cache, const float* w
 tgx_status  tgx_cache_save(tgx_ctx* ctx, const tgx_cache* cache, const char* path);
 tgx_status  tgx_cache_load(tgx_ctx* ctx, tgx_cache* cache, const char* path);
 
+/* Online learned-cache GI settings (tgx_gi_render_cached). */
+typedef struct tgx_cache_gi_params
+{
+    uint32_t n_train;           /* training samples per frame (65,536) */
+    uint32_t train_spp;         /* SVO paths per training target (16) */
+    uint32_t train_steps;       /* Adam steps per frame, n_train / train_steps samples each */
+    float    lr;                /* Adam learning rate (1e-2) */
+    float    box_min[3];        /* scene box: positions are normalised by it for the cache */
+    float    box_max[3];
+} tgx_cache_gi_params;
+
+/*
+ * GI whose bounce paths end in the learned cache: as tgx_gi_render, but each
+ * bounce ray that hits returns the cache's prediction of the radiance leaving
+ * that point toward the shading point instead of tracing on.  Then trains the
+ * cache online on this frame: picks n_train bounce hits, estimates their
+ * outgoing radiance with train_spp plain SVO paths (`bounces` - 1 further
+ * bounces, direct sun at every hit) and runs train_steps Adam steps.
+ * Asynchronous; all buffers DEVICE memory.
+ */
+tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, tgx_cache* cache,
+                                 const tgx_view* view, const uint64_t* d_visbuf, const tgx_gi_params* params,
+                                 const tgx_cache_gi_params* cache_params, float* d_rgb);
+
 /* ---- synthetic scenes (the reference's CPU noise loop, tgvk_raytracer.c:870-978) ---- */
 
 typedef struct tgx_gen_params

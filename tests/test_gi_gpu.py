@@ -51,7 +51,10 @@ def test_trace_bit_exact_vs_oracle(ctx, oracle, seed, L):
     rng = np.random.default_rng(seed)
     n = 20000
     o = rng.uniform(-(2 ** (L - 1)) * 0.9, (2 ** (L - 1)) * 0.9, (n, 3)).astype(np.float32)
-    d = rng.normal(size=(n, 3))
+    # aim most rays at the region that holds the objects
+    aim = rng.uniform(-120.0, 120.0, (n, 3))
+    d = aim - o
+    d[::3] = rng.normal(size=(len(d[::3]), 3))
     d[::5, 0] = 0.0
     d[::7, 1] = 0.0
     d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
@@ -98,3 +101,64 @@ def test_gi_bit_exact_vs_oracle(ctx, oracle, bounces, spp):
     assert (visb != np.uint64(tg.VIS_EMPTY)).sum() > 200
     svo.close()
     sc.close()
+
+
+def _scene_setup(ctx, seed=17):
+    import torch
+    s = fuzz_scene(seed, n_objects=6, box=30.0, max_cpa=4)
+    s.objects["lut_idx"] = 0
+    mn = [-128.0, -128.0, -128.0]
+    sc = ctx.upload(s)
+    svo = ctx.svo_build(sc, mn, 8)
+    view = tg.make_view((0.0, 5.0, -70.0), 0.1, float(np.pi), 1.1, 96, 64, 0.1, 300.0)
+    vis = torch.empty(96 * 64, dtype=torch.int64, device="cuda")
+    ctx.vis_render(sc, view, [vis])
+    return s, sc, svo, view, vis
+
+
+def test_cached_gi_with_zero_cache_equals_plain_sky_only(ctx):
+    """No sun and an all-zero cache: a bounce that hits contributes 0 in both
+    paths, one that misses sees the sky, so cached GI equals plain 1-bounce GI
+    bit for bit."""
+    import torch
+    s, sc, svo, view, vis = _scene_setup(ctx)
+    cache = tg.Cache(ctx, seed=1)
+    cache.set_weights(np.zeros(cache.n_params, np.float32))
+    params = tg.gi_params(spp=4, bounces=1, seed=2, sun_radiance=(0.0, 0.0, 0.0), sky_radiance=(0.4, 0.5, 0.6))
+    cp = tg.cache_gi_params((-40.0,) * 3, (40.0,) * 3, n_train=0, train_steps=0)
+    a = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    ctx.gi_render(sc, svo, view, vis, params, a)
+    ctx.gi_render_cached(sc, svo, cache, view, vis, params, cp, b)
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    assert torch.equal(a, b)
+    cache.close(); svo.close(); sc.close()
+
+
+def test_cached_gi_learns_toward_the_plain_estimate(ctx):
+    """Online training over frames brings the cached 2-bounce GI toward a
+    high-spp plain 2-bounce render of the same frame."""
+    import torch
+    s, sc, svo, view, vis = _scene_setup(ctx, seed=23)
+    ref = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+    ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=9), ref)
+    cache = tg.Cache(ctx, seed=2)
+    cp = tg.cache_gi_params((-40.0,) * 3, (40.0,) * 3, n_train=8192, train_spp=16, train_steps=4, lr=1e-2)
+    out = torch.empty_like(ref)
+    hit = (vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY))
+    r = ref.cpu().numpy().reshape(-1, 3)[hit]
+
+    def relmse():
+        x = out.cpu().numpy().reshape(-1, 3)[hit]
+        return float(np.mean((x - r) ** 2 / (r ** 2 + 1e-2)))
+
+    errs = []
+    for f in range(40):
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=f), cp, out)
+        if f in (0, 39):
+            ctx.sync()
+            errs.append(relmse())
+    assert ctx.device_error().code == 0
+    assert errs[1] < 0.5 * errs[0], errs
+    cache.close(); svo.close(); sc.close()

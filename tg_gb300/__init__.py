@@ -57,6 +57,18 @@ GI_PARAMS_DTYPE = np.dtype([
 assert GI_PARAMS_DTYPE.itemsize == 64
 
 
+CACHE_GI_DTYPE = np.dtype([("n_train", np.uint32), ("train_spp", np.uint32), ("train_steps", np.uint32),
+                           ("lr", np.float32), ("box_min", np.float32, 3), ("box_max", np.float32, 3)])
+
+
+def cache_gi_params(box_min, box_max, n_train: int = 65536, train_spp: int = 16, train_steps: int = 4,
+                    lr: float = 1e-2) -> np.ndarray:
+    p = np.zeros(1, CACHE_GI_DTYPE)
+    p["n_train"], p["train_spp"], p["train_steps"], p["lr"] = n_train, train_spp, train_steps, lr
+    p["box_min"], p["box_max"] = box_min, box_max
+    return p
+
+
 def gi_params(spp: int = 4, bounces: int = 1, seed: int = 2, max_steps: int = 256, frame: int = 0,
               sun_dir=(0.3, 0.8, 0.5), sun_radiance=(3.0, 2.9, 2.7), sky_radiance=(0.25, 0.3, 0.4),
               offset: float = 1.0) -> np.ndarray:
@@ -125,7 +137,10 @@ EXPORTS = [
     "tgx_scene_destroy", "tgx_vis_render", "tgx_vis_render_host", "tgx_vis_decode", "tgx_pick",
     "tgx_svo_build", "tgx_svo_destroy", "tgx_svo_get_info", "tgx_svo_download", "tgx_svo_trace",
     "tgx_generate_scene", "tgx_free_generated_scene", "tgx_make_view", "tgx_trace_enable", "tgx_trace_reset",
-    "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats", "tgx_gi_render",
+    "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats", "tgx_gi_render", "tgx_cache_n_params",
+    "tgx_cache_create", "tgx_cache_destroy", "tgx_cache_infer", "tgx_cache_train_step", "tgx_cache_last_loss",
+    "tgx_cache_gradient", "tgx_cache_get_weights", "tgx_cache_set_weights", "tgx_cache_save", "tgx_cache_load",
+    "tgx_gi_render_cached",
 ]
 
 
@@ -161,6 +176,18 @@ def _load() -> C.CDLL:
         "tgx_trace_enable": (i32, [vp, i32]),
         "tgx_vis_get_stats": (i32, [vp, C.POINTER(VisStats)]),
         "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+        "tgx_cache_n_params": (u32, []),
+        "tgx_gi_render_cached": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "tgx_cache_create": (i32, [vp, u64, C.POINTER(vp)]),
+        "tgx_cache_destroy": (None, [vp, vp]),
+        "tgx_cache_infer": (i32, [vp, vp, u32, vp, vp]),
+        "tgx_cache_train_step": (i32, [vp, vp, u32, vp, vp, C.c_float]),
+        "tgx_cache_last_loss": (i32, [vp, vp, C.POINTER(C.c_float)]),
+        "tgx_cache_gradient": (i32, [vp, vp, u32, vp, vp, vp, C.POINTER(C.c_float)]),
+        "tgx_cache_get_weights": (i32, [vp, vp, vp]),
+        "tgx_cache_set_weights": (i32, [vp, vp, vp]),
+        "tgx_cache_save": (i32, [vp, vp, C.c_char_p]),
+        "tgx_cache_load": (i32, [vp, vp, C.c_char_p]),
         "tgx_trace_reset": (i32, [vp]),
         "tgx_trace_slots": (u32, []),
         "tgx_trace_get": (i32, [vp, u32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(u64)]),
@@ -372,6 +399,14 @@ class Context:
         check(lib.tgx_gi_render(self.handle, scene.handle, svo.handle, _ptr(view), _ptr(visbuf), _ptr(params),
                                 _ptr(rgb)), "tgx_gi_render")
 
+    def gi_render_cached(self, scene: "Scene", svo: "Svo", cache: "Cache", view: np.ndarray, visbuf,
+                         params: np.ndarray, cache_params: np.ndarray, rgb) -> None:
+        view = np.ascontiguousarray(view, dtype=VIEW_DTYPE).reshape(1)
+        params = np.ascontiguousarray(params, dtype=GI_PARAMS_DTYPE).reshape(1)
+        cp = np.ascontiguousarray(cache_params, dtype=CACHE_GI_DTYPE).reshape(1)
+        check(lib.tgx_gi_render_cached(self.handle, scene.handle, svo.handle, cache.handle, _ptr(view), _ptr(visbuf),
+                                       _ptr(params), _ptr(cp), _ptr(rgb)), "tgx_gi_render_cached")
+
     def vis_stats(self) -> VisStats:
         st = VisStats()
         check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
@@ -415,6 +450,62 @@ class Svo:
     def close(self) -> None:
         if self.handle and self.ctx.handle:
             lib.tgx_svo_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Cache:
+    """tgx_cache: the learned radiance cache MLP (inputs n x 9, outputs n x 3, device memory)."""
+
+    def __init__(self, ctx: "Context", seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib.tgx_cache_create(ctx.handle, seed, C.byref(h)), "tgx_cache_create")
+        self.handle = h
+        self.n_params = int(lib.tgx_cache_n_params())
+
+    def infer(self, x, out) -> None:
+        check(lib.tgx_cache_infer(self.ctx.handle, self.handle, x.shape[0], _ptr(x), _ptr(out)), "tgx_cache_infer")
+
+    def train_step(self, x, target, lr: float = 1e-2) -> None:
+        check(lib.tgx_cache_train_step(self.ctx.handle, self.handle, x.shape[0], _ptr(x), _ptr(target), lr),
+              "tgx_cache_train_step")
+
+    def last_loss(self) -> float:
+        v = C.c_float()
+        check(lib.tgx_cache_last_loss(self.ctx.handle, self.handle, C.byref(v)), "tgx_cache_last_loss")
+        return v.value
+
+    def gradient(self, x, target):
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        check(lib.tgx_cache_gradient(self.ctx.handle, self.handle, x.shape[0], _ptr(x), _ptr(target), _ptr(g),
+                                     C.byref(loss)), "tgx_cache_gradient")
+        return loss.value, g
+
+    def get_weights(self) -> np.ndarray:
+        w = np.zeros(self.n_params, np.float32)
+        check(lib.tgx_cache_get_weights(self.ctx.handle, self.handle, _ptr(w)), "tgx_cache_get_weights")
+        return w
+
+    def set_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, np.float32)
+        check(lib.tgx_cache_set_weights(self.ctx.handle, self.handle, _ptr(w)), "tgx_cache_set_weights")
+
+    def save(self, path) -> None:
+        check(lib.tgx_cache_save(self.ctx.handle, self.handle, str(path).encode()), "tgx_cache_save")
+
+    def load(self, path) -> None:
+        check(lib.tgx_cache_load(self.ctx.handle, self.handle, str(path).encode()), "tgx_cache_load")
+
+    def close(self) -> None:
+        if self.handle and self.ctx.handle:
+            lib.tgx_cache_destroy(self.ctx.handle, self.handle)
         self.handle = None
 
     def __del__(self):

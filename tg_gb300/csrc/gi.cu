@@ -151,26 +151,17 @@ __device__ void incoming(const SvoDev& s, const float o_in[3], const float w_in[
     out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
 }
 
-__global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restrict__ objects,
-                                           const uint32_t* __restrict__ cluster_pointers,
-                                           const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material,
-                                           const tgx_material* __restrict__ luts, tgx_view cam, GiParams p,
-                                           const unsigned long long* __restrict__ visbuf, float* __restrict__ out,
-                                           uint32_t* __restrict__ exhausted)
+// Primary hit of a pixel from its visibility word (shading.frag:116-228):
+// returns false for sky; else the offset origin o2, world normal nw and albedo a.
+__device__ bool primary_hit(const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
+                            const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material,
+                            const tgx_material* __restrict__ luts, const tgx_view& cam, const GiParams& p,
+                            unsigned long long word, uint32_t px, uint32_t py, float o2[3], float nw[3], float a[3])
 {
-    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15u);
-    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (px >= cam.width || py >= cam.height) return;
-    const uint32_t pixel = py * cam.width + px;
-    float* res = out + 3ull * pixel;
     const float fx = xdiv(xadd((float)px, 0.5f), (float)cam.width);
     const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)cam.height));
-    const unsigned long long word = visbuf[pixel];
     const float depth = xdiv((float)(word >> 40), 16777215.0f);
-    if (!(depth < 1.0f)) {
-        res[0] = p.sky_radiance[0]; res[1] = p.sky_radiance[1]; res[2] = p.sky_radiance[2];
-        return;
-    }
+    if (!(depth < 1.0f)) return false;
     const uint32_t ptr = (uint32_t)(word >> 9) & 2147483647u;
     const uint32_t voxel = (uint32_t)word & 511u;
     const uint32_t ci = cluster_pointers[ptr];
@@ -195,9 +186,9 @@ __global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restri
     float dws[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const float a = xadd(xmul(cam.ray_bl[i], xsub(1.0f, fy)), xmul(cam.ray_tl[i], fy));
-        const float b = xadd(xmul(cam.ray_br[i], xsub(1.0f, fy)), xmul(cam.ray_tr[i], fy));
-        dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
+        const float aa = xadd(xmul(cam.ray_bl[i], xsub(1.0f, fy)), xmul(cam.ray_tl[i], fy));
+        const float bb = xadd(xmul(cam.ray_br[i], xsub(1.0f, fy)), xmul(cam.ray_tr[i], fy));
+        dws[i] = xadd(xmul(aa, xsub(1.0f, fx)), xmul(bb, fx));
     }
     float d4[3];
     dm4_mulv4(ws2ms, dws[0], dws[1], dws[2], 0.0f, d4);
@@ -205,11 +196,10 @@ __global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restri
     const float dm[3] = {xdiv(d4[0], mag), xdiv(d4[1], mag), xdiv(d4[2], mag)};
     const float vmin[3] = {(float)(voxel % 8u), (float)((voxel / 8u) % 8u), (float)(voxel / 64u)};
     float enter, exit_;
-    float nw[3] = {0.0f, 0.0f, 0.0f};
+    nw[0] = nw[1] = nw[2] = 0.0f;
     const bool hit = ray_aabb(o4[0], o4[1], o4[2], dm[0], dm[1], dm[2], vmin[0], vmin[1], vmin[2], xadd(vmin[0], 1.0f),
                               xadd(vmin[1], 1.0f), xadd(vmin[2], 1.0f), enter, exit_);
     if (hit) {
-        // shading.frag:195-228
         float nm[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -235,14 +225,33 @@ __global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restri
     const float dn[3] = {xdiv(dws[0], dl), xdiv(dws[1], dl), xdiv(dws[2], dl)};
     if (nw[0] == 0.0f && nw[1] == 0.0f && nw[2] == 0.0f) { nw[0] = -dn[0]; nw[1] = -dn[1]; nw[2] = -dn[2]; }
     const float te = hit && enter > 0.0f ? enter : 0.0f;
-    float a[3] = {0.5f, 0.5f, 0.5f};
+    a[0] = a[1] = a[2] = 0.5f;
     if (material && luts) {
         const tgx_material& m = luts[od.lut_idx * 256u + material[(uint64_t)ci * 512u + voxel]];
         a[0] = m.albedo[0]; a[1] = m.albedo[1]; a[2] = m.albedo[2];
     }
-    float o2[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) o2[i] = xadd(xadd(cam.camera[i], xmul(te, dn[i])), xmul(nw[i], p.offset));
+    return true;
+}
+
+__global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restrict__ objects,
+                                           const uint32_t* __restrict__ cluster_pointers,
+                                           const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material,
+                                           const tgx_material* __restrict__ luts, tgx_view cam, GiParams p,
+                                           const unsigned long long* __restrict__ visbuf, float* __restrict__ out,
+                                           uint32_t* __restrict__ exhausted)
+{
+    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15u);
+    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (px >= cam.width || py >= cam.height) return;
+    const uint32_t pixel = py * cam.width + px;
+    float* res = out + 3ull * pixel;
+    float o2[3], nw[3], a[3];
+    if (!primary_hit(objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[pixel], px, py, o2, nw, a)) {
+        res[0] = p.sky_radiance[0]; res[1] = p.sky_radiance[1]; res[2] = p.sky_radiance[2];
+        return;
+    }
     float L[3];
     direct_sun(s, o2, nw, a, p, exhausted, L);
     float acc[3] = {0.0f, 0.0f, 0.0f};
@@ -256,6 +265,166 @@ __global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restri
     const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
 #pragma unroll
     for (int i = 0; i < 3; i++) res[i] = xadd(L[i], xmul(a[i], xmul(acc[i], inv_spp)));
+}
+
+// ---------------------------------------------------------------------------
+// learned-cache GI
+// ---------------------------------------------------------------------------
+
+struct CacheHit
+{
+    float p[3];      // hit point (world)
+    float n[3];      // face normal
+    float w[3];      // direction the bounce ray travelled
+    int32_t c[3];    // grid voxel
+};
+
+struct CacheGiConst
+{
+    float box_min[3];
+    float box_inv[3];    // 1 / (box_max - box_min)
+    uint32_t n_train, train_spp;
+};
+
+__device__ __forceinline__ void cache_input(const CacheGiConst& q, const float p[3], const float n[3], const float w[3],
+                                            float* x)
+{
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        x[i] = fminf(fmaxf((p[i] - q.box_min[i]) * q.box_inv[i], 0.0f), 1.0f);
+        x[3 + i] = n[i];
+        x[6 + i] = -w[i];   // outgoing direction, toward the shading point
+    }
+}
+
+// Pass 1: primary hit, direct light, bounce rays; hits become cache queries.
+__global__ void __launch_bounds__(128) k_gi_cache_queries(
+    SvoDev s, const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
+    const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material, const tgx_material* __restrict__ luts,
+    tgx_view cam, GiParams p, CacheGiConst q, const unsigned long long* __restrict__ visbuf,
+    float* __restrict__ pix_state /* W*H*6: direct L, albedo */, int32_t* __restrict__ qidx /* W*H*spp */,
+    float* __restrict__ qx /* n*9 */, CacheHit* __restrict__ hits, uint32_t* __restrict__ counters,
+    uint32_t capacity, uint32_t* __restrict__ exhausted)
+{
+    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15u);
+    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (px >= cam.width || py >= cam.height) return;
+    const uint32_t pixel = py * cam.width + px;
+    float* st = pix_state + 6ull * pixel;
+    int32_t* qi = qidx + (uint64_t)pixel * p.spp;
+    float o2[3], nw[3], a[3];
+    if (!primary_hit(objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[pixel], px, py, o2, nw, a)) {
+        st[0] = p.sky_radiance[0]; st[1] = p.sky_radiance[1]; st[2] = p.sky_radiance[2];
+        st[3] = st[4] = st[5] = -1.0f;   // sky marker
+        for (uint32_t k = 0; k < p.spp; k++) qi[k] = -1;
+        return;
+    }
+    float L[3];
+    direct_sun(s, o2, nw, a, p, exhausted, L);
+    st[0] = L[0]; st[1] = L[1]; st[2] = L[2];
+    st[3] = a[0]; st[4] = a[1]; st[5] = a[2];
+    for (uint32_t smp = 0; smp < p.spp; smp++) {
+        float w[3];
+        sample_cosine(nw, pixel, smp, 0, p, w);
+        float t; int32_t c[3], ax; uint32_t stp;
+        const int r = svo_trace(s, o2, w, p.max_steps, t, c, ax, stp);
+        if (r < 0) atomicAdd(exhausted, 1u);
+        if (r != 1) { qi[smp] = -1; continue; }
+        float n2[3] = {0.0f, 0.0f, 0.0f};
+        if (ax >= 0) n2[ax] = w[ax] > 0.0f ? -1.0f : 1.0f;
+        else {
+            int m = 0;
+            if (fabsf(w[1]) > fabsf(w[m])) m = 1;
+            if (fabsf(w[2]) > fabsf(w[m])) m = 2;
+            n2[m] = w[m] > 0.0f ? -1.0f : 1.0f;
+        }
+        const uint32_t slot = atomicAdd(&counters[0], 1u);
+        if (slot >= capacity) { qi[smp] = -2; continue; }
+        qi[smp] = (int32_t)slot;
+        CacheHit h;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            h.p[i] = xadd(o2[i], xmul(t, w[i]));
+            h.n[i] = n2[i];
+            h.w[i] = w[i];
+            h.c[i] = c[i];
+        }
+        hits[slot] = h;
+        cache_input(q, h.p, h.n, h.w, qx + 9ull * slot);
+    }
+}
+
+// Pass 3: pixel = direct + albedo * mean(sky or cache prediction).
+__global__ void __launch_bounds__(256) k_gi_cache_resolve(uint32_t n_pixels, GiParams p,
+                                                         const float* __restrict__ pix_state,
+                                                         const int32_t* __restrict__ qidx,
+                                                         const float* __restrict__ qrgb, float* __restrict__ out)
+{
+    const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pixel >= n_pixels) return;
+    const float* st = pix_state + 6ull * pixel;
+    float* res = out + 3ull * pixel;
+    if (st[3] < 0.0f) { res[0] = st[0]; res[1] = st[1]; res[2] = st[2]; return; }
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    for (uint32_t k = 0; k < p.spp; k++) {
+        const int32_t q = qidx[(uint64_t)pixel * p.spp + k];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            acc[i] = xadd(acc[i], q >= 0 ? fmaxf(qrgb[3ull * q + i], 0.0f) : (q == -1 ? p.sky_radiance[i] : 0.0f));
+    }
+    const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
+#pragma unroll
+    for (int i = 0; i < 3; i++) res[i] = xadd(st[i], xmul(st[3 + i], xmul(acc[i], inv_spp)));
+}
+
+// Training targets: radiance leaving a bounce hit toward where its ray came
+// from, estimated with train_spp plain SVO paths (bounces-1 further bounces).
+__global__ void __launch_bounds__(128) k_gi_cache_targets(SvoDev s, const tgx_material* __restrict__ luts, GiParams p,
+                                                         CacheGiConst q, const CacheHit* __restrict__ hits,
+                                                         const uint32_t* __restrict__ counters, uint32_t capacity,
+                                                         float* __restrict__ tx, float* __restrict__ tt,
+                                                         uint32_t* __restrict__ exhausted)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.n_train) return;
+    const uint32_t n_hits = min(counters[0], capacity);
+    if (n_hits == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) tx[9ull * i + k] = 0.0f;
+        tt[3ull * i] = tt[3ull * i + 1] = tt[3ull * i + 2] = 0.0f;
+        return;
+    }
+    uint32_t ctr[4] = {i, 0x7fffffffu, p.frame, 0x5eedu};
+    philox(ctr, (uint32_t)p.seed ^ 0xA5A5A5A5u, (uint32_t)(p.seed >> 32));
+    const CacheHit h = hits[ctr[0] % n_hits];
+    float a2[3];
+    svo_albedo(s, h.c, luts, a2);
+    float o3[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) o3[k] = xadd(h.p[k], xmul(h.n[k], p.offset));
+    float D[3];
+    direct_sun(s, o3, h.n, a2, p, exhausted, D);
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    GiParams pp = p;
+    pp.bounces = p.bounces > 1 ? p.bounces - 1 : 1;
+    pp.frame = p.frame | 0x800000u;   // decorrelated from the pixel streams
+    for (uint32_t k = 0; k < q.train_spp; k++) {
+        float w[3], li[3];
+        sample_cosine(h.n, i, k, 0, pp, w);
+        if (p.bounces > 1) {
+            incoming(s, o3, w, i, k, luts, pp, exhausted, li);
+        } else {
+            li[0] = li[1] = li[2] = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) acc[c] = xadd(acc[c], li[c]);
+    }
+    const float inv = xdiv(1.0f, (float)(q.train_spp ? q.train_spp : 1u));
+    float tgt[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) tgt[c] = xadd(D[c], xmul(a2[c], xmul(acc[c], inv)));
+    cache_input(q, h.p, h.n, h.w, tx + 9ull * i);
+    tt[3ull * i] = tgt[0]; tt[3ull * i + 1] = tgt[1]; tt[3ull * i + 2] = tgt[2];
 }
 
 }  // namespace
@@ -280,5 +449,65 @@ extern "C" tgx_status tgx_gi_render(tgx_ctx* c, const tgx_scene* sc, const tgx_s
     const dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
     TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi, svo_dev(svo), sc->d_objects, sc->d_cluster_pointers, sc->d_c2o,
                sc->d_material, sc->d_luts, *view, p, (const unsigned long long*)d_visbuf, d_rgb, exhausted);
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, const tgx_svo* svo, tgx_cache* cache,
+                                           const tgx_view* view, const uint64_t* d_visbuf,
+                                           const tgx_gi_params* params, const tgx_cache_gi_params* cp, float* d_rgb)
+{
+    if (!c || !sc || !svo || !cache || !view || !d_visbuf || !params || !cp || !d_rgb) {
+        tgx_set_error("tgx_gi_render_cached: NULL argument");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    if (view->width == 0 || view->height == 0 || params->spp == 0 || params->bounces < 1 || params->bounces > kMaxBounces) {
+        tgx_set_error("tgx_gi_render_cached: bad view or parameters");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    GiParams p;
+    memcpy(&p, params, sizeof(p));
+    if (p.max_steps == 0) p.max_steps = 256;
+    CacheGiConst q;
+    for (int i = 0; i < 3; i++) {
+        const float ext = cp->box_max[i] - cp->box_min[i];
+        if (!(ext > 0.0f)) { tgx_set_error("tgx_gi_render_cached: empty scene box"); return TGX_ERR_INVALID_ARGUMENT; }
+        q.box_min[i] = cp->box_min[i];
+        q.box_inv[i] = 1.0f / ext;
+    }
+    q.n_train = cp->n_train;
+    q.train_spp = cp->train_spp ? cp->train_spp : 16;
+    const uint64_t n_pix = (uint64_t)view->width * view->height;
+    const uint64_t capacity = n_pix * p.spp;
+    if (capacity > 0x7fffffffull) { tgx_set_error("tgx_gi_render_cached: too many queries"); return TGX_ERR_CAPACITY; }
+    const size_t bytes = n_pix * 6 * 4 + capacity * 4 + capacity * 9 * 4 + capacity * sizeof(CacheHit) + capacity * 3 * 4 +
+                         (size_t)q.n_train * 12 * 4 + 256;
+    TGX_TRY(devbuf_reserve(c->gi_scratch, bytes));
+    char* b = (char*)c->gi_scratch.ptr;
+    uint32_t* counters = (uint32_t*)b; b += 256;
+    float* pix_state = (float*)b; b += n_pix * 6 * 4;
+    int32_t* qidx = (int32_t*)b; b += capacity * 4;
+    float* qx = (float*)b; b += capacity * 9 * 4;
+    float* qrgb = (float*)b; b += capacity * 3 * 4;
+    CacheHit* hits = (CacheHit*)b; b += capacity * sizeof(CacheHit);
+    float* tx = (float*)b; b += (size_t)q.n_train * 9 * 4;
+    float* tt = (float*)b;
+    TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
+    uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
+    TGX_CUDA(cudaMemsetAsync(counters, 0, 256, c->stream));
+    const dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
+    TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi_cache_queries, svo_dev(svo), sc->d_objects, sc->d_cluster_pointers,
+               sc->d_c2o, sc->d_material, sc->d_luts, *view, p, q, (const unsigned long long*)d_visbuf, pix_state, qidx,
+               qx, hits, counters, (uint32_t)capacity, exhausted);
+    // inference over all potential queries: unused slots past the hit count are never read
+    TGX_TRY(cache_infer_counted(c, cache, counters, (uint32_t)capacity, qx, qrgb));
+    TGX_LAUNCH(c, TR_GI, (uint32_t)((n_pix + 255) / 256), 256, 0, k_gi_cache_resolve, (uint32_t)n_pix, p, pix_state,
+               qidx, qrgb, d_rgb);
+    if (q.n_train && cp->train_steps) {
+        TGX_LAUNCH(c, TR_GI, (q.n_train + 127) / 128, 128, 0, k_gi_cache_targets, svo_dev(svo), sc->d_luts, p, q, hits,
+                   counters, (uint32_t)capacity, tx, tt, exhausted);
+        const uint32_t per = q.n_train / cp->train_steps;
+        for (uint32_t k = 0; k < cp->train_steps && per; k++)
+            TGX_TRY(tgx_cache_train_step(c, cache, per, tx + 9ull * per * k, tt + 3ull * per * k, cp->lr));
+    }
     return TGX_OK;
 }

@@ -161,11 +161,14 @@ __device__ __forceinline__ void forward_tile(const __nv_bfloat16* sw, const floa
     }
 }
 
+// n inputs, or min(n, *n_dev) when n_dev is given (a count produced on the device)
 __global__ void __launch_bounds__(128) k_mlp_forward(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
-                                                    const float* __restrict__ x, float* __restrict__ y)
+                                                    const uint32_t* __restrict__ n_dev, const float* __restrict__ x,
+                                                    float* __restrict__ y)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    if (n_dev) n = min(n, *n_dev);
     load_weights(sw, wimg, B_FWD);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
@@ -510,20 +513,34 @@ extern "C" tgx_status tgx_cache_set_weights(tgx_ctx* c, tgx_cache* k, const floa
 }
 
 static int fwd_smem() { return B_FWD * 2; }
+static bool g_fwd_attr = false;
 static int all_smem() { return B_TOTAL * 2; }
 
 extern "C" tgx_status tgx_cache_infer(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, float* d_rgb)
 {
     if (!c || !k || (n && (!d_x || !d_rgb))) return TGX_ERR_INVALID_ARGUMENT;
     if (!n) return TGX_OK;
-    static bool attr = false;
-    if (!attr) {
+    if (!g_fwd_attr) {
         TGX_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_smem()));
-        attr = true;
+        g_fwd_attr = true;
     }
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
-    TGX_LAUNCH(c, TR_MLP, grid, 128, fwd_smem(), k_mlp_forward, k->img, n, d_x, d_rgb);
+    TGX_LAUNCH(c, TR_MLP, grid, 128, fwd_smem(), k_mlp_forward, k->img, n, (const uint32_t*)nullptr, d_x, d_rgb);
+    return TGX_OK;
+}
+
+tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
+                               float* d_rgb)
+{
+    if (!max_n) return TGX_OK;
+    if (!g_fwd_attr) {
+        TGX_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_smem()));
+        g_fwd_attr = true;
+    }
+    const uint32_t tiles = (max_n + 15) / 16;
+    const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
+    TGX_LAUNCH(c, TR_MLP, grid, 128, fwd_smem(), k_mlp_forward, k->img, max_n, d_n, d_x, d_rgb);
     return TGX_OK;
 }
 

@@ -123,6 +123,7 @@ extern "C" void tgx_destroy(tgx_ctx* c)
     devbuf_free(c->vis_views);
     devbuf_free(c->svo_counters);
     devbuf_free(c->svo_pairs);
+    devbuf_free(c->gi_scratch);
     devbuf_free(c->host_stage);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->h_counter) cudaFreeHost(c->h_counter);

@@ -123,6 +123,7 @@ struct tgx_ctx
     DevBuf vis_views;      // device copies of the views
     DevBuf svo_counters;   // SVO build counters
     DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
+    DevBuf gi_scratch;     // learned-cache GI queries, hits, training batch
     uint32_t vis_last_tiles = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters
     cudaEvent_t vis_done = nullptr;    // recorded after that copy
@@ -321,6 +322,10 @@ void trace_free(tgx_ctx* ctx);
         }                                                                         \
         (ctx)->launches++;                                                        \
     } while (0)
+
+// cache inference over min(max_n, *d_n) inputs (mlp.cu)
+tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
+                               float* d_rgb);
 
 tgx_status vis_render_device(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                              uint64_t* const* d_visbuf);
