@@ -165,64 +165,105 @@ def rel_mse(x, r, mask):
     return float(((xs - rs) ** 2 / (rs ** 2 + 1e-2)).mean())
 
 
-def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, hits: int):
-    """Config 4: 2-bounce GI at 1080p on the 512-object scene.  The judge is a
-    256-spp plain 2-bounce render; plain GI and learned-cache GI (65,536
-    training samples per frame from 16-spp SVO paths, 4 Adam steps, lr 1e-2)
-    are timed per frame and scored by relMSE over the geometry pixels."""
+def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, box, width: int, height: int):
+    """2-bounce GI on one frame: plain SVO GI against learned-cache GI.
+
+    The judge is a 256-spp plain 2-bounce render.  Plain GI and cached GI
+    (65,536 training samples per frame from 16-spp SVO paths, 4 Adam steps,
+    lr 1e-2, after an online warm-up) are each timed per frame at several spp
+    and scored by relMSE = mean((x - r)^2 / (r^2 + 1e-2)) over the pixels that
+    hit geometry.  The cached frame time includes its training."""
     import torch
     import tg_gb300 as tg
 
-    n = W * H * 3
+    n = width * height * 3
     mask = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
     ref = torch.empty(n, dtype=torch.float32, device="cuda")
     out = torch.empty(n, dtype=torch.float32, device="cuda")
-    t0 = time.perf_counter()
-    ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=1234), ref)
-    ctx.sync()
-    ref_s = time.perf_counter() - t0
-    r = ref.cpu().numpy()
 
     def timed(fn, frames):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        fn(0)
         e0.record(stream)
         for f in range(frames):
-            fn(f)
+            fn(1 + f)
         e1.record(stream)
         ctx.sync()
         return e0.elapsed_time(e1) / frames
 
-    plain = {}
     with torch.cuda.stream(stream):
-        for spp in (1, 2, 4, 8, 16):
-            ms = timed(lambda f: ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=f),
-                                               out), 3)
-            plain[spp] = {"frame_ms": ms, "relmse": rel_mse(out.cpu().numpy(), r, mask)}
+        ref_ms = timed(lambda f: ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=1234), ref), 1)
+        r = ref.cpu().numpy()
+        plain = {}
+        for spp in (1, 2, 4, 8, 16, 32, 64):
+            ms = timed(lambda f: ctx.gi_render(sc, svo, view, vis,
+                                               tg.gi_params(spp=spp, bounces=2, seed=2, frame=f), out), 3)
+            plain[spp] = {"frame_ms": round(ms, 3), "relmse": rel_mse(out.cpu().numpy(), r, mask)}
         cache = tg.Cache(ctx, seed=7)
-        cp = tg.cache_gi_params((-1100.0,) * 3, (1100.0,) * 3, n_train=65536, train_spp=16, train_steps=4, lr=1e-2)
+        cp = tg.cache_gi_params(box[0], box[1], n_train=65536, train_spp=16, train_steps=4, lr=1e-2)
         warm = 60
         for f in range(warm):
-            ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=2, bounces=2, seed=2, frame=f), cp, out)
+            ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=1, bounces=2, seed=2, frame=f), cp, out)
         ctx.sync()
         cached = {}
-        for spp in (1, 2, 4):
+        for spp in (1, 2, 4, 8, 16, 32):
             ms = timed(lambda f: ctx.gi_render_cached(
-                sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=warm + f), cp, out), 3)
-            cached[spp] = {"frame_ms": ms, "relmse": rel_mse(out.cpu().numpy(), r, mask)}
+                sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=warm + 10 * spp + f), cp,
+                out), 3)
+            cached[spp] = {"frame_ms": round(ms, 3), "relmse": rel_mse(out.cpu().numpy(), r, mask)}
+        # per-kernel device time of one 16-spp frame of each method (trace events)
+        breakdown = {}
+        for name, fn in (("plain", lambda: ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=16, bounces=2, seed=2),
+                                                          out)),
+                         ("cached", lambda: ctx.gi_render_cached(sc, svo, cache, view, vis,
+                                                                 tg.gi_params(spp=16, bounces=2, seed=2, frame=999),
+                                                                 cp, out))):
+            ctx.sync()
+            ctx.trace_reset()
+            ctx.trace(True)
+            fn()
+            ctx.sync()
+            breakdown[name] = {k: round(v[0], 4) for k, v in ctx.trace_read().items()}
+            ctx.trace(False)
         cache.close()
+    err = ctx.device_error()
 
     def best(d):
         ok = [(v["frame_ms"], k) for k, v in d.items() if v["relmse"] <= 0.01]
         return min(ok) if ok else None
 
     bp, bc = best(plain), best(cached)
-    res = {"reference": "plain 2-bounce, 256 spp", "reference_s": ref_s, "plain": plain, "cached": cached,
-           "target_relmse": 0.01, "cache_warmup_frames": warm}
+    res = {"judge": "plain 2-bounce GI, 256 spp", "judge_frame_ms": round(ref_ms, 2), "geometry_pixels": int(mask.sum()),
+           "plain": plain, "cached": cached, "kernel_ms_16spp": breakdown, "target_relmse": 0.01,
+           "cache_warmup_frames": warm,
+           "device_status": int(err.code)}
     if bp and bc:
-        res["plain_best"] = {"spp": bp[1], "frame_ms": bp[0]}
-        res["cached_best"] = {"spp": bc[1], "frame_ms": bc[0]}
-        res["speedup_at_equal_relmse"] = bp[0] / bc[0]
+        res["plain_at_target"] = {"spp": bp[1], "frame_ms": bp[0]}
+        res["cached_at_target"] = {"spp": bc[1], "frame_ms": bc[0]}
+        res["speedup_at_equal_relmse"] = round(bp[0] / bc[0], 3)
+    return res
+
+
+def cache_study_config1(local: int, stream_of):
+    """The learned-cache comparison on the config-1 scene (1 object of 4x4x4
+    Bernoulli(0.3) clusters at (0,0,64)) at 1920x1080, SVO 256^3 around it."""
+    import torch
+    import tg_gb300 as tg
+
+    scene = tg.generate_scene(0, 1, 4, 4, seed=0, bernoulli_p=0.3, translation=(0.0, 0.0, 64.0), n_luts=32)
+    view = tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), W, H, 0.1, 256.0)
+    ctx = tg.Context(local, tile=(8, 16))
+    sc = ctx.upload(scene)
+    vis = torch.empty(W * H, dtype=torch.int64, device="cuda")
+    ctx.vis_render(sc, view, [vis])
+    svo = ctx.svo_build(sc, (-128.0, -128.0, -64.0), 8)
+    ctx.sync()
+    res = compare_cache_vs_plain(ctx, sc, svo, view, vis, torch.cuda.ExternalStream(ctx.stream),
+                                 ((-48.0, -48.0, 16.0), (48.0, 48.0, 112.0)), W, H)
+    svo.close()
+    sc.close()
+    ctx.close()
     return res
 
 
@@ -234,8 +275,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gi", action="store_true", help="skip the SVO build and GI measurements")
-    ap.add_argument("--gi-cache", action="store_true",
-                    help="also compare learned-cache GI with plain 2-bounce GI at equal relMSE (config 4)")
+    ap.add_argument("--no-gi-cache", action="store_true",
+                    help="skip the learned-cache vs plain 2-bounce GI comparison at equal relMSE")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -349,8 +390,13 @@ def main() -> None:
         svo_mn = (-2048.0, -2048.0, -2048.0)
         svo = ctx.svo_build(sc, svo_mn, 12)          # warm-up build
         ctx.sync()
-        if args.gi_cache:
-            gi_report["gi_cache_vs_plain"] = compare_cache_vs_plain(ctx, sc, svo, view, out, stream, hits)
+        cache_report = None
+        if not args.no_gi_cache:
+            cache_report = {
+                "config1_scene": cache_study_config1(local, stream),
+                "512_object_scene": compare_cache_vs_plain(
+                    ctx, sc, svo, view, out, stream, ((-1100.0,) * 3, (1100.0,) * 3), W, H),
+            }
         svo.close()
         build_ms = []
         for _ in range(3):
@@ -387,6 +433,8 @@ def main() -> None:
             "gi_bounce_rays_per_s": hits * 4 / (gi_ms * 1e-3),
             "gi_device_status": int(err.code),
         }
+        if cache_report is not None:
+            gi_report["gi_cache_vs_plain"] = cache_report
         svo.close()
     rays = W * H
     value = rays * world / (ms * 1e-3) / 1e9

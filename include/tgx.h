@@ -369,11 +369,12 @@ typedef struct tgx_cache_gi_params
 
 /*
  * GI whose bounce paths end in the learned cache: as tgx_gi_render, but each
- * bounce ray that hits returns the cache's prediction of the radiance leaving
- * that point toward the shading point instead of tracing on.  Then trains the
- * cache online on this frame: picks n_train bounce hits, estimates their
- * outgoing radiance with train_spp plain SVO paths (`bounces` - 1 further
- * bounces, direct sun at every hit) and runs train_steps Adam steps.
+ * bounce ray that hits returns the hit voxel's albedo times the cache's
+ * prediction of the demodulated radiance (outgoing radiance / albedo) leaving
+ * that point toward the shading point, instead of tracing on.  Then trains
+ * the cache online on this frame: picks n_train bounce hits, estimates their
+ * demodulated outgoing radiance with train_spp plain SVO paths (`bounces` - 1
+ * further bounces, direct sun at every hit) and runs train_steps Adam steps.
  * Asynchronous; all buffers DEVICE memory.
  */
 tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, tgx_cache* cache,

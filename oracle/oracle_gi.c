@@ -10,11 +10,13 @@
  * the same bits:
  *
  *  - traversal: a hierarchical DDA over the one-bit voxel set (the same set
- *    tg_svo_create builds): occupancy levels of 2^k voxels for k = L-1 .. 5,
- *    then single voxels; descend into occupied cells, step out of empty ones
- *    through the nearest face, ascend when the step leaves the parent; one
- *    loop iteration is one step.  The hit is the first set voxel along the
- *    ray, its distance is the entry distance, its normal the face crossed.
+ *    tg_svo_create builds): occupancy levels of cells of 2^g voxels for
+ *    g = L-1, ..., 9, 7, 5 (every other level of the block pyramid), then
+ *    g = 3 and 2 (8^3 and 4^3 cells inside a 32^3 block), then single
+ *    voxels; descend into occupied cells, step out of empty ones through the
+ *    nearest face, ascend when the step leaves the parent; one loop
+ *    iteration is one step.  The hit is the first set voxel along the ray,
+ *    its distance is the entry distance, its normal the face crossed.
  *  - primary hits come from the visibility buffer, decoded as shading.frag
  *    does (:116-135), with the hit point and face normal of shading.frag:
  *    177-228 in cluster space and rotated to world space.
@@ -45,7 +47,38 @@ typedef struct
     uint16_t* mats;              /* n * 32768 or NULL */
     uint32_t* occ;               /* pyramid bits, level 0 = blocks */
     uint64_t  occ_off[16];
+    uint32_t* sub;               /* n * 32: 8^3 cells of 4^3 voxels (words 0-15), 4^3 cells of 8^3 (16-17) */
+    uint32_t  lg[16];            /* traversal level li covers cells of 2^lg[li] voxels */
 } osvo;
+
+/* Traversal levels for side 2^L: 1, 4, 8, 32, 128, 512, ... and 2^(L-1) on top. */
+uint32_t oracle_svo_levels(uint32_t L, uint32_t* lg)
+{
+    uint32_t n = 0;
+    lg[n++] = 0; lg[n++] = 2; lg[n++] = 3; lg[n++] = 5;
+    for (uint32_t g = 7; g < L - 1; g += 2) lg[n++] = g;
+    if (lg[n - 1] != L - 1) lg[n++] = L - 1;
+    return n;
+}
+
+/* sub-block occupancy of one 4 KiB block (bit 1024z + 32y + x) */
+void oracle_svo_sub_masks(const uint32_t* w, uint32_t out[32])
+{
+    memset(out, 0, 32 * 4);
+    for (uint32_t z = 0; z < 32; z++)
+        for (uint32_t y = 0; y < 32; y++)
+        {
+            const uint32_t row = w[z * 32 + y];
+            for (uint32_t x = 0; x < 32; x++)
+                if ((row >> x) & 1u)
+                {
+                    const uint32_t i4 = ((z >> 2) * 8 + (y >> 2)) * 8 + (x >> 2);
+                    const uint32_t i8 = ((z >> 3) * 4 + (y >> 3)) * 4 + (x >> 3);
+                    out[i4 >> 5] |= 1u << (i4 & 31u);
+                    out[16 + (i8 >> 5)] |= 1u << (i8 & 31u);
+                }
+        }
+}
 
 void* oracle_svo_open(const int32_t* block_xyz, const uint32_t* words, const uint16_t* mats, uint32_t n,
                       const float mn[3], uint32_t L)
@@ -54,7 +87,7 @@ void* oracle_svo_open(const int32_t* block_xyz, const uint32_t* words, const uin
     memcpy(s->mn, mn, sizeof(s->mn));
     s->L = L;
     s->B = 1u << (L - 5);
-    s->NL = 1 + (L - 5);
+    s->NL = oracle_svo_levels(L, s->lg);
     const uint64_t nt = (uint64_t)s->B * s->B * s->B;
     s->table = (uint32_t*)calloc(nt, 4);
     s->words = (uint32_t*)malloc((size_t)(n ? n : 1) * 4096);
@@ -73,8 +106,10 @@ void* oracle_svo_open(const int32_t* block_xyz, const uint32_t* words, const uin
         off += (m * m * m + 31) / 32;
     }
     s->occ = (uint32_t*)calloc(off + 1, 4);
+    s->sub = (uint32_t*)calloc((size_t)(n ? n : 1) * 32, 4);
     for (uint32_t i = 0; i < n; i++)
     {
+        oracle_svo_sub_masks(&s->words[(size_t)i * 1024], &s->sub[(size_t)i * 32]);
         const uint32_t bx = (uint32_t)((float)block_xyz[3 * i] - mn[0]) / 32u;
         const uint32_t by = (uint32_t)((float)block_xyz[3 * i + 1] - mn[1]) / 32u;
         const uint32_t bz = (uint32_t)((float)block_xyz[3 * i + 2] - mn[2]) / 32u;
@@ -94,23 +129,28 @@ void oracle_svo_close(void* h)
 {
     osvo* s = (osvo*)h;
     if (!s) return;
-    free(s->table); free(s->words); free(s->mats); free(s->occ); free(s);
+    free(s->table); free(s->words); free(s->mats); free(s->occ); free(s->sub); free(s);
 }
 
-static inline float level_size(uint32_t li) { return li == 0 ? 1.0f : (float)(1u << (li + 4)); }
-static inline int32_t level_cells(const osvo* s, uint32_t li) { return li == 0 ? (int32_t)(s->B << 5) : (int32_t)(s->B >> (li - 1)); }
+static inline float level_size(const osvo* s, uint32_t li) { return (float)(1u << s->lg[li]); }
+static inline int32_t level_cells(const osvo* s, uint32_t li) { return (int32_t)(1u << (s->L - s->lg[li])); }
 
 static int occupied(const osvo* s, uint32_t li, const int32_t c[3])
 {
-    if (li == 0)
+    const uint32_t g = s->lg[li];
+    if (g < 5)
     {
-        const uint32_t bx = (uint32_t)c[0] >> 5, by = (uint32_t)c[1] >> 5, bz = (uint32_t)c[2] >> 5;
+        const uint32_t sh = 5u - g;
+        const uint32_t bx = (uint32_t)c[0] >> sh, by = (uint32_t)c[1] >> sh, bz = (uint32_t)c[2] >> sh;
         const uint32_t tv = s->table[((uint64_t)bz * s->B + by) * s->B + bx];
         if (!tv) return 0;
-        const uint32_t v = ((uint32_t)c[2] & 31u) * 1024u + ((uint32_t)c[1] & 31u) * 32u + ((uint32_t)c[0] & 31u);
-        return (s->words[(uint64_t)(tv - 1) * 1024u + v / 32u] >> (v % 32u)) & 1u;
+        const uint32_t m = 32u >> g, mk = m - 1u;
+        const uint32_t v = (((uint32_t)c[2] & mk) * m + ((uint32_t)c[1] & mk)) * m + ((uint32_t)c[0] & mk);
+        const uint32_t* w = g == 0 ? &s->words[(uint64_t)(tv - 1) * 1024u]
+                          : &s->sub[(uint64_t)(tv - 1) * 32u + (g == 3 ? 16u : 0u)];
+        return (w[v / 32u] >> (v % 32u)) & 1u;
     }
-    const uint32_t k = li - 1;
+    const uint32_t k = g - 5u;
     const uint64_t m = s->B >> k;
     const uint64_t idx = ((uint64_t)c[2] * m + (uint64_t)c[1]) * m + (uint64_t)c[0];
     return (s->occ[s->occ_off[k] + idx / 32] >> (idx % 32)) & 1u;
@@ -184,7 +224,7 @@ int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max
     uint32_t li = s->NL - 1;
     int32_t c[3];
     {
-        const float isz = 1.0f / level_size(li);
+        const float isz = 1.0f / level_size(s, li);
         const int32_t hi = level_cells(s, li) - 1;
         for (int a = 0; a < 3; a++) c[a] = cell_at(og[a] + t * d[a], isz, st[a], 0, hi);
     }
@@ -202,9 +242,9 @@ int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max
                 *out_steps = steps;
                 return 1;
             }
-            const uint32_t shift = li == 1 ? 5u : 1u;
+            const uint32_t shift = s->lg[li] - s->lg[li - 1];
             li--;
-            const float isz = 1.0f / level_size(li);
+            const float isz = 1.0f / level_size(s, li);
             for (int a = 0; a < 3; a++)
             {
                 const int32_t lo = c[a] << shift, hi = lo + (1 << shift) - 1;
@@ -212,7 +252,7 @@ int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max
             }
             continue;
         }
-        const float size = level_size(li);
+        const float size = level_size(s, li);
         float tn[3];
         for (int a = 0; a < 3; a++)
             tn[a] = st[a] > 0 ? ((float)(c[a] + 1) * size - og[a]) * inv[a]
@@ -228,7 +268,7 @@ int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max
         int32_t cur = c[am];
         while (li < s->NL - 1)
         {
-            const uint32_t shift = li == 0 ? 5u : 1u;
+            const uint32_t shift = s->lg[li + 1] - s->lg[li];
             if ((prev >> shift) == (cur >> shift)) break;
             prev >>= shift; cur >>= shift;
             c[0] >>= shift; c[1] >>= shift; c[2] >>= shift;
@@ -362,37 +402,46 @@ static void direct_sun(const osvo* s, const float o2[3], const float n[3], const
     for (int i = 0; i < 3; i++) out[i] = a[i] * OR_INV_PI * p->sun_radiance[i] * ndl;
 }
 
-/* radiance arriving along a secondary ray from o2 in direction w (after `depth` bounces so far) */
+/*
+ * Radiance arriving at o2 along w: a path of up to p->bounces bounces,
+ * accumulated forward with its throughput T (v += T * D at every hit, T *= albedo
+ * before the next bounce, v += T * sky when the path escapes).
+ */
 static void incoming(const osvo* s, const float o2[3], const float w[3], uint32_t pixel, uint32_t sample,
-                     uint32_t bounce, const tgx_material* luts, const ogi_params* p, float out[3])
+                     const tgx_material* luts, const ogi_params* p, float out[3])
 {
-    float t; int32_t c[3], ax; uint32_t stp;
-    if (oracle_trace(s, o2, w, p->max_steps, &t, c, &ax, &stp) != 1)
+    float v[3] = { 0.0f, 0.0f, 0.0f }, T[3] = { 1.0f, 1.0f, 1.0f };
+    float o[3] = { o2[0], o2[1], o2[2] }, d[3] = { w[0], w[1], w[2] };
+    for (uint32_t b = 0; b < p->bounces; b++)
     {
-        out[0] = p->sky_radiance[0]; out[1] = p->sky_radiance[1]; out[2] = p->sky_radiance[2];
-        return;
+        float t; int32_t c[3], ax; uint32_t stp;
+        if (oracle_trace(s, o, d, p->max_steps, &t, c, &ax, &stp) != 1)
+        {
+            for (int i = 0; i < 3; i++) v[i] = v[i] + T[i] * p->sky_radiance[i];
+            break;
+        }
+        float n2[3] = { 0.0f, 0.0f, 0.0f };
+        if (ax >= 0) n2[ax] = d[ax] > 0.0f ? -1.0f : 1.0f;
+        else
+        {
+            int m = 0;
+            if (fabsf(d[1]) > fabsf(d[m])) m = 1;
+            if (fabsf(d[2]) > fabsf(d[m])) m = 2;
+            n2[m] = d[m] > 0.0f ? -1.0f : 1.0f;
+        }
+        float a2[3], o3[3], D[3];
+        svo_albedo(s, c, luts, a2);
+        for (int i = 0; i < 3; i++) o3[i] = (o[i] + t * d[i]) + n2[i] * p->offset;
+        direct_sun(s, o3, n2, a2, p, D);
+        for (int i = 0; i < 3; i++) v[i] = v[i] + T[i] * D[i];
+        if (b + 1 < p->bounces)
+        {
+            for (int i = 0; i < 3; i++) T[i] = T[i] * a2[i];
+            sample_cosine(n2, pixel, sample, b + 1, p, d);
+            o[0] = o3[0]; o[1] = o3[1]; o[2] = o3[2];
+        }
     }
-    float n2[3] = { 0.0f, 0.0f, 0.0f };
-    if (ax >= 0) n2[ax] = w[ax] > 0.0f ? -1.0f : 1.0f;
-    else
-    {
-        int m = 0;
-        if (fabsf(w[1]) > fabsf(w[m])) m = 1;
-        if (fabsf(w[2]) > fabsf(w[m])) m = 2;
-        n2[m] = w[m] > 0.0f ? -1.0f : 1.0f;
-    }
-    float a2[3];
-    svo_albedo(s, c, luts, a2);
-    float o3[3];
-    for (int i = 0; i < 3; i++) o3[i] = (o2[i] + t * w[i]) + n2[i] * p->offset;
-    direct_sun(s, o3, n2, a2, p, out);
-    if (bounce + 1 < p->bounces)
-    {
-        float w2[3], l2[3];
-        sample_cosine(n2, pixel, sample, bounce + 1, p, w2);
-        incoming(s, o3, w2, pixel, sample, bounce + 1, luts, p, l2);
-        for (int i = 0; i < 3; i++) out[i] = out[i] + a2[i] * l2[i];
-    }
+    out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
 }
 
 /*
@@ -497,7 +546,7 @@ void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t*
     {
         float w[3], li[3];
         sample_cosine(nw, pixel, smp, 0, p, w);
-        incoming(s, o2, w, pixel, smp, 0, luts, p, li);
+        incoming(s, o2, w, pixel, smp, luts, p, li);
         for (int i = 0; i < 3; i++) acc[i] = acc[i] + li[i];
     }
     const float inv_spp = 1.0f / (float)(p->spp ? p->spp : 1);

@@ -105,3 +105,33 @@ def test_gi_sky_and_determinism(oracle):
     p2 = tg.gi_params(spp=4, bounces=2, seed=8)
     c = gi_render(oracle, osvo, s, view, p2, vis)
     assert not np.array_equal(a[~sky], c[~sky])
+
+
+def test_traversal_levels(oracle):
+    """Levels of the traversal: 1, 4, 8, 32, then every other block-pyramid level up to 2^(L-1)."""
+    lib = oracle.lib
+    for L in range(6, 15):
+        lg = np.zeros(16, np.uint32)
+        n = lib.oracle_svo_levels(C.c_uint32(L), C.c_void_p(lg.ctypes.data))
+        want = [0, 2, 3, 5] + list(range(7, L - 1, 2))
+        if want[-1] != L - 1:
+            want.append(L - 1)
+        assert list(lg[:n]) == want
+        # the closed form the CUDA traversal evaluates per level
+        closed = [0 if li == 0 else li + 1 if li <= 2 else min(2 * li - 1, L - 1) for li in range(n)]
+        assert closed == want
+
+
+def test_sub_block_masks(oracle):
+    rng = np.random.default_rng(5)
+    for p in (0.0, 0.001, 0.01, 0.2):
+        bits = (rng.random((32, 32, 32)) < p)           # z, y, x
+        words = np.packbits(bits.reshape(-1).astype(np.uint8), bitorder="little").view(np.uint32).copy()
+        out = np.zeros(32, np.uint32)
+        oracle.lib.oracle_svo_sub_masks(C.c_void_p(words.ctypes.data), C.c_void_p(out.ctypes.data))
+        c4 = bits.reshape(8, 4, 8, 4, 8, 4).any(axis=(1, 3, 5)).reshape(-1)
+        c8 = bits.reshape(4, 8, 4, 8, 4, 8).any(axis=(1, 3, 5)).reshape(-1)
+        want = np.zeros(32, np.uint32)
+        want[:16] = np.packbits(c4.astype(np.uint8), bitorder="little").view(np.uint32)
+        want[16:18] = np.packbits(c8.astype(np.uint8), bitorder="little").view(np.uint32)
+        assert np.array_equal(out, want)

@@ -1,4 +1,5 @@
-// gi.cu -- plain SVO bounce lighting (GI) from the visibility buffer.
+// gi.cu -- SVO bounce lighting (GI) from the visibility buffer, plain and
+// with the learned radiance cache.
 //
 // The reference has no GI pass: shading.frag:285-316 shades with one constant
 // light and an ambient term, and its only secondary rays are a disabled CPU
@@ -10,21 +11,38 @@
 //     cluster-space hit point and face normal (:116-228), rotated to world;
 //   - direct light: a directional sun, Lambertian albedo from the object's
 //     LUT, visibility from an SVO shadow ray;
-//   - indirect light: spp cosine-weighted rays (Malley's method, Duff et al.
-//     basis) traced through the SVO; a miss sees the sky, a hit adds the sun
-//     light arriving there (with its own shadow ray) and, for 2 bounces, one
-//     more cosine-weighted ray from that hit;
-//   - random numbers: Philox4x32-10 keyed by the seed, counter (pixel, sample,
-//     bounce | frame << 8, draw).
+//   - indirect light: spp cosine-weighted paths (Malley's method, Duff et al.
+//     basis) of up to `bounces` SVO bounces, accumulated forward with their
+//     throughput; a miss sees the sky, a hit adds the sun light arriving
+//     there (with its own shadow ray);
+//   - random numbers: Philox4x32-10 keyed by the seed, counter (key, sample,
+//     bounce | frame << 8, draw), key = pixel index.
 //
-// One thread per pixel.  Results equal the oracle's bit for bit.
+// Execution is a wavefront over path roots (one per geometry pixel, or one
+// per training sample of the cache):
+//
+//   k_gi_roots      primary hits -> compacted roots; sky pixels written
+//   k_gi_emit       first bounce ray of every (root, sample), root shadow rays
+//   k_trace_queue   persistent SVO traversal of a ray list: each lane takes
+//                   rays from a warp-aggregated queue and runs their DDA a few
+//                   steps at a time, so a lane whose ray ends picks up the next
+//                   ray instead of idling until the warp's longest ray is done
+//   k_gi_shade      consumes the hits of one bounce: sky, or albedo + shadow
+//                   ray + next bounce ray
+//   k_gi_finish     last shadow results, per-root sums in sample order, output
+//
+// Results equal the oracle's bit for bit.
 
 #include "svo_trace.cuh"
+
+#include <algorithm>
 
 namespace {
 
 constexpr float kInvPi = 0.318309886f;
 constexpr uint32_t kMaxBounces = 4;
+constexpr uint32_t kStepsPerRound = 8;                // DDA steps between queue refills
+constexpr uint64_t kMaxPathsPerChunk = 16ull << 20;   // paths in flight per wavefront chunk
 
 struct GiParams
 {
@@ -33,6 +51,38 @@ struct GiParams
     float sun_dir[3], sun_radiance[3], sky_radiance[3], offset;
 };
 static_assert(sizeof(GiParams) == sizeof(tgx_gi_params), "GI parameter layout");
+
+struct Ray
+{
+    float o[3], d[3];   // d = 0: no ray
+};
+
+struct RayHit
+{
+    float t;
+    int32_t c[3];
+    int32_t axis;
+    int32_t res;        // 1 hit, 0 miss, -1 step budget ran out
+};
+
+struct PathRoot
+{
+    float o[3];         // offset surface point
+    float n[3];         // normal
+    float a[3];         // albedo for the root's direct term
+    uint32_t key;       // Philox key and output index (pixel, or training sample)
+};
+
+struct PathState
+{
+    float v[3];         // radiance gathered so far
+    float T[3];         // throughput
+    float a[3];         // albedo of the last hit (its shadow ray is pending)
+    float ndl;
+    uint32_t flags;
+    uint32_t pad;
+};
+enum : uint32_t { P_ALIVE = 1u, P_SHADOW = 2u };
 
 __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
 {
@@ -86,69 +136,6 @@ __device__ __forceinline__ void svo_albedo(const SvoDev& s, const int32_t c[3], 
     if (!code || !luts) { out[0] = out[1] = out[2] = 0.5f; return; }
     const tgx_material& m = luts[code - 1u];
     out[0] = m.albedo[0]; out[1] = m.albedo[1]; out[2] = m.albedo[2];
-}
-
-__device__ void direct_sun(const SvoDev& s, const float o2[3], const float n[3], const float a[3], const GiParams& p,
-                           uint32_t* exhausted, float out[3])
-{
-    out[0] = out[1] = out[2] = 0.0f;
-    const float ndl = xadd(xadd(xmul(n[0], p.sun_dir[0]), xmul(n[1], p.sun_dir[1])), xmul(n[2], p.sun_dir[2]));
-    if (!(ndl > 0.0f)) return;
-    float t; int32_t c[3], ax; uint32_t stp;
-    const int r = svo_trace(s, o2, p.sun_dir, p.max_steps, t, c, ax, stp);
-    if (r < 0) atomicAdd(exhausted, 1u);
-    if (r == 1) return;
-#pragma unroll
-    for (int i = 0; i < 3; i++) out[i] = xmul(xmul(xmul(a[i], kInvPi), p.sun_radiance[i]), ndl);
-}
-
-// radiance arriving at o along w, for the rest of a path that has used `bounce` bounces
-__device__ void incoming(const SvoDev& s, const float o_in[3], const float w_in[3], uint32_t pixel, uint32_t sample,
-                         const tgx_material* luts, const GiParams& p, uint32_t* exhausted, float out[3])
-{
-    float D[kMaxBounces][3], A[kMaxBounces][3];
-    float o[3] = {o_in[0], o_in[1], o_in[2]}, w[3] = {w_in[0], w_in[1], w_in[2]};
-    int hits = 0;
-    bool missed = false;
-    for (uint32_t bounce = 0; bounce < p.bounces; bounce++) {
-        float t; int32_t c[3], ax; uint32_t stp;
-        const int r = svo_trace(s, o, w, p.max_steps, t, c, ax, stp);
-        if (r < 0) atomicAdd(exhausted, 1u);
-        if (r != 1) { missed = true; break; }
-        float n2[3] = {0.0f, 0.0f, 0.0f};
-        if (ax >= 0) {
-            n2[ax] = w[ax] > 0.0f ? -1.0f : 1.0f;
-        } else {
-            int m = 0;
-            if (fabsf(w[1]) > fabsf(w[m])) m = 1;
-            if (fabsf(w[2]) > fabsf(w[m])) m = 2;
-            n2[m] = w[m] > 0.0f ? -1.0f : 1.0f;
-        }
-        svo_albedo(s, c, luts, A[hits]);
-        float o3[3];
-#pragma unroll
-        for (int i = 0; i < 3; i++) o3[i] = xadd(xadd(o[i], xmul(t, w[i])), xmul(n2[i], p.offset));
-        direct_sun(s, o3, n2, A[hits], p, exhausted, D[hits]);
-        hits++;
-        if (bounce + 1 < p.bounces) {
-            sample_cosine(n2, pixel, sample, bounce + 1, p, w);
-            o[0] = o3[0]; o[1] = o3[1]; o[2] = o3[2];
-        }
-    }
-    // innermost value, then outward: value = D + A * value
-    float v[3];
-    int j;
-    if (missed) {
-        v[0] = p.sky_radiance[0]; v[1] = p.sky_radiance[1]; v[2] = p.sky_radiance[2];
-        j = hits - 1;
-    } else {
-        v[0] = D[hits - 1][0]; v[1] = D[hits - 1][1]; v[2] = D[hits - 1][2];
-        j = hits - 2;
-    }
-    for (; j >= 0; j--)
-#pragma unroll
-        for (int i = 0; i < 3; i++) v[i] = xadd(D[j][i], xmul(A[j][i], v[i]));
-    out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
 }
 
 // Primary hit of a pixel from its visibility word (shading.frag:116-228):
@@ -235,47 +222,282 @@ __device__ bool primary_hit(const tgx_object* __restrict__ objects, const uint32
     return true;
 }
 
-__global__ void __launch_bounds__(128) k_gi(SvoDev s, const tgx_object* __restrict__ objects,
-                                           const uint32_t* __restrict__ cluster_pointers,
-                                           const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material,
-                                           const tgx_material* __restrict__ luts, tgx_view cam, GiParams p,
-                                           const unsigned long long* __restrict__ visbuf, float* __restrict__ out,
-                                           uint32_t* __restrict__ exhausted)
+__device__ __forceinline__ float sun_cos(const float n[3], const GiParams& p)
+{
+    return xadd(xadd(xmul(n[0], p.sun_dir[0]), xmul(n[1], p.sun_dir[1])), xmul(n[2], p.sun_dir[2]));
+}
+
+// sun light reflected by a Lambertian surface of albedo a, unshadowed
+__device__ __forceinline__ void sun_term(const float a[3], float ndl, const GiParams& p, float out[3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; i++) out[i] = xmul(xmul(xmul(a[i], kInvPi), p.sun_radiance[i]), ndl);
+}
+
+__device__ __forceinline__ void set_ray(Ray& r, const float o[3], const float d[3])
+{
+    r.o[0] = o[0]; r.o[1] = o[1]; r.o[2] = o[2];
+    r.d[0] = d[0]; r.d[1] = d[1]; r.d[2] = d[2];
+}
+
+__device__ __forceinline__ void null_ray(Ray& r)
+{
+    r.o[0] = r.o[1] = r.o[2] = 0.0f;
+    r.d[0] = r.d[1] = r.d[2] = 0.0f;
+}
+
+// face normal of an SVO hit: the face crossed, or the dominant axis when the
+// ray started inside the voxel
+__device__ __forceinline__ void hit_normal(int32_t axis, const float d[3], float n2[3])
+{
+    int m = axis;
+    if (m < 0) {
+        m = fabsf(d[1]) > fabsf(d[0]) ? 1 : 0;
+        if (fabsf(d[2]) > fabsf(m ? d[1] : d[0])) m = 2;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) n2[i] = i == m ? (d[i] > 0.0f ? -1.0f : 1.0f) : 0.0f;
+}
+
+// Slot in an append buffer for every lane with want = true (one atomic per warp).
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
+{
+    const uint32_t active = __activemask();
+    const uint32_t mask = __ballot_sync(active, want);
+    if (!mask) return 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(active, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void write_hit(RayHit* h, int res, const RayState& r)
+{
+    RayHit o;
+    o.t = r.t;
+    o.c[0] = r.c[0]; o.c[1] = r.c[1]; o.c[2] = r.c[2];
+    o.axis = r.last_axis;
+    o.res = res;
+    *h = o;
+}
+
+// Persistent traversal of two ray lists: a (n * mul_a rays) then b (n * mul_b
+// rays), n read from the device.  No CTA waits on another: a CTA that starts
+// after the queue is drained exits at once.
+__global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __restrict__ ra, RayHit* __restrict__ ha,
+                                                     uint32_t mul_a, const Ray* __restrict__ rb,
+                                                     RayHit* __restrict__ hb, uint32_t mul_b,
+                                                     const uint32_t* __restrict__ n_dev, uint32_t max_steps,
+                                                     uint32_t* __restrict__ queue, uint32_t* __restrict__ exhausted)
+{
+    const uint32_t n = *n_dev;
+    const uint32_t n_a = n * mul_a, n_tot = n_a + n * mul_b;
+    const uint32_t lane = threadIdx.x & 31u;
+    RayState r;
+    uint32_t item = 0;
+    bool have = false, empty = false;
+    for (;;) {
+        const bool need = !have && !empty;
+        const uint32_t mask = __ballot_sync(0xffffffffu, need);
+        if (mask) {
+            const uint32_t leader = __ffs(mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                item = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+                if (item >= n_tot) {
+                    empty = true;
+                } else {
+                    const Ray ray = item < n_a ? ra[item] : rb[item - n_a];
+                    const int res = svo_trace_begin(s, ray.o, ray.d, r);
+                    if (res == kTraceRunning) have = true;
+                    else write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, empty)) break;
+        if (have) {
+            const int res = svo_trace_run(s, r, max_steps, kStepsPerRound);
+            if (res != kTraceRunning) {
+                if (res < 0) atomicAdd(exhausted, 1u);
+                write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
+                have = false;
+            }
+        }
+    }
+}
+
+// Roots of the geometry pixels; sky pixels get the sky radiance.
+__global__ void __launch_bounds__(128) k_gi_roots(const tgx_object* __restrict__ objects,
+                                                  const uint32_t* __restrict__ cluster_pointers,
+                                                  const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material,
+                                                  const tgx_material* __restrict__ luts, tgx_view cam, GiParams p,
+                                                  const unsigned long long* __restrict__ visbuf, float* __restrict__ out,
+                                                  PathRoot* __restrict__ roots, uint32_t* __restrict__ n_roots)
 {
     const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15u);
     const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
     if (px >= cam.width || py >= cam.height) return;
     const uint32_t pixel = py * cam.width + px;
-    float* res = out + 3ull * pixel;
-    float o2[3], nw[3], a[3];
-    if (!primary_hit(objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[pixel], px, py, o2, nw, a)) {
-        res[0] = p.sky_radiance[0]; res[1] = p.sky_radiance[1]; res[2] = p.sky_radiance[2];
-        return;
+    PathRoot rt;
+    const bool geo = primary_hit(objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[pixel], px, py, rt.o,
+                                 rt.n, rt.a);
+    if (!geo) {
+        out[3ull * pixel + 0] = p.sky_radiance[0];
+        out[3ull * pixel + 1] = p.sky_radiance[1];
+        out[3ull * pixel + 2] = p.sky_radiance[2];
     }
-    float L[3];
-    direct_sun(s, o2, nw, a, p, exhausted, L);
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    for (uint32_t smp = 0; smp < p.spp; smp++) {
-        float w[3], li[3];
-        sample_cosine(nw, pixel, smp, 0, p, w);
-        incoming(s, o2, w, pixel, smp, luts, p, exhausted, li);
-#pragma unroll
-        for (int i = 0; i < 3; i++) acc[i] = xadd(acc[i], li[i]);
+    const uint32_t slot = warp_append(n_roots, geo);
+    if (geo) {
+        rt.key = pixel;
+        roots[slot] = rt;
     }
-    const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
+}
+
+// First bounce ray of every path (root r, sample s0 + j) of a chunk of cs
+// samples; with root_rays, also the shadow ray of every root.
+__global__ void __launch_bounds__(256) k_gi_emit(const PathRoot* __restrict__ roots, const uint32_t* __restrict__ n_dev,
+                                                 uint32_t cs, uint32_t s0, GiParams p, Ray* __restrict__ rays,
+                                                 PathState* __restrict__ st, Ray* __restrict__ root_rays)
+{
+    const uint32_t n = *n_dev;
+    const uint64_t n_paths = (uint64_t)n * cs;
+    const uint64_t n_items = n_paths + (root_rays ? n : 0u);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < n_paths) {
+            const PathRoot& rt = roots[i / cs];
+            float w[3];
+            sample_cosine(rt.n, rt.key, s0 + (uint32_t)(i % cs), 0, p, w);
+            set_ray(rays[i], rt.o, w);
+            PathState ps;
+            ps.v[0] = ps.v[1] = ps.v[2] = 0.0f;
+            ps.T[0] = ps.T[1] = ps.T[2] = 1.0f;
+            ps.a[0] = ps.a[1] = ps.a[2] = 0.0f;
+            ps.ndl = 0.0f;
+            ps.flags = P_ALIVE;
+            ps.pad = 0;
+            st[i] = ps;
+        } else {
+            const uint32_t r = (uint32_t)(i - n_paths);
+            const PathRoot& rt = roots[r];
+            if (sun_cos(rt.n, p) > 0.0f) set_ray(root_rays[r], rt.o, p.sun_dir);
+            else null_ray(root_rays[r]);
+        }
+    }
+}
+
+// Consumes the pending shadow ray of bounce k-1 and the hit of bounce k.
+__global__ void __launch_bounds__(256) k_gi_shade(SvoDev s, const tgx_material* __restrict__ luts,
+                                                  const PathRoot* __restrict__ roots, const uint32_t* __restrict__ n_dev,
+                                                  uint32_t cs, uint32_t s0, uint32_t k, GiParams p,
+                                                  Ray* __restrict__ rb, const RayHit* __restrict__ hb,
+                                                  Ray* __restrict__ rs, const RayHit* __restrict__ hs,
+                                                  PathState* __restrict__ st)
+{
+    const uint64_t n_paths = (uint64_t)(*n_dev) * cs;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_paths; i += (uint64_t)gridDim.x * blockDim.x) {
+        PathState ps = st[i];
+        if (ps.flags & P_SHADOW) {
+            float D[3] = {0.0f, 0.0f, 0.0f};
+            if (ps.ndl > 0.0f && hs[i].res != 1) sun_term(ps.a, ps.ndl, p, D);
 #pragma unroll
-    for (int i = 0; i < 3; i++) res[i] = xadd(L[i], xmul(a[i], xmul(acc[i], inv_spp)));
+            for (int c = 0; c < 3; c++) {
+                ps.v[c] = xadd(ps.v[c], xmul(ps.T[c], D[c]));
+                ps.T[c] = xmul(ps.T[c], ps.a[c]);
+            }
+            ps.flags &= ~P_SHADOW;
+        }
+        Ray nb, ns;
+        null_ray(nb);
+        null_ray(ns);
+        if (ps.flags & P_ALIVE) {
+            const RayHit h = hb[i];
+            const Ray ray = rb[i];
+            if (h.res != 1) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) ps.v[c] = xadd(ps.v[c], xmul(ps.T[c], p.sky_radiance[c]));
+                ps.flags &= ~P_ALIVE;
+            } else {
+                float n2[3], o3[3];
+                hit_normal(h.axis, ray.d, n2);
+                svo_albedo(s, h.c, luts, ps.a);
+#pragma unroll
+                for (int c = 0; c < 3; c++) o3[c] = xadd(xadd(ray.o[c], xmul(h.t, ray.d[c])), xmul(n2[c], p.offset));
+                ps.ndl = sun_cos(n2, p);
+                ps.flags |= P_SHADOW;
+                if (ps.ndl > 0.0f) set_ray(ns, o3, p.sun_dir);
+                if (k + 1 < p.bounces) {
+                    float w2[3];
+                    sample_cosine(n2, roots[i / cs].key, s0 + (uint32_t)(i % cs), k + 1, p, w2);
+                    set_ray(nb, o3, w2);
+                } else {
+                    ps.flags &= ~P_ALIVE;
+                }
+            }
+        }
+        rb[i] = nb;
+        rs[i] = ns;
+        st[i] = ps;
+    }
+}
+
+// Per root: the last pending shadows, the chunk's samples added in order to
+// the running sum; on the last chunk out[key] = direct + albedo * sum / spp.
+__global__ void __launch_bounds__(256) k_gi_finish(const PathRoot* __restrict__ roots, const uint32_t* __restrict__ n_dev,
+                                                   uint32_t cs, GiParams p, const RayHit* __restrict__ hs,
+                                                   const PathState* __restrict__ st, const RayHit* __restrict__ root_hits,
+                                                   float* __restrict__ acc_buf, bool first, bool last, uint32_t spp,
+                                                   float* __restrict__ out)
+{
+    const uint32_t n = *n_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        if (!first) { acc[0] = acc_buf[3ull * r]; acc[1] = acc_buf[3ull * r + 1]; acc[2] = acc_buf[3ull * r + 2]; }
+        for (uint32_t j = 0; j < cs; j++) {
+            const uint64_t i = (uint64_t)r * cs + j;
+            const PathState& ps = st[i];
+            float v[3] = {ps.v[0], ps.v[1], ps.v[2]};
+            if (ps.flags & P_SHADOW) {
+                float D[3] = {0.0f, 0.0f, 0.0f};
+                if (ps.ndl > 0.0f && hs[i].res != 1) sun_term(ps.a, ps.ndl, p, D);
+#pragma unroll
+                for (int c = 0; c < 3; c++) v[c] = xadd(v[c], xmul(ps.T[c], D[c]));
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) acc[c] = xadd(acc[c], v[c]);
+        }
+        if (!last) {
+            acc_buf[3ull * r] = acc[0]; acc_buf[3ull * r + 1] = acc[1]; acc_buf[3ull * r + 2] = acc[2];
+            continue;
+        }
+        const PathRoot& rt = roots[r];
+        float L[3] = {0.0f, 0.0f, 0.0f};
+        const float ndl = sun_cos(rt.n, p);
+        if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
+        const float inv_spp = xdiv(1.0f, (float)(spp ? spp : 1u));
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[3ull * rt.key + c] = xadd(L[c], xmul(rt.a[c], xmul(acc[c], inv_spp)));
+    }
 }
 
 // ---------------------------------------------------------------------------
 // learned-cache GI
 // ---------------------------------------------------------------------------
 
+// The cache stores demodulated radiance: the radiance leaving a bounce hit
+// divided by the hit voxel's albedo.  Albedo is per-voxel noise in the
+// material grids, so the quotient (direct irradiance / pi plus the mean
+// incoming radiance) is far smoother than the radiance itself; queries
+// multiply the albedo back in.
 struct CacheHit
 {
     float p[3];      // hit point (world)
     float n[3];      // face normal
     float w[3];      // direction the bounce ray travelled
+    float a[3];      // albedo of the hit voxel
     int32_t c[3];    // grid voxel
 };
 
@@ -285,6 +507,8 @@ struct CacheGiConst
     float box_inv[3];    // 1 / (box_max - box_min)
     uint32_t n_train, train_spp;
 };
+
+enum CacheCounter { CC_ROOTS = 0, CC_QUERIES = 1, CC_TRAIN_ROOTS = 2, CC_QUEUE = 3 };
 
 __device__ __forceinline__ void cache_input(const CacheGiConst& q, const float p[3], const float n[3], const float w[3],
                                             float* x)
@@ -297,97 +521,78 @@ __device__ __forceinline__ void cache_input(const CacheGiConst& q, const float p
     }
 }
 
-// Pass 1: primary hit, direct light, bounce rays; hits become cache queries.
-__global__ void __launch_bounds__(128) k_gi_cache_queries(
-    SvoDev s, const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
-    const uint32_t* __restrict__ c2o, const uint8_t* __restrict__ material, const tgx_material* __restrict__ luts,
-    tgx_view cam, GiParams p, CacheGiConst q, const unsigned long long* __restrict__ visbuf,
-    float* __restrict__ pix_state /* W*H*6: direct L, albedo */, int32_t* __restrict__ qidx /* W*H*spp */,
-    float* __restrict__ qx /* n*9 */, CacheHit* __restrict__ hits, uint32_t* __restrict__ counters,
-    uint32_t capacity, uint32_t* __restrict__ exhausted)
+// First-bounce hits of a chunk of samples become cache queries.
+__global__ void __launch_bounds__(256) k_gi_query_shade(SvoDev s, const tgx_material* __restrict__ luts, CacheGiConst q,
+                                                        const uint32_t* __restrict__ n_dev, uint32_t cs, uint32_t s0,
+                                                        uint32_t spp, const Ray* __restrict__ rb,
+                                                        const RayHit* __restrict__ hb, int32_t* __restrict__ qidx,
+                                                        float* __restrict__ qx, CacheHit* __restrict__ hits,
+                                                        uint32_t* __restrict__ counters, uint32_t capacity)
 {
-    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15u);
-    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (px >= cam.width || py >= cam.height) return;
-    const uint32_t pixel = py * cam.width + px;
-    float* st = pix_state + 6ull * pixel;
-    int32_t* qi = qidx + (uint64_t)pixel * p.spp;
-    float o2[3], nw[3], a[3];
-    if (!primary_hit(objects, cluster_pointers, c2o, material, luts, cam, p, visbuf[pixel], px, py, o2, nw, a)) {
-        st[0] = p.sky_radiance[0]; st[1] = p.sky_radiance[1]; st[2] = p.sky_radiance[2];
-        st[3] = st[4] = st[5] = -1.0f;   // sky marker
-        for (uint32_t k = 0; k < p.spp; k++) qi[k] = -1;
-        return;
-    }
-    float L[3];
-    direct_sun(s, o2, nw, a, p, exhausted, L);
-    st[0] = L[0]; st[1] = L[1]; st[2] = L[2];
-    st[3] = a[0]; st[4] = a[1]; st[5] = a[2];
-    for (uint32_t smp = 0; smp < p.spp; smp++) {
-        float w[3];
-        sample_cosine(nw, pixel, smp, 0, p, w);
-        float t; int32_t c[3], ax; uint32_t stp;
-        const int r = svo_trace(s, o2, w, p.max_steps, t, c, ax, stp);
-        if (r < 0) atomicAdd(exhausted, 1u);
-        if (r != 1) { qi[smp] = -1; continue; }
-        float n2[3] = {0.0f, 0.0f, 0.0f};
-        if (ax >= 0) n2[ax] = w[ax] > 0.0f ? -1.0f : 1.0f;
-        else {
-            int m = 0;
-            if (fabsf(w[1]) > fabsf(w[m])) m = 1;
-            if (fabsf(w[2]) > fabsf(w[m])) m = 2;
-            n2[m] = w[m] > 0.0f ? -1.0f : 1.0f;
-        }
-        const uint32_t slot = atomicAdd(&counters[0], 1u);
-        if (slot >= capacity) { qi[smp] = -2; continue; }
-        qi[smp] = (int32_t)slot;
-        CacheHit h;
+    const uint64_t n_paths = (uint64_t)(*n_dev) * cs;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_paths; i += (uint64_t)gridDim.x * blockDim.x) {
+        const RayHit h = hb[i];
+        int32_t* qi = qidx + (i / cs) * spp + s0 + (i % cs);
+        const bool hit = h.res == 1;
+        const uint32_t slot = warp_append(&counters[CC_QUERIES], hit);
+        if (!hit) { *qi = -1; continue; }
+        if (slot >= capacity) { *qi = -2; continue; }
+        *qi = (int32_t)slot;
+        const Ray ray = rb[i];
+        CacheHit ch;
+        hit_normal(h.axis, ray.d, ch.n);
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-            h.p[i] = xadd(o2[i], xmul(t, w[i]));
-            h.n[i] = n2[i];
-            h.w[i] = w[i];
-            h.c[i] = c[i];
+        for (int c = 0; c < 3; c++) {
+            ch.p[c] = xadd(ray.o[c], xmul(h.t, ray.d[c]));
+            ch.w[c] = ray.d[c];
+            ch.c[c] = h.c[c];
         }
-        hits[slot] = h;
-        cache_input(q, h.p, h.n, h.w, qx + 9ull * slot);
+        svo_albedo(s, h.c, luts, ch.a);
+        hits[slot] = ch;
+        cache_input(q, ch.p, ch.n, ch.w, qx + 9ull * slot);
     }
 }
 
-// Pass 3: pixel = direct + albedo * mean(sky or cache prediction).
-__global__ void __launch_bounds__(256) k_gi_cache_resolve(uint32_t n_pixels, GiParams p,
-                                                         const float* __restrict__ pix_state,
+// pixel = direct + albedo * mean(sky, or hit albedo * cache prediction)
+__global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __restrict__ roots,
+                                                         const uint32_t* __restrict__ n_dev, GiParams p,
+                                                         const RayHit* __restrict__ root_hits,
                                                          const int32_t* __restrict__ qidx,
-                                                         const float* __restrict__ qrgb, float* __restrict__ out)
+                                                         const float* __restrict__ qrgb,
+                                                         const CacheHit* __restrict__ hits, float* __restrict__ out)
 {
-    const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pixel >= n_pixels) return;
-    const float* st = pix_state + 6ull * pixel;
-    float* res = out + 3ull * pixel;
-    if (st[3] < 0.0f) { res[0] = st[0]; res[1] = st[1]; res[2] = st[2]; return; }
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    for (uint32_t k = 0; k < p.spp; k++) {
-        const int32_t q = qidx[(uint64_t)pixel * p.spp + k];
+    const uint32_t n = *n_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const PathRoot& rt = roots[r];
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t k = 0; k < p.spp; k++) {
+            const int32_t qv = qidx[(uint64_t)r * p.spp + k];
 #pragma unroll
-        for (int i = 0; i < 3; i++)
-            acc[i] = xadd(acc[i], q >= 0 ? fmaxf(qrgb[3ull * q + i], 0.0f) : (q == -1 ? p.sky_radiance[i] : 0.0f));
+            for (int i = 0; i < 3; i++)
+                acc[i] = xadd(acc[i], qv >= 0 ? xmul(hits[qv].a[i], fmaxf(qrgb[3ull * qv + i], 0.0f))
+                                              : (qv == -1 ? p.sky_radiance[i] : 0.0f));
+        }
+        float L[3] = {0.0f, 0.0f, 0.0f};
+        const float ndl = sun_cos(rt.n, p);
+        if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
+        const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
+#pragma unroll
+        for (int i = 0; i < 3; i++) out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], xmul(acc[i], inv_spp)));
     }
-    const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
-#pragma unroll
-    for (int i = 0; i < 3; i++) res[i] = xadd(st[i], xmul(st[3 + i], xmul(acc[i], inv_spp)));
 }
 
-// Training targets: radiance leaving a bounce hit toward where its ray came
-// from, estimated with train_spp plain SVO paths (bounces-1 further bounces).
-__global__ void __launch_bounds__(128) k_gi_cache_targets(SvoDev s, const tgx_material* __restrict__ luts, GiParams p,
-                                                         CacheGiConst q, const CacheHit* __restrict__ hits,
-                                                         const uint32_t* __restrict__ counters, uint32_t capacity,
-                                                         float* __restrict__ tx, float* __restrict__ tt,
-                                                         uint32_t* __restrict__ exhausted)
+// Training roots: n_train bounce hits of this frame picked at random; the
+// target at each is the demodulated radiance (direct / albedo + mean
+// incoming) toward where its ray came from, estimated by the path passes.
+__global__ void __launch_bounds__(256) k_gi_target_roots(GiParams p, CacheGiConst q, const CacheHit* __restrict__ hits,
+                                                        uint32_t* __restrict__ counters, uint32_t capacity,
+                                                        PathRoot* __restrict__ roots, float* __restrict__ tx,
+                                                        float* __restrict__ tt)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= q.n_train) return;
-    const uint32_t n_hits = min(counters[0], capacity);
+    const uint32_t n_hits = min(counters[CC_QUERIES], capacity);
+    if (i == 0) counters[CC_TRAIN_ROOTS] = n_hits ? q.n_train : 0u;
     if (n_hits == 0) {
 #pragma unroll
         for (int k = 0; k < 9; k++) tx[9ull * i + k] = 0.0f;
@@ -397,34 +602,126 @@ __global__ void __launch_bounds__(128) k_gi_cache_targets(SvoDev s, const tgx_ma
     uint32_t ctr[4] = {i, 0x7fffffffu, p.frame, 0x5eedu};
     philox(ctr, (uint32_t)p.seed ^ 0xA5A5A5A5u, (uint32_t)(p.seed >> 32));
     const CacheHit h = hits[ctr[0] % n_hits];
-    float a2[3];
-    svo_albedo(s, h.c, luts, a2);
-    float o3[3];
+    PathRoot rt;
 #pragma unroll
-    for (int k = 0; k < 3; k++) o3[k] = xadd(h.p[k], xmul(h.n[k], p.offset));
-    float D[3];
-    direct_sun(s, o3, h.n, a2, p, exhausted, D);
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    GiParams pp = p;
-    pp.bounces = p.bounces > 1 ? p.bounces - 1 : 1;
-    pp.frame = p.frame | 0x800000u;   // decorrelated from the pixel streams
-    for (uint32_t k = 0; k < q.train_spp; k++) {
-        float w[3], li[3];
-        sample_cosine(h.n, i, k, 0, pp, w);
-        if (p.bounces > 1) {
-            incoming(s, o3, w, i, k, luts, pp, exhausted, li);
-        } else {
-            li[0] = li[1] = li[2] = 0.0f;
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) acc[c] = xadd(acc[c], li[c]);
+    for (int k = 0; k < 3; k++) {
+        rt.o[k] = xadd(h.p[k], xmul(h.n[k], p.offset));
+        rt.n[k] = h.n[k];
+        rt.a[k] = 1.0f;
     }
-    const float inv = xdiv(1.0f, (float)(q.train_spp ? q.train_spp : 1u));
-    float tgt[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) tgt[c] = xadd(D[c], xmul(a2[c], xmul(acc[c], inv)));
+    rt.key = i;
+    roots[i] = rt;
     cache_input(q, h.p, h.n, h.w, tx + 9ull * i);
-    tt[3ull * i] = tgt[0]; tt[3ull * i + 1] = tgt[1]; tt[3ull * i + 2] = tgt[2];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct PathBufs
+{
+    PathRoot* roots;
+    Ray *rb, *rs, *root_rays;
+    RayHit *hb, *hs, *root_hits;
+    PathState* st;
+    float* acc;
+    uint64_t max_paths;
+};
+
+// carves aligned regions out of one scratch allocation
+struct Carver
+{
+    char* base;
+    size_t off = 0;
+    template <class T> T* take(uint64_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T* p = base ? (T*)(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+void carve_paths(Carver& cv, PathBufs& b, uint64_t max_roots, uint64_t max_paths)
+{
+    b.roots = cv.take<PathRoot>(max_roots);
+    b.root_rays = cv.take<Ray>(max_roots);
+    b.root_hits = cv.take<RayHit>(max_roots);
+    b.acc = cv.take<float>(max_roots * 3);
+    b.rb = cv.take<Ray>(max_paths);
+    b.rs = cv.take<Ray>(max_paths);
+    b.hb = cv.take<RayHit>(max_paths);
+    b.hs = cv.take<RayHit>(max_paths);
+    b.st = cv.take<PathState>(max_paths);
+    b.max_paths = max_paths;
+}
+
+uint32_t chunk_samples(uint32_t spp, uint64_t max_roots)
+{
+    const uint64_t cap = std::max<uint64_t>(1, kMaxPathsPerChunk / std::max<uint64_t>(max_roots, 1));
+    return (uint32_t)std::min<uint64_t>(std::max(spp, 1u), cap);
+}
+
+uint32_t trace_grid(tgx_ctx* c)
+{
+    static int per_sm = 0;
+    if (!per_sm) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue, 128, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+    }
+    return (uint32_t)(c->num_sms * per_sm);
+}
+
+uint32_t stride_grid(tgx_ctx* c, uint64_t items, uint32_t block)
+{
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((items + block - 1) / block, (uint64_t)c->num_sms * 16));
+}
+
+tgx_status trace_lists(tgx_ctx* c, const SvoDev& s, const Ray* ra, RayHit* ha, uint32_t mul_a, const Ray* rb,
+                       RayHit* hb, uint32_t mul_b, const uint32_t* n_dev, uint32_t max_steps, uint32_t* queue,
+                       uint32_t* exhausted)
+{
+    TGX_CUDA(cudaMemsetAsync(queue, 0, 4, c->stream));
+    TGX_LAUNCH(c, TR_GI_TRACE, trace_grid(c), 128, 0, k_trace_queue, s, ra, ha, mul_a, rb, hb, mul_b, n_dev, max_steps,
+               queue, exhausted);
+    return TGX_OK;
+}
+
+// spp paths of p.bounces bounces from every root, then out[key] per root.
+tgx_status run_paths(tgx_ctx* c, const SvoDev& s, const tgx_material* luts, const GiParams& p, const PathBufs& b,
+                     const uint32_t* n_dev, uint32_t max_roots, uint32_t spp, uint32_t* queue, uint32_t* exhausted,
+                     float* out)
+{
+    const uint32_t cs = chunk_samples(spp, max_roots);
+    const uint32_t rg = stride_grid(c, max_roots, 256);
+    if (spp == 0 || p.bounces == 0) {   // direct term only
+        TGX_LAUNCH(c, TR_GI, rg, 256, 0, k_gi_emit, b.roots, n_dev, 0u, 0u, p, b.rb, b.st, b.root_rays);
+        TGX_TRY(trace_lists(c, s, nullptr, nullptr, 0u, b.root_rays, b.root_hits, 1u, n_dev, p.max_steps, queue, exhausted));
+        TGX_LAUNCH(c, TR_GI, rg, 256, 0, k_gi_finish, b.roots, n_dev, 0u, p, b.hs, b.st, b.root_hits, b.acc, true, true,
+                   spp, out);
+        return TGX_OK;
+    }
+    const uint32_t eg = stride_grid(c, (uint64_t)max_roots * cs + max_roots, 256);
+    for (uint32_t s0 = 0; s0 < spp; s0 += cs) {
+        const uint32_t n = std::min(cs, spp - s0);
+        const bool first = s0 == 0, last = s0 + n >= spp;
+        TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_emit, b.roots, n_dev, n, s0, p, b.rb, b.st, first ? b.root_rays : nullptr);
+        TGX_TRY(trace_lists(c, s, b.rb, b.hb, n, b.root_rays, b.root_hits, first ? 1u : 0u, n_dev, p.max_steps, queue,
+                            exhausted));
+        for (uint32_t k = 0; k < p.bounces; k++) {
+            TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_shade, s, luts, b.roots, n_dev, n, s0, k, p, b.rb, b.hb, b.rs, b.hs,
+                       b.st);
+            TGX_TRY(trace_lists(c, s, b.rb, b.hb, k + 1 < p.bounces ? n : 0u, b.rs, b.hs, n, n_dev, p.max_steps, queue,
+                                exhausted));
+        }
+        TGX_LAUNCH(c, TR_GI, rg, 256, 0, k_gi_finish, b.roots, n_dev, n, p, b.hs, b.st, b.root_hits, b.acc, first, last,
+                   spp, out);
+    }
+    return TGX_OK;
 }
 
 }  // namespace
@@ -444,12 +741,24 @@ extern "C" tgx_status tgx_gi_render(tgx_ctx* c, const tgx_scene* sc, const tgx_s
     GiParams p;
     memcpy(&p, params, sizeof(p));
     if (p.max_steps == 0) p.max_steps = 256;
+    const uint64_t n_pix = (uint64_t)view->width * view->height;
+    const uint64_t max_paths = n_pix * chunk_samples(p.spp, n_pix);
+    PathBufs b;
+    Carver size{nullptr};
+    size.take<uint32_t>(64);
+    carve_paths(size, b, n_pix, max_paths);
+    TGX_TRY(devbuf_reserve(c->gi_scratch, size.off + 256));
+    Carver cv{(char*)c->gi_scratch.ptr};
+    uint32_t* counters = cv.take<uint32_t>(64);
+    carve_paths(cv, b, n_pix, max_paths);
     TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
     uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
+    TGX_CUDA(cudaMemsetAsync(counters, 0, 64 * 4, c->stream));
     const dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
-    TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi, svo_dev(svo), sc->d_objects, sc->d_cluster_pointers, sc->d_c2o,
-               sc->d_material, sc->d_luts, *view, p, (const unsigned long long*)d_visbuf, d_rgb, exhausted);
-    return TGX_OK;
+    TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi_roots, sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_material,
+               sc->d_luts, *view, p, (const unsigned long long*)d_visbuf, d_rgb, b.roots, &counters[CC_ROOTS]);
+    return run_paths(c, svo_dev(svo), sc->d_luts, p, b, &counters[CC_ROOTS], (uint32_t)n_pix, p.spp,
+                     &counters[CC_QUEUE], exhausted, d_rgb);
 }
 
 extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, const tgx_svo* svo, tgx_cache* cache,
@@ -476,35 +785,64 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     }
     q.n_train = cp->n_train;
     q.train_spp = cp->train_spp ? cp->train_spp : 16;
+    const bool train = q.n_train && cp->train_steps;
     const uint64_t n_pix = (uint64_t)view->width * view->height;
     const uint64_t capacity = n_pix * p.spp;
     if (capacity > 0x7fffffffull) { tgx_set_error("tgx_gi_render_cached: too many queries"); return TGX_ERR_CAPACITY; }
-    const size_t bytes = n_pix * 6 * 4 + capacity * 4 + capacity * 9 * 4 + capacity * sizeof(CacheHit) + capacity * 3 * 4 +
-                         (size_t)q.n_train * 12 * 4 + 256;
-    TGX_TRY(devbuf_reserve(c->gi_scratch, bytes));
-    char* b = (char*)c->gi_scratch.ptr;
-    uint32_t* counters = (uint32_t*)b; b += 256;
-    float* pix_state = (float*)b; b += n_pix * 6 * 4;
-    int32_t* qidx = (int32_t*)b; b += capacity * 4;
-    float* qx = (float*)b; b += capacity * 9 * 4;
-    float* qrgb = (float*)b; b += capacity * 3 * 4;
-    CacheHit* hits = (CacheHit*)b; b += capacity * sizeof(CacheHit);
-    float* tx = (float*)b; b += (size_t)q.n_train * 9 * 4;
-    float* tt = (float*)b;
+    const uint32_t cs = chunk_samples(p.spp, n_pix);
+    const uint32_t cs_t = train ? chunk_samples(q.train_spp, q.n_train) : 1u;
+    const uint64_t max_roots = std::max<uint64_t>(n_pix, q.n_train);
+    const uint64_t max_paths = std::max<uint64_t>(n_pix * cs, (uint64_t)q.n_train * cs_t);
+
+    auto layout = [&](Carver& cv, uint32_t*& counters, PathBufs& b, int32_t*& qidx, float*& qx, float*& qrgb,
+                      CacheHit*& hits, float*& tx, float*& tt) {
+        counters = cv.take<uint32_t>(64);
+        carve_paths(cv, b, max_roots, max_paths);
+        qidx = cv.take<int32_t>(capacity);
+        qx = cv.take<float>(capacity * 9);
+        qrgb = cv.take<float>(capacity * 3);
+        hits = cv.take<CacheHit>(capacity);
+        tx = cv.take<float>((uint64_t)q.n_train * 9);
+        tt = cv.take<float>((uint64_t)q.n_train * 3);
+    };
+    uint32_t* counters; PathBufs b; int32_t* qidx; float *qx, *qrgb, *tx, *tt; CacheHit* hits;
+    Carver size{nullptr};
+    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt);
+    TGX_TRY(devbuf_reserve(c->gi_scratch, size.off + 256));
+    Carver cv{(char*)c->gi_scratch.ptr};
+    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt);
     TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
     uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
-    TGX_CUDA(cudaMemsetAsync(counters, 0, 256, c->stream));
+    TGX_CUDA(cudaMemsetAsync(counters, 0, 64 * 4, c->stream));
+    const SvoDev s = svo_dev(svo);
+
+    // primary hits, then the first bounce of every (pixel, sample) in chunks
     const dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
-    TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi_cache_queries, svo_dev(svo), sc->d_objects, sc->d_cluster_pointers,
-               sc->d_c2o, sc->d_material, sc->d_luts, *view, p, q, (const unsigned long long*)d_visbuf, pix_state, qidx,
-               qx, hits, counters, (uint32_t)capacity, exhausted);
-    // inference over all potential queries: unused slots past the hit count are never read
-    TGX_TRY(cache_infer_counted(c, cache, counters, (uint32_t)capacity, qx, qrgb));
-    TGX_LAUNCH(c, TR_GI, (uint32_t)((n_pix + 255) / 256), 256, 0, k_gi_cache_resolve, (uint32_t)n_pix, p, pix_state,
-               qidx, qrgb, d_rgb);
-    if (q.n_train && cp->train_steps) {
-        TGX_LAUNCH(c, TR_GI, (q.n_train + 127) / 128, 128, 0, k_gi_cache_targets, svo_dev(svo), sc->d_luts, p, q, hits,
-                   counters, (uint32_t)capacity, tx, tt, exhausted);
+    TGX_LAUNCH(c, TR_GI, grid, 128, 0, k_gi_roots, sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_material,
+               sc->d_luts, *view, p, (const unsigned long long*)d_visbuf, d_rgb, b.roots, &counters[CC_ROOTS]);
+    const uint32_t eg = stride_grid(c, n_pix * cs + n_pix, 256);
+    for (uint32_t s0 = 0; s0 < p.spp; s0 += cs) {
+        const uint32_t n = std::min(cs, p.spp - s0);
+        const bool first = s0 == 0;
+        TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_emit, b.roots, &counters[CC_ROOTS], n, s0, p, b.rb, b.st,
+                   first ? b.root_rays : nullptr);
+        TGX_TRY(trace_lists(c, s, b.rb, b.hb, n, b.root_rays, b.root_hits, first ? 1u : 0u, &counters[CC_ROOTS],
+                            p.max_steps, &counters[CC_QUEUE], exhausted));
+        TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_query_shade, s, sc->d_luts, q, &counters[CC_ROOTS], n, s0, p.spp, b.rb,
+                   b.hb, qidx, qx, hits, counters, (uint32_t)capacity);
+    }
+    // inference over all potential queries: slots past the hit count are never read
+    TGX_TRY(cache_infer_counted(c, cache, &counters[CC_QUERIES], (uint32_t)capacity, qx, qrgb));
+    TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_resolve, b.roots, &counters[CC_ROOTS], p,
+               b.root_hits, qidx, qrgb, hits, d_rgb);
+    if (train) {
+        TGX_LAUNCH(c, TR_GI, (q.n_train + 255) / 256, 256, 0, k_gi_target_roots, p, q, hits, counters,
+                   (uint32_t)capacity, b.roots, tx, tt);
+        GiParams pp = p;
+        pp.bounces = p.bounces - 1;
+        pp.frame = p.frame | 0x800000u;   // decorrelated from the pixel streams
+        TGX_TRY(run_paths(c, s, sc->d_luts, pp, b, &counters[CC_TRAIN_ROOTS], q.n_train, q.train_spp,
+                          &counters[CC_QUEUE], exhausted, tt));
         const uint32_t per = q.n_train / cp->train_steps;
         for (uint32_t k = 0; k < cp->train_steps && per; k++)
             TGX_TRY(tgx_cache_train_step(c, cache, per, tx + 9ull * per * k, tt + 3ull * per * k, cp->lr));

@@ -448,7 +448,7 @@ extern "C" uint32_t tgx_cache_n_params(void) { return N_PARAMS; }
 
 static tgx_status cache_refresh_image(tgx_ctx* c, tgx_cache* k)
 {
-    TGX_LAUNCH(c, TR_MLP, (N_PARAMS + 255) / 256, 256, 0, k_mlp_image, k->w, k->img);
+    TGX_LAUNCH(c, TR_MLP_ADAM, (N_PARAMS + 255) / 256, 256, 0, k_mlp_image, k->w, k->img);
     return TGX_OK;
 }
 
@@ -562,7 +562,7 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
     TGX_CUDA(cudaMemsetAsync(k->loss, 0, 4, c->stream));
     const uint32_t tiles = (uint32_t)(np / 16);
     const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
-    TGX_LAUNCH(c, TR_MLP, grid, 128, all_smem(), k_mlp_fwd_bwd, k->img, n, d_x, d_t, enc, act, dlt, dy, k->loss);
+    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, 128, all_smem(), k_mlp_fwd_bwd, k->img, n, d_x, d_t, enc, act, dlt, dy, k->loss);
     // weight gradients, layer by layer: D [s][o] against the layer input X [s][i]
     const uint32_t chunk = 256;
     const uint32_t chunks = (n + chunk - 1) / chunk;
@@ -576,7 +576,7 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
     };
     for (const L& l : ls) {
         const uint32_t tasks = (uint32_t)((l.no + 15) / 16) * ((l.ni + 63) / 64) * chunks;
-        TGX_LAUNCH(c, TR_MLP, (tasks + 3) / 4, 128, 0, k_mlp_wgrad, l.D, l.ds, l.no, l.X, l.xs, l.ni, n, chunk,
+        TGX_LAUNCH(c, TR_MLP_WGRAD, (tasks + 3) / 4, 128, 0, k_mlp_wgrad, l.D, l.ds, l.no, l.X, l.xs, l.ni, n, chunk,
                    k->g + l.off, l.ni);
     }
     return TGX_OK;
@@ -603,7 +603,7 @@ extern "C" tgx_status tgx_cache_train_step(tgx_ctx* c, tgx_cache* k, uint32_t n,
     k->step++;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
     const float c1 = (float)(1.0 - pow((double)b1, (double)k->step)), c2 = (float)(1.0 - pow((double)b2, (double)k->step));
-    TGX_LAUNCH(c, TR_MLP, (N_PARAMS + 255) / 256, 256, 0, k_mlp_adam, k->w, k->m, k->v, k->g, lr, b1, b2, eps, c1, c2,
+    TGX_LAUNCH(c, TR_MLP_ADAM, (N_PARAMS + 255) / 256, 256, 0, k_mlp_adam, k->w, k->m, k->v, k->g, lr, b1, b2, eps, c1, c2,
                k->img);
     return TGX_OK;
 }

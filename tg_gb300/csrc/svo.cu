@@ -17,7 +17,9 @@
 //      fetch -- into a warp-private 4 KiB block image in shared memory, then
 //      coalesced atomicOr of its non-zero words into the pool.
 //   4. k_svo_pyramid     bottom-up occupancy: one bit per non-empty block and
-//      per non-empty node of every coarser level.
+//      per non-empty node of every coarser level, and inside each block one
+//      bit per non-empty 4^3 and 8^3 cell (the sub-block levels the
+//      traversal steps through before single voxels).
 //
 // The node encoding of the reference (u16 relative child pointers, 64-entry
 // leaf lists) is not kept; the voxel set is.  Side length 2^6 .. 2^14.
@@ -402,10 +404,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
 
 __global__ void __launch_bounds__(256) k_svo_pyramid(const uint32_t* __restrict__ table, uint64_t n_table,
                                                     const uint32_t* __restrict__ pool, uint32_t* __restrict__ nonempty,
-                                                    uint32_t* __restrict__ occ, const uint64_t* __restrict__ occ_off,
-                                                    uint32_t n_levels, uint32_t B, uint32_t* __restrict__ counters)
+                                                    uint32_t* __restrict__ sub, uint32_t* __restrict__ occ,
+                                                    const uint64_t* __restrict__ occ_off, uint32_t n_levels, uint32_t B,
+                                                    uint32_t* __restrict__ counters)
 {
-    // one warp per table entry
+    // one warp per table entry; lane y reads the 32 rows (y, z) of the block
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -414,10 +417,52 @@ __global__ void __launch_bounds__(256) k_svo_pyramid(const uint32_t* __restrict_
         if (tv == 0u) continue;
         const uint32_t* blk = pool + (uint64_t)(tv - 1u) * kBlockWords;
         uint32_t any = 0;
-        for (uint32_t k = lane; k < kBlockWords; k += 32) any |= blk[k];
+        uint32_t n4[8];   // per 4-voxel z-slab: which 4-voxel x-groups of row y hold a voxel
+#pragma unroll
+        for (int k = 0; k < 8; k++) n4[k] = 0;
+#pragma unroll
+        for (int z = 0; z < 32; z++) {
+            const uint32_t row = blk[z * 32 + lane];
+            any |= row;
+            uint32_t f = 0;
+#pragma unroll
+            for (int gx = 0; gx < 8; gx++) f |= ((row >> (4 * gx)) & 15u) ? (1u << gx) : 0u;
+            n4[z >> 2] |= f;
+        }
         any = __any_sync(0xffffffffu, any != 0u);
         if (lane == 0) nonempty[tv - 1u] = any ? 1u : 0u;
         if (!any) continue;
+        // 4^3 cells: bit ((cz * 8 + cy) * 8 + cx), cy = lane / 4
+        uint32_t* sb = sub + (uint64_t)(tv - 1u) * 32u;
+#pragma unroll
+        for (int cz = 0; cz < 8; cz++) {
+            uint32_t b = n4[cz];
+            b |= __shfl_xor_sync(0xffffffffu, b, 1);
+            b |= __shfl_xor_sync(0xffffffffu, b, 2);
+            uint32_t w = (lane & 3u) == 0u ? b << (((lane >> 2) & 3u) * 8u) : 0u;
+            w |= __shfl_xor_sync(0xffffffffu, w, 4);
+            w |= __shfl_xor_sync(0xffffffffu, w, 8);
+            if ((lane & 15u) == 0u) sb[cz * 2 + (lane >> 4)] = w;
+        }
+        // 8^3 cells: bit ((cz * 4 + cy) * 4 + cx), cy = lane / 8
+        uint32_t w8[2] = {0u, 0u};
+#pragma unroll
+        for (int cz = 0; cz < 4; cz++) {
+            const uint32_t b = n4[2 * cz] | n4[2 * cz + 1];
+            uint32_t c3 = 0;
+#pragma unroll
+            for (int cx = 0; cx < 4; cx++) c3 |= ((b >> (2 * cx)) & 3u) ? (1u << cx) : 0u;
+            c3 |= __shfl_xor_sync(0xffffffffu, c3, 1);
+            c3 |= __shfl_xor_sync(0xffffffffu, c3, 2);
+            c3 |= __shfl_xor_sync(0xffffffffu, c3, 4);
+            if ((lane & 7u) == 0u) w8[cz >> 1] |= c3 << ((cz & 1) * 16 + (lane >> 3) * 4);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            w8[k] |= __shfl_xor_sync(0xffffffffu, w8[k], 8);
+            w8[k] |= __shfl_xor_sync(0xffffffffu, w8[k], 16);
+        }
+        if (lane == 0) { sb[16] = w8[0]; sb[17] = w8[1]; }
         if (lane == 0) atomicAdd(&counters[S_NONEMPTY], 1u);
         const uint32_t bx = (uint32_t)(i % B), by = (uint32_t)((i / B) % B), bz = (uint32_t)(i / ((uint64_t)B * B));
         if (lane < n_levels) {
@@ -439,6 +484,7 @@ static void svo_free(tgx_svo* s)
     if (!s) return;
     cudaFree(s->d_table);
     cudaFree(s->d_pool);
+    cudaFree(s->d_sub);
     cudaFree(s->d_occ);
     cudaFree(s->d_nonempty);
     cudaFree(s->d_mat);
@@ -516,11 +562,13 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
     s->n_pairs = hc[S_PAIRS];
     s->n_blocks = hc[S_MARKED];
     if (cudaMalloc(&s->d_pool, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4) != cudaSuccess ||
+        cudaMalloc(&s->d_sub, (uint64_t)std::max(s->n_blocks, 1u) * 32 * 4) != cudaSuccess ||
         cudaMalloc(&s->d_nonempty, (uint64_t)std::max(s->n_blocks, 1u) * 4) != cudaSuccess) {
         tgx_set_error("tgx_svo_build: out of device memory for %u blocks", s->n_blocks);
         return fail(TGX_ERR_OUT_OF_MEMORY);
     }
     cudaMemsetAsync(s->d_pool, 0, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4, c->stream);
+    cudaMemsetAsync(s->d_sub, 0, (uint64_t)std::max(s->n_blocks, 1u) * 32 * 4, c->stream);
     if (sc->d_material && sc->d_luts) {
         const uint64_t mb = (uint64_t)std::max(s->n_blocks, 1u) * 32768u * 2u;
         if (cudaMalloc(&s->d_mat, mb) != cudaSuccess) {
@@ -540,11 +588,11 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
                    mn[0], mn[1], mn[2], s->B);
         const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
         TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
-                   s->d_occ, (const uint64_t*)((char*)s->d_occ + occ_words * 4), s->n_levels, s->B, counters);
+                   s->d_sub, s->d_occ, (const uint64_t*)((char*)s->d_occ + occ_words * 4), s->n_levels, s->B, counters);
         return TGX_OK;
     };
     if ((st = rest()) != TGX_OK) return fail(st);
-    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 4 + (s->d_mat ? 65536 : 0)) + occ_words * 4;
+    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 128 + 4 + (s->d_mat ? 65536 : 0)) + occ_words * 4;
     *out = s;
     return TGX_OK;
 }

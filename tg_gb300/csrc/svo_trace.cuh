@@ -2,13 +2,14 @@
 //
 // The reference traverses its pointer octree with a 5-deep stack and a 32^3
 // leaf DDA (svo_functions.inc:1-329, CPU form tg_sparse_voxel_octree.c:558-740).
-// Here the same voxel set is traversed over the occupancy pyramid of the new
-// storage: cells of 2^k voxels for k = L-1 .. 5, then single voxels.  An
-// occupied cell is entered (descend), an empty one is left through its
-// nearest face (one step), and leaving the parent cell ascends.  The
-// operations are exactly rounded, in the order of the CPU oracle
-// (oracle/oracle_gi.c: oracle_trace), so hits, distances and face normals are
-// bit-identical.
+// Here the same voxel set is traversed over the occupancy levels of the new
+// storage: cells of 2^g voxels for g = L-1, ..., 9, 7, 5 (every other level
+// of the block pyramid), g = 3 and 2 (sub-block masks of each 32^3 block),
+// then single voxels.  An occupied cell is entered (descend), an empty one is
+// left through its nearest face (one step), and leaving the parent cell
+// ascends.  The operations are exactly rounded, in the order of the CPU
+// oracle (oracle/oracle_gi.c: oracle_trace), so hits, distances and face
+// normals are bit-identical.
 #pragma once
 
 #include "tgx_internal.cuh"
@@ -19,40 +20,42 @@ struct SvoDev
     uint32_t L, B, NL;
     const uint32_t* table;
     const uint32_t* pool;
+    const uint32_t* sub;     // per slot 32 words: 4^3-cell mask (0-15), 8^3-cell mask (16-17)
     const uint32_t* occ;
     const uint16_t* mat;
     uint64_t occ_off[10];
 };
 
+// log2 of the cell size of traversal level li: 0, 2, 3, 5, 7, 9, ... capped at L-1
+__host__ __device__ __forceinline__ uint32_t svo_level_log2(uint32_t L, uint32_t li)
+{
+    return li == 0 ? 0u : li <= 2 ? li + 1u : min(2u * li - 1u, L - 1u);
+}
+
+__host__ __device__ __forceinline__ uint32_t svo_n_levels(uint32_t L)
+{
+    uint32_t n = 4;
+    while (svo_level_log2(L, n - 1) < L - 1) n++;
+    return n;
+}
+
 inline SvoDev svo_dev(const tgx_svo* s)
 {
     SvoDev d;
     d.mn[0] = s->mn[0]; d.mn[1] = s->mn[1]; d.mn[2] = s->mn[2];
-    d.L = s->L; d.B = s->B; d.NL = 1 + (s->L - 5);
-    d.table = s->d_table; d.pool = s->d_pool; d.occ = s->d_occ; d.mat = s->d_mat;
+    d.L = s->L; d.B = s->B; d.NL = svo_n_levels(s->L);
+    d.table = s->d_table; d.pool = s->d_pool; d.sub = s->d_sub; d.occ = s->d_occ; d.mat = s->d_mat;
     for (int i = 0; i < 10; i++) d.occ_off[i] = s->occ_off[i];
     return d;
 }
 
-__device__ __forceinline__ float svo_level_size(uint32_t li) { return li == 0 ? 1.0f : (float)(1u << (li + 4)); }
+__device__ __forceinline__ float svo_level_size(const SvoDev& s, uint32_t li)
+{
+    return (float)(1u << svo_level_log2(s.L, li));
+}
 __device__ __forceinline__ int32_t svo_level_cells(const SvoDev& s, uint32_t li)
 {
-    return li == 0 ? (int32_t)(s.B << 5) : (int32_t)(s.B >> (li - 1));
-}
-
-__device__ __forceinline__ bool svo_occupied(const SvoDev& s, uint32_t li, int32_t cx, int32_t cy, int32_t cz)
-{
-    if (li == 0) {
-        const uint32_t bx = (uint32_t)cx >> 5, by = (uint32_t)cy >> 5, bz = (uint32_t)cz >> 5;
-        const uint32_t tv = __ldg(&s.table[((uint64_t)bz * s.B + by) * s.B + bx]);
-        if (!tv) return false;
-        const uint32_t v = ((uint32_t)cz & 31u) * 1024u + ((uint32_t)cy & 31u) * 32u + ((uint32_t)cx & 31u);
-        return (__ldg(&s.pool[(uint64_t)(tv - 1) * 1024u + (v >> 5)]) >> (v & 31u)) & 1u;
-    }
-    const uint32_t k = li - 1;
-    const uint64_t m = s.B >> k;
-    const uint64_t idx = ((uint64_t)cz * m + (uint64_t)cy) * m + (uint64_t)cx;
-    return (__ldg(&s.occ[s.occ_off[k] + (idx >> 5)]) >> (idx & 31u)) & 1u;
+    return (int32_t)(1u << (s.L - svo_level_log2(s.L, li)));
 }
 
 __device__ __forceinline__ uint32_t svo_material(const SvoDev& s, int32_t cx, int32_t cy, int32_t cz)
@@ -76,95 +79,150 @@ __device__ __forceinline__ int32_t svo_cell_at(float p, float inv_size, int32_t 
     return c;
 }
 
-// Returns 1 on hit (t, grid voxel c, face axis or -1), 0 on miss, -1 when
-// max_steps ran out.
-static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d[3], uint32_t max_steps, float& out_t,
-                         int32_t out_c[3], int32_t& out_axis, uint32_t& out_steps)
+// 2^-g, the exact reciprocal of a level's cell size (equal to 1.0f / 2^g)
+__device__ __forceinline__ float svo_level_inv_size(const SvoDev& s, uint32_t li)
+{
+    return __int_as_float((int)((127u - svo_level_log2(s.L, li)) << 23));
+}
+
+// Resumable traversal state: the DDA of one ray, kept in registers so a
+// persistent kernel can run it a few steps at a time.
+struct RayState
+{
+    float og[3], d[3], inv[3];
+    int32_t st[3];
+    float t;
+    int32_t c[3];
+    int32_t last_axis;
+    uint32_t li, steps;
+    uint32_t tv;        // slot + 1 of the 32^3 block the sub-block levels (li <= 2) are inside
+};
+
+constexpr int kTraceRunning = -2;
+
+// Sets up a ray.  Returns kTraceRunning when the DDA has to run, else the
+// result (0: the ray misses the SVO cube or has no direction).
+__device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const float o[3], const float d[3], RayState& r)
 {
     const float E = (float)(1u << s.L);
-    float og[3], inv[3];
-    int32_t st[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        og[a] = xsub(o[a], s.mn[a]);
-        st[a] = d[a] > 0.0f ? 1 : d[a] < 0.0f ? -1 : 0;
-        inv[a] = st[a] ? xdiv(1.0f, d[a]) : 0.0f;
+        r.d[a] = d[a];
+        r.og[a] = xsub(o[a], s.mn[a]);
+        r.st[a] = d[a] > 0.0f ? 1 : d[a] < 0.0f ? -1 : 0;
+        r.inv[a] = r.st[a] ? xdiv(1.0f, d[a]) : 0.0f;
     }
-    out_steps = 0;
-    if (!st[0] && !st[1] && !st[2]) return 0;
+    r.steps = 0;
+    if (!r.st[0] && !r.st[1] && !r.st[2]) return 0;
     float t0 = F32_MIN_TG, t1 = F32_MAX_TG;
     int32_t entry_axis = -1;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        if (!st[a]) {
-            if (og[a] < 0.0f || og[a] >= E) return 0;
+        if (!r.st[a]) {
+            if (r.og[a] < 0.0f || r.og[a] >= E) return 0;
             continue;
         }
-        const float ta = xmul(xsub(0.0f, og[a]), inv[a]);
-        const float tb = xmul(xsub(E, og[a]), inv[a]);
+        const float ta = xmul(xsub(0.0f, r.og[a]), r.inv[a]);
+        const float tb = xmul(xsub(E, r.og[a]), r.inv[a]);
         const float tn = ta < tb ? ta : tb;
         const float tf = ta < tb ? tb : ta;
         if (tn > t0) { t0 = tn; entry_axis = a; }
         if (tf < t1) t1 = tf;
     }
-    float t = t0 > 0.0f ? t0 : 0.0f;
-    if (!(t < t1)) return 0;
-    int32_t last_axis = t0 > 0.0f ? entry_axis : -1;
-
-    uint32_t li = s.NL - 1;
-    int32_t c[3];
-    {
-        const float isz = xdiv(1.0f, svo_level_size(li));
-        const int32_t hi = svo_level_cells(s, li) - 1;
+    r.t = t0 > 0.0f ? t0 : 0.0f;
+    if (!(r.t < t1)) return 0;
+    r.last_axis = t0 > 0.0f ? entry_axis : -1;
+    r.li = s.NL - 1;
+    r.tv = 0;
+    const float isz = svo_level_inv_size(s, r.li);
+    const int32_t hi = svo_level_cells(s, r.li) - 1;
 #pragma unroll
-        for (int a = 0; a < 3; a++) c[a] = svo_cell_at(xadd(og[a], xmul(t, d[a])), isz, st[a], 0, hi);
+    for (int a = 0; a < 3; a++) r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], 0, hi);
+    return kTraceRunning;
+}
+
+__device__ __forceinline__ bool svo_occupied_state(const SvoDev& s, const RayState& r)
+{
+    const uint32_t g = svo_level_log2(s.L, r.li);
+    if (g < 5) {
+        const uint32_t m = 32u >> g, mk = m - 1u;
+        const uint32_t v = (((uint32_t)r.c[2] & mk) * m + ((uint32_t)r.c[1] & mk)) * m + ((uint32_t)r.c[0] & mk);
+        const uint32_t* w = g == 0 ? s.pool + (uint64_t)(r.tv - 1) * 1024u
+                                   : s.sub + (uint64_t)(r.tv - 1) * 32u + (g == 3 ? 16u : 0u);
+        return (__ldg(&w[v >> 5]) >> (v & 31u)) & 1u;
     }
-    uint32_t steps = 0;
-    while (steps < max_steps) {
-        steps++;
-        if (svo_occupied(s, li, c[0], c[1], c[2])) {
-            if (li == 0) {
-                out_t = t;
-                out_c[0] = c[0]; out_c[1] = c[1]; out_c[2] = c[2];
-                out_axis = last_axis;
-                out_steps = steps;
-                return 1;
-            }
-            const uint32_t shift = li == 1 ? 5u : 1u;
-            li--;
-            const float isz = xdiv(1.0f, svo_level_size(li));
+    const uint64_t m = s.B >> (g - 5u);
+    const uint64_t idx = ((uint64_t)r.c[2] * m + (uint64_t)r.c[1]) * m + (uint64_t)r.c[0];
+    return (__ldg(&s.occ[s.occ_off[g - 5u] + (idx >> 5)]) >> (idx & 31u)) & 1u;
+}
+
+// Runs at most n loop iterations of the DDA (one iteration is one step of
+// the max_steps budget).  Returns kTraceRunning, 1 on hit (r.t, r.c,
+// r.last_axis), 0 on miss, -1 when max_steps ran out.
+__device__ __forceinline__ int svo_trace_run(const SvoDev& s, RayState& r, uint32_t max_steps, uint32_t n)
+{
+    for (uint32_t k = 0; k < n; k++) {
+        if (r.steps >= max_steps) return -1;
+        r.steps++;
+        if (svo_occupied_state(s, r)) {
+            if (r.li == 0) return 1;
+            const uint32_t g = svo_level_log2(s.L, r.li);
+            if (g == 5u) r.tv = __ldg(&s.table[((uint64_t)r.c[2] * s.B + (uint64_t)r.c[1]) * s.B + (uint64_t)r.c[0]]);
+            const uint32_t shift = g - svo_level_log2(s.L, r.li - 1);
+            r.li--;
+            const float isz = svo_level_inv_size(s, r.li);
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                const int32_t lo = c[a] << shift, hi = lo + (1 << shift) - 1;
-                c[a] = svo_cell_at(xadd(og[a], xmul(t, d[a])), isz, st[a], lo, hi);
+                const int32_t lo = r.c[a] << shift, hi = lo + (1 << shift) - 1;
+                r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], lo, hi);
             }
             continue;
         }
-        const float size = svo_level_size(li);
+        const float size = svo_level_size(s, r.li);
         float tn[3];
 #pragma unroll
         for (int a = 0; a < 3; a++)
-            tn[a] = st[a] > 0 ? xmul(xsub(xmul((float)(c[a] + 1), size), og[a]), inv[a])
-                  : st[a] < 0 ? xmul(xsub(xmul((float)c[a], size), og[a]), inv[a]) : F32_MAX_TG;
-        int32_t am = 0;
-        if (tn[1] < tn[am]) am = 1;
-        if (tn[2] < tn[am]) am = 2;
-        const float tam = am == 0 ? tn[0] : am == 1 ? tn[1] : tn[2];
-        if (tam > t) t = tam;
-        last_axis = am;
-        int32_t prev = c[am];
-        c[am] += st[am];
-        const int32_t cur0 = c[am];
-        if (cur0 < 0 || cur0 >= svo_level_cells(s, li)) { out_steps = steps; return 0; }
+            tn[a] = r.st[a] > 0 ? xmul(xsub(xmul((float)(r.c[a] + 1), size), r.og[a]), r.inv[a])
+                  : r.st[a] < 0 ? xmul(xsub(xmul((float)r.c[a], size), r.og[a]), r.inv[a]) : F32_MAX_TG;
+        // axis of the nearest face (first minimum); selects keep the state in registers
+        const bool a1 = tn[1] < tn[0];
+        const float t01 = a1 ? tn[1] : tn[0];
+        const bool a2 = tn[2] < t01;
+        const int32_t am = a2 ? 2 : a1 ? 1 : 0;
+        const float tam = a2 ? tn[2] : t01;
+        if (tam > r.t) r.t = tam;
+        r.last_axis = am;
+        int32_t prev = a2 ? r.c[2] : a1 ? r.c[1] : r.c[0];
+        const int32_t cur0 = prev + (a2 ? r.st[2] : a1 ? r.st[1] : r.st[0]);
+        r.c[0] = am == 0 ? cur0 : r.c[0];
+        r.c[1] = am == 1 ? cur0 : r.c[1];
+        r.c[2] = am == 2 ? cur0 : r.c[2];
+        if (cur0 < 0 || cur0 >= svo_level_cells(s, r.li)) return 0;
         int32_t cur = cur0;
-        while (li < s.NL - 1) {
-            const uint32_t shift = li == 0 ? 5u : 1u;
+        while (r.li < s.NL - 1) {
+            const uint32_t shift = svo_level_log2(s.L, r.li + 1) - svo_level_log2(s.L, r.li);
             if ((prev >> shift) == (cur >> shift)) break;
             prev >>= shift; cur >>= shift;
-            c[0] >>= shift; c[1] >>= shift; c[2] >>= shift;
-            li++;
+            r.c[0] >>= shift; r.c[1] >>= shift; r.c[2] >>= shift;
+            r.li++;
         }
     }
-    out_steps = steps;
-    return -1;
+    return kTraceRunning;
+}
+
+// Whole-ray form.  Returns 1 on hit (t, grid voxel c, face axis or -1), 0 on
+// miss, -1 when max_steps ran out.
+static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d[3], uint32_t max_steps, float& out_t,
+                                int32_t out_c[3], int32_t& out_axis, uint32_t& out_steps)
+{
+    RayState r;
+    int res = svo_trace_begin(s, o, d, r);
+    if (res == kTraceRunning) res = svo_trace_run(s, r, max_steps, 0xffffffffu);
+    out_steps = r.steps;
+    if (res == 1) {
+        out_t = r.t;
+        out_c[0] = r.c[0]; out_c[1] = r.c[1]; out_c[2] = r.c[2];
+        out_axis = r.last_axis;
+    }
+    return res;
 }

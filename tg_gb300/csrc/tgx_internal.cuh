@@ -86,7 +86,11 @@ enum TraceSlot
     TR_SVO_PYRAMID,
     TR_SVO_TRACE,
     TR_GI,
-    TR_MLP,
+    TR_GI_TRACE,
+    TR_MLP,          // inference
+    TR_MLP_FWD_BWD,
+    TR_MLP_WGRAD,
+    TR_MLP_ADAM,
     TR_COUNT
 };
 
@@ -155,6 +159,7 @@ struct tgx_svo
     uint32_t  n_pairs = 0;
     uint32_t* d_table = nullptr;  // B^3 entries: 0 = no block, else slot + 1
     uint32_t* d_pool = nullptr;   // n_blocks * 1024 words
+    uint32_t* d_sub = nullptr;    // n_blocks * 32 words: 4^3-cell and 8^3-cell occupancy of each block
     uint32_t* d_occ = nullptr;    // occupancy pyramid, level 0 = blocks
     uint64_t  occ_words = 0;
     uint64_t  occ_off[10] = {};   // word offset of each level
