@@ -316,11 +316,14 @@ typedef struct tgx_gi_params
 /*
  * Plain GI for one view from its visibility buffer (d_visbuf, DEVICE, as
  * tgx_vis_render wrote it) and the SVO: per pixel, direct sun light with an
- * SVO shadow ray plus `spp` cosine-weighted bounce rays through the SVO
- * (`bounces` deep), Lambertian albedo from the material LUTs (0.5 grey when
- * the scene has none).  Writes linear RGB, 3 floats per pixel, to d_rgb
- * (DEVICE).  Rays that run out of max_steps count as misses and are counted
- * in the device status.  Asynchronous.
+ * SVO shadow ray plus `spp` cosine-weighted bounce paths through the SVO
+ * (`bounces` deep, a sun shadow ray at every hit), Lambertian albedo from the
+ * material LUTs (0.5 grey when the scene has none).  The spp directions of a
+ * pixel are a stratified point set (R2 sequence, rotated per pixel and bounce
+ * by Philox4x32-10 keyed by `seed`, `frame`).  Writes linear RGB, 3 floats per
+ * pixel, to d_rgb (DEVICE).  Rays that run out of max_steps count as misses
+ * and are counted in the device status.  Asynchronous; scratch grows in the
+ * context (at most 16 M paths in flight).
  */
 tgx_status  tgx_gi_render(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, const tgx_view* view,
                           const uint64_t* d_visbuf, const tgx_gi_params* params, float* d_rgb);

@@ -22,10 +22,9 @@
  *    177-228 in cluster space and rotated to world space.
  *  - bounce lighting: Lambertian albedo from the material LUT, a directional
  *    sun with an SVO shadow ray, a constant sky, cosine-weighted secondary
- *    directions (Malley's method, rejection-sampled unit disk) in the
- *    orthonormal basis of Duff et al. 2017, random numbers from
- *    Philox4x32-10 (Salmon et al. 2011) keyed by the seed and counted by
- *    (pixel, sample, bounce|frame, draw).
+ *    directions from a randomised R2 point set per (pixel, bounce) (see
+ *    sample_cosine), random numbers from Philox4x32-10 (Salmon et al. 2011)
+ *    keyed by the seed and counted by (pixel, bounce, frame, tag).
  */
 #include "oracle_common.h"
 
@@ -266,6 +265,7 @@ int oracle_trace(const void* h, const float o[3], const float d[3], uint32_t max
         c[am] += st[am];
         if (c[am] < 0 || c[am] >= level_cells(s, li)) { *out_steps = steps; return 0; }
         int32_t cur = c[am];
+        /* the step left the parent cell: ascend to the level whose parent it stayed in */
         while (li < s->NL - 1)
         {
             const uint32_t shift = s->lg[li + 1] - s->lg[li];
@@ -353,8 +353,31 @@ typedef struct
 
 #define OR_INV_PI 0.318309886f
 
-/* cosine-weighted direction about unit n (Malley; Duff et al. basis) */
-static void sample_cosine(const float n[3], uint32_t pixel, uint32_t sample, uint32_t bounce, const ogi_params* p,
+/*
+ * sin and cos on [-pi/4, pi/4] from their Taylor series (degree 7 and 8),
+ * Horner form in binary32; only + and * so every platform rounds alike.
+ */
+static inline float sin_q(float x)
+{
+    const float x2 = x * x;
+    return x * (1.0f + x2 * (-0.16666667f + x2 * (0.0083333333f + x2 * -0.00019841270f)));
+}
+static inline float cos_q(float x)
+{
+    const float x2 = x * x;
+    return 1.0f + x2 * (-0.5f + x2 * (0.041666668f + x2 * (-0.0013888889f + x2 * 0.000024801587f)));
+}
+
+/*
+ * Cosine-weighted direction about unit n for sample `sample` of a pixel (or
+ * training point) `key`: randomised quasi-Monte Carlo.  The 2D point is the
+ * R2 sequence (Roberts 2018, plastic-number additive recurrence, in 32-bit
+ * fixed point) at index `sample`, rotated (Cranley-Patterson) by Philox
+ * counter (key, bounce, frame, tag); it is mapped to the unit disk by the
+ * concentric map of Shirley and Chiu (1997), lifted to the hemisphere
+ * (Malley) and expressed in the orthonormal basis of Duff et al. (2017).
+ */
+static void sample_cosine(const float n[3], uint32_t key, uint32_t sample, uint32_t bounce, const ogi_params* p,
                           float out[3])
 {
     const float sign = n[2] >= 0.0f ? 1.0f : -1.0f;
@@ -362,24 +385,35 @@ static void sample_cosine(const float n[3], uint32_t pixel, uint32_t sample, uin
     const float b = n[0] * n[1] * a;
     const float t1[3] = { 1.0f + sign * n[0] * n[0] * a, sign * b, -sign * n[0] };
     const float t2[3] = { b, sign + n[1] * n[1] * a, -n[1] };
-    for (uint32_t draw = 0; draw < 8; draw++)
+    uint32_t c[4] = { key, bounce, p->frame, 0x52325351u };
+    philox(c, (uint32_t)p->seed, (uint32_t)(p->seed >> 32));
+    const uint32_t qx = sample * 3242174889u + c[0];
+    const uint32_t qy = sample * 2447445413u + c[1];
+    const float u = 2.0f * u01(qx) - 1.0f;
+    const float v = 2.0f * u01(qy) - 1.0f;
+    float dx = 0.0f, dy = 0.0f;
+    if (fabsf(u) > fabsf(v))
     {
-        uint32_t c[4] = { pixel, sample, bounce | (p->frame << 8), draw };
-        philox(c, (uint32_t)p->seed, (uint32_t)(p->seed >> 32));
-        for (int k = 0; k < 2; k++)
-        {
-            const float u = 2.0f * u01(c[2 * k]) - 1.0f;
-            const float v = 2.0f * u01(c[2 * k + 1]) - 1.0f;
-            const float r2 = u * u + v * v;
-            if (r2 < 1.0f)
-            {
-                const float z = sqrtf(1.0f - r2);
-                for (int i = 0; i < 3; i++) out[i] = u * t1[i] + v * t2[i] + z * n[i];
-                return;
-            }
-        }
+        const float phi = 0.78539819f * (v / u);
+        dx = u * cos_q(phi);
+        dy = u * sin_q(phi);
     }
-    out[0] = n[0]; out[1] = n[1]; out[2] = n[2];
+    else if (v != 0.0f)
+    {
+        const float phi = 0.78539819f * (u / v);
+        dx = v * sin_q(phi);
+        dy = v * cos_q(phi);
+    }
+    const float r2 = dx * dx + dy * dy;
+    const float z = r2 < 1.0f ? sqrtf(1.0f - r2) : 0.0f;
+    for (int i = 0; i < 3; i++) out[i] = dx * t1[i] + dy * t2[i] + z * n[i];
+}
+
+/* test hook: the sampler above for n directions of one key */
+void oracle_sample_cosine(const float n[3], uint32_t key, uint32_t first_sample, uint32_t count, uint32_t bounce,
+                          const void* params, float* out)
+{
+    for (uint32_t k = 0; k < count; k++) sample_cosine(n, key, first_sample + k, bounce, (const ogi_params*)params, &out[3 * k]);
 }
 
 static void svo_albedo(const osvo* s, const int32_t c[3], const tgx_material* luts, float out[3])

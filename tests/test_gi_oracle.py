@@ -135,3 +135,36 @@ def test_sub_block_masks(oracle):
         want[:16] = np.packbits(c4.astype(np.uint8), bitorder="little").view(np.uint32)
         want[16:18] = np.packbits(c8.astype(np.uint8), bitorder="little").view(np.uint32)
         assert np.array_equal(out, want)
+
+
+def _sample(oracle, n, key, first, count, bounce=0, frame=0, seed=2):
+    p = tg.gi_params(spp=count, bounces=1, seed=seed, frame=frame)
+    nn = np.asarray(n, np.float32)
+    out = np.zeros((count, 3), np.float32)
+    oracle.lib.oracle_sample_cosine(C.c_void_p(nn.ctypes.data), C.c_uint32(key), C.c_uint32(first),
+                                    C.c_uint32(count), C.c_uint32(bounce), C.c_void_p(p.ctypes.data),
+                                    C.c_void_p(out.ctypes.data))
+    return out
+
+
+def test_sampler_is_cosine_weighted_and_stratified(oracle):
+    """The randomised R2 + concentric-map sampler gives unit directions in the
+    hemisphere with the cosine density (E[cos] = 2/3, E[cos^2] = 1/2), and
+    the mean over the samples of one key varies far less across keys than
+    independent samples would (stratification)."""
+    n = np.array([0.36, -0.48, 0.8], np.float32)
+    d = np.concatenate([_sample(oracle, n, key, 0, 64) for key in range(256)])
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=2e-6)
+    c = d @ n.astype(np.float64)
+    assert (c >= -1e-6).all()
+    assert abs(c.mean() - 2.0 / 3.0) < 0.005
+    assert abs((c ** 2).mean() - 0.5) < 0.005
+    means = c.reshape(256, 64).mean(axis=1)
+    iid_var = c.var() / 64
+    assert means.var() < 0.1 * iid_var
+    # other keys, bounces and frames rotate the point set differently
+    a = _sample(oracle, n, 5, 0, 8)
+    assert not np.array_equal(a, _sample(oracle, n, 6, 0, 8))
+    assert not np.array_equal(a, _sample(oracle, n, 5, 0, 8, bounce=1))
+    assert not np.array_equal(a, _sample(oracle, n, 5, 0, 8, frame=1))
+    assert np.array_equal(a[3:], _sample(oracle, n, 5, 3, 5))

@@ -3,7 +3,8 @@
 BF16 weights and activations with FP32 accumulation: outputs and gradients
 are compared with stated tolerances (the oracle runs on the same weights
 rounded to BF16, so the difference is the BF16 rounding of the activations
-and deltas): outputs within 3% relative + 0.02 absolute; per-layer gradients
+and deltas): outputs within 3% relative + 4% of the mean output magnitude,
+mean error below 0.6% of it; per-layer gradients
 within 5% relative L2 error (8% for W0, whose gradient sums 2000 samples of
 +-1 sin/cos features with heavy cancellation) and cosine similarity above
 0.998."""
@@ -41,20 +42,27 @@ def mlp_oracle(oracle):
     return OracleMlp(oracle)
 
 
-def test_forward_matches_fp64_oracle(ctx, mlp_oracle):
+@pytest.mark.parametrize("n", [1000, 40000])   # a partial tile; several 128-query tiles per CTA
+def test_forward_matches_fp64_oracle(ctx, mlp_oracle, n):
     import torch
     cache = tg.Cache(ctx, seed=3)
     w = cache.get_weights()
-    x, _ = batch(1000, 1)                      # not a multiple of 16
+    x, _ = batch(n, 1)
     dx = torch.from_numpy(x).cuda()
-    y = torch.empty((1000, 3), dtype=torch.float32, device="cuda")
+    y = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     cache.infer(dx, y)
     ctx.sync()
+    assert ctx.device_error().code == 0
     g = y.cpu().numpy()
     ref = mlp_oracle.forward(bf16_round(w).astype(np.float64), x)
     scale = np.abs(ref).mean()
     assert scale > 1e-3
-    assert np.all(np.abs(g - ref) <= 0.03 * np.abs(ref) + 0.02 * scale), np.abs(g - ref).max()
+    err = np.abs(g - ref)
+    # BF16 rounding of the features and of four hidden layers: every output
+    # within 3% + 4% of the mean magnitude, and the mean error below 0.6% of
+    # it (a layout or operand mistake gives errors of the order of the outputs)
+    assert np.all(err <= 0.03 * np.abs(ref) + 0.04 * scale), err.max()
+    assert err.mean() <= 0.006 * scale, (err.mean(), scale)
     cache.close()
 
 

@@ -15,8 +15,8 @@
 //     basis) of up to `bounces` SVO bounces, accumulated forward with their
 //     throughput; a miss sees the sky, a hit adds the sun light arriving
 //     there (with its own shadow ray);
-//   - random numbers: Philox4x32-10 keyed by the seed, counter (key, sample,
-//     bounce | frame << 8, draw), key = pixel index.
+//   - sample directions: a randomised R2 point set per (key, bounce) with
+//     Philox4x32-10 rotations keyed by the seed, key = pixel index.
 //
 // Execution is a wavefront over path roots (one per geometry pixel, or one
 // per training sample of the cache):
@@ -41,7 +41,6 @@ namespace {
 
 constexpr float kInvPi = 0.318309886f;
 constexpr uint32_t kMaxBounces = 4;
-constexpr uint32_t kStepsPerRound = 8;                // DDA steps between queue refills
 constexpr uint64_t kMaxPathsPerChunk = 16ull << 20;   // paths in flight per wavefront chunk
 
 struct GiParams
@@ -103,7 +102,26 @@ __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
 
 __device__ __forceinline__ float u01(uint32_t x) { return xmul((float)(x >> 8), 1.0f / 16777216.0f); }
 
-__device__ void sample_cosine(const float n[3], uint32_t pixel, uint32_t sample, uint32_t bounce, const GiParams& p,
+// sin and cos on [-pi/4, pi/4]: Taylor series of degree 7 and 8 in Horner
+// form with exactly rounded operations (the oracle evaluates the same steps)
+__device__ __forceinline__ float sin_q(float x)
+{
+    const float x2 = xmul(x, x);
+    return xmul(x, xadd(1.0f, xmul(x2, xadd(-0.16666667f, xmul(x2, xadd(0.0083333333f, xmul(x2, -0.00019841270f)))))));
+}
+__device__ __forceinline__ float cos_q(float x)
+{
+    const float x2 = xmul(x, x);
+    return xadd(1.0f, xmul(x2, xadd(-0.5f, xmul(x2, xadd(0.041666668f,
+                                                         xmul(x2, xadd(-0.0013888889f, xmul(x2, 0.000024801587f))))))));
+}
+
+// Cosine-weighted direction about unit n for sample `sample` of `key`:
+// randomised quasi-Monte Carlo.  R2 point (Roberts 2018, 32-bit fixed point)
+// at index `sample`, rotated by Philox counter (key, bounce, frame, tag);
+// concentric map to the disk (Shirley and Chiu 1997), lifted to the
+// hemisphere (Malley), in the basis of Duff et al. (2017).
+__device__ void sample_cosine(const float n[3], uint32_t key, uint32_t sample, uint32_t bounce, const GiParams& p,
                               float out[3])
 {
     const float sign = n[2] >= 0.0f ? 1.0f : -1.0f;
@@ -111,23 +129,24 @@ __device__ void sample_cosine(const float n[3], uint32_t pixel, uint32_t sample,
     const float b = xmul(xmul(n[0], n[1]), a);
     const float t1[3] = {xadd(1.0f, xmul(xmul(xmul(sign, n[0]), n[0]), a)), xmul(sign, b), xmul(-sign, n[0])};
     const float t2[3] = {b, xadd(sign, xmul(xmul(n[1], n[1]), a)), -n[1]};
-    for (uint32_t draw = 0; draw < 8; draw++) {
-        uint32_t c[4] = {pixel, sample, bounce | (p.frame << 8), draw};
-        philox(c, (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            const float u = xsub(xmul(2.0f, u01(c[2 * k])), 1.0f);
-            const float v = xsub(xmul(2.0f, u01(c[2 * k + 1])), 1.0f);
-            const float r2 = xadd(xmul(u, u), xmul(v, v));
-            if (r2 < 1.0f) {
-                const float z = xsqrt(xsub(1.0f, r2));
-#pragma unroll
-                for (int i = 0; i < 3; i++) out[i] = xadd(xadd(xmul(u, t1[i]), xmul(v, t2[i])), xmul(z, n[i]));
-                return;
-            }
-        }
+    uint32_t c[4] = {key, bounce, p.frame, 0x52325351u};
+    philox(c, (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
+    const float u = xsub(xmul(2.0f, u01(sample * 3242174889u + c[0])), 1.0f);
+    const float v = xsub(xmul(2.0f, u01(sample * 2447445413u + c[1])), 1.0f);
+    float dx = 0.0f, dy = 0.0f;
+    if (fabsf(u) > fabsf(v)) {
+        const float phi = xmul(0.78539819f, xdiv(v, u));
+        dx = xmul(u, cos_q(phi));
+        dy = xmul(u, sin_q(phi));
+    } else if (v != 0.0f) {
+        const float phi = xmul(0.78539819f, xdiv(u, v));
+        dx = xmul(v, sin_q(phi));
+        dy = xmul(v, cos_q(phi));
     }
-    out[0] = n[0]; out[1] = n[1]; out[2] = n[2];
+    const float r2 = xadd(xmul(dx, dx), xmul(dy, dy));
+    const float z = r2 < 1.0f ? xsqrt(xsub(1.0f, r2)) : 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) out[i] = xadd(xadd(xmul(dx, t1[i]), xmul(dy, t2[i])), xmul(z, n[i]));
 }
 
 __device__ __forceinline__ void svo_albedo(const SvoDev& s, const int32_t c[3], const tgx_material* luts, float out[3])
@@ -290,8 +309,15 @@ __global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __rest
                                                      uint32_t mul_a, const Ray* __restrict__ rb,
                                                      RayHit* __restrict__ hb, uint32_t mul_b,
                                                      const uint32_t* __restrict__ n_dev, uint32_t max_steps,
-                                                     uint32_t* __restrict__ queue, uint32_t* __restrict__ exhausted)
+                                                     uint32_t steps_per_round, uint32_t* __restrict__ queue,
+                                                     uint32_t* __restrict__ exhausted)
 {
+    __shared__ uint32_t occ_off[16];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) occ_off[i] = s.occ_off[i];
+    }
+    __syncthreads();
     const uint32_t n = *n_dev;
     const uint32_t n_a = n * mul_a, n_tot = n_a + n * mul_b;
     const uint32_t lane = threadIdx.x & 31u;
@@ -320,7 +346,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __rest
         }
         if (__all_sync(0xffffffffu, empty)) break;
         if (have) {
-            const int res = svo_trace_run(s, r, max_steps, kStepsPerRound);
+            const int res = svo_trace_run(s, occ_off, r, max_steps, steps_per_round);
             if (res != kTraceRunning) {
                 if (res < 0) atomicAdd(exhausted, 1u);
                 write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
@@ -372,6 +398,7 @@ __global__ void __launch_bounds__(256) k_gi_emit(const PathRoot* __restrict__ ro
             float w[3];
             sample_cosine(rt.n, rt.key, s0 + (uint32_t)(i % cs), 0, p, w);
             set_ray(rays[i], rt.o, w);
+            if (!st) continue;   // first-bounce queries keep no path state
             PathState ps;
             ps.v[0] = ps.v[1] = ps.v[2] = 0.0f;
             ps.T[0] = ps.T[1] = ps.T[2] = 1.0f;
@@ -687,7 +714,7 @@ tgx_status trace_lists(tgx_ctx* c, const SvoDev& s, const Ray* ra, RayHit* ha, u
 {
     TGX_CUDA(cudaMemsetAsync(queue, 0, 4, c->stream));
     TGX_LAUNCH(c, TR_GI_TRACE, trace_grid(c), 128, 0, k_trace_queue, s, ra, ha, mul_a, rb, hb, mul_b, n_dev, max_steps,
-               queue, exhausted);
+               c->trace_steps_per_round, queue, exhausted);
     return TGX_OK;
 }
 
@@ -824,7 +851,7 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     for (uint32_t s0 = 0; s0 < p.spp; s0 += cs) {
         const uint32_t n = std::min(cs, p.spp - s0);
         const bool first = s0 == 0;
-        TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_emit, b.roots, &counters[CC_ROOTS], n, s0, p, b.rb, b.st,
+        TGX_LAUNCH(c, TR_GI, eg, 256, 0, k_gi_emit, b.roots, &counters[CC_ROOTS], n, s0, p, b.rb, (PathState*)nullptr,
                    first ? b.root_rays : nullptr);
         TGX_TRY(trace_lists(c, s, b.rb, b.hb, n, b.root_rays, b.root_hits, first ? 1u : 0u, &counters[CC_ROOTS],
                             p.max_steps, &counters[CC_QUEUE], exhausted));

@@ -5,20 +5,24 @@
 //   9 inputs (position normalised to [0,1]^3, normal, direction) ->
 //   216 sin/cos features (12 octaves of pi) -> 4 ReLU layers of 64 -> RGB,
 //   no biases, relative L2 loss, Adam.
-// Weights and activations are BF16, accumulation is FP32 (mma.sync
-// m16n8k16 bf16), master weights and Adam moments are FP32.
+// Weights and activations are BF16, accumulation is FP32, master weights and
+// Adam moments are FP32.  Inference runs on tcgen05 (TMEM accumulators);
+// training on mma.sync m16n8k16.
 //
 // Kernels:
-//   k_mlp_forward   one warp per 16 inputs: encoding straight into A
-//                   fragments, four hidden layers with the accumulators of
-//                   one layer re-packed as the A fragments of the next, RGB.
-//   k_mlp_fwd_bwd   the same forward, the relative-L2 gradient, and the
+//   k_mlp_forward_tc inference on tcgen05: 128 queries per tile, operands in
+//                   shared memory, FP32 accumulators in TMEM, one elected
+//                   thread issues the MMAs of a layer (below).
+//   k_mlp_fwd_bwd   one warp per 16 samples: the forward with the accumulators
+//                   of one layer re-packed as the A fragments of the next, the
+//                   relative-L2 gradient, and the
 //                   backward pass through W4..W1 (deltas masked by ReLU');
 //                   writes each layer's input activations and output deltas
 //                   (BF16) for the weight gradients.
-//   k_mlp_wgrad     dW_l = sum_s delta_l[s] (x) act_l[s] on the tensor cores
-//                   (ldmatrix.trans tiles of 16 samples), split over samples,
-//                   FP32 atomics into the gradient.
+//   k_mlp_wgrad     dW_l = sum_s delta_l[s] (x) act_l[s] for all layers in one
+//                   launch, on the tensor cores (ldmatrix.trans tiles of 16
+//                   samples), split over samples, per-CTA sums in shared
+//                   memory, FP32 atomics into the gradient.
 //   k_mlp_adam      Adam on the FP32 master weights; refreshes the BF16
 //                   copies in the layouts the kernels read (row-major for the
 //                   forward, transposed for the backward).
@@ -52,7 +56,6 @@ constexpr int B_W2T = B_W1T + NH * SH;
 constexpr int B_W3T = B_W2T + NH * SH;
 constexpr int B_W4T = B_W3T + NH * SH;       // [64][S4T], cols >= 3 zero
 constexpr int B_TOTAL = B_W4T + NH * S4T;
-constexpr int B_FWD = B_W1T;                 // the forward needs only the first part
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
@@ -161,35 +164,226 @@ __device__ __forceinline__ void forward_tile(const __nv_bfloat16* sw, const floa
     }
 }
 
-// n inputs, or min(n, *n_dev) when n_dev is given (a count produced on the device)
-__global__ void __launch_bounds__(128) k_mlp_forward(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
-                                                    const uint32_t* __restrict__ n_dev, const float* __restrict__ x,
-                                                    float* __restrict__ y)
+// ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
+// ---------------------------------------------------------------------------
+//
+// One CTA of 128 threads per SM, persistent over tiles of 128 queries; thread
+// t owns query t of the tile, which is row t of every GEMM and TMEM lane t.
+// Shared memory holds the weights and the A operand of the current layer in
+// the canonical no-swizzle K-major layout: 8 x 8 BF16 core matrices (8 rows
+// of 16 contiguous bytes), K-adjacent core matrices LBO bytes apart and
+// row-group-adjacent ones SBO bytes apart.  Per layer one elected thread
+// issues tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) and
+// commits to an mbarrier; then each warp reads its 32 TMEM lanes with
+// tcgen05.ld, applies ReLU and writes the next layer's A operand.
+
+namespace tc {
+
+constexpr int M = 128;                      // queries per tile
+constexpr int KG0 = NEP / 8;                // 28 K core-matrix columns of layer 0
+constexpr int KGH = NH / 8;                 // 8 of the hidden layers
+// byte offsets in dynamic shared memory (all 1024-aligned)
+constexpr int W0 = 0;                                   // [28 kg][8 ng][128 B]
+constexpr int W1 = W0 + KG0 * 8 * 128;                  // [8 kg][8 ng][128 B] x 3
+constexpr int W4 = W1 + 3 * KGH * 8 * 128;              // [8 kg][2 ng][128 B] (16 rows, 3 real)
+constexpr int A0 = W4 + KGH * 2 * 128;                  // [28 kg][16 mg][128 B]
+constexpr int A1 = A0 + KG0 * 16 * 128;                 // [8 kg][16 mg][128 B]
+constexpr int BAR = A1 + KGH * 16 * 128;                // mbarrier (8 B) + TMEM address (4 B)
+constexpr int SMEM = BAR + 64;
+constexpr uint32_t TMEM_COLS = 64;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
+__host__ __device__ constexpr uint32_t idesc(uint32_t n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(M >> 4) << 24); }
+
+// shared-memory matrix descriptor, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    if (n_dev) n = min(n, *n_dev);
-    load_weights(sw, wimg, B_FWD);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
-    const uint32_t tiles = (n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
-        const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
-        float x0[NI], x1[NI];
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 :: "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+}
+
+// bounded wait for mbarrier phase `parity`; false when the limit ran out
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kWaitLimit; i++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
 #pragma unroll
-        for (int i = 0; i < NI; i++) {
-            x0[i] = r0 < n ? x[(uint64_t)r0 * NI + i] : 0.0f;
-            x1[i] = r1 < n ? x[(uint64_t)r1 * NI + i] : 0.0f;
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// row `row` of an A tile: the 8 BF16 values of core-matrix column kg
+__device__ __forceinline__ void put8(unsigned char* a, int kg, int row, const float* v)
+{
+    uint4 q;
+    q.x = pack_bf16(v[0], v[1]); q.y = pack_bf16(v[2], v[3]);
+    q.z = pack_bf16(v[4], v[5]); q.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(a + kg * (16 * 128) + (row >> 3) * 128 + (row & 7) * 16) = q;
+}
+
+// copies rows [0, n_rows) of a BF16 image matrix ([row][stride], K real columns
+// padded to kgs * 8) into the core-matrix layout [kg][row / 8][128 B]; rows up
+// to pad_rows are zero
+__device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfloat16* src, int stride, int n_rows,
+                                              int pad_rows, int kgs)
+{
+    const int ngs = pad_rows / 8;
+    for (int e = threadIdx.x; e < pad_rows * kgs; e += blockDim.x) {
+        const int row = e % pad_rows, kg = e / pad_rows;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (row < n_rows) v = *reinterpret_cast<const uint4*>(src + (size_t)row * stride + kg * 8);
+        *reinterpret_cast<uint4*>(dst + kg * (ngs * 128) + (row >> 3) * 128 + (row & 7) * 16) = v;
+    }
+}
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
+                                                          const uint32_t* __restrict__ n_dev,
+                                                          const float* __restrict__ x, float* __restrict__ y,
+                                                          tgx_dev_status* __restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    using namespace tc;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + BAR);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + BAR + 8);
+    if (n_dev) n = min(n, *n_dev);
+    // weights into the core-matrix layout
+    stage_weights(sm + W0, wimg + B_W0, S0, NH, NH, KG0);
+    stage_weights(sm + W1 + 0 * KGH * 8 * 128, wimg + B_W1, SH, NH, NH, KGH);
+    stage_weights(sm + W1 + 1 * KGH * 8 * 128, wimg + B_W2, SH, NH, NH, KGH);
+    stage_weights(sm + W1 + 2 * KGH * 8 * 128, wimg + B_W3, SH, NH, NH, KGH);
+    stage_weights(sm + W4, wimg + B_W4, SH, 8, 16, KGH);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(saddr(tmem_slot)), "r"(TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = tmem + ((warp * 32u) << 16);   // this warp's 32 TMEM lanes
+    const uint32_t b = saddr(bar);
+    uint32_t phase = 0;
+    bool ok = true;
+    const uint32_t tiles = (n + M - 1) / M;
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const uint32_t row = tile * M + tid;
+        // layer 0 input: the 216 sin/cos features of this thread's query
+        {
+            float xi[NI];
+#pragma unroll
+            for (int i = 0; i < NI; i++) xi[i] = row < n ? x[(uint64_t)row * NI + i] : 0.0f;
+            float f[8];
+#pragma unroll
+            for (int kg = 0; kg < KG0; kg++) {
+#pragma unroll
+                for (int j = 0; j < 8; j += 2) {
+                    const int c = kg * 8 + j;   // feature pair (sin, cos) of input c / 24, octave (c / 2) % 12
+                    if (c < NE) sincospif(xi[c / (2 * NF)] * (float)(1 << ((c / 2) % NF)), &f[j], &f[j + 1]);
+                    else f[j] = f[j + 1] = 0.0f;
+                }
+                put8(sm + A0, kg, (int)tid, f);
+            }
         }
-        uint32_t H[4][4][4];
-        float acc4[4];
-        forward_tile(sw, x0, x1, g, t, H, acc4, nullptr, 0, 0);
-        // output columns 2t, 2t+1: real for t = 0 (0, 1) and t = 1 (2)
-        if (t < 2) {
-            if (r0 < n) { y[(uint64_t)r0 * NO + 2 * t] = acc4[0]; if (t == 0) y[(uint64_t)r0 * NO + 1] = acc4[1]; }
-            if (r1 < n) { y[(uint64_t)r1 * NO + 2 * t] = acc4[2]; if (t == 0) y[(uint64_t)r1 * NO + 1] = acc4[3]; }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        // five layers; the hidden ones write the next A operand into A1
+        for (int l = 0; l < 5 && ok; l++) {
+            if (tid == 0) {
+                fence_after();
+                const int kgs = l == 0 ? KG0 : KGH;
+                const uint32_t a_base = saddr(sm + (l == 0 ? A0 : A1));
+                const uint32_t w_base = saddr(sm + (l == 0 ? W0 : l < 4 ? W1 + (l - 1) * KGH * 8 * 128 : W4));
+                const uint32_t n_out = l < 4 ? 64u : 16u;
+                const uint32_t w_sbo = 128, w_lbo = (n_out / 8) * 128;
+                for (int k = 0; k < kgs / 2; k++)
+                    mma(tmem, sdesc(a_base + 2 * k * (16 * 128), 16 * 128, 128),
+                        sdesc(w_base + 2 * k * w_lbo, w_lbo, w_sbo), idesc(n_out), k > 0);
+                commit(b);
+            }
+            // every thread waits; one that gives up makes the whole CTA stop
+            if (__syncthreads_or(!wait(b, phase))) {
+                if (tid == 0) dev_error(status, TGX_ERR_TIMEOUT, 40 + l, tile);
+                ok = false;
+                break;
+            }
+            phase ^= 1u;
+            fence_after();
+            if (l < 4) {
+                float v[16];
+#pragma unroll 1
+                for (int q = 0; q < 4; q++) {
+                    ld16(lane_base + q * 16, v);
+                    ld_wait();
+#pragma unroll
+                    for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i], 0.0f);
+                    put8(sm + A1, 2 * q, (int)tid, v);
+                    put8(sm + A1, 2 * q + 1, (int)tid, v + 8);
+                }
+                fence_async_smem();
+            } else {
+                float v[16];
+                ld16(lane_base, v);
+                ld_wait();
+                if (row < n) {
+                    y[(uint64_t)row * NO + 0] = v[0];
+                    y[(uint64_t)row * NO + 1] = v[1];
+                    y[(uint64_t)row * NO + 2] = v[2];
+                }
+            }
+            fence_before();
+            __syncthreads();
         }
     }
+    if (!ok) wait(b, phase);   // let MMAs still in flight land (bounded) before the columns are freed
+    fence_after();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
 // Training forward + backward.  Writes, per sample s:
@@ -304,23 +498,43 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t& r0, uint32_t& r1, uint32
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
 }
 
-// Weight gradient of one layer: grad[o][i] += sum_s D[s][o] * X[s][i] for an
-// o-range of 16 and i-range of 64, over a range of samples.  D rows have
-// dstride elements (o), X rows xstride (i).  One warp per (o-tile, i-group, chunk).
-__global__ void __launch_bounds__(128) k_mlp_wgrad(const __nv_bfloat16* __restrict__ D, int dstride, int n_o,
-                                                  const __nv_bfloat16* __restrict__ X, int xstride, int n_i,
-                                                  uint32_t n, uint32_t chunk, float* __restrict__ grad, int gstride)
+// Weight gradients of all five layers in one launch: grad_l[o][i] +=
+// sum_s D_l[s][o] * X_l[s][i].  A CTA owns one 16 (o) x 64 (i) tile of one
+// layer and a range of 4 * chunk samples; each of its warps reduces `chunk`
+// samples on the tensor cores (ldmatrix.trans tiles of 16 samples), the four
+// partial tiles are summed in shared memory and added to the gradient with
+// FP32 atomics.
+struct WgradLayer
+{
+    const __nv_bfloat16* D;   // [s][ds], o < no real
+    const __nv_bfloat16* X;   // [s][xs], i < ni real
+    float* grad;              // [no][ni]
+    int ds, no, xs, ni;
+    int o_tiles, i_groups;
+    uint32_t first_cta;
+};
+struct WgradArgs
+{
+    WgradLayer l[5];
+    uint32_t n, chunk, ctas_per_tile;
+};
+
+__global__ void __launch_bounds__(128) k_mlp_wgrad(WgradArgs args)
 {
     __shared__ __align__(16) __nv_bfloat16 sD[4][16][24];
     __shared__ __align__(16) __nv_bfloat16 sX[4][16][72];
+    __shared__ float red[3][32][33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
-    const int o_tiles = (n_o + 15) / 16, i_groups = (n_i + 63) / 64;
-    const uint32_t chunks = (n + chunk - 1) / chunk;
-    const uint32_t task = blockIdx.x * 4 + warp;
-    if (task >= (uint32_t)o_tiles * i_groups * chunks) return;
-    const int ot = task % o_tiles, ig = (task / o_tiles) % i_groups;
-    const uint32_t ck = task / (o_tiles * i_groups);
-    const uint32_t s_begin = ck * chunk, s_end = min(n, s_begin + chunk);
+    int li = 0;
+#pragma unroll
+    for (int k = 1; k < 5; k++)
+        if (blockIdx.x >= args.l[k].first_cta) li = k;
+    const WgradLayer& L = args.l[li];
+    const uint32_t local = blockIdx.x - L.first_cta;
+    const uint32_t tile = local / args.ctas_per_tile, part = local % args.ctas_per_tile;
+    const int ot = (int)(tile % L.o_tiles), ig = (int)(tile / L.o_tiles);
+    const uint32_t s_begin = (part * 4 + warp) * args.chunk;
+    const uint32_t s_end = min(args.n, s_begin + args.chunk);
     float acc[8][4];
 #pragma unroll
     for (int q = 0; q < 8; q++) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
@@ -332,7 +546,7 @@ __global__ void __launch_bounds__(128) k_mlp_wgrad(const __nv_bfloat16* __restri
             const uint32_t s = s0 + r;
             uint4 v = make_uint4(0, 0, 0, 0);
             const int oc = ot * 16 + h * 8;
-            if (s < s_end && oc < dstride) v = *reinterpret_cast<const uint4*>(D + (uint64_t)s * dstride + oc);
+            if (s < s_end && oc < L.ds) v = *reinterpret_cast<const uint4*>(L.D + (uint64_t)s * L.ds + oc);
             *reinterpret_cast<uint4*>(&sD[warp][r][h * 8]) = v;
         }
         for (int e = lane; e < 16 * 8; e += 32) {
@@ -340,7 +554,7 @@ __global__ void __launch_bounds__(128) k_mlp_wgrad(const __nv_bfloat16* __restri
             const uint32_t s = s0 + r;
             const int ic = ig * 64 + h * 8;
             uint4 v = make_uint4(0, 0, 0, 0);
-            if (s < s_end && ic < xstride) v = *reinterpret_cast<const uint4*>(X + (uint64_t)s * xstride + ic);
+            if (s < s_end && ic < L.xs) v = *reinterpret_cast<const uint4*>(L.X + (uint64_t)s * L.xs + ic);
             *reinterpret_cast<uint4*>(&sX[warp][r][h * 8]) = v;
         }
         __syncwarp();
@@ -364,15 +578,29 @@ __global__ void __launch_bounds__(128) k_mlp_wgrad(const __nv_bfloat16* __restri
             mma16816(acc[2 * q + 1], a, b2, b3);
         }
     }
-    // accumulate: C rows o = ot*16 + g (+8), cols i = ig*64 + q*8 + 2t (+1)
+    // sum the four warps' tiles in shared memory, then one atomic per element
+    if (warp > 0) {
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int i = ig * 64 + q * 8 + 2 * t;
-        const int o0 = ot * 16 + g, o1 = o0 + 8;
-        if (o0 < n_o && i < n_i) atomicAdd(&grad[o0 * gstride + i], acc[q][0]);
-        if (o0 < n_o && i + 1 < n_i) atomicAdd(&grad[o0 * gstride + i + 1], acc[q][1]);
-        if (o1 < n_o && i < n_i) atomicAdd(&grad[o1 * gstride + i], acc[q][2]);
-        if (o1 < n_o && i + 1 < n_i) atomicAdd(&grad[o1 * gstride + i + 1], acc[q][3]);
+        for (int q = 0; q < 8; q++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) red[warp - 1][lane][q * 4 + e] = acc[q][e];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[q][e] += red[0][lane][q * 4 + e] + red[1][lane][q * 4 + e] + red[2][lane][q * 4 + e];
+        // C rows o = ot*16 + g (+8), cols i = ig*64 + q*8 + 2t (+1)
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int i = ig * 64 + q * 8 + 2 * t;
+            const int o0 = ot * 16 + g, o1 = o0 + 8;
+            if (o0 < L.no && i < L.ni) atomicAdd(&L.grad[o0 * L.ni + i], acc[q][0]);
+            if (o0 < L.no && i + 1 < L.ni) atomicAdd(&L.grad[o0 * L.ni + i + 1], acc[q][1]);
+            if (o1 < L.no && i < L.ni) atomicAdd(&L.grad[o1 * L.ni + i], acc[q][2]);
+            if (o1 < L.no && i + 1 < L.ni) atomicAdd(&L.grad[o1 * L.ni + i + 1], acc[q][3]);
+        }
     }
 }
 
@@ -512,36 +740,35 @@ extern "C" tgx_status tgx_cache_set_weights(tgx_ctx* c, tgx_cache* k, const floa
     return TGX_OK;
 }
 
-static int fwd_smem() { return B_FWD * 2; }
-static bool g_fwd_attr = false;
 static int all_smem() { return B_TOTAL * 2; }
+
+// inference of n queries (min(n, *d_n) when d_n is given) on the tcgen05 kernel
+static tgx_status cache_forward(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t n, const float* d_x,
+                                float* d_rgb)
+{
+    static bool attr = false;
+    if (!attr) {
+        TGX_CUDA(cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM));
+        attr = true;
+    }
+    const uint32_t tiles = (n + tc::M - 1) / tc::M;
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)c->num_sms));
+    TGX_LAUNCH(c, TR_MLP, grid, 128, tc::SMEM, k_mlp_forward_tc, k->img, n, d_n, d_x, d_rgb, c->d_status);
+    return TGX_OK;
+}
 
 extern "C" tgx_status tgx_cache_infer(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, float* d_rgb)
 {
     if (!c || !k || (n && (!d_x || !d_rgb))) return TGX_ERR_INVALID_ARGUMENT;
     if (!n) return TGX_OK;
-    if (!g_fwd_attr) {
-        TGX_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_smem()));
-        g_fwd_attr = true;
-    }
-    const uint32_t tiles = (n + 15) / 16;
-    const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
-    TGX_LAUNCH(c, TR_MLP, grid, 128, fwd_smem(), k_mlp_forward, k->img, n, (const uint32_t*)nullptr, d_x, d_rgb);
-    return TGX_OK;
+    return cache_forward(c, k, nullptr, n, d_x, d_rgb);
 }
 
 tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
                                float* d_rgb)
 {
     if (!max_n) return TGX_OK;
-    if (!g_fwd_attr) {
-        TGX_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, fwd_smem()));
-        g_fwd_attr = true;
-    }
-    const uint32_t tiles = (max_n + 15) / 16;
-    const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
-    TGX_LAUNCH(c, TR_MLP, grid, 128, fwd_smem(), k_mlp_forward, k->img, max_n, d_n, d_x, d_rgb);
-    return TGX_OK;
+    return cache_forward(c, k, d_n, max_n, d_x, d_rgb);
 }
 
 // Computes the batch gradient into the accumulator (no update); returns the loss if out_loss.
@@ -563,22 +790,27 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
     const uint32_t tiles = (uint32_t)(np / 16);
     const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
     TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, 128, all_smem(), k_mlp_fwd_bwd, k->img, n, d_x, d_t, enc, act, dlt, dy, k->loss);
-    // weight gradients, layer by layer: D [s][o] against the layer input X [s][i]
-    const uint32_t chunk = 256;
-    const uint32_t chunks = (n + chunk - 1) / chunk;
-    struct L { const __nv_bfloat16* D; int ds; int no; const __nv_bfloat16* X; int xs; int ni; int off; };
-    const L ls[5] = {
-        {dlt + 0 * np * NH, NH, NH, enc, NEP, NE, OFF_W0},
-        {dlt + 1 * np * NH, NH, NH, act + 0 * np * NH, NH, NH, OFF_W1},
-        {dlt + 2 * np * NH, NH, NH, act + 1 * np * NH, NH, NH, OFF_W2},
-        {dlt + 3 * np * NH, NH, NH, act + 2 * np * NH, NH, NH, OFF_W3},
-        {dy, 16, NO, act + 3 * np * NH, NH, NH, OFF_W4},
+    // weight gradients of all layers: D [s][o] against the layer input X [s][i]
+    WgradArgs a;
+    a.n = n;
+    a.chunk = 256;
+    a.ctas_per_tile = (n + 4 * a.chunk - 1) / (4 * a.chunk);
+    const WgradLayer ls[5] = {
+        {dlt + 0 * np * NH, enc, k->g + OFF_W0, NH, NH, NEP, NE, 0, 0, 0},
+        {dlt + 1 * np * NH, act + 0 * np * NH, k->g + OFF_W1, NH, NH, NH, NH, 0, 0, 0},
+        {dlt + 2 * np * NH, act + 1 * np * NH, k->g + OFF_W2, NH, NH, NH, NH, 0, 0, 0},
+        {dlt + 3 * np * NH, act + 2 * np * NH, k->g + OFF_W3, NH, NH, NH, NH, 0, 0, 0},
+        {dy, act + 3 * np * NH, k->g + OFF_W4, 16, NO, NH, NH, 0, 0, 0},
     };
-    for (const L& l : ls) {
-        const uint32_t tasks = (uint32_t)((l.no + 15) / 16) * ((l.ni + 63) / 64) * chunks;
-        TGX_LAUNCH(c, TR_MLP_WGRAD, (tasks + 3) / 4, 128, 0, k_mlp_wgrad, l.D, l.ds, l.no, l.X, l.xs, l.ni, n, chunk,
-                   k->g + l.off, l.ni);
+    uint32_t ctas = 0;
+    for (int l = 0; l < 5; l++) {
+        a.l[l] = ls[l];
+        a.l[l].o_tiles = (ls[l].no + 15) / 16;
+        a.l[l].i_groups = (ls[l].ni + 63) / 64;
+        a.l[l].first_cta = ctas;
+        ctas += (uint32_t)(a.l[l].o_tiles * a.l[l].i_groups) * a.ctas_per_tile;
     }
+    TGX_LAUNCH(c, TR_MLP_WGRAD, ctas, 128, 0, k_mlp_wgrad, a);
     return TGX_OK;
 }
 

@@ -524,7 +524,7 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
     }
     if (cudaMemsetAsync(s->d_table, 0, n_table * 4, c->stream) != cudaSuccess ||
         cudaMemsetAsync(s->d_occ, 0, occ_words * 4, c->stream) != cudaSuccess ||
-        cudaMemcpyAsync((char*)s->d_occ + occ_words * 4, s->occ_off, sizeof(s->occ_off), cudaMemcpyHostToDevice,
+        cudaMemcpyAsync((char*)s->d_occ + svo_occ_off_bytes(occ_words), s->occ_off, sizeof(s->occ_off), cudaMemcpyHostToDevice,
                         c->stream) != cudaSuccess) {
         tgx_set_error("tgx_svo_build: memset failed");
         return fail(TGX_ERR_CUDA);
@@ -588,7 +588,8 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
                    mn[0], mn[1], mn[2], s->B);
         const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
         TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
-                   s->d_sub, s->d_occ, (const uint64_t*)((char*)s->d_occ + occ_words * 4), s->n_levels, s->B, counters);
+                   s->d_sub, s->d_occ, (const uint64_t*)((char*)s->d_occ + svo_occ_off_bytes(occ_words)), s->n_levels,
+                   s->B, counters);
         return TGX_OK;
     };
     if ((st = rest()) != TGX_OK) return fail(st);

@@ -23,7 +23,7 @@ struct SvoDev
     const uint32_t* sub;     // per slot 32 words: 4^3-cell mask (0-15), 8^3-cell mask (16-17)
     const uint32_t* occ;
     const uint16_t* mat;
-    uint64_t occ_off[10];
+    uint32_t occ_off[16];    // word offset of each pyramid level (level 0 = 32^3 blocks), zero padded
 };
 
 // log2 of the cell size of traversal level li: 0, 2, 3, 5, 7, 9, ... capped at L-1
@@ -39,23 +39,17 @@ __host__ __device__ __forceinline__ uint32_t svo_n_levels(uint32_t L)
     return n;
 }
 
+// byte offset, after the pyramid words, of the device copy of the level offsets (16-byte aligned)
+inline uint64_t svo_occ_off_bytes(uint64_t occ_words) { return (occ_words * 4 + 15) & ~(uint64_t)15; }
+
 inline SvoDev svo_dev(const tgx_svo* s)
 {
     SvoDev d;
     d.mn[0] = s->mn[0]; d.mn[1] = s->mn[1]; d.mn[2] = s->mn[2];
     d.L = s->L; d.B = s->B; d.NL = svo_n_levels(s->L);
     d.table = s->d_table; d.pool = s->d_pool; d.sub = s->d_sub; d.occ = s->d_occ; d.mat = s->d_mat;
-    for (int i = 0; i < 10; i++) d.occ_off[i] = s->occ_off[i];
+    for (int i = 0; i < 16; i++) d.occ_off[i] = i < 10 ? (uint32_t)s->occ_off[i] : 0u;
     return d;
-}
-
-__device__ __forceinline__ float svo_level_size(const SvoDev& s, uint32_t li)
-{
-    return (float)(1u << svo_level_log2(s.L, li));
-}
-__device__ __forceinline__ int32_t svo_level_cells(const SvoDev& s, uint32_t li)
-{
-    return (int32_t)(1u << (s.L - svo_level_log2(s.L, li)));
 }
 
 __device__ __forceinline__ uint32_t svo_material(const SvoDev& s, int32_t cx, int32_t cy, int32_t cz)
@@ -79,12 +73,6 @@ __device__ __forceinline__ int32_t svo_cell_at(float p, float inv_size, int32_t 
     return c;
 }
 
-// 2^-g, the exact reciprocal of a level's cell size (equal to 1.0f / 2^g)
-__device__ __forceinline__ float svo_level_inv_size(const SvoDev& s, uint32_t li)
-{
-    return __int_as_float((int)((127u - svo_level_log2(s.L, li)) << 23));
-}
-
 // Resumable traversal state: the DDA of one ray, kept in registers so a
 // persistent kernel can run it a few steps at a time.
 struct RayState
@@ -94,8 +82,8 @@ struct RayState
     float t;
     int32_t c[3];
     int32_t last_axis;
-    uint32_t li, steps;
-    uint32_t tv;        // slot + 1 of the 32^3 block the sub-block levels (li <= 2) are inside
+    uint32_t li, g, steps;    // level, log2 of its cell size, steps used
+    uint32_t tv;              // slot + 1 of the 32^3 block the sub-block levels (g < 5) are inside
 };
 
 constexpr int kTraceRunning = -2;
@@ -133,79 +121,87 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const float o[3]
     if (!(r.t < t1)) return 0;
     r.last_axis = t0 > 0.0f ? entry_axis : -1;
     r.li = s.NL - 1;
+    r.g = s.L - 1u;
     r.tv = 0;
-    const float isz = svo_level_inv_size(s, r.li);
-    const int32_t hi = svo_level_cells(s, r.li) - 1;
+    const float isz = __int_as_float((int)((127u - r.g) << 23));
+    const int32_t hi = (1 << (s.L - r.g)) - 1;
 #pragma unroll
     for (int a = 0; a < 3; a++) r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], 0, hi);
     return kTraceRunning;
 }
 
-__device__ __forceinline__ bool svo_occupied_state(const SvoDev& s, const RayState& r)
-{
-    const uint32_t g = svo_level_log2(s.L, r.li);
-    if (g < 5) {
-        const uint32_t m = 32u >> g, mk = m - 1u;
-        const uint32_t v = (((uint32_t)r.c[2] & mk) * m + ((uint32_t)r.c[1] & mk)) * m + ((uint32_t)r.c[0] & mk);
-        const uint32_t* w = g == 0 ? s.pool + (uint64_t)(r.tv - 1) * 1024u
-                                   : s.sub + (uint64_t)(r.tv - 1) * 32u + (g == 3 ? 16u : 0u);
-        return (__ldg(&w[v >> 5]) >> (v & 31u)) & 1u;
-    }
-    const uint64_t m = s.B >> (g - 5u);
-    const uint64_t idx = ((uint64_t)r.c[2] * m + (uint64_t)r.c[1]) * m + (uint64_t)r.c[0];
-    return (__ldg(&s.occ[s.occ_off[g - 5u] + (idx >> 5)]) >> (idx & 31u)) & 1u;
-}
-
 // Runs at most n loop iterations of the DDA (one iteration is one step of
 // the max_steps budget).  Returns kTraceRunning, 1 on hit (r.t, r.c,
-// r.last_axis), 0 on miss, -1 when max_steps ran out.
-__device__ __forceinline__ int svo_trace_run(const SvoDev& s, RayState& r, uint32_t max_steps, uint32_t n)
+// r.last_axis), 0 on miss, -1 when max_steps ran out.  occ_off: the pyramid
+// level offsets (shared memory in the persistent kernel).  Every iteration
+// does one occupancy load and computes both the descent into the child cell
+// and the step to the neighbour cell, then keeps one, so the lanes of a warp
+// stay on one instruction stream whichever way their rays go.
+__device__ __forceinline__ int svo_trace_run(const SvoDev& s, const uint32_t* occ_off, RayState& r,
+                                             uint32_t max_steps, uint32_t n)
 {
     for (uint32_t k = 0; k < n; k++) {
         if (r.steps >= max_steps) return -1;
         r.steps++;
-        if (svo_occupied_state(s, r)) {
-            if (r.li == 0) return 1;
-            const uint32_t g = svo_level_log2(s.L, r.li);
-            if (g == 5u) r.tv = __ldg(&s.table[((uint64_t)r.c[2] * s.B + (uint64_t)r.c[1]) * s.B + (uint64_t)r.c[0]]);
-            const uint32_t shift = g - svo_level_log2(s.L, r.li - 1);
-            r.li--;
-            const float isz = svo_level_inv_size(s, r.li);
+        const uint32_t g = r.g;
+        // occupancy of the current cell
+        const bool sub = g < 5u;
+        const uint32_t m = sub ? (32u >> g) : (s.B >> (g - 5u));
+        const uint32_t mk = sub ? m - 1u : 0xffffffffu;
+        const uint32_t v = (((uint32_t)r.c[2] & mk) * m + ((uint32_t)r.c[1] & mk)) * m + ((uint32_t)r.c[0] & mk);
+        const uint32_t* base = !sub ? s.occ + occ_off[(g - 5u) & 15u]
+                             : g == 0 ? s.pool + (uint64_t)(r.tv - 1u) * 1024u
+                                      : s.sub + (uint64_t)(r.tv - 1u) * 32u + (g == 3 ? 16u : 0u);
+        const bool occ = (__ldg(&base[v >> 5]) >> (v & 31u)) & 1u;
+        if (occ && r.li == 0) return 1;
+        // candidate 1: descend, the child cell by point location
+        const uint32_t g_c = svo_level_log2(s.L, r.li ? r.li - 1u : 0u);
+        const uint32_t sh_c = g - g_c;
+        const float isz = __int_as_float((int)((127u - g_c) << 23));
+        int32_t cd[3];
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const int32_t lo = r.c[a] << shift, hi = lo + (1 << shift) - 1;
-                r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], lo, hi);
-            }
-            continue;
+        for (int a = 0; a < 3; a++) {
+            const int32_t lo = r.c[a] << sh_c, hi = lo + (1 << sh_c) - 1;
+            cd[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], lo, hi);
         }
-        const float size = svo_level_size(s, r.li);
+        // candidate 2: step through the nearest face
+        const float size = (float)(1u << g);
         float tn[3];
 #pragma unroll
         for (int a = 0; a < 3; a++)
             tn[a] = r.st[a] > 0 ? xmul(xsub(xmul((float)(r.c[a] + 1), size), r.og[a]), r.inv[a])
                   : r.st[a] < 0 ? xmul(xsub(xmul((float)r.c[a], size), r.og[a]), r.inv[a]) : F32_MAX_TG;
-        // axis of the nearest face (first minimum); selects keep the state in registers
         const bool a1 = tn[1] < tn[0];
         const float t01 = a1 ? tn[1] : tn[0];
         const bool a2 = tn[2] < t01;
         const int32_t am = a2 ? 2 : a1 ? 1 : 0;
         const float tam = a2 ? tn[2] : t01;
-        if (tam > r.t) r.t = tam;
-        r.last_axis = am;
         int32_t prev = a2 ? r.c[2] : a1 ? r.c[1] : r.c[0];
         const int32_t cur0 = prev + (a2 ? r.st[2] : a1 ? r.st[1] : r.st[0]);
-        r.c[0] = am == 0 ? cur0 : r.c[0];
-        r.c[1] = am == 1 ? cur0 : r.c[1];
-        r.c[2] = am == 2 ? cur0 : r.c[2];
-        if (cur0 < 0 || cur0 >= svo_level_cells(s, r.li)) return 0;
+        int32_t cs[3] = {am == 0 ? cur0 : r.c[0], am == 1 ? cur0 : r.c[1], am == 2 ? cur0 : r.c[2]};
+        if (!occ && (cur0 < 0 || cur0 >= (1 << (s.L - g)))) return 0;
+        // ascend to the level whose parent the step stayed in
+        uint32_t li_u = r.li, g_u = g;
         int32_t cur = cur0;
-        while (r.li < s.NL - 1) {
-            const uint32_t shift = svo_level_log2(s.L, r.li + 1) - svo_level_log2(s.L, r.li);
+        while (li_u < s.NL - 1) {
+            const uint32_t gp = svo_level_log2(s.L, li_u + 1);
+            const uint32_t shift = gp - g_u;
             if ((prev >> shift) == (cur >> shift)) break;
             prev >>= shift; cur >>= shift;
-            r.c[0] >>= shift; r.c[1] >>= shift; r.c[2] >>= shift;
-            r.li++;
+            cs[0] >>= shift; cs[1] >>= shift; cs[2] >>= shift;
+            li_u++;
+            g_u = gp;
         }
+        // keep one candidate; entering a 32^3 block loads its slot
+        const uint32_t tv_c = occ && g == 5u
+            ? __ldg(&s.table[((uint64_t)r.c[2] * s.B + (uint64_t)r.c[1]) * s.B + (uint64_t)r.c[0]]) : r.tv;
+        r.tv = tv_c;
+        r.t = occ ? r.t : (tam > r.t ? tam : r.t);
+        r.last_axis = occ ? r.last_axis : am;
+        r.li = occ ? r.li - 1u : li_u;
+        r.g = occ ? g_c : g_u;
+#pragma unroll
+        for (int a = 0; a < 3; a++) r.c[a] = occ ? cd[a] : cs[a];
     }
     return kTraceRunning;
 }
@@ -217,7 +213,7 @@ static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d
 {
     RayState r;
     int res = svo_trace_begin(s, o, d, r);
-    if (res == kTraceRunning) res = svo_trace_run(s, r, max_steps, 0xffffffffu);
+    if (res == kTraceRunning) res = svo_trace_run(s, s.occ_off, r, max_steps, 0xffffffffu);
     out_steps = r.steps;
     if (res == 1) {
         out_t = r.t;

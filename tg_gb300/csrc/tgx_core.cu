@@ -88,6 +88,11 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     c->tile_h = th;
     c->flags = cfg->flags;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+    // tuning override of the traversal's steps per queue round (1..256)
+    if (const char* e = getenv("TGX_TRACE_STEPS_PER_ROUND")) {
+        const long v = strtol(e, nullptr, 10);
+        if (v >= 1 && v <= 256) c->trace_steps_per_round = (uint32_t)v;
+    }
     if (cfg->stream) {
         c->stream = (cudaStream_t)cfg->stream;
     } else {

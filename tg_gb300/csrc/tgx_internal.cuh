@@ -135,6 +135,7 @@ struct tgx_ctx
     void*  h_pinned = nullptr;
     size_t h_pinned_bytes = 0;
     uint64_t* h_counter = nullptr;   // pinned u64 readback slot
+    uint32_t trace_steps_per_round = 8;   // DDA steps a traversal lane runs between queue refills
 };
 
 struct tgx_scene

@@ -7,13 +7,16 @@
 //   1. k_vis_cluster_setup  one thread per (view, cluster pointer): drops
 //      clusters outside the frustum or beyond the far plane (bounding
 //      sphere, then box corners) and empty clusters, computes a conservative
-//      screen-tile rectangle and a lower bound of the packed depth, and for
-//      kept clusters the ws2ms matrix and the camera position in cluster
-//      space exactly as the shader does; appends a 32-byte record.
+//      screen-tile rectangle and a lower bound of the packed depth, and
+//      appends a 32-byte record.
+//   1b. k_vis_record_origin one thread per record: the ws2ms matrix and the
+//      camera position in cluster space exactly as the shader does.
 //   2. k_vis_count          one warp per record: counts it per (tile, depth bucket).
-//   3. k_vis_prefix         per tile: offsets of its 16 depth buckets.
-//   4. k_vis_scan           exclusive scan of the tile totals; tile launch
-//                           order, heaviest first.
+//   3. k_vis_prefix         per tile: offsets of its 16 depth buckets; per
+//                           256 tiles: their sum and class histogram.
+//   4. k_vis_scan           one CTA: bases of the 256-tile groups and the
+//      k_vis_finalize       cursors of the launch order (heaviest class
+//                           first); then per group: tile offsets and order.
 //   5. k_vis_bin_fill       one warp per record: scatters it into the
 //                           (tile, bucket) bins, so every tile's list runs
 //                           near to far.
@@ -82,7 +85,7 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
 // 1. per-cluster setup
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) k_vis_cluster_setup(
+__global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
     const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp,
     const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
@@ -192,18 +195,7 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
                 }
             }
             if (keep) {
-                // ---- exact ws2ms and ray origin (visibility.frag:57-66) ----
-                float m0[16], m1[16], m2[16], m3[16], ws2ms[16];
-                dm4_translate(-od.translation[0], -od.translation[1], -od.translation[2], m0);
-                dm4_inverse(rot, m1);
-                dm4_translate(ohx, ohy, ohz, m2);
-                dm4_translate(-offx, -offy, -offz, m3);
-                dm4_mul(m3, m2, ws2ms);
-                dm4_mul(ws2ms, m1, ws2ms);
-                dm4_mul(ws2ms, m0, ws2ms);
-                float o[3];
-                dm4_mulv4(ws2ms, vc.cam[0], vc.cam[1], vc.cam[2], 1.0f, o);
-                rec.ox = o[0]; rec.oy = o[1]; rec.oz = o[2];
+                // the exact cluster-space origin is computed by k_vis_record_origin
                 rec.cluster_idx = ci;
                 rec.cluster_pointer = cp;
                 rec.object_idx = oi;
@@ -222,6 +214,44 @@ __global__ void __launch_bounds__(256) k_vis_cluster_setup(
     }
     records[slot] = rec;
     rects[slot] = make_uint2(tx0 | (ty0 << 16), tx1 | (ty1 << 16));
+}
+
+// ---------------------------------------------------------------------------
+// 1b. exact ws2ms and ray origin of every kept record (visibility.frag:57-66);
+//     kept apart from the cull so the cull runs at high occupancy
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_vis_record_origin(VisRecord* __restrict__ records,
+                                                          const uint32_t* __restrict__ counters,
+                                                          uint32_t record_capacity,
+                                                          const tgx_object* __restrict__ objects,
+                                                          const ViewConst* __restrict__ views)
+{
+    const uint32_t n = min(counters[C_RECORDS], record_capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        VisRecord& rec = records[i];
+        const tgx_object& od = objects[rec.object_idx];
+        const ViewConst& vc = views[rec.view];
+        const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
+        const uint32_t rel = rec.cluster_pointer - od.first_cluster_pointer;
+        const float offx = (float)((rel % nx) * kCluster), offy = (float)(((rel / nx) % ny) * kCluster);
+        const float offz = (float)((rel / (nx * ny)) * kCluster);
+        const float half = xmul((float)kCluster, 0.5f);
+        float rot[16], m0[16], m1[16], m2[16], m3[16], ws2ms[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
+        dm4_translate(-od.translation[0], -od.translation[1], -od.translation[2], m0);
+        dm4_inverse(rot, m1);
+        dm4_translate(xmul(half, (float)od.n_cluster_pointers_per_dim[0]), xmul(half, (float)od.n_cluster_pointers_per_dim[1]),
+                      xmul(half, (float)od.n_cluster_pointers_per_dim[2]), m2);
+        dm4_translate(-offx, -offy, -offz, m3);
+        dm4_mul(m3, m2, ws2ms);
+        dm4_mul(ws2ms, m1, ws2ms);
+        dm4_mul(ws2ms, m0, ws2ms);
+        float o[3];
+        dm4_mulv4(ws2ms, vc.cam[0], vc.cam[1], vc.cam[2], 1.0f, o);
+        rec.ox = o[0]; rec.oy = o[1]; rec.oz = o[2];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -250,45 +280,75 @@ __global__ void __launch_bounds__(256) k_vis_count(const VisRecord* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// 3. per-tile bucket offsets (one thread per tile, bucket-major = coalesced)
+// 3. per-tile bucket offsets (one thread per tile, bucket-major = coalesced),
+//    and per CTA of 256 tiles: the sum of the tile totals and the histogram
+//    of tile classes (cta_aux = [n_ctas sums][n_ctas x kOrderClasses])
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) k_vis_prefix(uint32_t* __restrict__ bucket_cnt, uint32_t* __restrict__ bucket_off,
-                                                   uint32_t* __restrict__ tile_total, uint32_t n_tiles)
+constexpr uint32_t kScanTiles = 256;   // tiles per CTA of the prefix and finalize kernels
+
+__device__ __forceinline__ uint32_t tile_class(uint32_t total) { return total ? 32u - __clz(total) : 0u; }
+
+__global__ void __launch_bounds__(kScanTiles) k_vis_prefix(uint32_t* __restrict__ bucket_cnt,
+                                                          uint32_t* __restrict__ bucket_off,
+                                                          uint32_t* __restrict__ tile_total, uint32_t n_tiles,
+                                                          uint32_t* __restrict__ cta_aux)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_tiles) return;
+    __shared__ uint32_t cls[kOrderClasses];
+    __shared__ uint32_t wsum[kScanTiles / 32];
+    if (threadIdx.x < kOrderClasses) cls[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t t = blockIdx.x * kScanTiles + threadIdx.x;
     uint32_t run = 0;
+    if (t < n_tiles) {
+        uint32_t c[kBuckets];   // all loads first: the cursor reset below must not wait on them one by one
 #pragma unroll
-    for (uint32_t b = 0; b < kBuckets; b++) {
-        const uint32_t c = bucket_cnt[b * n_tiles + t];
-        bucket_off[b * n_tiles + t] = run;
-        bucket_cnt[b * n_tiles + t] = 0;   // becomes the fill cursor
-        run += c;
+        for (uint32_t b = 0; b < kBuckets; b++) c[b] = bucket_cnt[b * n_tiles + t];
+#pragma unroll
+        for (uint32_t b = 0; b < kBuckets; b++) {
+            bucket_off[b * n_tiles + t] = run;
+            bucket_cnt[b * n_tiles + t] = 0;   // becomes the fill cursor
+            run += c[b];
+        }
+        tile_total[t] = run;
+        atomicAdd(&cls[tile_class(run)], 1u);
     }
-    tile_total[t] = run;
+    uint32_t sum = run;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31u) == 0) wsum[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kScanTiles / 32; w++) tot += wsum[w];
+        cta_aux[blockIdx.x] = tot;
+    }
+    if (threadIdx.x < kOrderClasses) cta_aux[n_ctas + blockIdx.x * kOrderClasses + threadIdx.x] = cls[threadIdx.x];
 }
 
 // ---------------------------------------------------------------------------
-// 4. exclusive scan of tile totals and the launch order of the tiles
-//    (single CTA; n_tiles is a few 10^4).
+// 4. one CTA: exclusive scan of the per-CTA sums (-> CTA bases) and, per
+//    tile class (heaviest first), the exclusive scan over CTAs of the class
+//    counts (-> per-(CTA, class) cursors of the launch order)
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(1024) k_vis_scan(const uint32_t* __restrict__ tile_total, uint32_t* __restrict__ tile_off,
-                                                   uint32_t* __restrict__ tile_order, uint32_t n_tiles,
-                                                   uint32_t bin_capacity, uint32_t* __restrict__ counters)
+__global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_aux, uint32_t n_tiles,
+                                                   uint32_t* __restrict__ tile_off, uint32_t bin_capacity,
+                                                   uint32_t* __restrict__ counters)
 {
     __shared__ uint32_t warp_sums[32];
-    __shared__ uint32_t carry;
-    __shared__ uint32_t cls_cnt[kOrderClasses];
-    if (threadIdx.x == 0) carry = 0;
-    if (threadIdx.x < kOrderClasses) cls_cnt[threadIdx.x] = 0;
-    __syncthreads();
+    __shared__ uint32_t cls_tot[kOrderClasses];
+    __shared__ uint32_t cls_base[kOrderClasses];
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    for (uint32_t base = 0; base < n_tiles; base += 1024) {
+    const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    uint32_t* cls_cnt = cta_aux + n_ctas;
+    // CTA bases
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < n_ctas; base += 1024) {
         const uint32_t i = base + threadIdx.x;
-        const uint32_t x = i < n_tiles ? tile_total[i] : 0u;
-        if (i < n_tiles) atomicAdd(&cls_cnt[x ? 32u - __clz(x) : 0u], 1u);
+        const uint32_t x = i < n_ctas ? cta_aux[i] : 0u;
         uint32_t incl = x;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -298,37 +358,84 @@ __global__ void __launch_bounds__(1024) k_vis_scan(const uint32_t* __restrict__ 
         if (lane == 31) warp_sums[wid] = incl;
         __syncthreads();
         if (wid == 0) {
-            uint32_t s = warp_sums[lane];
+            uint32_t w = warp_sums[lane];
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-                if ((int)lane >= o) s += y;
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if ((int)lane >= o) w += y;
             }
-            warp_sums[lane] = s;
+            warp_sums[lane] = w;
         }
         __syncthreads();
-        const uint32_t warp_prefix = wid ? warp_sums[wid - 1] : 0u;
-        if (i < n_tiles) tile_off[i] = carry + warp_prefix + incl - x;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += warp_sums[31];
+        if (i < n_ctas) cta_aux[i] = carry + (wid ? warp_sums[wid - 1] : 0u) + incl - x;
+        carry += warp_sums[31];
         __syncthreads();
     }
+    // class totals (warp c sums class c over the CTAs)
+    uint32_t tot = 0;
+    for (uint32_t b = lane; b < n_ctas; b += 32) tot += cls_cnt[b * kOrderClasses + wid];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0) cls_tot[wid] = tot;
+    __syncthreads();
     if (threadIdx.x == 0) {
         tile_off[n_tiles] = carry;
         counters[C_ENTRIES] = carry;
         counters[C_OVERFLOW] = carry > bin_capacity ? 1u : 0u;
-        // class cursors, heaviest class first
-        uint32_t run = 0;
+        uint32_t run = 0;   // heaviest class first
         for (int c = (int)kOrderClasses - 1; c >= 0; c--) {
-            const uint32_t n = cls_cnt[c];
-            cls_cnt[c] = run;
-            run += n;
+            cls_base[c] = run;
+            run += cls_tot[c];
         }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n_tiles; i += blockDim.x) {
-        const uint32_t x = tile_total[i];
-        tile_order[atomicAdd(&cls_cnt[x ? 32u - __clz(x) : 0u], 1u)] = i;
+    // per-(CTA, class) cursors: warp c scans class c over the CTAs
+    uint32_t run = cls_base[wid];
+    for (uint32_t b0 = 0; b0 < n_ctas; b0 += 32) {
+        const uint32_t b = b0 + lane;
+        const uint32_t x = b < n_ctas ? cls_cnt[b * kOrderClasses + wid] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        if (b < n_ctas) cls_cnt[b * kOrderClasses + wid] = run + incl - x;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4b. per CTA of 256 tiles: tile offsets (CTA base + scan of the totals) and
+//     each tile's place in the launch order
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kScanTiles) k_vis_finalize(const uint32_t* __restrict__ tile_total, uint32_t n_tiles,
+                                                            const uint32_t* __restrict__ cta_aux,
+                                                            uint32_t* __restrict__ tile_off,
+                                                            uint32_t* __restrict__ tile_order)
+{
+    __shared__ uint32_t cur[kOrderClasses];
+    __shared__ uint32_t wsum[kScanTiles / 32];
+    const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    if (threadIdx.x < kOrderClasses) cur[threadIdx.x] = cta_aux[n_ctas + blockIdx.x * kOrderClasses + threadIdx.x];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t t = blockIdx.x * kScanTiles + threadIdx.x;
+    const bool valid = t < n_tiles;
+    const uint32_t x = valid ? tile_total[t] : 0u;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    uint32_t before = cta_aux[blockIdx.x];
+    for (uint32_t w = 0; w < wid; w++) before += wsum[w];
+    if (valid) {
+        tile_off[t] = before + incl - x;
+        tile_order[atomicAdd(&cur[tile_class(x)], 1u)] = t;
     }
 }
 
@@ -693,7 +800,9 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     const uint32_t rec_cap = (uint32_t)n_pairs;
     TGX_TRY(devbuf_reserve(c->vis_records, (size_t)rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
     TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
-    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4));
+    const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4 +
+                                                (size_t)n_scan_ctas * (1 + kOrderClasses) * 4));
     TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4 * 2));
     VisRecord* records = (VisRecord*)c->vis_records.ptr;
     uint2* rects = (uint2*)(records + rec_cap);
@@ -701,6 +810,7 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     uint32_t* bucket_cnt = (uint32_t*)c->vis_tile_cnt.ptr;
     uint32_t* bucket_off = bucket_cnt + (size_t)n_tiles * kBuckets;
     uint32_t* tile_total = bucket_off + (size_t)n_tiles * kBuckets;
+    uint32_t* cta_aux = tile_total + n_tiles;
     uint32_t* tile_off = (uint32_t*)c->vis_tile_off.ptr;
     uint32_t* tile_order = tile_off + (n_tiles + 1);
     TGX_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
@@ -711,10 +821,14 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
                s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
                records, rects, rec_cap, counters, c->d_status);
     const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
+    TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, records, counters, rec_cap,
+               s->d_objects, d_vc);
     TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
-    TGX_LAUNCH(c, TR_VIS_PREFIX, (n_tiles + 255) / 256, 256, 0, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles);
-    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, tile_total, tile_off, tile_order, n_tiles, bin_capacity,
-               counters);
+    TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles,
+               cta_aux);
+    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, cta_aux, n_tiles, tile_off, bin_capacity, counters);
+    TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off,
+               tile_order);
     TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
                records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, (uint32_t*)c->vis_bins.ptr,
                n_tiles, bin_capacity, c->d_status);
@@ -815,7 +929,8 @@ constexpr size_t kNaRects = kNaRecords + na_align((size_t)kNaMaxClusterPointers 
 constexpr size_t kNaBucketCnt = kNaRects + na_align((size_t)kNaMaxClusterPointers * 8);
 constexpr size_t kNaBucketOff = kNaBucketCnt + na_align((size_t)kNaMaxTiles * kBuckets * 4);
 constexpr size_t kNaTileTotal = kNaBucketOff + na_align((size_t)kNaMaxTiles * kBuckets * 4);
-constexpr size_t kNaTileOff = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
+constexpr size_t kNaScanAux = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
+constexpr size_t kNaTileOff = kNaScanAux + na_align(((size_t)kNaMaxTiles / kScanTiles + 1) * (1 + kOrderClasses) * 4);
 constexpr size_t kNaTileOrder = kNaTileOff + na_align(((size_t)kNaMaxTiles + 1) * 4);
 constexpr size_t kNaBinsOff = kNaTileOrder + na_align((size_t)kNaMaxTiles * 4);
 constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * 4);   // about 31 MiB
@@ -922,6 +1037,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     uint32_t* bucket_cnt = (uint32_t*)(base + kNaBucketCnt);
     uint32_t* bucket_off = (uint32_t*)(base + kNaBucketOff);
     uint32_t* tile_total = (uint32_t*)(base + kNaTileTotal);
+    uint32_t* cta_aux = (uint32_t*)(base + kNaScanAux);
     uint32_t* tile_off = (uint32_t*)(base + kNaTileOff);
     uint32_t* tile_order = (uint32_t*)(base + kNaTileOrder);
     uint32_t* bins = (uint32_t*)(base + kNaBinsOff);
@@ -943,9 +1059,12 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
               d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
               kNaMaxClusterPointers, counters, status);
+    NA_LAUNCH((uint32_t)sms * 4, 128, k_vis_record_origin, records, counters, kNaMaxClusterPointers, d_objects, d_vc);
     NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
-    NA_LAUNCH((n_tiles + 255) / 256, 256, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles);
-    NA_LAUNCH(1, 1024, k_vis_scan, tile_total, tile_off, tile_order, n_tiles, kNaBins, counters);
+    const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
+    NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
+    NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
     NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, bins,
               n_tiles, kNaBins, status);
     NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), records, rects, bins, tile_off, tile_order, d_vc, 1u,
