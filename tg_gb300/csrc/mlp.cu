@@ -168,34 +168,43 @@ __device__ __forceinline__ void forward_tile(const __nv_bfloat16* sw, const floa
 // Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
 // ---------------------------------------------------------------------------
 //
-// One CTA of 128 threads per SM, persistent over tiles of 128 queries; thread
-// t owns query t of the tile, which is row t of every GEMM and TMEM lane t.
-// Shared memory holds the weights and the A operand of the current layer in
-// the canonical no-swizzle K-major layout: 8 x 8 BF16 core matrices (8 rows
-// of 16 contiguous bytes), K-adjacent core matrices LBO bytes apart and
-// row-group-adjacent ones SBO bytes apart.  Per layer one elected thread
-// issues tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) and
-// commits to an mbarrier; then each warp reads its 32 TMEM lanes with
-// tcgen05.ld, applies ReLU and writes the next layer's A operand.
+// A CTA of 256 threads holds two independent groups of 4 warps that share the
+// weights in shared memory.  Each group works through tiles of 128 queries:
+// thread t of the group owns query t of its tile, which is row t of every
+// GEMM and TMEM lane t.  While one group waits for its MMAs the other encodes
+// or drains its accumulators, so the tensor core and the CUDA cores overlap.
+// Operands use the canonical no-swizzle K-major layout: 8 x 8 BF16 core
+// matrices (8 rows of 16 contiguous bytes), K-adjacent core matrices LBO
+// bytes apart and row-group-adjacent ones SBO bytes apart.  Per layer one
+// thread of the group issues tcgen05.mma (M = 128, N = 64 or 16, K = 16 per
+// instruction) into the group's 64 TMEM columns and commits to the group's
+// mbarrier; then each warp reads its 32 TMEM lanes with tcgen05.ld, applies
+// ReLU and writes the next layer's A operand.
 
 namespace tc {
 
 constexpr int M = 128;                      // queries per tile
 constexpr int KG0 = NEP / 8;                // 28 K core-matrix columns of layer 0
 constexpr int KGH = NH / 8;                 // 8 of the hidden layers
+constexpr int THREADS = 256;                // two groups of 128
 // byte offsets in dynamic shared memory (all 1024-aligned)
 constexpr int W0 = 0;                                   // [28 kg][8 ng][128 B]
 constexpr int W1 = W0 + KG0 * 8 * 128;                  // [8 kg][8 ng][128 B] x 3
 constexpr int W4 = W1 + 3 * KGH * 8 * 128;              // [8 kg][2 ng][128 B] (16 rows, 3 real)
-constexpr int A0 = W4 + KGH * 2 * 128;                  // [28 kg][16 mg][128 B]
-constexpr int A1 = A0 + KG0 * 16 * 128;                 // [8 kg][16 mg][128 B]
-constexpr int BAR = A1 + KGH * 16 * 128;                // mbarrier (8 B) + TMEM address (4 B)
+constexpr int GROUP = W4 + KGH * 2 * 128;               // per group:
+constexpr int A0 = 0;                                   //   [28 kg][16 mg][128 B]
+constexpr int A1 = A0 + KG0 * 16 * 128;                 //   [8 kg][16 mg][128 B]
+constexpr int GROUP_BYTES = A1 + KGH * 16 * 128;
+constexpr int BAR = GROUP + 2 * GROUP_BYTES;            // 2 mbarriers, TMEM address
 constexpr int SMEM = BAR + 64;
-constexpr uint32_t TMEM_COLS = 64;
+constexpr uint32_t TMEM_COLS = 128;                     // 64 per group
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
-__host__ __device__ constexpr uint32_t idesc(uint32_t n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(M >> 4) << 24); }
+__host__ __device__ constexpr uint32_t idesc(uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 // shared-memory matrix descriptor, no swizzle
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
@@ -234,6 +243,17 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// barrier of the 128 threads of one group (ids 1 and 2)
+__device__ __forceinline__ void group_sync(uint32_t g) { asm volatile("bar.sync %0, 128;" :: "r"(g + 1u) : "memory"); }
+// the same barrier, returning whether any thread of the group passed pred = true
+__device__ __forceinline__ bool group_sync_or(uint32_t g, bool pred)
+{
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, 128, p;\n selp.u32 %0, 1, 0, q;\n}"
+                 : "=r"(r) : "r"((uint32_t)pred), "r"(g + 1u) : "memory");
+    return r != 0;
+}
+
 // 16 consecutive FP32 columns of this thread's TMEM lane
 __device__ __forceinline__ void ld16(uint32_t taddr, float* v)
 {
@@ -271,27 +291,55 @@ __device__ __forceinline__ void stage_weights(unsigned char* dst, const __nv_bfl
     }
 }
 
+// The 24 features of one input (sin, cos of 2^k pi x for k = 0..11) into core
+// columns 3i .. 3i+2 of the A tile.  sincospif anchors octaves 0 and 6; the
+// others follow by angle doubling (sin 2a = 2 sin a cos a, cos 2a =
+// (cos a - sin a)(cos a + sin a)), whose error (a few ulp times 2^5) stays far
+// below the BF16 rounding of the features.
+__device__ __forceinline__ void encode_input(unsigned char* a, int i, int row, float x)
+{
+    float f[24];
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float sv, cv;
+        sincospif(half ? x * 64.0f : x, &sv, &cv);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            f[(half * 6 + k) * 2 + 0] = sv;
+            f[(half * 6 + k) * 2 + 1] = cv;
+            const float s2 = 2.0f * sv * cv, c2 = (cv - sv) * (cv + sv);
+            sv = s2;
+            cv = c2;
+        }
+    }
+    put8(a, 3 * i + 0, row, f);
+    put8(a, 3 * i + 1, row, f + 8);
+    put8(a, 3 * i + 2, row, f + 16);
+}
+
 }  // namespace tc
 
-__global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
-                                                          const uint32_t* __restrict__ n_dev,
-                                                          const float* __restrict__ x, float* __restrict__ y,
-                                                          tgx_dev_status* __restrict__ status)
+__global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
+                                                                  const uint32_t* __restrict__ n_dev,
+                                                                  const float* __restrict__ x, float* __restrict__ y,
+                                                                  tgx_dev_status* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     using namespace tc;
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + BAR);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + BAR + 8);
+    const uint32_t g = warp >> 2, gt = tid & 127u;         // group, thread (= tile row) in the group
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + BAR);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + BAR + 16);
+    unsigned char* ga = sm + GROUP + g * GROUP_BYTES;
     if (n_dev) n = min(n, *n_dev);
-    // weights into the core-matrix layout
     stage_weights(sm + W0, wimg + B_W0, S0, NH, NH, KG0);
     stage_weights(sm + W1 + 0 * KGH * 8 * 128, wimg + B_W1, SH, NH, NH, KGH);
     stage_weights(sm + W1 + 1 * KGH * 8 * 128, wimg + B_W2, SH, NH, NH, KGH);
     stage_weights(sm + W1 + 2 * KGH * 8 * 128, wimg + B_W3, SH, NH, NH, KGH);
     stage_weights(sm + W4, wimg + B_W4, SH, 8, 16, KGH);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&bars[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&bars[1])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -303,40 +351,29 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* 
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_base = tmem + ((warp * 32u) << 16);   // this warp's 32 TMEM lanes
-    const uint32_t b = saddr(bar);
+    const uint32_t tmem = *tmem_slot + g * 64u;                          // this group's 64 columns
+    const uint32_t lanes = tmem + (((warp & 3u) * 32u) << 16);           // this warp's 32 lanes
+    const uint32_t b = saddr(&bars[g]);
     uint32_t phase = 0;
     bool ok = true;
     const uint32_t tiles = (n + M - 1) / M;
-    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-        const uint32_t row = tile * M + tid;
-        // layer 0 input: the 216 sin/cos features of this thread's query
+    for (uint32_t tile = blockIdx.x * 2 + g; tile < tiles && ok; tile += gridDim.x * 2) {
+        const uint32_t row = tile * M + gt;
+#pragma unroll
+        for (int i = 0; i < NI; i++) encode_input(ga + A0, i, (int)gt, row < n ? x[(uint64_t)row * NI + i] : 0.0f);
         {
-            float xi[NI];
-#pragma unroll
-            for (int i = 0; i < NI; i++) xi[i] = row < n ? x[(uint64_t)row * NI + i] : 0.0f;
-            float f[8];
-#pragma unroll
-            for (int kg = 0; kg < KG0; kg++) {
-#pragma unroll
-                for (int j = 0; j < 8; j += 2) {
-                    const int c = kg * 8 + j;   // feature pair (sin, cos) of input c / 24, octave (c / 2) % 12
-                    if (c < NE) sincospif(xi[c / (2 * NF)] * (float)(1 << ((c / 2) % NF)), &f[j], &f[j + 1]);
-                    else f[j] = f[j + 1] = 0.0f;
-                }
-                put8(sm + A0, kg, (int)tid, f);
-            }
+            const float z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            put8(ga + A0, KG0 - 1, (int)gt, z);   // features 216..223
         }
         fence_async_smem();
         fence_before();
-        __syncthreads();
+        group_sync(g);
         // five layers; the hidden ones write the next A operand into A1
         for (int l = 0; l < 5 && ok; l++) {
-            if (tid == 0) {
+            if (gt == 0) {
                 fence_after();
                 const int kgs = l == 0 ? KG0 : KGH;
-                const uint32_t a_base = saddr(sm + (l == 0 ? A0 : A1));
+                const uint32_t a_base = saddr(ga + (l == 0 ? A0 : A1));
                 const uint32_t w_base = saddr(sm + (l == 0 ? W0 : l < 4 ? W1 + (l - 1) * KGH * 8 * 128 : W4));
                 const uint32_t n_out = l < 4 ? 64u : 16u;
                 const uint32_t w_sbo = 128, w_lbo = (n_out / 8) * 128;
@@ -345,9 +382,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* 
                         sdesc(w_base + 2 * k * w_lbo, w_lbo, w_sbo), idesc(n_out), k > 0);
                 commit(b);
             }
-            // every thread waits; one that gives up makes the whole CTA stop
-            if (__syncthreads_or(!wait(b, phase))) {
-                if (tid == 0) dev_error(status, TGX_ERR_TIMEOUT, 40 + l, tile);
+            // every thread of the group waits; one that gives up stops the group
+            if (group_sync_or(g, !wait(b, phase))) {
+                if (gt == 0) dev_error(status, TGX_ERR_TIMEOUT, 40 + l, tile);
                 ok = false;
                 break;
             }
@@ -357,17 +394,17 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* 
                 float v[16];
 #pragma unroll 1
                 for (int q = 0; q < 4; q++) {
-                    ld16(lane_base + q * 16, v);
+                    ld16(lanes + q * 16, v);
                     ld_wait();
 #pragma unroll
-                    for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i], 0.0f);
-                    put8(sm + A1, 2 * q, (int)tid, v);
-                    put8(sm + A1, 2 * q + 1, (int)tid, v + 8);
+                    for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.0f);
+                    put8(ga + A1, 2 * q, (int)gt, v);
+                    put8(ga + A1, 2 * q + 1, (int)gt, v + 8);
                 }
                 fence_async_smem();
             } else {
                 float v[16];
-                ld16(lane_base, v);
+                ld16(lanes, v);
                 ld_wait();
                 if (row < n) {
                     y[(uint64_t)row * NO + 0] = v[0];
@@ -376,14 +413,15 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward_tc(const __nv_bfloat16* 
                 }
             }
             fence_before();
-            __syncthreads();
+            group_sync(g);
         }
     }
     if (!ok) wait(b, phase);   // let MMAs still in flight land (bounded) before the columns are freed
-    fence_after();
+    fence_before();
     __syncthreads();
+    fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TMEM_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tmem_slot), "r"(TMEM_COLS) : "memory");
 }
 
 // Training forward + backward.  Writes, per sample s:
@@ -752,8 +790,8 @@ static tgx_status cache_forward(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, u
         attr = true;
     }
     const uint32_t tiles = (n + tc::M - 1) / tc::M;
-    const uint32_t grid = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)c->num_sms));
-    TGX_LAUNCH(c, TR_MLP, grid, 128, tc::SMEM, k_mlp_forward_tc, k->img, n, d_n, d_x, d_rgb, c->d_status);
+    const uint32_t grid = std::max(1u, std::min<uint32_t>((tiles + 1) / 2, (uint32_t)c->num_sms));
+    TGX_LAUNCH(c, TR_MLP, grid, tc::THREADS, tc::SMEM, k_mlp_forward_tc, k->img, n, d_n, d_x, d_rgb, c->d_status);
     return TGX_OK;
 }
 
