@@ -267,6 +267,85 @@ def cache_study_config1(local: int, stream_of):
     return res
 
 
+RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+
+
+def look_at_view(pos, target, w, h, far):
+    """tgx_make_view from a position looking at a target (tg's camera looks down -z at yaw 0)."""
+    import tg_gb300 as tg
+    d = np.asarray(target, np.float64) - np.asarray(pos, np.float64)
+    yaw = float(np.arctan2(-d[0], -d[2]))
+    pitch = float(np.arctan2(d[1], np.hypot(d[0], d[2])))
+    return tg.make_view(tuple(float(x) for x in pos), pitch, yaw, float(np.pi / 3), w, h, 0.1, far)
+
+
+def bench_batched(local: int, frames: int = 10):
+    """Config 3: one batched frame of 64 views of the config-1 object (resolutions
+    drawn from 320x240 .. 3840x2160, cameras on a sphere around it, seed 3) plus
+    16 scenes of 32-4096 objects (log-uniform; clusters per axis U[2,8]), one view
+    each, captured once as a CUDA graph (tgx_frame_graph) and replayed."""
+    import torch
+    import tg_gb300 as tg
+
+    rng = np.random.default_rng(3)
+    ctx = tg.Context(local, tile=(8, 16))
+    jobs, keep = [], []
+    obj = ctx.upload(tg.generate_scene(0, 1, 4, 4, seed=0, bernoulli_p=0.3, translation=(0.0, 0.0, 64.0)))
+    keep.append(obj)
+    views, outs = [], []
+    for _ in range(64):
+        w, h = RESOLUTIONS[rng.integers(len(RESOLUTIONS))]
+        u = rng.normal(size=3)
+        pos = np.array([0.0, 0.0, 64.0]) + u / np.linalg.norm(u) * rng.uniform(40.0, 160.0)
+        views.append(look_at_view(pos, (0.0, 0.0, 64.0), w, h, 400.0))
+        outs.append(torch.empty(w * h, dtype=torch.int64, device="cuda"))
+    jobs.append((obj, np.concatenate(views), outs))
+    n_objects = np.exp(rng.uniform(np.log(32), np.log(4096), 16)).astype(int)
+    for k, n in enumerate(n_objects):
+        half = 64.0 * float(n) ** (1.0 / 3.0)
+        sc = ctx.upload(tg.generate_scene(1, int(n), 2, 8, seed=100 + k, noise_period=64.0, noise_threshold=0.5,
+                                          box_min=(-half,) * 3, box_max=(half,) * 3, n_luts=1))
+        keep.append(sc)
+        w, h = RESOLUTIONS[rng.integers(len(RESOLUTIONS))]
+        v = tg.make_view((0.0, 0.0, 0.0), 0.0, float(rng.uniform(0, 2 * np.pi)), float(np.pi / 3), w, h, 0.1,
+                         4.0 * half)
+        jobs.append((sc, v, [torch.empty(w * h, dtype=torch.int64, device="cuda")]))
+    pixels = sum(int(o.numel()) for _, _, os_ in jobs for o in os_)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    graph = ctx.frame_graph(jobs)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            fn()
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1) / frames
+
+    def separate():
+        for sc, v, o in jobs:
+            ctx.vis_render(sc, v, o)
+
+    with torch.cuda.stream(stream):
+        ms_graph = timed(graph.launch)
+        ms_sep = timed(separate)
+    err = ctx.device_error()
+    res = {"views": 64 + 16, "scenes": 17, "pixels": pixels, "objects": [1] + [int(n) for n in n_objects],
+           "graph_kernels": graph.kernels, "graph_frame_ms": round(ms_graph, 3),
+           "graph_grays_per_s": pixels / (ms_graph * 1e-3) / 1e9,
+           "separate_calls_frame_ms": round(ms_sep, 3), "separate_grays_per_s": pixels / (ms_sep * 1e-3) / 1e9,
+           "device_status": int(err.code)}
+    graph.close()
+    for sc in keep:
+        sc.close()
+    ctx.close()
+    return res
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -275,6 +354,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gi", action="store_true", help="skip the SVO build and GI measurements")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched many-view frame (config 3)")
     ap.add_argument("--no-gi-cache", action="store_true",
                     help="skip the learned-cache vs plain 2-bounce GI comparison at equal relMSE")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
@@ -436,6 +516,7 @@ def main() -> None:
         if cache_report is not None:
             gi_report["gi_cache_vs_plain"] = cache_report
         svo.close()
+    batched = None if args.no_batched else bench_batched(local)
     rays = W * H
     value = rays * world / (ms * 1e-3) / 1e9
 
@@ -477,6 +558,7 @@ def main() -> None:
         "clocks": clocks.summary(),
         "hit_pixels": hits,
         **gi_report,
+        **({"batched_frame": batched} if batched else {}),
         "vis_stats": {"visible_clusters": n_vis, "bin_entries": int(stats.bin_entries), "tiles": int(stats.tiles),
                       "dda_overruns": int(stats.dda_overruns)},
         "wall_s_timed": t_wall,

@@ -250,6 +250,38 @@ int         tgx_vis_decode(uint64_t packed, float* out_depth, uint32_t* out_clus
 tgx_status  tgx_pick(tgx_ctx* ctx, const uint64_t* d_visbuf, uint32_t w, uint32_t h, uint32_t x, uint32_t y,
                      float* out_depth, uint32_t* out_cluster_pointer, uint32_t* out_voxel_idx, int* out_hit);
 
+/* ---- batched frames captured as a CUDA graph ---- */
+
+/* One job of a batched frame: n_views views (any resolutions) of one scene. */
+typedef struct tgx_vis_job
+{
+    const tgx_scene*    scene;
+    const tgx_view*     views;        /* [n_views] */
+    uint32_t            n_views;
+    uint64_t* const*    d_visbuf;     /* [n_views] DEVICE outputs, width*height words each */
+} tgx_vis_job;
+
+typedef struct tgx_frame_graph tgx_frame_graph;
+
+/*
+ * Captures the visibility passes of n_jobs jobs (several scenes, many views of
+ * uneven resolution) once into a CUDA graph, so a whole batched frame replays
+ * with one tgx_frame_graph_launch.  The graph owns its scratch and its copies
+ * of the view tables and output pointers; the scenes and outputs must outlive
+ * it.  Creation renders every job once, uncaptured, to size the bins (a
+ * replayed frame that still overflows them takes the exact record scan).
+ * Synchronous.
+ */
+tgx_status  tgx_frame_graph_create(tgx_ctx* ctx, const tgx_vis_job* jobs, uint32_t n_jobs,
+                                   tgx_frame_graph** out_graph);
+/* Replays the frame on the context stream.  Asynchronous. */
+tgx_status  tgx_frame_graph_launch(tgx_ctx* ctx, tgx_frame_graph* graph);
+/* New cameras for job `job` (same count and resolutions); ordered before later launches. */
+tgx_status  tgx_frame_graph_set_views(tgx_ctx* ctx, tgx_frame_graph* graph, uint32_t job, const tgx_view* views);
+/* Kernels one launch of the graph runs. */
+uint32_t    tgx_frame_graph_kernels(const tgx_frame_graph* graph);
+void        tgx_frame_graph_destroy(tgx_ctx* ctx, tgx_frame_graph* graph);
+
 /* ---- one-bit SVO (tg_sparse_voxel_octree.c) ---- */
 
 /*

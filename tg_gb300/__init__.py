@@ -81,6 +81,11 @@ def gi_params(spp: int = 4, bounces: int = 1, seed: int = 2, max_steps: int = 25
     return p
 
 
+class VisJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("views", C.c_void_p), ("n_views", C.c_uint32),
+                ("d_visbuf", C.POINTER(C.c_void_p))]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("n_objects", C.c_uint32), ("objects", C.c_void_p),
@@ -140,7 +145,8 @@ EXPORTS = [
     "tgx_trace_slots", "tgx_trace_get", "tgx_vis_get_stats", "tgx_gi_render", "tgx_cache_n_params",
     "tgx_cache_create", "tgx_cache_destroy", "tgx_cache_infer", "tgx_cache_train_step", "tgx_cache_last_loss",
     "tgx_cache_gradient", "tgx_cache_get_weights", "tgx_cache_set_weights", "tgx_cache_save", "tgx_cache_load",
-    "tgx_gi_render_cached",
+    "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
+    "tgx_frame_graph_kernels", "tgx_frame_graph_destroy",
 ]
 
 
@@ -188,6 +194,11 @@ def _load() -> C.CDLL:
         "tgx_cache_set_weights": (i32, [vp, vp, vp]),
         "tgx_cache_save": (i32, [vp, vp, C.c_char_p]),
         "tgx_cache_load": (i32, [vp, vp, C.c_char_p]),
+        "tgx_frame_graph_create": (i32, [vp, C.POINTER(VisJob), u32, C.POINTER(vp)]),
+        "tgx_frame_graph_launch": (i32, [vp, vp]),
+        "tgx_frame_graph_set_views": (i32, [vp, vp, u32, vp]),
+        "tgx_frame_graph_kernels": (u32, [vp]),
+        "tgx_frame_graph_destroy": (None, [vp, vp]),
         "tgx_trace_reset": (i32, [vp]),
         "tgx_trace_slots": (u32, []),
         "tgx_trace_get": (i32, [vp, u32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(u64)]),
@@ -386,6 +397,11 @@ class Context:
         check(lib.tgx_vis_render_host(self.handle, scene.handle, _ptr(views), len(views), ptrs),
               "tgx_vis_render_host")
 
+    def frame_graph(self, jobs) -> "FrameGraph":
+        """Captures a batched frame: `jobs` is a list of (scene, views, outs) with device
+        outputs; returns a FrameGraph whose launch() replays all of it with one graph launch."""
+        return FrameGraph(self, jobs)
+
     def svo_build(self, scene: "Scene", mn, extent_log2: int) -> Svo:
         m = np.asarray(mn, dtype=np.float32)
         h = C.c_void_p()
@@ -417,6 +433,48 @@ class Context:
         check(lib.tgx_pick(self.handle, _ptr(d_visbuf), w, h, x, y, C.byref(d), C.byref(cp), C.byref(vx),
                            C.byref(hit)), "tgx_pick")
         return bool(hit.value), d.value, cp.value, vx.value
+
+
+class FrameGraph:
+    """tgx_frame_graph: the visibility passes of many (scene, views) jobs as one CUDA graph."""
+
+    def __init__(self, ctx: "Context", jobs):
+        self.ctx = ctx
+        self._keep = []
+        arr = (VisJob * len(jobs))()
+        for i, (scene, views, outs) in enumerate(jobs):
+            v = np.ascontiguousarray(views, dtype=VIEW_DTYPE).reshape(-1)
+            ptrs = (C.c_void_p * len(v))(*[_ptr(o) for o in outs])
+            self._keep += [v, ptrs, outs]
+            arr[i].scene = scene.handle
+            arr[i].views = v.ctypes.data
+            arr[i].n_views = len(v)
+            arr[i].d_visbuf = ptrs
+        h = C.c_void_p()
+        check(lib.tgx_frame_graph_create(ctx.handle, arr, len(jobs), C.byref(h)), "tgx_frame_graph_create")
+        self.handle = h
+
+    @property
+    def kernels(self) -> int:
+        return int(lib.tgx_frame_graph_kernels(self.handle))
+
+    def launch(self) -> None:
+        check(lib.tgx_frame_graph_launch(self.ctx.handle, self.handle), "tgx_frame_graph_launch")
+
+    def set_views(self, job: int, views) -> None:
+        v = np.ascontiguousarray(views, dtype=VIEW_DTYPE).reshape(-1)
+        check(lib.tgx_frame_graph_set_views(self.ctx.handle, self.handle, job, _ptr(v)), "tgx_frame_graph_set_views")
+
+    def close(self) -> None:
+        if self.handle and self.ctx.handle:
+            lib.tgx_frame_graph_destroy(self.ctx.handle, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Svo:

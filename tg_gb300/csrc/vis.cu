@@ -752,90 +752,68 @@ static tgx_status check_views(const tgx_view* views, uint32_t n_views, uint32_t 
     return TGX_OK;
 }
 
-tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
-                             uint64_t* const* d_visbuf)
+// Scratch of one visibility frame (context buffers, or a frame graph's own).
+struct VisScratch
 {
-    if (!c || !s || !d_visbuf) { tgx_set_error("tgx_vis_render: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
-    TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
-    for (uint32_t i = 0; i < n_views; i++)
-        if (!d_visbuf[i]) { tgx_set_error("tgx_vis_render: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
-    TGX_CUDA(cudaSetDevice(c->device));
-
-    // view constants + output pointer table, copied from pageable memory (staged by the driver, no sync)
-    std::vector<ViewConst> vcs(n_views);
-    uint32_t n_tiles = 0;
-    for (uint32_t i = 0; i < n_views; i++) {
-        make_view_const(views[i], c->tile_w, c->tile_h, n_tiles, vcs[i]);
-        n_tiles += vcs[i].tiles_x * vcs[i].tiles_y;
-    }
-    const size_t vc_bytes = n_views * sizeof(ViewConst);
-    const size_t ptr_off = (vc_bytes + 15) & ~(size_t)15;
-    const size_t stage_bytes = ptr_off + n_views * sizeof(void*);
-    std::vector<unsigned char> stage(stage_bytes);
-    memcpy(stage.data(), vcs.data(), vc_bytes);
-    memcpy(stage.data() + ptr_off, d_visbuf, n_views * sizeof(void*));
-    TGX_TRY(devbuf_reserve(c->vis_views, stage_bytes));
-    TGX_CUDA(cudaMemcpyAsync(c->vis_views.ptr, stage.data(), stage_bytes, cudaMemcpyHostToDevice, c->stream));
-    const ViewConst* d_vc = (const ViewConst*)c->vis_views.ptr;
-    unsigned long long* const* d_outs = (unsigned long long* const*)((char*)c->vis_views.ptr + ptr_off);
-
-    // bin capacity: grown from earlier frames' totals (read back without waiting); a frame
-    // that still overflows is rendered correctly by the tile kernel's record scan
+    VisRecord* records;
+    uint2* rects;
+    uint32_t rec_cap;
+    uint32_t* counters;
+    uint32_t* bucket_cnt;
+    uint32_t* bucket_off;
+    uint32_t* tile_total;
+    uint32_t* cta_aux;
+    uint32_t* tile_off;
+    uint32_t* tile_order;
+    uint32_t* bins;
     uint32_t bin_capacity;
-    if (c->flags & TGX_FLAG_MIN_BIN_CAPACITY) {
-        TGX_TRY(devbuf_reserve(c->vis_bins, 64 * 4));
-        bin_capacity = 64;
-    } else {
-        if (c->vis_done && cudaEventQuery(c->vis_done) == cudaSuccess) {
-            const uint32_t prev = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
-            if ((size_t)prev * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)prev * 2 * 4));
-        }
-        cudaGetLastError();
-        TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 64, (size_t)1 << 20) * 4));
-        bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
-    }
+};
 
-    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
-    if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
-    const uint32_t rec_cap = (uint32_t)n_pairs;
-    TGX_TRY(devbuf_reserve(c->vis_records, (size_t)rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
-    TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
+// bytes of the tile-sized part of the scratch
+static size_t vis_tile_bytes(uint32_t n_tiles)
+{
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
-    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4 +
-                                                (size_t)n_scan_ctas * (1 + kOrderClasses) * 4));
-    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4 * 2));
-    VisRecord* records = (VisRecord*)c->vis_records.ptr;
-    uint2* rects = (uint2*)(records + rec_cap);
-    uint32_t* counters = (uint32_t*)c->vis_counters.ptr;
-    uint32_t* bucket_cnt = (uint32_t*)c->vis_tile_cnt.ptr;
-    uint32_t* bucket_off = bucket_cnt + (size_t)n_tiles * kBuckets;
-    uint32_t* tile_total = bucket_off + (size_t)n_tiles * kBuckets;
-    uint32_t* cta_aux = tile_total + n_tiles;
-    uint32_t* tile_off = (uint32_t*)c->vis_tile_off.ptr;
-    uint32_t* tile_order = tile_off + (n_tiles + 1);
-    TGX_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
-    TGX_CUDA(cudaMemsetAsync(bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
+    return (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4 + (size_t)n_scan_ctas * (1 + kOrderClasses) * 4;
+}
 
+static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_off, uint32_t n_tiles)
+{
+    w.bucket_cnt = tile_cnt;
+    w.bucket_off = w.bucket_cnt + (size_t)n_tiles * kBuckets;
+    w.tile_total = w.bucket_off + (size_t)n_tiles * kBuckets;
+    w.cta_aux = w.tile_total + n_tiles;
+    w.tile_off = tile_off;
+    w.tile_order = w.tile_off + (n_tiles + 1);
+}
+
+// The launches of one frame (n_views views of scene s, view table d_vc / d_outs on the device).
+static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs,
+                             uint32_t n_views, uint32_t n_tiles, const VisScratch& w)
+{
+    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
+    const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
+    TGX_CUDA(cudaMemsetAsync(w.bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
     const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
     TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
                s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-               records, rects, rec_cap, counters, c->d_status);
+               w.records, w.rects, w.rec_cap, w.counters, c->d_status);
     const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
-    TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, records, counters, rec_cap,
+    TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, w.records, w.counters, w.rec_cap,
                s->d_objects, d_vc);
-    TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
-    TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles,
-               cta_aux);
-    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, cta_aux, n_tiles, tile_off, bin_capacity, counters);
-    TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off,
-               tile_order);
+    TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, d_vc, w.bucket_cnt,
+               n_tiles);
+    TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off, w.tile_total,
+               n_tiles, w.cta_aux);
+    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity, w.counters);
+    TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux, w.tile_off,
+               w.tile_order);
     TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
-               records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, (uint32_t*)c->vis_bins.ptr,
-               n_tiles, bin_capacity, c->d_status);
-    c->vis_last_tiles = n_tiles;
+               w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
+               n_tiles, w.bin_capacity, c->d_status);
     const uint32_t threads = c->tile_w * c->tile_h;
-#define VIS_TILES_ARGS records, rects, (const uint32_t*)c->vis_bins.ptr, tile_off, tile_order, d_vc, n_views, \
-                       s->d_bits, s->d_inv_rot, d_outs, counters, c->d_status
+#define VIS_TILES_ARGS w.records, w.rects, (const uint32_t*)w.bins, w.tile_off, w.tile_order, d_vc, n_views, \
+                       s->d_bits, s->d_inv_rot, d_outs, w.counters, c->d_status
     if (threads == 64) {
         TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 16>), VIS_TILES_ARGS);
     } else if (threads == 128) {
@@ -846,11 +824,245 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
         TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), VIS_TILES_ARGS);
     }
 #undef VIS_TILES_ARGS
+    return TGX_OK;
+}
+
+// host view table: ViewConst per view (tile bases) and the output pointer table
+static std::vector<unsigned char> vis_view_table(tgx_ctx* c, const tgx_view* views, uint32_t n_views,
+                                                 uint64_t* const* d_visbuf, uint32_t& n_tiles, size_t& ptr_off)
+{
+    std::vector<ViewConst> vcs(n_views);
+    n_tiles = 0;
+    for (uint32_t i = 0; i < n_views; i++) {
+        make_view_const(views[i], c->tile_w, c->tile_h, n_tiles, vcs[i]);
+        n_tiles += vcs[i].tiles_x * vcs[i].tiles_y;
+    }
+    const size_t vc_bytes = n_views * sizeof(ViewConst);
+    ptr_off = (vc_bytes + 15) & ~(size_t)15;
+    std::vector<unsigned char> stage(ptr_off + n_views * sizeof(void*));
+    memcpy(stage.data(), vcs.data(), vc_bytes);
+    memcpy(stage.data() + ptr_off, d_visbuf, n_views * sizeof(void*));
+    return stage;
+}
+
+tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
+                             uint64_t* const* d_visbuf)
+{
+    if (!c || !s || !d_visbuf) { tgx_set_error("tgx_vis_render: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
+    for (uint32_t i = 0; i < n_views; i++)
+        if (!d_visbuf[i]) { tgx_set_error("tgx_vis_render: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
+    TGX_CUDA(cudaSetDevice(c->device));
+
+    // view constants + output pointer table, copied from pageable memory (staged by the driver, no sync)
+    uint32_t n_tiles = 0;
+    size_t ptr_off = 0;
+    const std::vector<unsigned char> stage = vis_view_table(c, views, n_views, d_visbuf, n_tiles, ptr_off);
+    TGX_TRY(devbuf_reserve(c->vis_views, stage.size()));
+    TGX_CUDA(cudaMemcpyAsync(c->vis_views.ptr, stage.data(), stage.size(), cudaMemcpyHostToDevice, c->stream));
+    const ViewConst* d_vc = (const ViewConst*)c->vis_views.ptr;
+    unsigned long long* const* d_outs = (unsigned long long* const*)((char*)c->vis_views.ptr + ptr_off);
+
+    // bin capacity: grown from earlier frames' totals (read back without waiting); a frame
+    // that still overflows is rendered correctly by the tile kernel's record scan
+    VisScratch w;
+    if (c->flags & TGX_FLAG_MIN_BIN_CAPACITY) {
+        TGX_TRY(devbuf_reserve(c->vis_bins, 64 * 4));
+        w.bin_capacity = 64;
+    } else {
+        if (c->vis_done && cudaEventQuery(c->vis_done) == cudaSuccess) {
+            const uint32_t prev = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
+            if ((size_t)prev * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)prev * 2 * 4));
+        }
+        cudaGetLastError();
+        TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 64, (size_t)1 << 20) * 4));
+        w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
+    }
+
+    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
+    if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
+    w.rec_cap = (uint32_t)n_pairs;
+    TGX_TRY(devbuf_reserve(c->vis_records, (size_t)w.rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
+    TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
+    TGX_TRY(devbuf_reserve(c->vis_tile_cnt, vis_tile_bytes(n_tiles)));
+    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4 * 2));
+    w.records = (VisRecord*)c->vis_records.ptr;
+    w.rects = (uint2*)(w.records + w.rec_cap);
+    w.counters = (uint32_t*)c->vis_counters.ptr;
+    w.bins = (uint32_t*)c->vis_bins.ptr;
+    vis_carve_tiles(w, (uint32_t*)c->vis_tile_cnt.ptr, (uint32_t*)c->vis_tile_off.ptr, n_tiles);
+    TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w));
+    c->vis_last_tiles = n_tiles;
     // counters of this frame to pinned memory, read by the next call without waiting
-    TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, w.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
     if (!c->vis_done) TGX_CUDA(cudaEventCreateWithFlags(&c->vis_done, cudaEventDisableTiming));
     TGX_CUDA(cudaEventRecord(c->vis_done, c->stream));
     return TGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched frames: the visibility passes of many jobs captured as one CUDA graph
+// ---------------------------------------------------------------------------
+
+struct tgx_frame_graph
+{
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void* d_mem = nullptr;                       // view tables, then the shared scratch
+    struct Job
+    {
+        const tgx_scene* scene;
+        std::vector<tgx_view> views;             // resolutions fixed at capture
+        std::vector<uint64_t*> outs;
+        size_t table_off, ptr_off;
+        uint32_t n_tiles;
+    };
+    std::vector<Job> jobs;
+    uint32_t kernels = 0;
+};
+
+static void frame_graph_free(tgx_frame_graph* g)
+{
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->d_mem);
+    delete g;
+}
+
+extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs, uint32_t n_jobs,
+                                             tgx_frame_graph** out)
+{
+    if (!c || !jobs || !n_jobs || !out) { tgx_set_error("tgx_frame_graph_create: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    TGX_CUDA(cudaSetDevice(c->device));
+    tgx_frame_graph* g = new (std::nothrow) tgx_frame_graph();
+    if (!g) return TGX_ERR_OUT_OF_MEMORY;
+    auto fail = [&](tgx_status st) { cudaStreamSynchronize(c->stream); frame_graph_free(g); return st; };
+    // sizes, and one uncaptured frame per job to size the bins
+    size_t table_bytes = 0, tile_bytes = 0, off_bytes = 0;
+    uint64_t rec_cap = 0, bin_cap = (size_t)1 << 20;
+    std::vector<std::vector<unsigned char>> tables(n_jobs);
+    for (uint32_t j = 0; j < n_jobs; j++) {
+        const tgx_vis_job& jb = jobs[j];
+        if (!jb.scene || !jb.views || !jb.d_visbuf || !jb.n_views) {
+            tgx_set_error("tgx_frame_graph_create: job %u has a NULL member or no views", j);
+            return fail(TGX_ERR_INVALID_ARGUMENT);
+        }
+        tgx_status st = vis_render_device(c, jb.scene, jb.views, jb.n_views, jb.d_visbuf);
+        if (st != TGX_OK) return fail(st);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) { tgx_set_error("tgx_frame_graph_create: frame failed"); return fail(TGX_ERR_CUDA); }
+        const uint32_t entries = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
+        tgx_frame_graph::Job job;
+        job.scene = jb.scene;
+        job.views.assign(jb.views, jb.views + jb.n_views);
+        job.outs.assign(jb.d_visbuf, jb.d_visbuf + jb.n_views);
+        tables[j] = vis_view_table(c, jb.views, jb.n_views, jb.d_visbuf, job.n_tiles, job.ptr_off);
+        job.table_off = table_bytes;
+        table_bytes += (tables[j].size() + 255) & ~(size_t)255;
+        tile_bytes = std::max(tile_bytes, vis_tile_bytes(job.n_tiles));
+        off_bytes = std::max(off_bytes, (size_t)(job.n_tiles + 1) * 4 * 2);
+        rec_cap = std::max<uint64_t>(rec_cap, (uint64_t)jb.scene->n_cluster_pointers * jb.n_views);
+        bin_cap = std::max<uint64_t>(bin_cap, std::max<uint64_t>((uint64_t)job.n_tiles * 64, (uint64_t)entries * 3 / 2));
+        g->jobs.push_back(std::move(job));
+    }
+    if (rec_cap > 0xffffffffull || bin_cap > 0xffffffffull) {
+        tgx_set_error("tgx_frame_graph_create: a job has too many (view, cluster) pairs");
+        return fail(TGX_ERR_CAPACITY);
+    }
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t rec_bytes = al((size_t)rec_cap * (sizeof(VisRecord) + sizeof(uint2)));
+    const size_t total = table_bytes + rec_bytes + 256 + al(tile_bytes) + al(off_bytes) + al((size_t)bin_cap * 4);
+    if (cudaMalloc(&g->d_mem, total) != cudaSuccess) {
+        cudaGetLastError();
+        tgx_set_error("tgx_frame_graph_create: out of device memory (%zu bytes)", total);
+        return fail(TGX_ERR_OUT_OF_MEMORY);
+    }
+    char* base = (char*)g->d_mem;
+    for (uint32_t j = 0; j < n_jobs; j++)
+        if (cudaMemcpy(base + g->jobs[j].table_off, tables[j].data(), tables[j].size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            tgx_set_error("tgx_frame_graph_create: view table upload failed");
+            return fail(TGX_ERR_CUDA);
+        }
+    VisScratch w;
+    char* p = base + table_bytes;
+    w.records = (VisRecord*)p;
+    w.rec_cap = (uint32_t)rec_cap;
+    w.rects = (uint2*)(w.records + rec_cap);
+    p += rec_bytes;
+    w.counters = (uint32_t*)p;
+    p += 256;
+    uint32_t* tile_cnt = (uint32_t*)p;
+    p += al(tile_bytes);
+    uint32_t* tile_off = (uint32_t*)p;
+    p += al(off_bytes);
+    w.bins = (uint32_t*)p;
+    w.bin_capacity = (uint32_t)bin_cap;
+    // capture (no trace events inside the graph)
+    const bool tracing = c->trace.enabled;
+    c->trace.enabled = false;
+    const uint64_t launches0 = c->launches;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        c->trace.enabled = tracing;
+        tgx_set_error("tgx_frame_graph_create: stream capture refused (%s)", cudaGetErrorString(cudaGetLastError()));
+        return fail(TGX_ERR_CUDA);
+    }
+    tgx_status st = TGX_OK;
+    for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++) {
+        const tgx_frame_graph::Job& job = g->jobs[j];
+        vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
+        const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
+        unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
+        st = vis_launch(c, job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, w);
+    }
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g->graph);
+    c->trace.enabled = tracing;
+    g->kernels = (uint32_t)(c->launches - launches0);
+    c->launches = launches0;
+    if (st != TGX_OK) return fail(st);
+    if (ce != cudaSuccess || cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) {
+        tgx_set_error("tgx_frame_graph_create: graph capture failed (%s)", cudaGetErrorString(cudaGetLastError()));
+        return fail(TGX_ERR_CUDA);
+    }
+    *out = g;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_frame_graph_launch(tgx_ctx* c, tgx_frame_graph* g)
+{
+    if (!c || !g) return TGX_ERR_INVALID_ARGUMENT;
+    TGX_CUDA(cudaGraphLaunch(g->exec, c->stream));
+    c->launches += g->kernels;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_frame_graph_set_views(tgx_ctx* c, tgx_frame_graph* g, uint32_t job, const tgx_view* views)
+{
+    if (!c || !g || !views || job >= g->jobs.size()) return TGX_ERR_INVALID_ARGUMENT;
+    tgx_frame_graph::Job& jb = g->jobs[job];
+    const uint32_t n = (uint32_t)jb.views.size();
+    for (uint32_t i = 0; i < n; i++)
+        if (views[i].width != jb.views[i].width || views[i].height != jb.views[i].height) {
+            tgx_set_error("tgx_frame_graph_set_views: view %u changes its resolution", i);
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+    TGX_TRY(check_views(views, n, c->tile_w, c->tile_h));
+    uint32_t n_tiles = 0;
+    size_t ptr_off = 0;
+    const std::vector<unsigned char> t = vis_view_table(c, views, n, jb.outs.data(), n_tiles, ptr_off);
+    // the pinned-free staging copy is ordered on the stream before the next launch
+    TGX_CUDA(cudaMemcpyAsync((char*)g->d_mem + jb.table_off, t.data(), t.size(), cudaMemcpyHostToDevice, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    jb.views.assign(views, views + n);
+    return TGX_OK;
+}
+
+extern "C" uint32_t tgx_frame_graph_kernels(const tgx_frame_graph* g) { return g ? g->kernels : 0u; }
+
+extern "C" void tgx_frame_graph_destroy(tgx_ctx* c, tgx_frame_graph* g)
+{
+    if (c) cudaStreamSynchronize(c->stream);
+    frame_graph_free(g);
 }
 
 extern "C" tgx_status tgx_vis_render(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
