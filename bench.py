@@ -346,6 +346,105 @@ def bench_batched(local: int, frames: int = 10):
     return res
 
 
+def bench_large(local: int):
+    """Config 5: 2^24 clusters (4096 objects of 16^3 clusters, Bernoulli(0.3) bits as
+    in config 1, uniform rotations, translations in an 8192^3 box; 1 GiB of bits,
+    8 GiB of material bytes), 8 views of uneven resolution up to 3840x2160 in one
+    tgx_vis_render call, the 16384^3 SVO (without its per-voxel material grid),
+    and 2-bounce GI at 8 spp on the 3840x2160 view: learned cache and the plain
+    fallback, both scored by relMSE against a 64-spp plain render."""
+    import torch
+    import tg_gb300 as tg
+
+    res = {}
+    t0 = time.perf_counter()
+    host = tg.generate_scene(0, 4096, 16, 16, seed=5, bernoulli_p=0.3, box_min=(-4096.0,) * 3,
+                             box_max=(4096.0,) * 3, n_luts=32)
+    res["generate_s"] = round(time.perf_counter() - t0, 2)
+    res["clusters"] = int(host.n_clusters)
+    res["scene_gib"] = round((host.voxel_bits.nbytes + host.material_idx.nbytes) / 2**30, 2)
+    ctx = tg.Context(local, tile=(8, 16))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    free0 = torch.cuda.mem_get_info()[0]
+    t0 = time.perf_counter()
+    sc = ctx.upload(host)
+    ctx.sync()
+    res["upload_s"] = round(time.perf_counter() - t0, 2)
+    del host
+    rng = np.random.default_rng(5)
+    sizes = [(3840, 2160), (2560, 1440), (1920, 1080), (1920, 1080), (1280, 720), (1280, 720), (640, 480), (320, 240)]
+    views = np.concatenate([tg.make_view(tuple(rng.uniform(-2048.0, 2048.0, 3)), float(rng.uniform(-0.3, 0.3)),
+                                         float(rng.uniform(0, 2 * np.pi)), float(np.pi / 3), w, h, 0.1, 16384.0)
+                            for w, h in sizes])
+    outs = [torch.empty(w * h, dtype=torch.int64, device="cuda") for w, h in sizes]
+    pixels = sum(w * h for w, h in sizes)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            ctx.vis_render(sc, views, outs)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            ctx.vis_render(sc, views, outs)
+        e1.record(stream)
+        ctx.sync()
+    vis_ms = e0.elapsed_time(e1) / 5
+    res.update({"views": len(sizes), "pixels": pixels, "vis_frame_ms": round(vis_ms, 3),
+                "vis_grays_per_s": pixels / (vis_ms * 1e-3) / 1e9})
+    mn = (-8192.0, -8192.0, -8192.0)
+    svo = ctx.svo_build(sc, mn, 14, materials=False)
+    ctx.sync()
+    svo.close()
+    t0 = time.perf_counter()
+    svo = ctx.svo_build(sc, mn, 14, materials=False)
+    ctx.sync()
+    res["svo_build_ms"] = round((time.perf_counter() - t0) * 1e3, 1)
+    info = svo.info()
+    res["svo"] = {"extent": 16384, "blocks": int(info.n_blocks), "nonempty_blocks": int(info.n_nonempty_blocks),
+                  "device_gib": round(info.device_bytes / 2**30, 2)}
+    # GI on the 3840x2160 view
+    v0, vis0 = views[0:1], outs[0]
+    n = 3840 * 2160 * 3
+    mask = vis0.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
+    ref = torch.empty(n, dtype=torch.float32, device="cuda")
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    box = ((-4200.0,) * 3, (4200.0,) * 3)
+    with torch.cuda.stream(stream):
+        ctx.gi_render(sc, svo, v0, vis0, tg.gi_params(spp=64, bounces=2, seed=77), ref)
+        ctx.sync()
+        r = ref.cpu().numpy()
+
+        def timed(fn, frames=3):
+            fn(0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for f in range(frames):
+                fn(1 + f)
+            e1.record(stream)
+            ctx.sync()
+            return e0.elapsed_time(e1) / frames
+
+        plain_ms = timed(lambda f: ctx.gi_render(sc, svo, v0, vis0, tg.gi_params(spp=8, bounces=2, seed=2, frame=f),
+                                                 out))
+        plain_err = rel_mse(out.cpu().numpy(), r, mask)
+        cache = tg.Cache(ctx, seed=7)
+        cp = tg.cache_gi_params(box[0], box[1])
+        for f in range(20):
+            ctx.gi_render_cached(sc, svo, cache, v0, vis0, tg.gi_params(spp=1, bounces=2, seed=2, frame=f), cp, out)
+        cached_ms = timed(lambda f: ctx.gi_render_cached(sc, svo, cache, v0, vis0,
+                                                          tg.gi_params(spp=8, bounces=2, seed=2, frame=40 + f), cp, out))
+        cached_err = rel_mse(out.cpu().numpy(), r, mask)
+        cache.close()
+    res["gi_4k"] = {"geometry_pixels": int(mask.sum()), "judge": "plain 2-bounce GI, 64 spp",
+                    "plain_8spp": {"frame_ms": round(plain_ms, 2), "relmse": plain_err},
+                    "cached_8spp": {"frame_ms": round(cached_ms, 2), "relmse": cached_err}}
+    res["device_gib_used"] = round((free0 - torch.cuda.mem_get_info()[0]) / 2**30, 2)
+    res["device_status"] = int(ctx.device_error().code)
+    svo.close()
+    sc.close()
+    ctx.close()
+    return res
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -355,6 +454,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gi", action="store_true", help="skip the SVO build and GI measurements")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched many-view frame (config 3)")
+    ap.add_argument("--large", action="store_true",
+                    help="also run the 2^24-cluster config 5 (about 30 GB of device memory and a minute of setup)")
     ap.add_argument("--no-gi-cache", action="store_true",
                     help="skip the learned-cache vs plain 2-bounce GI comparison at equal relMSE")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
@@ -517,6 +618,7 @@ def main() -> None:
             gi_report["gi_cache_vs_plain"] = cache_report
         svo.close()
     batched = None if args.no_batched else bench_batched(local)
+    large = bench_large(local) if args.large else None
     rays = W * H
     value = rays * world / (ms * 1e-3) / 1e9
 
@@ -559,6 +661,7 @@ def main() -> None:
         "hit_pixels": hits,
         **gi_report,
         **({"batched_frame": batched} if batched else {}),
+        **({"large_config": large} if large else {}),
         "vis_stats": {"visible_clusters": n_vis, "bin_entries": int(stats.bin_entries), "tiles": int(stats.tiles),
                       "dda_overruns": int(stats.dda_overruns)},
         "wall_s_timed": t_wall,

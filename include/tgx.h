@@ -296,6 +296,14 @@ void        tgx_frame_graph_destroy(tgx_ctx* ctx, tgx_frame_graph* graph);
  */
 tgx_status  tgx_svo_build(tgx_ctx* ctx, const tgx_scene* scene, const float min[3], uint32_t extent_log2,
                           tgx_svo** out_svo);
+
+/* Leaves out the per-voxel material codes (2 bytes per voxel of every
+ * allocated 32^3 block, i.e. 64 KiB per block); GI then shades with grey
+ * albedo.  For extents where that grid would not fit. */
+#define TGX_SVO_NO_MATERIALS            1u
+/* tgx_svo_build with TGX_SVO_* flags. */
+tgx_status  tgx_svo_build_flags(tgx_ctx* ctx, const tgx_scene* scene, const float min[3], uint32_t extent_log2,
+                                uint32_t flags, tgx_svo** out_svo);
 void        tgx_svo_destroy(tgx_ctx* ctx, tgx_svo* svo);
 
 typedef struct tgx_svo_info
@@ -428,9 +436,9 @@ typedef struct tgx_gen_params
     float    noise_period;       /* kind 1, lattice spacing in voxels */
     float    noise_threshold;    /* kind 1 */
     uint64_t seed;
-    float    box_min[3];         /* translations uniform in [box_min, box_max) (kind 1) */
+    float    box_min[3];         /* translations uniform in [box_min, box_max) (kind 1; kind 0 when not empty) */
     float    box_max[3];
-    float    fixed_translation[3]; /* kind 0 */
+    float    fixed_translation[3]; /* kind 0 with an empty box */
     uint32_t n_luts;
     uint32_t threads;            /* host threads, 0 = all */
 } tgx_gen_params;

@@ -146,7 +146,7 @@ EXPORTS = [
     "tgx_cache_create", "tgx_cache_destroy", "tgx_cache_infer", "tgx_cache_train_step", "tgx_cache_last_loss",
     "tgx_cache_gradient", "tgx_cache_get_weights", "tgx_cache_set_weights", "tgx_cache_save", "tgx_cache_load",
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
-    "tgx_frame_graph_kernels", "tgx_frame_graph_destroy",
+    "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags",
 ]
 
 
@@ -172,6 +172,7 @@ def _load() -> C.CDLL:
         "tgx_vis_decode": (i32, [u64, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32)]),
         "tgx_pick": (i32, [vp, vp, u32, u32, u32, u32, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32), C.POINTER(i32)]),
         "tgx_svo_build": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_svo_build_flags": (i32, [vp, vp, vp, u32, u32, C.POINTER(vp)]),
         "tgx_svo_destroy": (None, [vp, vp]),
         "tgx_svo_get_info": (i32, [vp, vp, C.POINTER(SvoInfo)]),
         "tgx_svo_download": (i32, [vp, vp, vp, vp, u32, C.POINTER(u32)]),
@@ -402,10 +403,12 @@ class Context:
         outputs; returns a FrameGraph whose launch() replays all of it with one graph launch."""
         return FrameGraph(self, jobs)
 
-    def svo_build(self, scene: "Scene", mn, extent_log2: int) -> Svo:
+    def svo_build(self, scene: "Scene", mn, extent_log2: int, materials: bool = True) -> Svo:
+        """materials=False leaves out the per-voxel material grid (TGX_SVO_NO_MATERIALS)."""
         m = np.asarray(mn, dtype=np.float32)
         h = C.c_void_p()
-        check(lib.tgx_svo_build(self.handle, scene.handle, _ptr(m), extent_log2, C.byref(h)), "tgx_svo_build")
+        check(lib.tgx_svo_build_flags(self.handle, scene.handle, _ptr(m), extent_log2, 0 if materials else 1,
+                                      C.byref(h)), "tgx_svo_build")
         return Svo(self, h)
 
     def gi_render(self, scene: "Scene", svo: "Svo", view: np.ndarray, visbuf, params: np.ndarray, rgb) -> None:

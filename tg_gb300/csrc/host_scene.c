@@ -125,9 +125,12 @@ tgx_status tgx_generate_scene(const tgx_gen_params* p, tgx_gen_scene* out)
             o->n_cluster_pointers_per_dim[a] = p->min_clusters_per_axis + (uint32_t)(hash3(p->seed, ST_DIMS, 3ull * i + a) % span);
         o->first_cluster_pointer = (uint32_t)total;
         total += (uint64_t)o->n_cluster_pointers_per_dim[0] * o->n_cluster_pointers_per_dim[1] * o->n_cluster_pointers_per_dim[2];
+        /* kind 1 always spreads objects over the box; kind 0 only when the box is not empty */
+        const int use_box = p->kind != 0 || (p->box_max[0] > p->box_min[0] && p->box_max[1] > p->box_min[1] &&
+                                             p->box_max[2] > p->box_min[2]);
         for (int a = 0; a < 3; a++)
         {
-            if (p->kind == 0)
+            if (!use_box)
                 o->translation[a] = p->fixed_translation[a];
             else
                 o->translation[a] = p->box_min[a] + unit_f32(hash3(p->seed, ST_TRANS, 3ull * i + a)) * (p->box_max[a] - p->box_min[a]);

@@ -493,6 +493,13 @@ static void svo_free(tgx_svo* s)
 
 extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float* mn, uint32_t L, tgx_svo** out)
 {
+    return tgx_svo_build_flags(c, sc, mn, L, 0u, out);
+}
+
+extern "C" tgx_status tgx_svo_build_flags(tgx_ctx* c, const tgx_scene* sc, const float* mn, uint32_t L, uint32_t flags,
+                                          tgx_svo** out)
+{
+    if (flags & ~TGX_SVO_NO_MATERIALS) { tgx_set_error("tgx_svo_build: unknown flags %u", flags); return TGX_ERR_INVALID_ARGUMENT; }
     if (!c || !sc || !mn || !out) { tgx_set_error("tgx_svo_build: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
     *out = nullptr;
     if (L < 6 || L > 14) { tgx_set_error("tgx_svo_build: extent_log2 %u outside 6..14", L); return TGX_ERR_INVALID_ARGUMENT; }
@@ -569,7 +576,7 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
     }
     cudaMemsetAsync(s->d_pool, 0, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4, c->stream);
     cudaMemsetAsync(s->d_sub, 0, (uint64_t)std::max(s->n_blocks, 1u) * 32 * 4, c->stream);
-    if (sc->d_material && sc->d_luts) {
+    if (sc->d_material && sc->d_luts && !(flags & TGX_SVO_NO_MATERIALS)) {
         const uint64_t mb = (uint64_t)std::max(s->n_blocks, 1u) * 32768u * 2u;
         if (cudaMalloc(&s->d_mat, mb) != cudaSuccess) {
             tgx_set_error("tgx_svo_build: out of device memory for the material grid");
@@ -584,7 +591,7 @@ extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float
                                                                                   (uint64_t)c->num_sms * 16));
         TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects,
                    sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
-                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, sc->d_material, s->d_mat,
+                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, s->d_mat ? sc->d_material : nullptr, s->d_mat,
                    mn[0], mn[1], mn[2], s->B);
         const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
         TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
