@@ -357,20 +357,17 @@ def bench_large(local: int):
     import tg_gb300 as tg
 
     res = {}
-    t0 = time.perf_counter()
-    host = tg.generate_scene(0, 4096, 16, 16, seed=5, bernoulli_p=0.3, box_min=(-4096.0,) * 3,
-                             box_max=(4096.0,) * 3, n_luts=32)
-    res["generate_s"] = round(time.perf_counter() - t0, 2)
-    res["clusters"] = int(host.n_clusters)
-    res["scene_gib"] = round((host.voxel_bits.nbytes + host.material_idx.nbytes) / 2**30, 2)
     ctx = tg.Context(local, tile=(8, 16))
     stream = torch.cuda.ExternalStream(ctx.stream)
     free0 = torch.cuda.mem_get_info()[0]
+    # the store is generated in device memory (tgx_generate_scene_device), byte-equal to the host generator
     t0 = time.perf_counter()
-    sc = ctx.upload(host)
+    sc = ctx.generate_scene(0, 4096, 16, 16, seed=5, bernoulli_p=0.3, box_min=(-4096.0,) * 3,
+                            box_max=(4096.0,) * 3, n_luts=32)
     ctx.sync()
-    res["upload_s"] = round(time.perf_counter() - t0, 2)
-    del host
+    res["generate_on_device_s"] = round(time.perf_counter() - t0, 2)
+    res["clusters"] = 4096 * 16 ** 3
+    res["scene_gib"] = round(res["clusters"] * (64 + 512) / 2**30, 2)
     rng = np.random.default_rng(5)
     sizes = [(3840, 2160), (2560, 1440), (1920, 1080), (1920, 1080), (1280, 720), (1280, 720), (640, 480), (320, 240)]
     views = np.concatenate([tg.make_view(tuple(rng.uniform(-2048.0, 2048.0, 3)), float(rng.uniform(-0.3, 0.3)),
@@ -459,6 +456,8 @@ def main() -> None:
     ap.add_argument("--no-gi-cache", action="store_true",
                     help="skip the learned-cache vs plain 2-bounce GI comparison at equal relMSE")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
+    ap.add_argument("--launch", choices=["graph", "calls"], default="graph",
+                    help="time the frame as one CUDA graph replay (tgx_frame_graph) or as separate launches")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -496,16 +495,32 @@ def main() -> None:
     out = torch.empty(W * H, dtype=torch.int64, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def step():
+    def call():
         ctx.vis_render(sc, view, [out])
+
+    def timed_frames(fn, n):
+        e = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for i, (a, b) in enumerate(e):
+            flush.fill_(i & 0xFF)
+            a.record(stream)
+            fn()
+            b.record(stream)
+        ctx.sync()
+        return statistics.mean(x.elapsed_time(y) for x, y in e)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            step()
+            call()
         ctx.sync()
         err = ctx.device_error()
         if err.code:
             raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
+        # the frame as one CUDA graph (tgx_frame_graph) or as separate launches
+        graph = ctx.frame_graph([(sc, view, [out])]) if args.launch == "graph" else None
+        step = graph.launch if graph else call
+        for _ in range(args.warmup):
+            step()
+        ms_other = timed_frames(call, args.steps) if graph else None
 
         # ---- timed region: K steps, per-step CUDA events on the launching stream ----
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -532,12 +547,14 @@ def main() -> None:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
 
-        # ---- per-kernel times (trace events) for the roofline ----
+        if graph is not None:
+            graph.close()
+        # ---- per-kernel times (trace events, separate launches) for the roofline ----
         ctx.trace_reset()
         ctx.trace(True)
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
-            step()
+            call()
         trace = ctx.trace_read()
         ctx.trace(False)
 
@@ -652,6 +669,9 @@ def main() -> None:
                 "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e,
                 "path": "tgx_vis_render_host (views from host, visibility buffer back to pinned host memory)"},
         "gpu_launches": int(launches),
+        "launch": ("one CUDA graph replay per frame (tgx_frame_graph), same kernels as tgx_vis_render"
+                   if args.launch == "graph" else "separate launches per frame (tgx_vis_render)"),
+        **({"ms_per_step_separate_calls": ms_other} if ms_other is not None else {}),
         "kernels_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in trace.items()},
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,

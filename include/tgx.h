@@ -250,6 +250,31 @@ int         tgx_vis_decode(uint64_t packed, float* out_depth, uint32_t* out_clus
 tgx_status  tgx_pick(tgx_ctx* ctx, const uint64_t* d_visbuf, uint32_t w, uint32_t h, uint32_t x, uint32_t y,
                      float* out_depth, uint32_t* out_cluster_pointer, uint32_t* out_voxel_idx, int* out_hit);
 
+/* ---- shading pass (shading.frag) ---- */
+
+/* Modes of tgx_shade, numbered like the reference's debug views (shading.frag:16-25). */
+#define TGX_SHADE_NONE                  0u   /* direct GGX shading with the LUT albedo */
+#define TGX_SHADE_OBJECT_INDEX          1u
+#define TGX_SHADE_DEPTH                 2u
+#define TGX_SHADE_CLUSTER_INDEX         3u
+#define TGX_SHADE_VOXEL_INDEX           4u
+#define TGX_SHADE_BLOCKS                5u
+#define TGX_SHADE_COLOR_LUT_INDEX       6u
+#define TGX_SHADE_COLOR                 7u
+#define TGX_SHADE_NORMAL                8u
+#define TGX_SHADE_SHADING               9u   /* direct shading with white albedo */
+
+/*
+ * Shades a visibility buffer the way tg's shading.frag:116-316 does: per pixel
+ * the primary surface (face normal from the voxel box), the voxel's LUT
+ * albedo, GGX/Smith/Schlick direct light from normalize(0, 0.8, 0.3) with
+ * radiance 3, metallic 0.1, roughness 0.8, plus 0.1 * albedo ambient; or one
+ * of the debug views.  Sky pixels are magenta.  Writes RGBA, 4 floats per
+ * pixel, to d_rgba (DEVICE).  Asynchronous.
+ */
+tgx_status  tgx_shade(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* view, const uint64_t* d_visbuf,
+                      uint32_t mode, float* d_rgba);
+
 /* ---- batched frames captured as a CUDA graph ---- */
 
 /* One job of a batched frame: n_views views (any resolutions) of one scene. */
@@ -456,6 +481,22 @@ typedef struct tgx_gen_scene
 
 tgx_status  tgx_generate_scene(const tgx_gen_params* params, tgx_gen_scene* out_scene);
 void        tgx_free_generated_scene(tgx_gen_scene* scene);
+
+/*
+ * The same scene built directly in device memory (the reference's "TODO: gen
+ * on GPU", tgvk_raytracer.c:868): object records on the host, every cluster's
+ * bits and material bytes by one GPU thread per voxel.  Equal byte for byte to
+ * tgx_generate_scene + tgx_scene_upload, without the host arrays.  Synchronous.
+ */
+tgx_status  tgx_generate_scene_device(tgx_ctx* ctx, const tgx_gen_params* params, tgx_scene** out_scene);
+
+/* Sizes of a scene's arrays (any argument may be NULL). */
+tgx_status  tgx_scene_counts(const tgx_scene* scene, uint32_t* n_objects, uint32_t* n_cluster_pointers,
+                             uint32_t* n_clusters, uint32_t* n_luts);
+/* Copies a scene's arrays back to HOST buffers sized by tgx_scene_counts (NULL skips an array). */
+tgx_status  tgx_scene_download(tgx_ctx* ctx, const tgx_scene* scene, tgx_object* objects, uint32_t* cluster_pointers,
+                               uint32_t* cluster_idx_to_object_idx, uint32_t* voxel_bits, uint8_t* material_idx,
+                               tgx_material* luts);
 
 /* Pinhole view from a position, yaw/pitch (radians) and vertical field of
  * view, with tg's corner-ray construction (tgvk_core.c:382-444): view

@@ -478,28 +478,30 @@ static void incoming(const osvo* s, const float o2[3], const float w[3], uint32_
     out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
 }
 
-/*
- * One pixel of plain GI.  The primary hit comes from the visibility word (as
- * shading.frag:116-228 decodes it); world hit point = camera + enter * the
- * normalised pixel ray.  Writes RGB.
- */
-void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t* cluster_pointers,
-                     const uint32_t* c2o, const uint8_t* material, const tgx_material* luts, const tgx_view* cam,
-                     const ogi_params* p, uint64_t word, uint32_t px, uint32_t py, float out[3])
+/* Primary surface of a visibility word (shading.frag:116-228): cluster-space
+ * ray, voxel box hit and dominant-axis face normal rotated to world space. */
+typedef struct
 {
-    const osvo* s = (const osvo*)svo;
+    float    depth;
+    uint32_t ptr, voxel, ci, oi, mat_byte;
+    int      box_hit;
+    float    nw[3], dws[3], dn[3], te, albedo[3];
+} surface;
+
+static int decode_surface(const tgx_object* objects, const uint32_t* cluster_pointers, const uint32_t* c2o,
+                          const uint8_t* material, const tgx_material* luts, const tgx_view* cam, uint64_t word,
+                          uint32_t px, uint32_t py, surface* sf)
+{
     const float fx = ((float)px + 0.5f) / (float)cam->width;
     const float fy = 1.0f - ((float)py + 0.5f) / (float)cam->height;
-    const float depth = (float)(word >> 40) / 16777215.0f;
-    if (!(depth < 1.0f))
-    {
-        out[0] = p->sky_radiance[0]; out[1] = p->sky_radiance[1]; out[2] = p->sky_radiance[2];
-        return;
-    }
+    sf->depth = (float)(word >> 40) / 16777215.0f;
+    if (!(sf->depth < 1.0f)) return 0;
     const uint32_t ptr = (uint32_t)(word >> 9) & 2147483647u;
     const uint32_t voxel = (uint32_t)word & 511u;
     const uint32_t ci = cluster_pointers[ptr];
-    const tgx_object* od = &objects[c2o[ci]];
+    const uint32_t oi = c2o[ci];
+    sf->ptr = ptr; sf->voxel = voxel; sf->ci = ci; sf->oi = oi;
+    const tgx_object* od = &objects[oi];
     /* shading.frag:147-181: the same ws2ms, origin and direction as the visibility pass */
     const uint32_t nx = od->n_cluster_pointers_per_dim[0], ny = od->n_cluster_pointers_per_dim[1];
     const uint32_t rel = ptr - od->first_cluster_pointer;
@@ -523,6 +525,7 @@ void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t*
         const float a = cam->ray_bl[i] * (1.0f - fy) + cam->ray_tl[i] * fy;
         const float b = cam->ray_br[i] * (1.0f - fy) + cam->ray_tr[i] * fy;
         dws[i] = a * (1.0f - fx) + b * fx;
+        sf->dws[i] = dws[i];
     }
     dws[3] = 0.0f;
     float d4[4];
@@ -532,9 +535,9 @@ void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t*
     const float vmin[3] = { (float)(voxel % 8u), (float)((voxel / 8u) % 8u), (float)(voxel / 64u) };
     const float vmax[3] = { vmin[0] + 1.0f, vmin[1] + 1.0f, vmin[2] + 1.0f };
     float enter, exit_;
-    float nw[3] = { 0.0f, 0.0f, 0.0f };
-    const int hit = or_ray_aabb(o4, dm, vmin, vmax, &enter, &exit_);
-    if (hit)
+    sf->nw[0] = sf->nw[1] = sf->nw[2] = 0.0f;
+    sf->box_hit = or_ray_aabb(o4, dm, vmin, vmax, &enter, &exit_);
+    if (sf->box_hit)
     {
         /* shading.frag:195-228 */
         float hm[3], nm[3];
@@ -558,20 +561,43 @@ void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t*
         float r4[4];
         or_m4_mulv4(od->rotation, n4, r4);
         const float rl = sqrtf(r4[0] * r4[0] + r4[1] * r4[1] + r4[2] * r4[2]);
-        if (rl > 0.0f) { nw[0] = r4[0] / rl; nw[1] = r4[1] / rl; nw[2] = r4[2] / rl; }
+        if (rl > 0.0f) { sf->nw[0] = r4[0] / rl; sf->nw[1] = r4[1] / rl; sf->nw[2] = r4[2] / rl; }
     }
     const float dl = sqrtf(dws[0] * dws[0] + dws[1] * dws[1] + dws[2] * dws[2]);
-    const float dn[3] = { dws[0] / dl, dws[1] / dl, dws[2] / dl };
-    if (nw[0] == 0.0f && nw[1] == 0.0f && nw[2] == 0.0f) { nw[0] = -dn[0]; nw[1] = -dn[1]; nw[2] = -dn[2]; }
-    const float te = hit && enter > 0.0f ? enter : 0.0f;
-    float a[3] = { 0.5f, 0.5f, 0.5f };
+    for (int i = 0; i < 3; i++) sf->dn[i] = dws[i] / dl;
+    sf->te = sf->box_hit && enter > 0.0f ? enter : 0.0f;
+    sf->albedo[0] = sf->albedo[1] = sf->albedo[2] = 0.5f;
+    sf->mat_byte = material ? material[(uint64_t)ci * 512u + voxel] : 0u;
     if (material && luts)
     {
-        const tgx_material* m = &luts[od->lut_idx * 256u + material[(uint64_t)ci * 512u + voxel]];
-        a[0] = m->albedo[0]; a[1] = m->albedo[1]; a[2] = m->albedo[2];
+        const tgx_material* m = &luts[od->lut_idx * 256u + sf->mat_byte];
+        sf->albedo[0] = m->albedo[0]; sf->albedo[1] = m->albedo[1]; sf->albedo[2] = m->albedo[2];
     }
+    return 1;
+}
+
+/*
+ * One pixel of plain GI.  The primary hit comes from the visibility word (as
+ * shading.frag:116-228 decodes it); world hit point = camera + enter * the
+ * normalised pixel ray.  Writes RGB.
+ */
+void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t* cluster_pointers,
+                     const uint32_t* c2o, const uint8_t* material, const tgx_material* luts, const tgx_view* cam,
+                     const ogi_params* p, uint64_t word, uint32_t px, uint32_t py, float out[3])
+{
+    const osvo* s = (const osvo*)svo;
+    surface sf;
+    if (!decode_surface(objects, cluster_pointers, c2o, material, luts, cam, word, px, py, &sf))
+    {
+        out[0] = p->sky_radiance[0]; out[1] = p->sky_radiance[1]; out[2] = p->sky_radiance[2];
+        return;
+    }
+    /* no voxel-box hit in cluster space: face the camera */
+    float nw[3] = { sf.nw[0], sf.nw[1], sf.nw[2] };
+    if (nw[0] == 0.0f && nw[1] == 0.0f && nw[2] == 0.0f) { nw[0] = -sf.dn[0]; nw[1] = -sf.dn[1]; nw[2] = -sf.dn[2]; }
+    const float* a = sf.albedo;
     float o2[3];
-    for (int i = 0; i < 3; i++) o2[i] = (cam->camera[i] + te * dn[i]) + nw[i] * p->offset;
+    for (int i = 0; i < 3; i++) o2[i] = (cam->camera[i] + sf.te * sf.dn[i]) + nw[i] * p->offset;
     float L[3];
     direct_sun(s, o2, nw, a, p, L);
     const uint32_t pixel = py * cam->width + px;
@@ -585,6 +611,125 @@ void oracle_gi_pixel(const void* svo, const tgx_object* objects, const uint32_t*
     }
     const float inv_spp = 1.0f / (float)(p->spp ? p->spp : 1);
     for (int i = 0; i < 3; i++) out[i] = L[i] + a[i] * (acc[i] * inv_spp);
+}
+
+/* ------------------------------------------------------------------ */
+/* shading pass (shading.frag:53-110, 285-336)                          */
+/* ------------------------------------------------------------------ */
+
+#define OR_PI 3.14159265358979323846f
+
+static inline float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline void normalize3(const float* v, float* out)
+{
+    const float l = sqrtf(dot3(v, v));
+    out[0] = v[0] / l; out[1] = v[1] / l; out[2] = v[2] / l;
+}
+/* GLSL max(x, y) = x < y ? y : x, min(x, y) = y < x ? y : x */
+static inline float gl_max(float x, float y) { return x < y ? y : x; }
+static inline float gl_min(float x, float y) { return y < x ? y : x; }
+static inline float clamp01(float x) { return gl_min(gl_max(x, 0.0f), 1.0f); }
+
+static float ggx_distribution(float c_ndh, float roughness)
+{
+    const float a = roughness * roughness;
+    const float a2 = a * a;
+    float den = c_ndh * c_ndh * (a2 - 1.0f) + 1.0f;
+    den = OR_PI * den * den;
+    return a2 / den;
+}
+static float schlick_ggx(float n_dot_v, float roughness)
+{
+    const float r = roughness + 1.0f;
+    const float k = (r * r) / 8.0f;
+    return n_dot_v / (n_dot_v * (1.0f - k) + k);
+}
+/* pow(1 - u, 5) as (t t)(t t) t */
+static float fresnel_schlick(float u, float roughness)
+{
+    const float fl = 1.0f - roughness;
+    const float t = 1.0f - u;
+    const float t2 = t * t;
+    return fl + (1.0f - fl) * ((t2 * t2) * t);
+}
+static void tg_shade(const float* n, const float* v, const float* l, const float* diffuse_albedo,
+                     const float* specular_albedo, float metallic, float roughness, float radiance, float* out)
+{
+    const float hv[3] = { v[0] + l[0], v[1] + l[1], v[2] + l[2] };
+    float h[3];
+    normalize3(hv, h);
+    const float c_hdn = clamp01(dot3(h, n));
+    const float c_ldn = clamp01(dot3(n, l));
+    const float c_ndv = clamp01(dot3(n, v));
+    const float d = ggx_distribution(c_hdn, roughness);
+    const float f = fresnel_schlick(c_ndv, roughness);
+    const float g = schlick_ggx(c_ldn, roughness) * schlick_ggx(c_ndv, roughness);
+    const float dfg = d * f * g;
+    const float den = 4.0f * c_ndv * c_ldn;
+    const float q = dfg / gl_max(den, 0.001f);
+    const float kd = (1.0f - f) * (1.0f - metallic);
+    for (int i = 0; i < 3; i++)
+    {
+        const float spec = specular_albedo[i] * q;
+        const float diff = (kd * diffuse_albedo[i]) / OR_PI;
+        out[i] = ((diff + spec) * radiance) * c_ldn;
+    }
+}
+/* MurmurHash3 finaliser (util.inc:47-56) */
+static inline uint32_t hash_u32(uint32_t v)
+{
+    v ^= v >> 16; v *= 0x85ebca6bu; v ^= v >> 13; v *= 0xc2b2ae35u; v ^= v >> 16;
+    return v;
+}
+static void hash_color(uint32_t v, float* out)
+{
+    const uint32_t h0 = hash_u32(v), h1 = hash_u32(h0), h2 = hash_u32(h1);
+    out[0] = (float)h0 / 4294967295.0f; out[1] = (float)h1 / 4294967295.0f; out[2] = (float)h2 / 4294967295.0f;
+}
+
+/* one frame of the shading pass; out = W*H*4 floats (RGBA) */
+void oracle_shade_render(const tgx_object* objects, const uint32_t* cluster_pointers, const uint32_t* c2o,
+                         const uint8_t* material, const tgx_material* luts, const tgx_view* cam, const uint64_t* visbuf,
+                         uint32_t mode, float* out)
+{
+    for (uint32_t py = 0; py < cam->height; py++)
+        for (uint32_t px = 0; px < cam->width; px++)
+        {
+            const uint64_t pixel = (uint64_t)py * cam->width + px;
+            float* o = &out[4 * pixel];
+            surface sf;
+            o[3] = 1.0f;
+            if (!decode_surface(objects, cluster_pointers, c2o, material, luts, cam, visbuf[pixel], px, py, &sf))
+            {
+                o[0] = 1.0f; o[1] = 0.0f; o[2] = 1.0f;
+                continue;
+            }
+            switch (mode)
+            {
+            case 1: hash_color(sf.oi, o); break;
+            case 2: o[0] = o[1] = o[2] = gl_min(1.0f, 8.0f * sf.depth); break;
+            case 3: case 5: hash_color(sf.ci, o); break;
+            case 4: hash_color(sf.voxel, o); break;
+            case 6: hash_color(sf.mat_byte, o); break;
+            case 7: o[0] = sf.albedo[0]; o[1] = sf.albedo[1]; o[2] = sf.albedo[2]; break;
+            case 8: for (int i = 0; i < 3; i++) o[i] = sf.nw[i] * 0.5f + 0.5f; break;
+            default:
+            {
+                const float metallic = 0.1f, roughness = 0.8f, radiance = 3.0f;
+                const float white[3] = { 1.0f, 1.0f, 1.0f };
+                const float* albedo = mode == 9 ? white : sf.albedo;
+                const float dm = sf.depth * cam->far_plane;
+                float vv[3], v[3], l[3], spec[3], lo[3];
+                for (int i = 0; i < 3; i++) vv[i] = cam->camera[i] - (cam->camera[i] + dm * sf.dws[i]);
+                normalize3(vv, v);
+                const float l0[3] = { 0.0f, 0.8f, 0.3f };
+                normalize3(l0, l);
+                for (int i = 0; i < 3; i++) spec[i] = 0.04f * (1.0f - metallic) + albedo[i] * metallic;
+                tg_shade(sf.nw, v, l, albedo, spec, metallic, roughness, radiance, lo);
+                for (int i = 0; i < 3; i++) o[i] = 0.1f * albedo[i] + lo[i];
+            }
+            }
+        }
 }
 
 /* whole frame (rows [row0, row1)); out = W*H*3 floats */

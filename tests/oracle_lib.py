@@ -193,3 +193,16 @@ class OracleMlp:
     def adam(self, w, m, v, g, step, lr=1e-2, b1=0.9, b2=0.99, eps=1e-15):
         self.lib.oracle_mlp_adam(_p(w), _p(m), _p(v), _p(np.ascontiguousarray(g, np.float64)), self.n_params, step,
                                  lr, b1, b2, eps)
+
+
+def shade_render(oracle: "Oracle", scene, view, visbuf, mode: int) -> np.ndarray:
+    """oracle_shade_render: RGBA float32 [H*W, 4] of the shading pass."""
+    v = np.ascontiguousarray(view).reshape(1)
+    W, H = int(v["width"][0]), int(v["height"][0])
+    out = np.zeros((W * H, 4), np.float32)
+    vb = np.ascontiguousarray(visbuf, np.uint64)
+    oracle.lib.oracle_shade_render(C.c_void_p(_p(scene.objects)), C.c_void_p(_p(scene.cluster_pointers)),
+                                   C.c_void_p(_p(scene.cluster_idx_to_object_idx)), C.c_void_p(_p(scene.material_idx)),
+                                   C.c_void_p(_p(scene.luts)), C.c_void_p(_p(v)), C.c_void_p(_p(vb)),
+                                   C.c_uint32(mode), C.c_void_p(_p(out)))
+    return out

@@ -146,7 +146,8 @@ EXPORTS = [
     "tgx_cache_create", "tgx_cache_destroy", "tgx_cache_infer", "tgx_cache_train_step", "tgx_cache_last_loss",
     "tgx_cache_gradient", "tgx_cache_get_weights", "tgx_cache_set_weights", "tgx_cache_save", "tgx_cache_load",
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
-    "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags",
+    "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
+    "tgx_scene_counts", "tgx_scene_download", "tgx_shade",
 ]
 
 
@@ -173,6 +174,10 @@ def _load() -> C.CDLL:
         "tgx_pick": (i32, [vp, vp, u32, u32, u32, u32, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32), C.POINTER(i32)]),
         "tgx_svo_build": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
         "tgx_svo_build_flags": (i32, [vp, vp, vp, u32, u32, C.POINTER(vp)]),
+        "tgx_generate_scene_device": (i32, [vp, C.POINTER(GenParams), C.POINTER(vp)]),
+        "tgx_scene_counts": (i32, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
+        "tgx_scene_download": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "tgx_shade": (i32, [vp, vp, vp, vp, u32, vp]),
         "tgx_svo_destroy": (None, [vp, vp]),
         "tgx_svo_get_info": (i32, [vp, vp, C.POINTER(SvoInfo)]),
         "tgx_svo_download": (i32, [vp, vp, vp, vp, u32, C.POINTER(u32)]),
@@ -270,17 +275,22 @@ class HostScene:
         return d
 
 
-def generate_scene(kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, *,
-                   bernoulli_p: float = 0.3, noise_period: float = 64.0, noise_threshold: float = 0.5,
-                   box_min=(0.0, 0.0, 0.0), box_max=(0.0, 0.0, 0.0), translation=(0.0, 0.0, 0.0),
-                   n_luts: int = 1, threads: int = 0) -> HostScene:
-    """Seeded synthetic scene (tgx_generate_scene); arrays are copied into numpy."""
+def gen_params(kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, *,
+               bernoulli_p: float = 0.3, noise_period: float = 64.0, noise_threshold: float = 0.5,
+               box_min=(0.0, 0.0, 0.0), box_max=(0.0, 0.0, 0.0), translation=(0.0, 0.0, 0.0),
+               n_luts: int = 1, threads: int = 0) -> GenParams:
     p = GenParams(kind=kind, n_objects=n_objects, min_clusters_per_axis=min_cpa, max_clusters_per_axis=max_cpa,
                   bernoulli_p=bernoulli_p, noise_period=noise_period, noise_threshold=noise_threshold, seed=seed,
                   n_luts=n_luts, threads=threads)
     p.box_min[:] = box_min
     p.box_max[:] = box_max
     p.fixed_translation[:] = translation
+    return p
+
+
+def generate_scene(kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, **kw) -> HostScene:
+    """Seeded synthetic scene (tgx_generate_scene); arrays are copied into numpy."""
+    p = gen_params(kind, n_objects, min_cpa, max_cpa, seed, **kw)
     g = GenScene()
     check(lib.tgx_generate_scene(C.byref(p), C.byref(g)), "tgx_generate_scene")
     try:
@@ -397,6 +407,18 @@ class Context:
         ptrs = (C.c_void_p * len(views))(*[_ptr(o) for o in outs])
         check(lib.tgx_vis_render_host(self.handle, scene.handle, _ptr(views), len(views), ptrs),
               "tgx_vis_render_host")
+
+    def generate_scene(self, kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, **kw) -> "Scene":
+        """The generate_scene scene built in device memory (tgx_generate_scene_device)."""
+        p = gen_params(kind, n_objects, min_cpa, max_cpa, seed, **kw)
+        h = C.c_void_p()
+        check(lib.tgx_generate_scene_device(self.handle, C.byref(p), C.byref(h)), "tgx_generate_scene_device")
+        return Scene(self, h)
+
+    def shade(self, scene: "Scene", view: np.ndarray, visbuf, mode: int, rgba) -> None:
+        """tgx_shade: device visbuf (W*H u64) -> device rgba (W*H*4 float32)."""
+        view = np.ascontiguousarray(view, dtype=VIEW_DTYPE).reshape(1)
+        check(lib.tgx_shade(self.handle, scene.handle, _ptr(view), _ptr(visbuf), mode, _ptr(rgba)), "tgx_shade")
 
     def frame_graph(self, jobs) -> "FrameGraph":
         """Captures a batched frame: `jobs` is a list of (scene, views, outs) with device
@@ -580,6 +602,21 @@ class Scene:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self.handle = handle
+
+    def download(self) -> HostScene:
+        """The scene's arrays back in host memory (tgx_scene_download)."""
+        n = [C.c_uint32() for _ in range(4)]
+        check(lib.tgx_scene_counts(self.handle, *[C.byref(x) for x in n]), "tgx_scene_counts")
+        n_obj, n_cp, n_cl, n_lut = (x.value for x in n)
+        objs = np.zeros(n_obj, OBJECT_DTYPE)
+        cp = np.zeros(n_cp, np.uint32)
+        c2o = np.zeros(n_cl, np.uint32)
+        bits = np.zeros((n_cl, 16), np.uint32)
+        mat = np.zeros(n_cl * 512, np.uint8)
+        luts = np.zeros(n_lut * 256, MATERIAL_DTYPE)
+        check(lib.tgx_scene_download(self.ctx.handle, self.handle, _ptr(objs), _ptr(cp), _ptr(c2o), _ptr(bits),
+                                     _ptr(mat), _ptr(luts) if n_lut else None), "tgx_scene_download")
+        return HostScene(objs, cp, c2o, bits, mat, luts if n_lut else None)
 
     def close(self) -> None:
         if self.handle and self.ctx.handle:

@@ -33,6 +33,7 @@
 //
 // Results equal the oracle's bit for bit.
 
+#include "primary.cuh"
 #include "svo_trace.cuh"
 
 #include <algorithm>
@@ -164,80 +165,17 @@ __device__ bool primary_hit(const tgx_object* __restrict__ objects, const uint32
                             const tgx_material* __restrict__ luts, const tgx_view& cam, const GiParams& p,
                             unsigned long long word, uint32_t px, uint32_t py, float o2[3], float nw[3], float a[3])
 {
-    const float fx = xdiv(xadd((float)px, 0.5f), (float)cam.width);
-    const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)cam.height));
-    const float depth = xdiv((float)(word >> 40), 16777215.0f);
-    if (!(depth < 1.0f)) return false;
-    const uint32_t ptr = (uint32_t)(word >> 9) & 2147483647u;
-    const uint32_t voxel = (uint32_t)word & 511u;
-    const uint32_t ci = cluster_pointers[ptr];
-    const tgx_object& od = objects[c2o[ci]];
-    const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
-    const uint32_t rel = ptr - od.first_cluster_pointer;
-    const float offx = (float)((rel % nx) * 8u), offy = (float)(((rel / nx) % ny) * 8u), offz = (float)((rel / (nx * ny)) * 8u);
-    const float half = xmul(8.0f, 0.5f);
-    float rot[16], m0[16], m1[16], m2[16], m3[16], ws2ms[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
-    dm4_translate(-od.translation[0], -od.translation[1], -od.translation[2], m0);
-    dm4_inverse(rot, m1);
-    dm4_translate(xmul(half, (float)od.n_cluster_pointers_per_dim[0]), xmul(half, (float)od.n_cluster_pointers_per_dim[1]),
-                  xmul(half, (float)od.n_cluster_pointers_per_dim[2]), m2);
-    dm4_translate(-offx, -offy, -offz, m3);
-    dm4_mul(m3, m2, ws2ms);
-    dm4_mul(ws2ms, m1, ws2ms);
-    dm4_mul(ws2ms, m0, ws2ms);
-    float o4[3];
-    dm4_mulv4(ws2ms, cam.camera[0], cam.camera[1], cam.camera[2], 1.0f, o4);
-    float dws[3];
+    PrimarySurface ps;
+    if (!primary_surface(objects, cluster_pointers, c2o, material, luts, cam, word, px, py, ps)) return false;
+    // no voxel-box hit in cluster space: face the camera
+    const bool none = ps.nw[0] == 0.0f && ps.nw[1] == 0.0f && ps.nw[2] == 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const float aa = xadd(xmul(cam.ray_bl[i], xsub(1.0f, fy)), xmul(cam.ray_tl[i], fy));
-        const float bb = xadd(xmul(cam.ray_br[i], xsub(1.0f, fy)), xmul(cam.ray_tr[i], fy));
-        dws[i] = xadd(xmul(aa, xsub(1.0f, fx)), xmul(bb, fx));
-    }
-    float d4[3];
-    dm4_mulv4(ws2ms, dws[0], dws[1], dws[2], 0.0f, d4);
-    const float mag = xsqrt(xadd(xadd(xmul(d4[0], d4[0]), xmul(d4[1], d4[1])), xmul(d4[2], d4[2])));
-    const float dm[3] = {xdiv(d4[0], mag), xdiv(d4[1], mag), xdiv(d4[2], mag)};
-    const float vmin[3] = {(float)(voxel % 8u), (float)((voxel / 8u) % 8u), (float)(voxel / 64u)};
-    float enter, exit_;
-    nw[0] = nw[1] = nw[2] = 0.0f;
-    const bool hit = ray_aabb(o4[0], o4[1], o4[2], dm[0], dm[1], dm[2], vmin[0], vmin[1], vmin[2], xadd(vmin[0], 1.0f),
-                              xadd(vmin[1], 1.0f), xadd(vmin[2], 1.0f), enter, exit_);
-    if (hit) {
-        float nm[3];
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const float hm = enter > 0.0f ? xadd(o4[i], xmul(enter, dm[i])) : o4[i];
-            nm[i] = xsub(hm, xadd(vmin[i], 0.5f));
-        }
-        auto sgn = [](float v) { return v > 0.0f ? 1.0f : v < 0.0f ? -1.0f : 0.0f; };
-        if (fabsf(nm[0]) > fabsf(nm[1])) {
-            nm[1] = 0.0f;
-            if (fabsf(nm[0]) > fabsf(nm[2])) { nm[0] = sgn(nm[0]); nm[2] = 0.0f; }
-            else { nm[2] = sgn(nm[2]); nm[0] = 0.0f; }
-        } else {
-            nm[0] = 0.0f;
-            if (fabsf(nm[1]) > fabsf(nm[2])) { nm[1] = sgn(nm[1]); nm[2] = 0.0f; }
-            else { nm[2] = sgn(nm[2]); nm[1] = 0.0f; }
-        }
-        float r4[3];
-        dm4_mulv4(rot, nm[0], nm[1], nm[2], 0.0f, r4);
-        const float rl = xsqrt(xadd(xadd(xmul(r4[0], r4[0]), xmul(r4[1], r4[1])), xmul(r4[2], r4[2])));
-        if (rl > 0.0f) { nw[0] = xdiv(r4[0], rl); nw[1] = xdiv(r4[1], rl); nw[2] = xdiv(r4[2], rl); }
-    }
-    const float dl = xsqrt(xadd(xadd(xmul(dws[0], dws[0]), xmul(dws[1], dws[1])), xmul(dws[2], dws[2])));
-    const float dn[3] = {xdiv(dws[0], dl), xdiv(dws[1], dl), xdiv(dws[2], dl)};
-    if (nw[0] == 0.0f && nw[1] == 0.0f && nw[2] == 0.0f) { nw[0] = -dn[0]; nw[1] = -dn[1]; nw[2] = -dn[2]; }
-    const float te = hit && enter > 0.0f ? enter : 0.0f;
-    a[0] = a[1] = a[2] = 0.5f;
-    if (material && luts) {
-        const tgx_material& m = luts[od.lut_idx * 256u + material[(uint64_t)ci * 512u + voxel]];
-        a[0] = m.albedo[0]; a[1] = m.albedo[1]; a[2] = m.albedo[2];
+        nw[i] = none ? -ps.dn[i] : ps.nw[i];
+        a[i] = ps.albedo[i];
     }
 #pragma unroll
-    for (int i = 0; i < 3; i++) o2[i] = xadd(xadd(cam.camera[i], xmul(te, dn[i])), xmul(nw[i], p.offset));
+    for (int i = 0; i < 3; i++) o2[i] = xadd(xadd(cam.camera[i], xmul(ps.te, ps.dn[i])), xmul(nw[i], p.offset));
     return true;
 }
 

@@ -105,22 +105,17 @@ void tgx_free_generated_scene(tgx_gen_scene* s)
     memset(s, 0, sizeof(*s));
 }
 
-tgx_status tgx_generate_scene(const tgx_gen_params* p, tgx_gen_scene* out)
+/* Object records of a generated scene (dims, first pointer, translation, LUT,
+ * rotation); returns the cluster count, or 0 when it would reach 2^31. */
+uint64_t tgx__gen_objects(const tgx_gen_params* p, tgx_object* objects)
 {
-    if (!p || !out || p->n_objects == 0 || p->min_clusters_per_axis == 0 ||
-        p->max_clusters_per_axis < p->min_clusters_per_axis || p->kind > 1)
-        return TGX_ERR_INVALID_ARGUMENT;
-    memset(out, 0, sizeof(*out));
     const uint32_t n_obj = p->n_objects;
     const uint32_t span = p->max_clusters_per_axis - p->min_clusters_per_axis + 1;
     const uint32_t n_luts = p->n_luts ? p->n_luts : 1;
-
-    out->objects = (tgx_object*)calloc(n_obj, sizeof(tgx_object));
-    if (!out->objects) return TGX_ERR_OUT_OF_MEMORY;
     uint64_t total = 0;
     for (uint32_t i = 0; i < n_obj; i++)
     {
-        tgx_object* o = &out->objects[i];
+        tgx_object* o = &objects[i];
         for (int a = 0; a < 3; a++)
             o->n_cluster_pointers_per_dim[a] = p->min_clusters_per_axis + (uint32_t)(hash3(p->seed, ST_DIMS, 3ull * i + a) % span);
         o->first_cluster_pointer = (uint32_t)total;
@@ -138,7 +133,33 @@ tgx_status tgx_generate_scene(const tgx_gen_params* p, tgx_gen_scene* out)
         o->lut_idx = (uint32_t)(hash3(p->seed, ST_OBJLUT, i) % n_luts);
         random_rotation(p->seed, i, o->rotation);
     }
-    if (total >= (1ull << 31)) { tgx_free_generated_scene(out); return TGX_ERR_CAPACITY; }
+    return total >= (1ull << 31) ? 0 : total;
+}
+
+/* LUT entries: albedo U[0.05, 0.95], roughness U[0.1, 1.0] */
+void tgx__gen_luts(const tgx_gen_params* p, tgx_material* luts)
+{
+    const uint32_t n_luts = p->n_luts ? p->n_luts : 1;
+    for (uint32_t l = 0; l < n_luts * 256; l++)
+    {
+        for (int a = 0; a < 3; a++) luts[l].albedo[a] = 0.05f + 0.9f * unit_f32(hash3(p->seed, ST_LUT, 4ull * l + a));
+        luts[l].roughness = 0.1f + 0.9f * unit_f32(hash3(p->seed, ST_LUT, 4ull * l + 3));
+    }
+}
+
+tgx_status tgx_generate_scene(const tgx_gen_params* p, tgx_gen_scene* out)
+{
+    if (!p || !out || p->n_objects == 0 || p->min_clusters_per_axis == 0 ||
+        p->max_clusters_per_axis < p->min_clusters_per_axis || p->kind > 1)
+        return TGX_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    const uint32_t n_obj = p->n_objects;
+    const uint32_t n_luts = p->n_luts ? p->n_luts : 1;
+
+    out->objects = (tgx_object*)calloc(n_obj, sizeof(tgx_object));
+    if (!out->objects) return TGX_ERR_OUT_OF_MEMORY;
+    const uint64_t total = tgx__gen_objects(p, out->objects);
+    if (total == 0) { tgx_free_generated_scene(out); return TGX_ERR_CAPACITY; }
     const uint32_t n_clusters = (uint32_t)total;
 
     out->cluster_pointers = (uint32_t*)malloc((size_t)n_clusters * 4);
@@ -201,11 +222,7 @@ tgx_status tgx_generate_scene(const tgx_gen_params* p, tgx_gen_scene* out)
             mat[v] = (uint8_t)(hash3(p->seed, ST_MAT, gvi) & 255u);
         }
     }
-    for (uint32_t l = 0; l < n_luts * 256; l++)
-    {
-        for (int a = 0; a < 3; a++) out->luts[l].albedo[a] = 0.05f + 0.9f * unit_f32(hash3(p->seed, ST_LUT, 4ull * l + a));
-        out->luts[l].roughness = 0.1f + 0.9f * unit_f32(hash3(p->seed, ST_LUT, 4ull * l + 3));
-    }
+    tgx__gen_luts(p, out->luts);
 
     tgx_scene_desc* d = &out->desc;
     d->n_objects = n_obj;

@@ -281,7 +281,7 @@ __global__ void k_object_setup(const tgx_object* __restrict__ objs, uint32_t n, 
         for (int c = 0; c < 3; c++) inv_rot[9 * i + 3 * r + c] = DM(inv, r, c);
 }
 
-static void scene_free(tgx_scene* s)
+void scene_release(tgx_scene* s)
 {
     if (!s) return;
     cudaFree(s->d_objects);
@@ -292,6 +292,23 @@ static void scene_free(tgx_scene* s)
     cudaFree(s->d_material);
     cudaFree(s->d_luts);
     delete s;
+}
+static void scene_free(tgx_scene* s) { scene_release(s); }
+
+// per-object inverse rotations of a scene whose arrays are on the device; synchronous
+tgx_status scene_finish(tgx_ctx* c, tgx_scene* s)
+{
+    trace_begin(c, TR_OBJECT_SETUP);
+    k_object_setup<<<(s->n_objects + 127) / 128, 128, 0, c->stream>>>(s->d_objects, s->n_objects, s->d_inv_rot);
+    cudaError_t le = cudaGetLastError();
+    trace_end(c, TR_OBJECT_SETUP);
+    if (le == cudaSuccess) c->launches++;
+    if (le == cudaSuccess) le = cudaStreamSynchronize(c->stream);
+    if (le != cudaSuccess) {
+        tgx_set_error("scene setup: %s", cudaGetErrorString(le));
+        return TGX_ERR_CUDA;
+    }
+    return TGX_OK;
 }
 
 extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_scene** out)
@@ -350,16 +367,10 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
         scene_free(s);
         return e == cudaErrorMemoryAllocation ? TGX_ERR_OUT_OF_MEMORY : TGX_ERR_CUDA;
     }
-    trace_begin(c, TR_OBJECT_SETUP);
-    k_object_setup<<<(d->n_objects + 127) / 128, 128, 0, c->stream>>>(s->d_objects, d->n_objects, s->d_inv_rot);
-    cudaError_t le = cudaGetLastError();
-    trace_end(c, TR_OBJECT_SETUP);
-    if (le == cudaSuccess) c->launches++;
-    if (le == cudaSuccess) le = cudaStreamSynchronize(c->stream);
-    if (le != cudaSuccess) {
-        tgx_set_error("tgx_scene_upload: %s", cudaGetErrorString(le));
+    const tgx_status st = scene_finish(c, s);
+    if (st != TGX_OK) {
         scene_free(s);
-        return TGX_ERR_CUDA;
+        return st;
     }
     *out = s;
     return TGX_OK;

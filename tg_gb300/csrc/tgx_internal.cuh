@@ -129,6 +129,7 @@ struct tgx_ctx
     DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
     DevBuf gi_scratch;     // learned-cache GI queries, hits, training batch
     uint32_t vis_last_tiles = 0;
+    uint64_t vis_last_pairs = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters
     cudaEvent_t vis_done = nullptr;    // recorded after that copy
     DevBuf host_stage;     // pinned host staging (views)

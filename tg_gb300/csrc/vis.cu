@@ -786,28 +786,34 @@ static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_of
     w.tile_order = w.tile_off + (n_tiles + 1);
 }
 
-// The launches of one frame (n_views views of scene s, view table d_vc / d_outs on the device).
+enum VisPhase { VIS_ALL = 0, VIS_TO_SCAN = 1, VIS_FROM_BINS = 2 };
+
+// The launches of one frame (n_views views of scene s, view table d_vc / d_outs
+// on the device): all of them, or the part up to the tile scan, or the rest.
 static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs,
-                             uint32_t n_views, uint32_t n_tiles, const VisScratch& w)
+                             uint32_t n_views, uint32_t n_tiles, const VisScratch& w, int phase = VIS_ALL)
 {
     const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
-    TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
-    TGX_CUDA(cudaMemsetAsync(w.bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
-    const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
-    TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
-               s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-               w.records, w.rects, w.rec_cap, w.counters, c->d_status);
     const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
-    TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, w.records, w.counters, w.rec_cap,
-               s->d_objects, d_vc);
-    TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, d_vc, w.bucket_cnt,
-               n_tiles);
-    TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off, w.tile_total,
-               n_tiles, w.cta_aux);
-    TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity, w.counters);
-    TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux, w.tile_off,
-               w.tile_order);
+    if (phase != VIS_FROM_BINS) {
+        TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
+        TGX_CUDA(cudaMemsetAsync(w.bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
+        const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
+        TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
+                   s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
+                   w.records, w.rects, w.rec_cap, w.counters, c->d_status);
+        TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, w.records, w.counters,
+                   w.rec_cap, s->d_objects, d_vc);
+        TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, d_vc, w.bucket_cnt,
+                   n_tiles);
+        TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off, w.tile_total,
+                   n_tiles, w.cta_aux);
+        TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity, w.counters);
+        TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux,
+                   w.tile_off, w.tile_order);
+    }
+    if (phase == VIS_TO_SCAN) return TGX_OK;
     TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
                w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
                n_tiles, w.bin_capacity, c->d_status);
@@ -865,22 +871,30 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
 
     // bin capacity: grown from earlier frames' totals (read back without waiting); a frame
     // that still overflows is rendered correctly by the tile kernel's record scan
+    // Bin capacity.  Grown from earlier frames' totals, read back without
+    // waiting.  A frame that could outgrow what is known (the first one, one
+    // with more tiles or (view, cluster) pairs than before, or the one after an
+    // overflow) is sized exactly instead: the host reads this frame's total
+    // after the tile scan, once.  A frame that still overflows is rendered
+    // correctly, but slowly, by the tile kernel's record scan.
+    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
+    if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
     VisScratch w;
+    bool exact = false;
     if (c->flags & TGX_FLAG_MIN_BIN_CAPACITY) {
         TGX_TRY(devbuf_reserve(c->vis_bins, 64 * 4));
         w.bin_capacity = 64;
     } else {
+        exact = c->vis_last_tiles == 0 || n_tiles > c->vis_last_tiles || n_pairs > c->vis_last_pairs;
         if (c->vis_done && cudaEventQuery(c->vis_done) == cudaSuccess) {
-            const uint32_t prev = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
-            if ((size_t)prev * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)prev * 2 * 4));
+            const uint32_t* hc = (const uint32_t*)c->h_vis_counters;
+            if (hc[C_OVERFLOW]) exact = true;
+            if ((size_t)hc[C_ENTRIES] * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)hc[C_ENTRIES] * 2 * 4));
         }
         cudaGetLastError();
         TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 64, (size_t)1 << 20) * 4));
         w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
     }
-
-    const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
-    if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
     w.rec_cap = (uint32_t)n_pairs;
     TGX_TRY(devbuf_reserve(c->vis_records, (size_t)w.rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
     TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
@@ -891,8 +905,23 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     w.counters = (uint32_t*)c->vis_counters.ptr;
     w.bins = (uint32_t*)c->vis_bins.ptr;
     vis_carve_tiles(w, (uint32_t*)c->vis_tile_cnt.ptr, (uint32_t*)c->vis_tile_off.ptr, n_tiles);
-    TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w));
+    if (!exact) {
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w));
+    } else {
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_TO_SCAN));
+        TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, w.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+        TGX_CUDA(cudaStreamSynchronize(c->stream));
+        const uint32_t entries = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
+        if (entries > w.bin_capacity) {
+            TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)entries * 4));
+            w.bins = (uint32_t*)c->vis_bins.ptr;
+            w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
+            if (entries <= w.bin_capacity) TGX_CUDA(cudaMemsetAsync(w.counters + C_OVERFLOW, 0, 4, c->stream));
+        }
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_FROM_BINS));
+    }
     c->vis_last_tiles = n_tiles;
+    c->vis_last_pairs = n_pairs;
     // counters of this frame to pinned memory, read by the next call without waiting
     TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, w.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
     if (!c->vis_done) TGX_CUDA(cudaEventCreateWithFlags(&c->vis_done, cudaEventDisableTiming));
