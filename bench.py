@@ -606,6 +606,22 @@ def main() -> None:
             if _ < 2:
                 svo.close()
         info = svo.info()
+        # incremental update after 8 objects move (tgx_scene_set_objects + tgx_svo_update),
+        # against the full builds above; the scene is moved back (untimed) for the GI frames
+        rng = np.random.default_rng(7)
+        objs = scene.objects.copy()
+        update_ms = []
+        for _ in range(3):
+            idx = rng.choice(len(objs), 8, replace=False)
+            objs["translation"][idx] += rng.uniform(-40.0, 40.0, (8, 3)).astype(np.float32)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sc.set_objects(0, objs)
+            n_moved = svo.update(sc)
+            ctx.sync()
+            update_ms.append((time.perf_counter() - t0) * 1e3)
+        sc.set_objects(0, scene.objects)
+        svo.update(sc)
         params = tg.gi_params(spp=4, bounces=1, seed=2, max_steps=256)
         rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
         with torch.cuda.stream(stream):
@@ -624,6 +640,9 @@ def main() -> None:
         err = ctx.device_error()
         gi_report = {
             "svo_build_ms": statistics.median(build_ms),
+            "svo_update_ms": statistics.median(update_ms),
+            "svo_update": f"{n_moved} of {len(objs)} objects moved by up to 40 voxels per axis; host wall time "
+                          "of tgx_scene_set_objects + tgx_svo_update",
             "svo": {"extent": 4096, "blocks": int(info.n_blocks), "nonempty_blocks": int(info.n_nonempty_blocks),
                     "pairs": int(info.n_pairs), "device_mb": round(info.device_bytes / 2**20, 1)},
             "gi_plain_frame_ms": gi_ms,

@@ -331,6 +331,22 @@ tgx_status  tgx_svo_build_flags(tgx_ctx* ctx, const tgx_scene* scene, const floa
                                 uint32_t flags, tgx_svo** out_svo);
 void        tgx_svo_destroy(tgx_ctx* ctx, tgx_svo* svo);
 
+/*
+ * Brings an SVO up to date with the scene's current object records after
+ * tgx_scene_set_objects moved objects -- the incremental insert the reference
+ * intends but leaves commented out (tg_svo_insert_object,
+ * tgvk_raytracer.c:982-989; README.md:48).  Objects whose record differs from
+ * the one the SVO last saw are "moved"; every 32^3 block one of their
+ * non-empty clusters could touch before or after the move is cleared and
+ * rebuilt from all clusters, so the voxel set, materials, block counts and
+ * pyramid equal those of a fresh tgx_svo_build of the moved scene.  Blocks
+ * that end up empty return their slots to a free list the next update reuses;
+ * the pool grows (blocking) when it runs out.  `scene` must have the object and
+ * cluster-pointer counts of the build.  Blocks the host once for the counts.
+ * *out_n_moved (may be NULL) receives the number of moved objects.
+ */
+tgx_status  tgx_svo_update(tgx_ctx* ctx, tgx_svo* svo, const tgx_scene* scene, uint32_t* out_n_moved);
+
 typedef struct tgx_svo_info
 {
     float    min[3];
@@ -338,7 +354,7 @@ typedef struct tgx_svo_info
     uint32_t blocks_per_axis;     /* 2^(extent_log2-5) */
     uint32_t n_blocks;            /* allocated 32^3 blocks (candidates) */
     uint32_t n_nonempty_blocks;   /* blocks with at least one voxel set */
-    uint32_t n_pairs;             /* (cluster, block) voxelisation pairs */
+    uint32_t n_pairs;             /* (cluster, block) pairs the last build or update voxelised */
     uint64_t device_bytes;        /* table + pool + pyramid */
 } tgx_svo_info;
 
@@ -493,6 +509,16 @@ tgx_status  tgx_generate_scene_device(tgx_ctx* ctx, const tgx_gen_params* params
 /* Sizes of a scene's arrays (any argument may be NULL). */
 tgx_status  tgx_scene_counts(const tgx_scene* scene, uint32_t* n_objects, uint32_t* n_cluster_pointers,
                              uint32_t* n_clusters, uint32_t* n_luts);
+/*
+ * Replaces the records of objects first .. first+n-1 with HOST records that
+ * keep each object's cluster layout (first_cluster_pointer and
+ * n_cluster_pointers_per_dim) and change its pose (translation, rotation) or
+ * LUT: the reference's per-frame object transform write.  Later visibility,
+ * shading and GI launches see the new poses; an SVO follows after
+ * tgx_svo_update.  Synchronous.
+ */
+tgx_status  tgx_scene_set_objects(tgx_ctx* ctx, tgx_scene* scene, uint32_t first, uint32_t n, const tgx_object* objects);
+
 /* Copies a scene's arrays back to HOST buffers sized by tgx_scene_counts (NULL skips an array). */
 tgx_status  tgx_scene_download(tgx_ctx* ctx, const tgx_scene* scene, tgx_object* objects, uint32_t* cluster_pointers,
                                uint32_t* cluster_idx_to_object_idx, uint32_t* voxel_bits, uint8_t* material_idx,

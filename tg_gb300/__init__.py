@@ -147,7 +147,7 @@ EXPORTS = [
     "tgx_cache_gradient", "tgx_cache_get_weights", "tgx_cache_set_weights", "tgx_cache_save", "tgx_cache_load",
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
-    "tgx_scene_counts", "tgx_scene_download", "tgx_shade",
+    "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
 ]
 
 
@@ -178,6 +178,8 @@ def _load() -> C.CDLL:
         "tgx_scene_counts": (i32, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
         "tgx_scene_download": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "tgx_shade": (i32, [vp, vp, vp, vp, u32, vp]),
+        "tgx_svo_update": (i32, [vp, vp, vp, C.POINTER(u32)]),
+        "tgx_scene_set_objects": (i32, [vp, vp, u32, u32, vp]),
         "tgx_svo_destroy": (None, [vp, vp]),
         "tgx_svo_get_info": (i32, [vp, vp, C.POINTER(SvoInfo)]),
         "tgx_svo_download": (i32, [vp, vp, vp, vp, u32, C.POINTER(u32)]),
@@ -524,6 +526,12 @@ class Svo:
               "tgx_svo_download")
         return xyz, words
 
+    def update(self, scene: "Scene") -> int:
+        """tgx_svo_update: follow the scene's moved objects; returns how many moved."""
+        n = C.c_uint32()
+        check(lib.tgx_svo_update(self.ctx.handle, self.handle, scene.handle, C.byref(n)), "tgx_svo_update")
+        return n.value
+
     def trace(self, origins, dirs, t_out, voxel_out, max_steps: int = 4096) -> None:
         """Device arrays: origins/dirs float32[n,3], t_out float32[n], voxel_out int32[n,3]."""
         n = origins.shape[0]
@@ -617,6 +625,12 @@ class Scene:
         check(lib.tgx_scene_download(self.ctx.handle, self.handle, _ptr(objs), _ptr(cp), _ptr(c2o), _ptr(bits),
                                      _ptr(mat), _ptr(luts) if n_lut else None), "tgx_scene_download")
         return HostScene(objs, cp, c2o, bits, mat, luts if n_lut else None)
+
+    def set_objects(self, first: int, objects) -> None:
+        """tgx_scene_set_objects: new poses (or LUTs) for objects first .. first+len-1 (OBJECT_DTYPE records)."""
+        objs = np.ascontiguousarray(objects, OBJECT_DTYPE)
+        check(lib.tgx_scene_set_objects(self.ctx.handle, self.handle, first, objs.shape[0], _ptr(objs)),
+              "tgx_scene_set_objects")
 
     def close(self) -> None:
         if self.handle and self.ctx.handle:

@@ -198,3 +198,32 @@ extern "C" tgx_status tgx_scene_download(tgx_ctx* c, const tgx_scene* s, tgx_obj
     TGX_CUDA(cudaStreamSynchronize(c->stream));
     return TGX_OK;
 }
+
+extern "C" tgx_status tgx_scene_set_objects(tgx_ctx* c, tgx_scene* s, uint32_t first, uint32_t n, const tgx_object* objects)
+{
+    if (!c || !s || (n && !objects)) { tgx_set_error("tgx_scene_set_objects: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    if ((uint64_t)first + n > s->n_objects) {
+        tgx_set_error("tgx_scene_set_objects: objects %u..%u outside the scene's %u", first, first + n, s->n_objects);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return TGX_OK;
+    TGX_CUDA(cudaSetDevice(c->device));
+    std::vector<tgx_object> cur(n);
+    TGX_CUDA(cudaMemcpyAsync(cur.data(), s->d_objects + first, (size_t)n * sizeof(tgx_object), cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    for (uint32_t i = 0; i < n; i++) {
+        const tgx_object &o = objects[i], &w = cur[i];
+        if (o.first_cluster_pointer != w.first_cluster_pointer || o.n_cluster_pointers_per_dim[0] != w.n_cluster_pointers_per_dim[0] ||
+            o.n_cluster_pointers_per_dim[1] != w.n_cluster_pointers_per_dim[1] ||
+            o.n_cluster_pointers_per_dim[2] != w.n_cluster_pointers_per_dim[2]) {
+            tgx_set_error("tgx_scene_set_objects: object %u changes its cluster layout", first + i);
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+        if (s->d_luts && o.lut_idx >= s->n_luts) {
+            tgx_set_error("tgx_scene_set_objects: object %u lut_idx out of range", first + i);
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+    }
+    TGX_CUDA(cudaMemcpyAsync(s->d_objects + first, objects, (size_t)n * sizeof(tgx_object), cudaMemcpyHostToDevice, c->stream));
+    return scene_finish(c, s);
+}

@@ -44,7 +44,7 @@ struct SvoPair
     uint32_t block;
 };
 
-enum SvoCounter { S_PAIRS = 0, S_MARKED = 1, S_SLOTS = 2, S_NONEMPTY = 3, S_COUNT = 4 };
+enum SvoCounter { S_PAIRS = 0, S_MARKED = 1, S_SLOTS = 2, S_NONEMPTY = 3, S_FREED = 4, S_MOVED = 5, S_COUNT = 8 };
 
 struct dv3 { float x, y, z; };
 
@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(128) k_svo_candidates(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
     const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp, float mnx, float mny,
     float mnz, uint32_t L, uint32_t B, uint32_t* __restrict__ table, SvoPair* __restrict__ pairs,
-    uint32_t pair_capacity, uint32_t* __restrict__ counters, tgx_dev_status* __restrict__ status)
+    uint32_t pair_capacity, uint32_t* __restrict__ counters, tgx_dev_status* __restrict__ status,
+    const uint8_t* __restrict__ dirty /* null: every block; else only blocks marked dirty */)
 {
     const uint32_t cp = blockIdx.x * blockDim.x + threadIdx.x;
     if (cp >= n_cp) return;
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(128) k_svo_candidates(
     for (int bz = b0[2]; bz <= b1[2]; bz++)
         for (int by = b0[1]; by <= b1[1]; by++)
             for (int bx = b0[0]; bx <= b1[0]; bx++) {
+                if (dirty && !dirty[((uint32_t)bz * B + (uint32_t)by) * B + (uint32_t)bx]) continue;
                 // walk the reference's recursion from the root to this block
                 dv3 pmin = dv3{mnx, mny, mnz};
                 dv3 pmax = dv3{xadd(mnx, ext), xadd(mny, ext), xadd(mnz, ext)};
@@ -255,15 +257,19 @@ __global__ void __launch_bounds__(128) k_svo_candidates(
 // 2. slot allocation
 // ---------------------------------------------------------------------------
 
+// Marked blocks take slots from the end of the free list first (free[n_free-1],
+// free[n_free-2], ...), then fresh slots from `next_slot` on.
 __global__ void __launch_bounds__(256) k_svo_alloc(uint32_t* __restrict__ table, uint64_t n_table,
-                                                  uint32_t* __restrict__ counters, uint32_t pool_blocks,
+                                                  uint32_t* __restrict__ counters, const uint32_t* __restrict__ free_list,
+                                                  uint32_t n_free, uint32_t next_slot, uint32_t pool_blocks,
                                                   tgx_dev_status* __restrict__ status)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_table;
          i += (uint64_t)gridDim.x * blockDim.x) {
         if (table[i] == kMark) {
             const uint32_t s = atomicAdd(&counters[S_SLOTS], 1u);
-            if (s < pool_blocks) table[i] = s + 1u;
+            const uint32_t slot = s < n_free ? free_list[n_free - 1u - s] : next_slot + (s - n_free);
+            if (slot < pool_blocks) table[i] = slot + 1u;
             else { table[i] = 0u; dev_error(status, TGX_ERR_CAPACITY, 12, s); }
         }
     }
@@ -473,6 +479,120 @@ __global__ void __launch_bounds__(256) k_svo_pyramid(const uint32_t* __restrict_
     }
 }
 
+// ---------------------------------------------------------------------------
+// incremental update: blocks a moved object covered before or covers now
+// ---------------------------------------------------------------------------
+
+// Conservative world box of every non-empty cluster of one object -- the box
+// k_svo_candidates selects blocks with -- marked into the dirty-block map.
+__device__ void mark_object_blocks(const tgx_object& od, const uint32_t* __restrict__ cluster_pointers,
+                                   const uint32_t* __restrict__ bits, const float mn[3], uint32_t B,
+                                   uint8_t* __restrict__ dirty)
+{
+    const uint32_t n = od.n_cluster_pointers_per_dim[0] * od.n_cluster_pointers_per_dim[1] * od.n_cluster_pointers_per_dim[2];
+    for (uint32_t rel = threadIdx.x; rel < n; rel += blockDim.x) {
+        const uint32_t ci = cluster_pointers[od.first_cluster_pointer + rel];
+        const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
+        const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
+        if (!(a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w)) continue;
+        float off[3], ohe[3];
+        cluster_offsets(od, rel, off, ohe);
+        float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float lx = off[0] + ((k & 1) ? 8.0f : 0.0f) - ohe[0];
+            const float ly = off[1] + ((k & 2) ? 8.0f : 0.0f) - ohe[1];
+            const float lz = off[2] + ((k & 4) ? 8.0f : 0.0f) - ohe[2];
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                const float p = DM(od.rotation, r, 0) * lx + DM(od.rotation, r, 1) * ly + DM(od.rotation, r, 2) * lz +
+                                od.translation[r];
+                lo[r] = fminf(lo[r], p);
+                hi[r] = fmaxf(hi[r], p);
+            }
+        }
+        int b0[3], b1[3];
+        bool empty = false;
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const float slack = 0.5f + 1e-5f * fabsf(lo[r]) + 1e-5f * fabsf(hi[r]);
+            b0[r] = max((int)floorf((lo[r] - slack - mn[r]) / 32.0f), 0);
+            b1[r] = min((int)floorf((hi[r] + slack - mn[r]) / 32.0f), (int)B - 1);
+            empty |= b0[r] > b1[r];
+        }
+        if (empty) continue;
+        for (int bz = b0[2]; bz <= b1[2]; bz++)
+            for (int by = b0[1]; by <= b1[1]; by++)
+                for (int bx = b0[0]; bx <= b1[0]; bx++) dirty[((uint32_t)bz * B + (uint32_t)by) * B + (uint32_t)bx] = 1;
+    }
+}
+
+// One CTA per object: when the scene's record differs from the one the SVO
+// was built from, the blocks its clusters touched before (old record) and
+// touch now (new record) become dirty, and the stored record is replaced.
+__global__ void __launch_bounds__(128) k_svo_mark_dirty(const tgx_object* __restrict__ cur, tgx_object* __restrict__ built,
+                                                       const uint32_t* __restrict__ cluster_pointers,
+                                                       const uint32_t* __restrict__ bits, float mnx, float mny,
+                                                       float mnz, uint32_t B, uint8_t* __restrict__ dirty,
+                                                       uint32_t* __restrict__ counters)
+{
+    const tgx_object now = cur[blockIdx.x], was = built[blockIdx.x];
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(&now);
+    const uint32_t* b = reinterpret_cast<const uint32_t*>(&was);
+    bool same = true;
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(tgx_object) / 4); k++) same &= a[k] == b[k];
+    if (same) return;
+    const float mn[3] = {mnx, mny, mnz};
+    mark_object_blocks(was, cluster_pointers, bits, mn, B, dirty);
+    mark_object_blocks(now, cluster_pointers, bits, mn, B, dirty);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        built[blockIdx.x] = now;
+        atomicAdd(&counters[S_MOVED], 1u);
+    }
+}
+
+// One warp per dirty block that holds a slot: its voxel bits, sub-block masks,
+// non-empty flag and materials are zeroed, the table entry is emptied and the
+// slot goes on the free list.  k_svo_candidates re-marks the block if any
+// cluster still reaches it.
+__global__ void __launch_bounds__(256) k_svo_release_dirty(uint32_t* __restrict__ table, uint64_t n_table,
+                                                          const uint8_t* __restrict__ dirty, uint32_t* __restrict__ pool,
+                                                          uint32_t* __restrict__ sub, uint32_t* __restrict__ nonempty,
+                                                          uint16_t* __restrict__ mat, uint32_t* __restrict__ free_tail,
+                                                          uint32_t* __restrict__ counters)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = warp; i < n_table; i += n_warps) {
+        if (!dirty[i]) continue;
+        const uint32_t tv = table[i];
+        if (tv == 0u) continue;
+        const uint32_t slot = tv - 1u;
+        uint4* blk = reinterpret_cast<uint4*>(pool + (uint64_t)slot * kBlockWords);
+        for (uint32_t k = lane; k < kBlockWords / 4u; k += 32) blk[k] = make_uint4(0u, 0u, 0u, 0u);
+        sub[(uint64_t)slot * 32u + lane] = 0u;
+        if (mat) {
+            uint4* m = reinterpret_cast<uint4*>(mat + (uint64_t)slot * 32768u);
+            for (uint32_t k = lane; k < 32768u / 8u; k += 32) m[k] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        if (lane == 0) {
+            nonempty[slot] = 0u;
+            table[i] = 0u;
+            free_tail[atomicAdd(&counters[S_FREED], 1u)] = slot;
+        }
+    }
+}
+
+// Table entries still marked after an overflowed candidate pass go back to empty.
+__global__ void __launch_bounds__(256) k_svo_unmark(uint32_t* __restrict__ table, uint64_t n_table)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_table; i += (uint64_t)gridDim.x * blockDim.x)
+        if (table[i] == kMark) table[i] = 0u;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -488,7 +608,104 @@ static void svo_free(tgx_svo* s)
     cudaFree(s->d_occ);
     cudaFree(s->d_nonempty);
     cudaFree(s->d_mat);
+    cudaFree(s->d_free);
+    cudaFree(s->d_counters);
+    cudaFree(s->d_objs);
     delete s;
+}
+
+static uint64_t svo_device_bytes(const tgx_svo* s)
+{
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    return n_table * 4 + (uint64_t)s->pool_cap * (kBlockWords * 4 + 128 + 4 + 4 + (s->d_mat ? 65536 : 0)) +
+           s->occ_words * 4 + (uint64_t)s->n_objects * sizeof(tgx_object);
+}
+
+// Per-slot arrays (pool, sub masks, non-empty flags, free list, materials)
+// sized for `cap` slots; the first `keep` slots are carried over, the rest
+// start zero.
+static tgx_status svo_resize_slots(tgx_ctx* c, tgx_svo* s, uint32_t cap, uint32_t keep, bool materials)
+{
+    struct Arr { void** p; uint64_t per_slot; };
+    void* mat = s->d_mat;
+    Arr arrs[5] = {{(void**)&s->d_pool, kBlockWords * 4}, {(void**)&s->d_sub, 128}, {(void**)&s->d_nonempty, 4},
+                   {(void**)&s->d_free, 4}, {&mat, 65536}};
+    const int n_arr = materials ? 5 : 4;
+    void* fresh[5] = {};
+    for (int a = 0; a < n_arr; a++)
+        if (cudaMalloc(&fresh[a], (uint64_t)cap * arrs[a].per_slot) != cudaSuccess) {
+            for (int k = 0; k < a; k++) cudaFree(fresh[k]);
+            cudaGetLastError();
+            tgx_set_error("tgx_svo: out of device memory for %u blocks", cap);
+            return TGX_ERR_OUT_OF_MEMORY;
+        }
+    for (int a = 0; a < n_arr; a++) {
+        const uint64_t kept = (uint64_t)keep * arrs[a].per_slot, total = (uint64_t)cap * arrs[a].per_slot;
+        if (kept) TGX_CUDA(cudaMemcpyAsync(fresh[a], *arrs[a].p, kept, cudaMemcpyDeviceToDevice, c->stream));
+        TGX_CUDA(cudaMemsetAsync((char*)fresh[a] + kept, 0, total - kept, c->stream));
+    }
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    for (int a = 0; a < n_arr; a++) {
+        cudaFree(*arrs[a].p);
+        *arrs[a].p = fresh[a];
+    }
+    s->d_mat = (uint16_t*)mat;
+    s->pool_cap = cap;
+    return TGX_OK;
+}
+
+// Candidate pass over every cluster pointer (only blocks marked in `dirty` when
+// it is given), with the pair storage grown to the exact count and the pass
+// rerun once when the first estimate was short.  Leaves the counters on the host.
+static tgx_status svo_candidates(tgx_ctx* c, tgx_svo* s, const tgx_scene* sc, const uint8_t* dirty, uint64_t cap)
+{
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    uint32_t* counters = s->d_counters;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        TGX_TRY(devbuf_reserve(c->svo_pairs, cap * sizeof(SvoPair)));
+        TGX_CUDA(cudaMemsetAsync(counters + S_PAIRS, 0, 2 * 4, c->stream));   // pairs, marks
+        if (sc->n_cluster_pointers)
+            TGX_LAUNCH(c, TR_SVO_CANDIDATES, (sc->n_cluster_pointers + 127) / 128, 128, 0, k_svo_candidates, sc->d_objects,
+                       sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, sc->n_cluster_pointers, s->mn[0], s->mn[1], s->mn[2],
+                       s->L, s->B, s->d_table, (SvoPair*)c->svo_pairs.ptr, (uint32_t)cap, counters, c->d_status, dirty);
+        if (cudaMemcpyAsync(c->h_counter, counters, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+            cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            tgx_set_error("tgx_svo: %s", cudaGetErrorString(cudaGetLastError()));
+            return TGX_ERR_CUDA;
+        }
+        const uint32_t n_pairs = ((uint32_t*)c->h_counter)[S_PAIRS];
+        if (n_pairs <= cap) return TGX_OK;
+        // the capacity error recorded by the first attempt is expected; clear it and the marks it left
+        TGX_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(tgx_dev_status), c->stream));
+        const uint32_t grid = (uint32_t)std::min<uint64_t>((n_table + 255) / 256, (uint64_t)c->num_sms * 32);
+        TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_unmark, s->d_table, n_table);
+        cap = (uint64_t)n_pairs + 1024;
+    }
+    tgx_set_error("tgx_svo: pair count grew between two identical passes");
+    return TGX_ERR_CAPACITY;
+}
+
+// Slots for the marked blocks, voxelisation of the pairs, and the occupancy
+// pyramid of the whole table (cleared first).
+static tgx_status svo_fill(tgx_ctx* c, tgx_svo* s, const tgx_scene* sc, uint32_t n_free, uint32_t next_slot)
+{
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    uint32_t* counters = s->d_counters;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((n_table + 255) / 256, (uint64_t)c->num_sms * 32);
+    TGX_CUDA(cudaMemsetAsync(counters + S_SLOTS, 0, 2 * 4, c->stream));   // slots, non-empty
+    TGX_CUDA(cudaMemsetAsync(s->d_occ, 0, s->occ_words * 4, c->stream));
+    TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_alloc, s->d_table, n_table, counters, s->d_free, n_free, next_slot,
+               s->pool_cap, c->d_status);
+    const uint32_t vgrid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((s->n_pairs + kWarpsPerVoxCta - 1) / kWarpsPerVoxCta,
+                                                                              (uint64_t)c->num_sms * 16));
+    TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects, sc->d_cluster_pointers,
+               sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
+               (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, s->d_mat ? sc->d_material : nullptr,
+               s->d_mat, s->mn[0], s->mn[1], s->mn[2], s->B);
+    const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
+    TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty, s->d_sub,
+               s->d_occ, (const uint64_t*)((char*)s->d_occ + svo_occ_off_bytes(s->occ_words)), s->n_levels, s->B, counters);
+    return TGX_OK;
 }
 
 extern "C" tgx_status tgx_svo_build(tgx_ctx* c, const tgx_scene* sc, const float* mn, uint32_t L, tgx_svo** out)
@@ -514,6 +731,8 @@ extern "C" tgx_status tgx_svo_build_flags(tgx_ctx* c, const tgx_scene* sc, const
     s->mn[0] = mn[0]; s->mn[1] = mn[1]; s->mn[2] = mn[2];
     s->L = L;
     s->B = 1u << (L - 5);
+    s->n_objects = sc->n_objects;
+    s->n_cluster_pointers = sc->n_cluster_pointers;
     const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
     s->n_levels = L - 5 + 1;
     uint64_t occ_words = 0;
@@ -525,83 +744,76 @@ extern "C" tgx_status tgx_svo_build_flags(tgx_ctx* c, const tgx_scene* sc, const
     s->occ_words = occ_words;
 
     auto fail = [&](tgx_status st) { cudaStreamSynchronize(c->stream); svo_free(s); return st; };
-    if (cudaMalloc(&s->d_table, n_table * 4) != cudaSuccess || cudaMalloc(&s->d_occ, occ_words * 4 + 128) != cudaSuccess) {
+    if (cudaMalloc(&s->d_table, n_table * 4) != cudaSuccess || cudaMalloc(&s->d_occ, occ_words * 4 + 128) != cudaSuccess ||
+        cudaMalloc(&s->d_counters, S_COUNT * 4) != cudaSuccess ||
+        cudaMalloc(&s->d_objs, std::max<uint64_t>(1, (uint64_t)sc->n_objects) * sizeof(tgx_object)) != cudaSuccess) {
+        cudaGetLastError();
         tgx_set_error("tgx_svo_build: out of device memory for the block table");
         return fail(TGX_ERR_OUT_OF_MEMORY);
     }
     if (cudaMemsetAsync(s->d_table, 0, n_table * 4, c->stream) != cudaSuccess ||
-        cudaMemsetAsync(s->d_occ, 0, occ_words * 4, c->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->d_counters, 0, S_COUNT * 4, c->stream) != cudaSuccess ||
+        (sc->n_objects && cudaMemcpyAsync(s->d_objs, sc->d_objects, (uint64_t)sc->n_objects * sizeof(tgx_object),
+                                          cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess) ||
         cudaMemcpyAsync((char*)s->d_occ + svo_occ_off_bytes(occ_words), s->occ_off, sizeof(s->occ_off), cudaMemcpyHostToDevice,
                         c->stream) != cudaSuccess) {
         tgx_set_error("tgx_svo_build: memset failed");
         return fail(TGX_ERR_CUDA);
     }
     tgx_status st;
-    if ((st = devbuf_reserve(c->svo_counters, S_COUNT * 4)) != TGX_OK) return fail(st);
-    uint32_t* counters = (uint32_t*)c->svo_counters.ptr;
-    cudaMemsetAsync(counters, 0, S_COUNT * 4, c->stream);
     // pair storage: start from a per-cluster estimate, retry once with the exact count
-    uint64_t cap = std::max<uint64_t>(1024, (uint64_t)sc->n_cluster_pointers * 4);
-    for (int attempt = 0; attempt < 2; attempt++) {
-        if ((st = devbuf_reserve(c->svo_pairs, cap * sizeof(SvoPair))) != TGX_OK) return fail(st);
-        cudaMemsetAsync(counters, 0, S_COUNT * 4, c->stream);
-        cudaMemsetAsync(s->d_table, 0, n_table * 4, c->stream);
-        auto launch = [&]() -> tgx_status {
-            TGX_LAUNCH(c, TR_SVO_CANDIDATES, (sc->n_cluster_pointers + 127) / 128, 128, 0, k_svo_candidates,
-                       sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, sc->n_cluster_pointers, mn[0],
-                       mn[1], mn[2], L, s->B, s->d_table, (SvoPair*)c->svo_pairs.ptr, (uint32_t)cap, counters,
-                       c->d_status);
-            return TGX_OK;
-        };
-        if ((st = launch()) != TGX_OK) return fail(st);
-        if (cudaMemcpyAsync(c->h_counter, counters, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-            cudaStreamSynchronize(c->stream) != cudaSuccess) {
-            tgx_set_error("tgx_svo_build: %s", cudaGetErrorString(cudaGetLastError()));
-            return fail(TGX_ERR_CUDA);
-        }
-        const uint32_t n_pairs = ((uint32_t*)c->h_counter)[S_PAIRS];
-        if (n_pairs <= cap) break;
-        // the capacity error recorded by the first attempt is expected; clear it
-        cudaMemsetAsync(c->d_status, 0, sizeof(tgx_dev_status), c->stream);
-        cap = (uint64_t)n_pairs + 1024;
-    }
+    if ((st = svo_candidates(c, s, sc, nullptr, std::max<uint64_t>(1024, (uint64_t)sc->n_cluster_pointers * 4))) != TGX_OK)
+        return fail(st);
     const uint32_t* hc = (const uint32_t*)c->h_counter;
     s->n_pairs = hc[S_PAIRS];
     s->n_blocks = hc[S_MARKED];
-    if (cudaMalloc(&s->d_pool, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4) != cudaSuccess ||
-        cudaMalloc(&s->d_sub, (uint64_t)std::max(s->n_blocks, 1u) * 32 * 4) != cudaSuccess ||
-        cudaMalloc(&s->d_nonempty, (uint64_t)std::max(s->n_blocks, 1u) * 4) != cudaSuccess) {
-        tgx_set_error("tgx_svo_build: out of device memory for %u blocks", s->n_blocks);
-        return fail(TGX_ERR_OUT_OF_MEMORY);
-    }
-    cudaMemsetAsync(s->d_pool, 0, (uint64_t)std::max(s->n_blocks, 1u) * kBlockWords * 4, c->stream);
-    cudaMemsetAsync(s->d_sub, 0, (uint64_t)std::max(s->n_blocks, 1u) * 32 * 4, c->stream);
-    if (sc->d_material && sc->d_luts && !(flags & TGX_SVO_NO_MATERIALS)) {
-        const uint64_t mb = (uint64_t)std::max(s->n_blocks, 1u) * 32768u * 2u;
-        if (cudaMalloc(&s->d_mat, mb) != cudaSuccess) {
-            tgx_set_error("tgx_svo_build: out of device memory for the material grid");
-            return fail(TGX_ERR_OUT_OF_MEMORY);
-        }
-        cudaMemsetAsync(s->d_mat, 0, mb, c->stream);
-    }
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((n_table + 255) / 256, (uint64_t)c->num_sms * 32);
-    auto rest = [&]() -> tgx_status {
-        TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_alloc, s->d_table, n_table, counters, s->n_blocks, c->d_status);
-        const uint32_t vgrid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((s->n_pairs + kWarpsPerVoxCta - 1) / kWarpsPerVoxCta,
-                                                                                  (uint64_t)c->num_sms * 16));
-        TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects,
-                   sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
-                   (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, s->d_mat ? sc->d_material : nullptr, s->d_mat,
-                   mn[0], mn[1], mn[2], s->B);
-        const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
-        TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty,
-                   s->d_sub, s->d_occ, (const uint64_t*)((char*)s->d_occ + svo_occ_off_bytes(occ_words)), s->n_levels,
-                   s->B, counters);
-        return TGX_OK;
-    };
-    if ((st = rest()) != TGX_OK) return fail(st);
-    s->device_bytes = n_table * 4 + (uint64_t)s->n_blocks * (kBlockWords * 4 + 128 + 4 + (s->d_mat ? 65536 : 0)) + occ_words * 4;
+    s->n_slots = s->n_blocks;
+    const bool materials = sc->d_material && sc->d_luts && !(flags & TGX_SVO_NO_MATERIALS);
+    if ((st = svo_resize_slots(c, s, std::max(s->n_blocks, 1u), 0, materials)) != TGX_OK) return fail(st);
+    if ((st = svo_fill(c, s, sc, 0, 0)) != TGX_OK) return fail(st);
+    s->device_bytes = svo_device_bytes(s);
     *out = s;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_svo_update(tgx_ctx* c, tgx_svo* s, const tgx_scene* sc, uint32_t* out_n_moved)
+{
+    if (!c || !s || !sc) { tgx_set_error("tgx_svo_update: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
+    if (sc->n_objects != s->n_objects || sc->n_cluster_pointers != s->n_cluster_pointers) {
+        tgx_set_error("tgx_svo_update: the scene has %u objects / %u cluster pointers, the SVO was built from %u / %u",
+                      sc->n_objects, sc->n_cluster_pointers, s->n_objects, s->n_cluster_pointers);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    if (out_n_moved) *out_n_moved = 0;
+    if (sc->n_objects == 0) return TGX_OK;
+    TGX_CUDA(cudaSetDevice(c->device));
+    const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
+    TGX_TRY(devbuf_reserve(c->svo_scratch, n_table));
+    uint8_t* dirty = (uint8_t*)c->svo_scratch.ptr;
+    uint32_t* counters = s->d_counters;
+    TGX_CUDA(cudaMemsetAsync(dirty, 0, n_table, c->stream));
+    TGX_CUDA(cudaMemsetAsync(counters + S_FREED, 0, 2 * 4, c->stream));   // freed, moved
+    TGX_LAUNCH(c, TR_SVO_CANDIDATES, sc->n_objects, 128, 0, k_svo_mark_dirty, sc->d_objects, s->d_objs, sc->d_cluster_pointers,
+               sc->d_bits, s->mn[0], s->mn[1], s->mn[2], s->B, dirty, counters);
+    const uint32_t wgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
+    TGX_LAUNCH(c, TR_SVO_ALLOC, wgrid, 256, 0, k_svo_release_dirty, s->d_table, n_table, dirty, s->d_pool, s->d_sub,
+               s->d_nonempty, s->d_mat, s->d_free + s->n_free, counters);
+    // pairs of the dirty blocks, into the pair storage the last build left (grown when short)
+    TGX_TRY(svo_candidates(c, s, sc, dirty, std::max<uint64_t>(1024, c->svo_pairs.bytes / sizeof(SvoPair))));
+    const uint32_t* hc = (const uint32_t*)c->h_counter;
+    const uint32_t n_moved = hc[S_MOVED], n_freed = hc[S_FREED], n_marked = hc[S_MARKED];
+    if (out_n_moved) *out_n_moved = n_moved;
+    if (n_moved == 0) return TGX_OK;
+    const uint32_t n_free = s->n_free + n_freed;
+    const uint32_t fresh = n_marked > n_free ? n_marked - n_free : 0u;
+    const uint32_t need = s->n_slots + fresh;
+    if (need > s->pool_cap) TGX_TRY(svo_resize_slots(c, s, need + need / 4 + 64, s->n_slots, s->d_mat != nullptr));
+    s->n_pairs = hc[S_PAIRS];
+    TGX_TRY(svo_fill(c, s, sc, n_free, s->n_slots));
+    s->n_free = n_free - (n_marked - fresh);
+    s->n_slots = need;
+    s->n_blocks = s->n_blocks - n_freed + n_marked;
+    s->device_bytes = svo_device_bytes(s);
     return TGX_OK;
 }
 
@@ -614,7 +826,7 @@ extern "C" void tgx_svo_destroy(tgx_ctx* c, tgx_svo* s)
 extern "C" tgx_status tgx_svo_get_info(tgx_ctx* c, const tgx_svo* s, tgx_svo_info* out)
 {
     if (!c || !s || !out) return TGX_ERR_INVALID_ARGUMENT;
-    TGX_CUDA(cudaMemcpyAsync(c->h_counter, c->svo_counters.ptr, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaMemcpyAsync(c->h_counter, s->d_counters, S_COUNT * 4, cudaMemcpyDeviceToHost, c->stream));
     TGX_CUDA(cudaStreamSynchronize(c->stream));
     out->min[0] = s->mn[0]; out->min[1] = s->mn[1]; out->min[2] = s->mn[2];
     out->extent_log2 = s->L;
@@ -631,7 +843,7 @@ extern "C" tgx_status tgx_svo_download(tgx_ctx* c, const tgx_svo* s, int32_t* ou
 {
     if (!c || !s || !out_n) return TGX_ERR_INVALID_ARGUMENT;
     const uint64_t n_table = (uint64_t)s->B * s->B * s->B;
-    std::vector<uint32_t> table(n_table), nonempty(std::max(s->n_blocks, 1u));
+    std::vector<uint32_t> table(n_table), nonempty(std::max(s->n_slots, 1u));
     TGX_CUDA(cudaMemcpyAsync(table.data(), s->d_table, n_table * 4, cudaMemcpyDeviceToHost, c->stream));
     TGX_CUDA(cudaMemcpyAsync(nonempty.data(), s->d_nonempty, nonempty.size() * 4, cudaMemcpyDeviceToHost, c->stream));
     TGX_CUDA(cudaStreamSynchronize(c->stream));

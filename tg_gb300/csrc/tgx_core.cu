@@ -337,6 +337,14 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
             return TGX_ERR_INVALID_ARGUMENT;
         }
     }
+    for (uint32_t i = 0; i < d->n_objects; i++) {
+        const tgx_object& o = d->objects[i];
+        const uint64_t cnt = (uint64_t)o.n_cluster_pointers_per_dim[0] * o.n_cluster_pointers_per_dim[1] * o.n_cluster_pointers_per_dim[2];
+        if ((uint64_t)o.first_cluster_pointer + cnt > d->n_cluster_pointers) {
+            tgx_set_error("object %u's cluster pointers run past the %u given", i, d->n_cluster_pointers);
+            return TGX_ERR_INVALID_ARGUMENT;
+        }
+    }
     if (d->luts && d->n_luts == 0) { tgx_set_error("luts given with n_luts = 0"); return TGX_ERR_INVALID_ARGUMENT; }
     if (d->luts) {
         for (uint32_t i = 0; i < d->n_objects; i++)

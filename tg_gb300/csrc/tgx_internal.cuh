@@ -128,6 +128,7 @@ struct tgx_ctx
     DevBuf svo_counters;   // SVO build counters
     DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
     DevBuf gi_scratch;     // learned-cache GI queries, hits, training batch
+    DevBuf svo_scratch;    // SVO update: dirty-block marks, old object records
     uint32_t vis_last_tiles = 0;
     uint64_t vis_last_pairs = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters
@@ -157,17 +158,24 @@ struct tgx_svo
     float     mn[3] = {0, 0, 0};
     uint32_t  L = 0;              // extent_log2
     uint32_t  B = 0;              // blocks per axis
-    uint32_t  n_blocks = 0;       // allocated (candidate) blocks
+    uint32_t  n_blocks = 0;       // live blocks: table entries that hold a slot
+    uint32_t  n_slots = 0;        // slots handed out so far (live blocks + free slots)
+    uint32_t  pool_cap = 0;       // slots the pool, sub, nonempty, material and free arrays hold
+    uint32_t  n_free = 0;         // slots released by updates, d_free[0 .. n_free)
+    uint32_t* d_free = nullptr;
+    uint32_t* d_counters = nullptr;  // this SVO's build counters (pairs, marks, slots, non-empty, freed)
+    tgx_object* d_objs = nullptr; // object records the SVO reflects (updates diff the scene against them)
+    uint32_t  n_objects = 0, n_cluster_pointers = 0;
     uint32_t  n_pairs = 0;
     uint32_t* d_table = nullptr;  // B^3 entries: 0 = no block, else slot + 1
-    uint32_t* d_pool = nullptr;   // n_blocks * 1024 words
-    uint32_t* d_sub = nullptr;    // n_blocks * 32 words: 4^3-cell and 8^3-cell occupancy of each block
+    uint32_t* d_pool = nullptr;   // pool_cap * 1024 words
+    uint32_t* d_sub = nullptr;    // pool_cap * 32 words: 4^3-cell and 8^3-cell occupancy of each block
     uint32_t* d_occ = nullptr;    // occupancy pyramid, level 0 = blocks
     uint64_t  occ_words = 0;
     uint64_t  occ_off[10] = {};   // word offset of each level
     uint32_t  n_levels = 0;       // L - 5 + 1 levels (blocks .. root)
     uint32_t* d_nonempty = nullptr;  // per slot: 1 if any bit set
-    uint16_t* d_mat = nullptr;    // n_blocks * 32768 material codes ((lut << 8 | byte) + 1, 0 = none) or null
+    uint16_t* d_mat = nullptr;    // pool_cap * 32768 material codes ((lut << 8 | byte) + 1, 0 = none) or null
     uint64_t  device_bytes = 0;
 };
 

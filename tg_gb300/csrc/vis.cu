@@ -477,17 +477,31 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
 // ---------------------------------------------------------------------------
 
 // One (pixel, cluster) fragment of visibility.frag:78-207 given the cluster-space
-// ray (o, d) and the cluster's 16 bit words.  Returns the packed word or ~0.
+// ray (o, d), the correctly rounded reciprocals (ix, iy, iz) of its non-zero
+// direction components and the cluster's 16 bit words.  Returns the packed
+// word or ~0.  The DDA's per-axis steps 1/|d| are |ix| etc. exactly: a
+// correctly rounded 1/(-d) is the negated 1/d.
 __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float oz, float dx, float dy, float dz,
+                                                       float ix, float iy, float iz, bool sure_hit,
                                                        const uint32_t* __restrict__ w, uint32_t cluster_pointer,
                                                        float far_plane, uint32_t* overrun)
 {
-    float enter, exit_;
-    if (!ray_aabb(ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f, enter, exit_)) return ULLONG_MAX;
-    // a ray parallel to a slab it does not cross is never rasterised
-    if ((dx == 0.0f && (ox < 0.0f || ox > 8.0f)) || (dy == 0.0f && (oy < 0.0f || oy > 8.0f)) ||
-        (dz == 0.0f && (oz < 0.0f || oz > 8.0f)))
-        return ULLONG_MAX;
+    float enter;
+    if (sure_hit) {
+        // the box test surely passes: only the entry distance is needed, and of
+        // each axis only the near-plane quotient can be ray_aabb's minimum
+        const float nx = dx > 0.0f ? xdiv(xsub(0.0f, ox), dx) : dx < 0.0f ? xdiv(xsub(8.0f, ox), dx) : F32_MIN_TG;
+        const float ny = dy > 0.0f ? xdiv(xsub(0.0f, oy), dy) : dy < 0.0f ? xdiv(xsub(8.0f, oy), dy) : F32_MIN_TG;
+        const float nz = dz > 0.0f ? xdiv(xsub(0.0f, oz), dz) : dz < 0.0f ? xdiv(xsub(8.0f, oz), dz) : F32_MIN_TG;
+        enter = gmax(gmax(nx, ny), nz);
+    } else {
+        float exit_;
+        if (!ray_aabb(ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f, enter, exit_)) return ULLONG_MAX;
+        // a ray parallel to a slab it does not cross is never rasterised
+        if ((dx == 0.0f && (ox < 0.0f || ox > 8.0f)) || (dy == 0.0f && (oy < 0.0f || oy > 8.0f)) ||
+            (dz == 0.0f && (oz < 0.0f || oz > 8.0f)))
+            return ULLONG_MAX;
+    }
     const bool ent = enter > 0.0f;
     const float hx = ent ? xadd(ox, xmul(enter, dx)) : ox;
     const float hy = ent ? xadd(oy, xmul(enter, dy)) : oy;
@@ -498,12 +512,12 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     int sx = 0, sy = 0, sz = 0;
     float tmx = F32_MAX_TG, tmy = F32_MAX_TG, tmz = F32_MAX_TG;
     float tdx = F32_MAX_TG, tdy = F32_MAX_TG, tdz = F32_MAX_TG;
-    if (dx > 0.0f) { sx = 1; tmx = xadd(enter, xdiv(xsub((float)(x + 1), hx), dx)); tdx = xdiv(1.0f, dx); }
-    else if (dx < 0.0f) { sx = -1; tmx = xadd(enter, xdiv(xsub(hx, (float)x), -dx)); tdx = xdiv(1.0f, -dx); }
-    if (dy > 0.0f) { sy = 1; tmy = xadd(enter, xdiv(xsub((float)(y + 1), hy), dy)); tdy = xdiv(1.0f, dy); }
-    else if (dy < 0.0f) { sy = -1; tmy = xadd(enter, xdiv(xsub(hy, (float)y), -dy)); tdy = xdiv(1.0f, -dy); }
-    if (dz > 0.0f) { sz = 1; tmz = xadd(enter, xdiv(xsub((float)(z + 1), hz), dz)); tdz = xdiv(1.0f, dz); }
-    else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = xdiv(1.0f, -dz); }
+    if (dx > 0.0f) { sx = 1; tmx = xadd(enter, xdiv(xsub((float)(x + 1), hx), dx)); tdx = ix; }
+    else if (dx < 0.0f) { sx = -1; tmx = xadd(enter, xdiv(xsub(hx, (float)x), -dx)); tdx = -ix; }
+    if (dy > 0.0f) { sy = 1; tmy = xadd(enter, xdiv(xsub((float)(y + 1), hy), dy)); tdy = iy; }
+    else if (dy < 0.0f) { sy = -1; tmy = xadd(enter, xdiv(xsub(hy, (float)y), -dy)); tdy = -iy; }
+    if (dz > 0.0f) { sz = 1; tmz = xadd(enter, xdiv(xsub((float)(z + 1), hz), dz)); tdz = iz; }
+    else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = -iz; }
     for (uint32_t step = 0; step < kMaxDdaSteps; step++) {
         const uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
         if (w[rvi >> 5] & (1u << (rvi & 31u))) {
@@ -530,22 +544,28 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     return ULLONG_MAX;
 }
 
-// Conservative reject: true only if the exact test of vis_pair surely misses.
-// Slab distances use a correctly rounded reciprocal (error < 2 ulp against
-// the exact quotient); a miss is declared only with a 1e-5 relative margin.
-__device__ __forceinline__ bool surely_misses(float ox, float oy, float oz, float dx, float dy, float dz, float ix,
-                                              float iy, float iz)
+// Conservative classification of the exact box test of vis_pair: kMiss or
+// kHit only when the exact test surely gives that answer, else kUnsure.  Slab
+// distances use a correctly rounded reciprocal (error < 2 ulp against the
+// exact quotient of the same numerator); an answer is given only with a 1e-5
+// relative margin.
+enum SlabClass { kMiss = 0, kUnsure = 1, kHit = 2 };
+__device__ __forceinline__ int slab_class(float ox, float oy, float oz, float dx, float dy, float dz, float ix,
+                                          float iy, float iz)
 {
+    if (ox != ox || oy != oy || oz != oz) return kUnsure;   // NaN origin: the exact test decides
     float en = -3.0e38f, ex = 3.0e38f;
-    if (dx == 0.0f) { if (ox < 0.0f || ox > 8.0f) return true; }
+    if (dx == 0.0f) { if (ox < 0.0f || ox > 8.0f) return kMiss; }
     else { const float a = -ox * ix, b = (8.0f - ox) * ix; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
-    if (dy == 0.0f) { if (oy < 0.0f || oy > 8.0f) return true; }
+    if (dy == 0.0f) { if (oy < 0.0f || oy > 8.0f) return kMiss; }
     else { const float a = -oy * iy, b = (8.0f - oy) * iy; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
-    if (dz == 0.0f) { if (oz < 0.0f || oz > 8.0f) return true; }
+    if (dz == 0.0f) { if (oz < 0.0f || oz > 8.0f) return kMiss; }
     else { const float a = -oz * iz, b = (8.0f - oz) * iz; en = fmaxf(en, fminf(a, b)); ex = fminf(ex, fmaxf(a, b)); }
-    if (!(fabsf(en) < 1e37f) || !(fabsf(ex) < 1e37f)) return false;
+    if (!(fabsf(en) < 1e37f) || !(fabsf(ex) < 1e37f)) return kUnsure;
     const float tol = 1e-5f * (fabsf(en) + fabsf(ex)) + 1e-30f;
-    return ex < -tol || en > ex + 2.0f * tol;
+    if (ex < -tol || en > ex + 2.0f * tol) return kMiss;
+    if (ex > tol && en < ex - 2.0f * tol) return kHit;
+    return kUnsure;
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -671,9 +691,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRec
                 iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
                 iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
             }
-            if (surely_misses(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz)) continue;
-            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, &s_bits[k * 16], r.cluster_pointer,
-                                                  vc.far_plane, &counters[C_DDA_OVERRUN]);
+            const int sc = slab_class(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz);
+            if (sc == kMiss) continue;
+            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit, &s_bits[k * 16],
+                                                  r.cluster_pointer, vc.far_plane, &counters[C_DDA_OVERRUN]);
             if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
         }
     }
