@@ -449,6 +449,9 @@ typedef struct tgx_cache_gi_params
     float    lr;                /* Adam learning rate (1e-2) */
     float    box_min[3];        /* scene box: positions are normalised by it for the cache */
     float    box_max[3];
+    float    primary_weight;    /* 0..1: largest share of a pixel's incoming light taken from the
+                                   cache's pixel-point network instead of its samples (0: off) */
+    uint32_t n_train_primary;   /* training samples of the pixel-point network per frame (0) */
 } tgx_cache_gi_params;
 
 /*
@@ -459,7 +462,13 @@ typedef struct tgx_cache_gi_params
  * the cache online on this frame: picks n_train bounce hits, estimates their
  * demodulated outgoing radiance with train_spp plain SVO paths (`bounces` - 1
  * further bounces, direct sun at every hit) and runs train_steps Adam steps.
- * Asynchronous; all buffers DEVICE memory.
+ * The cache also holds a second network for the pixels' own surface points.
+ * It is trained (n_train_primary random pixels per frame, no extra paths) on
+ * each pixel's sample mean m of incoming light.  With primary_weight w > 0 a
+ * pixel's incoming light becomes m + k (P - m), P the network's prediction
+ * and k = min(w, v / max(|P - m|^2, v)) with v the variance of m estimated
+ * from the pixel's samples: the prediction counts where it agrees with the
+ * samples within their noise.  Asynchronous; all buffers DEVICE memory.
  */
 tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, tgx_cache* cache,
                                  const tgx_view* view, const uint64_t* d_visbuf, const tgx_gi_params* params,

@@ -162,3 +162,50 @@ def test_cached_gi_learns_toward_the_plain_estimate(ctx):
     assert ctx.device_error().code == 0
     assert errs[1] < 0.5 * errs[0], errs
     cache.close(); svo.close(); sc.close()
+
+
+def _cached_relmse_after(ctx, sc, svo, view, vis, ref, hit, cp, frames=40, spp=4):
+    import torch
+    cache = tg.Cache(ctx, seed=2)
+    out = torch.empty_like(ref)
+    for f in range(frames):
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=f), cp, out)
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    cache.close()
+    r = ref.cpu().numpy().reshape(-1, 3)[hit]
+    x = out.cpu().numpy().reshape(-1, 3)[hit]
+    return float(np.mean((x - r) ** 2 / (r ** 2 + 1e-2))), out
+
+
+def test_pixel_point_network_lowers_the_error(ctx):
+    """The cache's second network, trained on the pixels' own sample means,
+    lowers the error of 4-spp cached GI against a 256-spp plain render.  With
+    weight 0 it trains but leaves every pixel bit-equal to cached GI without
+    it (bounce network frozen: its training sums gradients with atomics, so
+    two trained runs differ in the last bits)."""
+    import torch
+    s, sc, svo, view, vis = _scene_setup(ctx, seed=23)
+    ref = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+    ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=9), ref)
+    hit = (vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY))
+    box = ((-40.0,) * 3, (40.0,) * 3)
+    frozen = dict(n_train=0, train_spp=8, train_steps=4, lr=1e-2)
+    _, out0 = _cached_relmse_after(ctx, sc, svo, view, vis, ref, hit, tg.cache_gi_params(*box, **frozen), frames=8)
+    _, out_off = _cached_relmse_after(ctx, sc, svo, view, vis, ref, hit,
+                                      tg.cache_gi_params(*box, **frozen, primary_weight=0.0, n_train_primary=4096),
+                                      frames=8)
+    assert torch.equal(out0, out_off)
+    base = dict(n_train=8192, train_spp=8, train_steps=4, lr=1e-2)
+    e0, _ = _cached_relmse_after(ctx, sc, svo, view, vis, ref, hit, tg.cache_gi_params(*box, **base))
+    e1, _ = _cached_relmse_after(ctx, sc, svo, view, vis, ref, hit,
+                                 tg.cache_gi_params(*box, **base, primary_weight=1.0, n_train_primary=4096))
+    assert e1 < 0.8 * e0, (e0, e1)
+    with pytest.raises(tg.TgxError):
+        cache = tg.Cache(ctx, seed=2)
+        try:
+            ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2),
+                                 tg.cache_gi_params(*box, **base, primary_weight=1.5), torch.empty_like(ref))
+        finally:
+            cache.close()
+    svo.close(); sc.close()

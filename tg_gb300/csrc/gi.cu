@@ -471,6 +471,8 @@ struct CacheGiConst
     float box_min[3];
     float box_inv[3];    // 1 / (box_max - box_min)
     uint32_t n_train, train_spp;
+    uint32_t n_train_primary;   // training samples of the pixel-point network per frame
+    float primary_weight;
 };
 
 enum CacheCounter { CC_ROOTS = 0, CC_QUERIES = 1, CC_TRAIN_ROOTS = 2, CC_QUEUE = 3 };
@@ -518,31 +520,110 @@ __global__ void __launch_bounds__(256) k_gi_query_shade(SvoDev s, const tgx_mate
     }
 }
 
+// Queries of the pixel-point network: each pixel's surface point (root origin
+// less the offset), its normal and the camera ray's direction.
+__global__ void __launch_bounds__(256) k_gi_primary_queries(const PathRoot* __restrict__ roots,
+                                                            const uint32_t* __restrict__ n_dev, GiParams p,
+                                                            CacheGiConst q, float cam_x, float cam_y, float cam_z,
+                                                            float* __restrict__ qx)
+{
+    const uint32_t n = *n_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const PathRoot& rt = roots[r];
+        const float cam[3] = {cam_x, cam_y, cam_z};
+        float x[3], w[3], len2 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            x[c] = rt.o[c] - rt.n[c] * p.offset;
+            w[c] = x[c] - cam[c];
+            len2 += w[c] * w[c];
+        }
+        const float inv = len2 > 0.0f ? rsqrtf(len2) : 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) w[c] *= inv;
+        cache_input(q, x, rt.n, w, qx + 9ull * r);
+    }
+}
+
+// The pixel-point network's training batch: n_train_primary random pixels,
+// each with its query and this frame's sample mean of incoming light.
+__global__ void __launch_bounds__(256) k_gi_primary_batch(GiParams p, CacheGiConst q, const uint32_t* __restrict__ n_dev,
+                                                          const float* __restrict__ pqx, const float* __restrict__ pmean,
+                                                          float* __restrict__ tx, float* __restrict__ tt)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.n_train_primary) return;
+    const uint32_t n = *n_dev;
+    uint32_t ctr[4] = {i, 0x7ffffffeu, p.frame, 0x9e1du};
+    philox(ctr, (uint32_t)p.seed ^ 0x3C3C3C3Cu, (uint32_t)(p.seed >> 32));
+    const uint32_t r = n ? ctr[0] % n : 0u;
+#pragma unroll
+    for (int k = 0; k < 9; k++) tx[9ull * i + k] = n ? pqx[9ull * r + k] : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) tt[3ull * i + k] = n ? pmean[3ull * r + k] : 0.0f;
+}
+
 // pixel = direct + albedo * mean(sky, or hit albedo * cache prediction)
+// With the pixel-point network (prim_rgb), the incoming light is shrunk from
+// the sample mean m toward the network's prediction P at the pixel's point:
+// e = m + k (P - m) with k = min(w, v / max(|P - m|^2, v)), v the variance of
+// the mean estimated from the pixel's own samples (k = w with one sample).
+// A prediction within the samples' noise is taken up to the weight w; one far
+// outside it (where the network is wrong) is mostly ignored.  The sample mean
+// is kept (pmean) as that network's training target.
 __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __restrict__ roots,
                                                          const uint32_t* __restrict__ n_dev, GiParams p,
                                                          const RayHit* __restrict__ root_hits,
                                                          const int32_t* __restrict__ qidx,
                                                          const float* __restrict__ qrgb,
-                                                         const CacheHit* __restrict__ hits, float* __restrict__ out)
+                                                         const CacheHit* __restrict__ hits,
+                                                         const float* __restrict__ prim_rgb, float primary_weight,
+                                                         float* __restrict__ pmean, float* __restrict__ out)
 {
     const uint32_t n = *n_dev;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const PathRoot& rt = roots[r];
-        float acc[3] = {0.0f, 0.0f, 0.0f};
+        float acc[3] = {0.0f, 0.0f, 0.0f}, sq = 0.0f;
         for (uint32_t k = 0; k < p.spp; k++) {
             const int32_t qv = qidx[(uint64_t)r * p.spp + k];
 #pragma unroll
-            for (int i = 0; i < 3; i++)
-                acc[i] = xadd(acc[i], qv >= 0 ? xmul(hits[qv].a[i], fmaxf(qrgb[3ull * qv + i], 0.0f))
-                                              : (qv == -1 ? p.sky_radiance[i] : 0.0f));
+            for (int i = 0; i < 3; i++) {
+                const float f = qv >= 0 ? xmul(hits[qv].a[i], fmaxf(qrgb[3ull * qv + i], 0.0f))
+                                        : (qv == -1 ? p.sky_radiance[i] : 0.0f);
+                acc[i] = xadd(acc[i], f);
+                if (prim_rgb) sq += f * f;
+            }
         }
         float L[3] = {0.0f, 0.0f, 0.0f};
         const float ndl = sun_cos(rt.n, p);
         if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
         const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
+        float m[3], pr[3], kw = 0.0f;
 #pragma unroll
-        for (int i = 0; i < 3; i++) out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], xmul(acc[i], inv_spp)));
+        for (int i = 0; i < 3; i++) {
+            m[i] = xmul(acc[i], inv_spp);
+            if (pmean) pmean[3ull * r + i] = m[i];
+        }
+        if (prim_rgb) {
+            float d2 = 0.0f, m2 = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                pr[i] = fmaxf(prim_rgb[3ull * r + i], 0.0f);
+                d2 += (pr[i] - m[i]) * (pr[i] - m[i]);
+                m2 += m[i] * m[i];
+            }
+            kw = primary_weight;
+            if (p.spp > 1) {
+                const float n = (float)p.spp;
+                const float v = fmaxf(sq - n * m2, 0.0f) / ((n - 1.0f) * n);   // variance of the mean, summed over channels
+                if (d2 > v) kw = fminf(kw, v / d2);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float e = prim_rgb ? m[i] + kw * (pr[i] - m[i]) : m[i];
+            out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], e));
+        }
     }
 }
 
@@ -750,6 +831,15 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     }
     q.n_train = cp->n_train;
     q.train_spp = cp->train_spp ? cp->train_spp : 16;
+    if (!(cp->primary_weight >= 0.0f && cp->primary_weight <= 1.0f)) {
+        tgx_set_error("tgx_gi_render_cached: primary_weight must be in [0, 1]");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    q.primary_weight = cp->primary_weight;
+    q.n_train_primary = cp->n_train_primary;
+    const bool primary = q.primary_weight > 0.0f || (q.n_train_primary && cp->train_steps);
+    tgx_cache* pnet = nullptr;
+    if (primary) TGX_TRY(cache_primary(c, cache, &pnet));
     const bool train = q.n_train && cp->train_steps;
     const uint64_t n_pix = (uint64_t)view->width * view->height;
     const uint64_t capacity = n_pix * p.spp;
@@ -759,8 +849,10 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     const uint64_t max_roots = std::max<uint64_t>(n_pix, q.n_train);
     const uint64_t max_paths = std::max<uint64_t>(n_pix * cs, (uint64_t)q.n_train * cs_t);
 
+    const uint64_t n_prim = primary ? n_pix : 0;
     auto layout = [&](Carver& cv, uint32_t*& counters, PathBufs& b, int32_t*& qidx, float*& qx, float*& qrgb,
-                      CacheHit*& hits, float*& tx, float*& tt) {
+                      CacheHit*& hits, float*& tx, float*& tt, float*& pqx, float*& pqrgb, float*& pmean,
+                      float*& ptx, float*& ptt) {
         counters = cv.take<uint32_t>(64);
         carve_paths(cv, b, max_roots, max_paths);
         qidx = cv.take<int32_t>(capacity);
@@ -769,13 +861,19 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         hits = cv.take<CacheHit>(capacity);
         tx = cv.take<float>((uint64_t)q.n_train * 9);
         tt = cv.take<float>((uint64_t)q.n_train * 3);
+        pqx = cv.take<float>(n_prim * 9);
+        pqrgb = cv.take<float>(n_prim * 3);
+        pmean = cv.take<float>(n_prim * 3);
+        ptx = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 9);
+        ptt = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 3);
     };
-    uint32_t* counters; PathBufs b; int32_t* qidx; float *qx, *qrgb, *tx, *tt; CacheHit* hits;
+    uint32_t* counters; PathBufs b; int32_t* qidx; CacheHit* hits;
+    float *qx, *qrgb, *tx, *tt, *pqx, *pqrgb, *pmean, *ptx, *ptt;
     Carver size{nullptr};
-    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt);
+    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->gi_scratch, size.off + 256));
     Carver cv{(char*)c->gi_scratch.ptr};
-    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt);
+    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
     uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
     TGX_CUDA(cudaMemsetAsync(counters, 0, 64 * 4, c->stream));
@@ -798,8 +896,22 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     }
     // inference over all potential queries: slots past the hit count are never read
     TGX_TRY(cache_infer_counted(c, cache, &counters[CC_QUERIES], (uint32_t)capacity, qx, qrgb));
+    if (primary) {
+        TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_primary_queries, b.roots, &counters[CC_ROOTS], p,
+                   q, view->camera[0], view->camera[1], view->camera[2], pqx);
+        if (q.primary_weight > 0.0f)
+            TGX_TRY(cache_infer_counted(c, pnet, &counters[CC_ROOTS], (uint32_t)n_pix, pqx, pqrgb));
+    }
     TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_resolve, b.roots, &counters[CC_ROOTS], p,
-               b.root_hits, qidx, qrgb, hits, d_rgb);
+               b.root_hits, qidx, qrgb, hits, q.primary_weight > 0.0f ? pqrgb : nullptr, q.primary_weight,
+               primary ? pmean : nullptr, d_rgb);
+    if (primary && q.n_train_primary && cp->train_steps) {
+        TGX_LAUNCH(c, TR_GI, (q.n_train_primary + 255) / 256, 256, 0, k_gi_primary_batch, p, q, &counters[CC_ROOTS], pqx,
+                   pmean, ptx, ptt);
+        const uint32_t per = q.n_train_primary / cp->train_steps;
+        for (uint32_t k = 0; k < cp->train_steps && per; k++)
+            TGX_TRY(tgx_cache_train_step(c, pnet, per, ptx + 9ull * per * k, ptt + 3ull * per * k, cp->lr));
+    }
     if (train) {
         TGX_LAUNCH(c, TR_GI, (q.n_train + 255) / 256, 256, 0, k_gi_target_roots, p, q, hits, counters,
                    (uint32_t)capacity, b.roots, tx, tt);

@@ -699,7 +699,9 @@ struct tgx_cache
     __nv_bfloat16* img = nullptr;
     float* loss = nullptr;
     uint32_t step = 0;
+    uint64_t seed = 0;
     DevBuf scratch;            // training activations/deltas
+    tgx_cache* primary = nullptr;  // second network: mean incoming light at pixel surface points (cached GI)
 };
 
 static uint64_t mix64(uint64_t x)
@@ -725,6 +727,7 @@ extern "C" tgx_status tgx_cache_create(tgx_ctx* c, uint64_t seed, tgx_cache** ou
     TGX_CUDA(cudaSetDevice(c->device));
     tgx_cache* k = new (std::nothrow) tgx_cache();
     if (!k) return TGX_ERR_OUT_OF_MEMORY;
+    k->seed = seed;
     bool ok = cudaMalloc(&k->w, N_PARAMS * 4) == cudaSuccess && cudaMalloc(&k->m, N_PARAMS * 4) == cudaSuccess &&
               cudaMalloc(&k->v, N_PARAMS * 4) == cudaSuccess && cudaMalloc(&k->g, N_PARAMS * 4) == cudaSuccess &&
               cudaMalloc(&k->img, B_TOTAL * 2) == cudaSuccess && cudaMalloc(&k->loss, 16) == cudaSuccess;
@@ -756,9 +759,18 @@ extern "C" void tgx_cache_destroy(tgx_ctx* c, tgx_cache* k)
 {
     if (!k) return;
     if (c) cudaStreamSynchronize(c->stream);
+    tgx_cache_destroy(c, k->primary);
     cudaFree(k->w); cudaFree(k->m); cudaFree(k->v); cudaFree(k->g); cudaFree(k->img); cudaFree(k->loss);
     devbuf_free(k->scratch);
     delete k;
+}
+
+// The cache's second network, created on first use from a seed derived from the cache's.
+tgx_status cache_primary(tgx_ctx* c, tgx_cache* k, tgx_cache** out)
+{
+    if (!k->primary) TGX_TRY(tgx_cache_create(c, mix64(k->seed ^ 0x7072696d617279ull), &k->primary));
+    *out = k->primary;
+    return TGX_OK;
 }
 
 extern "C" tgx_status tgx_cache_get_weights(tgx_ctx* c, const tgx_cache* k, float* out_w)

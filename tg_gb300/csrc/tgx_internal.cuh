@@ -339,6 +339,7 @@ void trace_free(tgx_ctx* ctx);
     } while (0)
 
 // cache inference over min(max_n, *d_n) inputs (mlp.cu)
+tgx_status cache_primary(tgx_ctx* c, tgx_cache* k, tgx_cache** out);
 tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
                                float* d_rgb);
 
