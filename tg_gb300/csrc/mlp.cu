@@ -6,26 +6,19 @@
 //   216 sin/cos features (12 octaves of pi) -> 4 ReLU layers of 64 -> RGB,
 //   no biases, relative L2 loss, Adam.
 // Weights and activations are BF16, accumulation is FP32, master weights and
-// Adam moments are FP32.  Inference runs on tcgen05 (TMEM accumulators);
-// training on mma.sync m16n8k16.
+// Adam moments are FP32.  Inference and training run on tcgen05 (operands in
+// shared memory, FP32 accumulators in TMEM).
 //
 // Kernels:
-//   k_mlp_forward_tc inference on tcgen05: 128 queries per tile, operands in
-//                   shared memory, FP32 accumulators in TMEM, one elected
-//                   thread issues the MMAs of a layer (below).
-//   k_mlp_fwd_bwd   one warp per 16 samples: the forward with the accumulators
-//                   of one layer re-packed as the A fragments of the next, the
-//                   relative-L2 gradient, and the
-//                   backward pass through W4..W1 (deltas masked by ReLU');
-//                   writes each layer's input activations and output deltas
-//                   (BF16) for the weight gradients.
-//   k_mlp_wgrad     dW_l = sum_s delta_l[s] (x) act_l[s] for all layers in one
-//                   launch, on the tensor cores (ldmatrix.trans tiles of 16
-//                   samples), split over samples, per-CTA sums in shared
-//                   memory, FP32 atomics into the gradient.
+//   k_mlp_forward_tc inference: 128 queries per tile, one elected thread
+//                   issues the MMAs of a layer (below).
+//   k_mlp_train_tc  training: forward, relative-L2 output delta, backward and
+//                   the weight gradients of 128-sample tiles in one kernel;
+//                   gradients summed in TMEM over a CTA's tiles, then written
+//                   to the CTA's slice of a partial buffer.
+//   k_mlp_reduce    adds the slices in a fixed order (deterministic).
 //   k_mlp_adam      Adam on the FP32 master weights; refreshes the BF16
-//                   copies in the layouts the kernels read (row-major for the
-//                   forward, transposed for the backward).
+//                   image the kernels stage from.
 
 #include "tgx_internal.cuh"
 
@@ -37,133 +30,26 @@
 
 namespace {
 
-constexpr int NI = 9, NF = 12, NE = 216, NEP = 224, NH = 64, NO = 3;
+constexpr int NI = 9, NE = 216, NEP = 224, NH = 64, NO = 3;
 constexpr int OFF_W0 = 0, OFF_W1 = OFF_W0 + NH * NE, OFF_W2 = OFF_W1 + NH * NH, OFF_W3 = OFF_W2 + NH * NH,
               OFF_W4 = OFF_W3 + NH * NH, N_PARAMS = OFF_W4 + NO * NH;
 
-// BF16 weight images (element strides padded against shared-memory bank conflicts)
+// BF16 weight image, row-major [out][in] per layer (row strides padded)
 constexpr int S0 = 232;   // W0  [64][S0]   k < 216 real
-constexpr int SH = 72;    // W1..W3 [64][SH] and their transposes
-constexpr int S4T = 24;   // W4t [64][S4T]  k < 3 real
+constexpr int SH = 72;    // W1..W3 [64][SH]
 // offsets in bf16 elements inside the packed image
 constexpr int B_W0 = 0;
 constexpr int B_W1 = B_W0 + NH * S0;
 constexpr int B_W2 = B_W1 + NH * SH;
 constexpr int B_W3 = B_W2 + NH * SH;
 constexpr int B_W4 = B_W3 + NH * SH;         // [8][SH], rows >= 3 zero
-constexpr int B_W1T = B_W4 + 8 * SH;
-constexpr int B_W2T = B_W1T + NH * SH;
-constexpr int B_W3T = B_W2T + NH * SH;
-constexpr int B_W4T = B_W3T + NH * SH;       // [64][S4T], cols >= 3 zero
-constexpr int B_TOTAL = B_W4T + NH * S4T;
+constexpr int B_TOTAL = B_W4 + 8 * SH;
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
 }
-__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
-__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
-
-__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-// feature pair (sin, cos) of column c (even) for input row x
-__device__ __forceinline__ uint32_t feature_pair(const float* x, int c)
-{
-    if (c >= NE) return 0u;
-    const int i = c / (2 * NF), k = (c / 2) % NF;
-    float s, co;
-    sincospif(ldexpf(x[i], k), &s, &co);
-    return pack_bf16(s, co);
-}
-
-// One hidden layer: acc[8][4] = A(16 x K) * W^T, W is [64][stride] bf16 in shared memory
-template <int KSTEPS>
-__device__ __forceinline__ void layer(const uint32_t (*A)[4], const __nv_bfloat16* W, int stride, float acc[8][4],
-                                      int g, int t)
-{
-#pragma unroll
-    for (int n = 0; n < 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < KSTEPS; kt++)
-#pragma unroll
-        for (int n = 0; n < 8; n++) {
-            const __nv_bfloat16* row = W + (n * 8 + g) * stride + kt * 16 + 2 * t;
-            mma16816(acc[n], A[kt], lds32(row), lds32(row + 8));
-        }
-}
-
-// accumulators -> ReLU -> BF16 A fragments of the next layer (the C layout of
-// n-tiles 2k, 2k+1 is the A layout of k-step k)
-__device__ __forceinline__ void relu_pack(const float acc[8][4], uint32_t A[4][4])
-{
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        A[k][0] = pack_bf16(fmaxf(acc[2 * k][0], 0.0f), fmaxf(acc[2 * k][1], 0.0f));
-        A[k][1] = pack_bf16(fmaxf(acc[2 * k][2], 0.0f), fmaxf(acc[2 * k][3], 0.0f));
-        A[k][2] = pack_bf16(fmaxf(acc[2 * k + 1][0], 0.0f), fmaxf(acc[2 * k + 1][1], 0.0f));
-        A[k][3] = pack_bf16(fmaxf(acc[2 * k + 1][2], 0.0f), fmaxf(acc[2 * k + 1][3], 0.0f));
-    }
-}
-
-__device__ __forceinline__ void load_weights(__nv_bfloat16* dst, const __nv_bfloat16* src, int n)
-{
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    for (int i = threadIdx.x; i < n / 8; i += blockDim.x) d[i] = s[i];
-}
-
-// The forward of one 16-sample tile; x0/x1 are this lane's two sample rows.
-// Leaves the hidden activations h1..h4 as A fragments and y in acc4.
-__device__ __forceinline__ void forward_tile(const __nv_bfloat16* sw, const float* x0, const float* x1, int g, int t,
-                                             uint32_t H[4][4][4], float acc4[4], __nv_bfloat16* enc_out,
-                                             uint64_t row0, uint64_t row1)
-{
-    float acc[8][4];
-#pragma unroll
-    for (int n = 0; n < 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
-    for (int kt = 0; kt < NEP / 16; kt++) {
-        const int c0 = kt * 16 + 2 * t, c1 = c0 + 8;
-        uint32_t a[4];
-        a[0] = feature_pair(x0, c0);
-        a[1] = feature_pair(x1, c0);
-        a[2] = feature_pair(x0, c1);
-        a[3] = feature_pair(x1, c1);
-        if (enc_out) {
-            *reinterpret_cast<uint32_t*>(enc_out + row0 * NEP + c0) = a[0];
-            *reinterpret_cast<uint32_t*>(enc_out + row1 * NEP + c0) = a[1];
-            *reinterpret_cast<uint32_t*>(enc_out + row0 * NEP + c1) = a[2];
-            *reinterpret_cast<uint32_t*>(enc_out + row1 * NEP + c1) = a[3];
-        }
-#pragma unroll
-        for (int n = 0; n < 8; n++) {
-            const __nv_bfloat16* row = sw + B_W0 + (n * 8 + g) * S0 + kt * 16 + 2 * t;
-            mma16816(acc[n], a, lds32(row), lds32(row + 8));
-        }
-    }
-    relu_pack(acc, H[0]);
-    layer<4>(H[0], sw + B_W1, SH, acc, g, t);
-    relu_pack(acc, H[1]);
-    layer<4>(H[1], sw + B_W2, SH, acc, g, t);
-    relu_pack(acc, H[2]);
-    layer<4>(H[2], sw + B_W3, SH, acc, g, t);
-    relu_pack(acc, H[3]);
-    acc4[0] = acc4[1] = acc4[2] = acc4[3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const __nv_bfloat16* row = sw + B_W4 + g * SH + kt * 16 + 2 * t;
-        mma16816(acc4, H[3][kt], lds32(row), lds32(row + 8));
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
 // ---------------------------------------------------------------------------
@@ -424,238 +310,302 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tmem_slot), "r"(TMEM_COLS) : "memory");
 }
 
-// Training forward + backward.  Writes, per sample s:
-//   enc[s][224]          layer-0 input (features)
-//   act[l][s][64]        input of layer l+1 (h1..h4), BF16
-//   dlt[l][s][64]        delta at the output of layer l (pre-activation of h_{l+1}), l = 0..3
-//   dy[s][16]            delta at the network output (3 real columns), BF16
-// and adds the batch loss (times 1/(3n)) to *loss.
-__global__ void __launch_bounds__(128) k_mlp_fwd_bwd(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
-                                                    const float* __restrict__ x, const float* __restrict__ target,
-                                                    __nv_bfloat16* __restrict__ enc, __nv_bfloat16* __restrict__ act,
-                                                    __nv_bfloat16* __restrict__ dlt, __nv_bfloat16* __restrict__ dy,
-                                                    float* __restrict__ loss)
+// ---------------------------------------------------------------------------
+// Training on tcgen05: forward, backward and weight gradients in one kernel
+// ---------------------------------------------------------------------------
+//
+// One CTA of 128 threads per SM works through tiles of 128 samples; thread t
+// owns sample t (row t of the forward and backward GEMMs, TMEM lane t).  All
+// operands stay in shared memory in the core-matrix layout the forward uses
+// ([column group][row group][8 rows x 16 B]).  The backward reads the
+// forward's weight tiles, and the weight gradients read the activation and
+// delta tiles, through MN-major descriptors (the transpose bits of the
+// instruction descriptor), so nothing is copied or transposed:
+//   forward   z_{l+1} = W_l h_l (M = 128 samples), ReLU into BF16 tiles h1..h4
+//   output    dy = d(relative L2)/dy, a 128 x 16 tile (3 real columns)
+//   backward  d_l = (d_{l+1} W_l) * relu'(z_l), ping-ponging two tiles
+//   gradients dW_l^T += h_l^T d_{l+1}: M = 128 layer inputs, N = outputs,
+//             K = the tile's samples, accumulated in TMEM over all of the
+//             CTA's tiles.  Layers with fewer than 128 inputs read the next
+//             tile's rows as the rest of M; those accumulator rows are never
+//             read out.
+// At the end each CTA writes its summed gradient into its own slice of a
+// partial buffer, and k_mlp_reduce adds the slices in a fixed order, so a
+// training step is deterministic.
+
+namespace tt {
+
+using tc::KG0;
+using tc::KGH;
+constexpr int THREADS = 128;
+constexpr int W0 = 0;                                 // [28 kg][8 ng][128 B]
+constexpr int W1 = W0 + KG0 * 8 * 128;                // [8 kg][8 ng][128 B] x 3 (W1, W2, W3)
+constexpr int W4 = W1 + 3 * KGH * 8 * 128;            // [8 kg][2 ng][128 B] (16 rows, 3 real)
+constexpr int X0 = W4 + KGH * 2 * 128;                // features: [28 kg][16 mg][128 B]
+constexpr int H = X0 + KG0 * 16 * 128;                // h1..h4: [8 kg][16 mg][128 B] each
+constexpr int TILE64 = KGH * 16 * 128;
+constexpr int DA = H + 4 * TILE64;                    // delta tiles (dy uses the first 2 kg of DB)
+constexpr int DB = DA + TILE64;
+constexpr int BAR = DB + TILE64;                      // mbarrier, TMEM address
+constexpr int SMEM = BAR + 64;
+// gradient reads of M = 128 rows run 16 column groups past a tile's base
+static_assert(X0 + 32 * 16 * 128 <= SMEM && H + 3 * TILE64 + 16 * 16 * 128 <= SMEM, "gradient operand over-read");
+// TMEM columns
+constexpr uint32_t ACC = 0;        // layer accumulator (64 columns)
+constexpr uint32_t G0A = 64;       // dW0^T inputs 0..127
+constexpr uint32_t G0B = 128;      // dW0^T inputs 128..255 (216 real)
+constexpr uint32_t G1 = 192, G2 = 256, G3 = 320;   // dW1^T .. dW3^T (64 real rows)
+constexpr uint32_t G4 = 384;       // dW4^T (64 real rows, 16 columns, 3 real)
+constexpr uint32_t TMEM_COLS = 512;
+
+__host__ __device__ constexpr uint32_t idesc_t(uint32_t n, bool ta, bool tb)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    load_weights(sw, wimg, B_TOTAL);
+    return tc::idesc(n) | (ta ? 1u << 15 : 0u) | (tb ? 1u << 16 : 0u);
+}
+
+}  // namespace tt
+
+__global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
+                                                                const float* __restrict__ x,
+                                                                const float* __restrict__ target,
+                                                                float* __restrict__ partial, float* __restrict__ loss,
+                                                                tgx_dev_status* __restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    using namespace tc;
+    const uint32_t t = threadIdx.x, warp = t >> 5;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tt::BAR);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + tt::BAR + 16);
+    stage_weights(sm + tt::W0, wimg + B_W0, S0, NH, NH, KG0);
+    stage_weights(sm + tt::W1 + 0 * KGH * 8 * 128, wimg + B_W1, SH, NH, NH, KGH);
+    stage_weights(sm + tt::W1 + 1 * KGH * 8 * 128, wimg + B_W2, SH, NH, NH, KGH);
+    stage_weights(sm + tt::W1 + 2 * KGH * 8 * 128, wimg + B_W3, SH, NH, NH, KGH);
+    stage_weights(sm + tt::W4, wimg + B_W4, SH, 8, 16, KGH);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(saddr(tmem_slot)), "r"(tt::TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
-    const uint32_t tiles = (n + 15) / 16;
-    const uint64_t np = (uint64_t)tiles * 16;   // per-layer stride of act and dlt
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lanes = tmem + ((warp * 32u) << 16);   // this warp's 32 lanes
+    const uint32_t b = saddr(bar);
+    const uint32_t x0 = saddr(sm + tt::X0), hb = saddr(sm + tt::H), da = saddr(sm + tt::DA), db = saddr(sm + tt::DB);
+    const uint32_t w0 = saddr(sm + tt::W0), w1 = saddr(sm + tt::W1), w4 = saddr(sm + tt::W4);
+    uint32_t phase = 0;
+    bool ok = true;
     const float inv = 1.0f / (3.0f * (float)n);
     float lsum = 0.0f;
-    for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
-        const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
-        const bool v0 = r0 < n, v1 = r1 < n;
-        float x0[NI], x1[NI];
-#pragma unroll
-        for (int i = 0; i < NI; i++) {
-            x0[i] = v0 ? x[(uint64_t)r0 * NI + i] : 0.0f;
-            x1[i] = v1 ? x[(uint64_t)r1 * NI + i] : 0.0f;
+    const uint32_t tiles = (n + 127) / 128;
+    uint32_t acc_g = 0;   // gradient accumulators hold a previous tile's sums
+    // all threads wait for the MMAs of one commit; any thread that gives up stops the CTA
+    auto sync_mma = [&](int where, uint32_t tile) -> bool {
+        const bool late = !wait(b, phase);
+        if (__syncthreads_or(late)) {
+            if (t == 0) dev_error(status, TGX_ERR_TIMEOUT, where, tile);
+            return false;   // phase stays on the commit still in flight
         }
-        uint32_t H[4][4][4];
-        float y[4];
-        forward_tile(sw, x0, x1, g, t, H, y, enc, r0, r1);
-        // output delta: columns 2t, 2t+1 of rows r0 (y0,y1) and r1 (y2,y3)
-        float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        phase ^= 1u;
+        fence_after();
+        return true;
+    };
+    auto publish = [&]() {   // this thread's shared-memory writes, visible to the tensor core
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+    };
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const uint32_t row = tile * 128 + t;
+        const bool valid = row < n;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int col = 2 * t + (q & 1);
-            const bool row_ok = (q < 2) ? v0 : v1;
-            const uint32_t r = (q < 2) ? r0 : r1;
-            if (col < NO && row_ok) {
-                const float tv = target[(uint64_t)r * NO + col];
-                const float den = y[q] * y[q] + 0.01f;
-                const float res = y[q] - tv;
-                lsum += res * res / den;
-                d[q] = 2.0f * res / den * inv;
-            }
-        }
-        // dy as an A fragment (16 x 16, columns 8..15 zero)
-        uint32_t A[4][4];
-        uint32_t ady[4] = {pack_bf16(d[0], d[1]), pack_bf16(d[2], d[3]), 0u, 0u};
+        for (int i = 0; i < NI; i++) encode_input(sm + tt::X0, i, (int)t, valid ? x[(uint64_t)row * NI + i] : 0.0f);
         {
-            __nv_bfloat16* p0 = dy + (uint64_t)r0 * 16 + 2 * t;
-            __nv_bfloat16* p1 = dy + (uint64_t)r1 * 16 + 2 * t;
-            *reinterpret_cast<uint32_t*>(p0) = ady[0];
-            *reinterpret_cast<uint32_t*>(p1) = ady[1];
-            *reinterpret_cast<uint32_t*>(p0 + 8) = 0u;
-            *reinterpret_cast<uint32_t*>(p1 + 8) = 0u;
+            const float z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            put8(sm + tt::X0, KG0 - 1, (int)t, z);   // features 216..223
         }
-        // delta into h4: dy * W4 (B = W4^T slice [in][k]), masked by h4 > 0
-        float acc[8][4];
+        // ---- forward ----
+        uint32_t mask[4][2];
+        float y[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-            const __nv_bfloat16* row = sw + B_W4T + (nt * 8 + g) * S4T + 2 * t;
-            mma16816(acc[nt], ady, lds32(row), lds32(row + 8));
-        }
-        const int WT[3] = {B_W3T, B_W2T, B_W1T};
-        for (int l = 3; l >= 0; l--) {
-            // mask with relu'(h_{l+1}) where h_{l+1} = H[l]; pack as A; store the delta
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const uint32_t m0 = H[l][k][0], m1 = H[l][k][1], m2 = H[l][k][2], m3 = H[l][k][3];
-                A[k][0] = pack_bf16(bf_lo(m0) > 0.0f ? acc[2 * k][0] : 0.0f, bf_hi(m0) > 0.0f ? acc[2 * k][1] : 0.0f);
-                A[k][1] = pack_bf16(bf_lo(m1) > 0.0f ? acc[2 * k][2] : 0.0f, bf_hi(m1) > 0.0f ? acc[2 * k][3] : 0.0f);
-                A[k][2] = pack_bf16(bf_lo(m2) > 0.0f ? acc[2 * k + 1][0] : 0.0f, bf_hi(m2) > 0.0f ? acc[2 * k + 1][1] : 0.0f);
-                A[k][3] = pack_bf16(bf_lo(m3) > 0.0f ? acc[2 * k + 1][2] : 0.0f, bf_hi(m3) > 0.0f ? acc[2 * k + 1][3] : 0.0f);
-                __nv_bfloat16* q0 = dlt + ((uint64_t)l * np + r0) * NH + k * 16 + 2 * t;
-                __nv_bfloat16* q1 = dlt + ((uint64_t)l * np + r1) * NH + k * 16 + 2 * t;
-                __nv_bfloat16* h0 = act + ((uint64_t)l * np + r0) * NH + k * 16 + 2 * t;
-                __nv_bfloat16* h1 = act + ((uint64_t)l * np + r1) * NH + k * 16 + 2 * t;
-                if (v0) {
-                    *reinterpret_cast<uint32_t*>(q0) = A[k][0];
-                    *reinterpret_cast<uint32_t*>(q0 + 8) = A[k][2];
-                    *reinterpret_cast<uint32_t*>(h0) = m0;
-                    *reinterpret_cast<uint32_t*>(h0 + 8) = m2;
+        for (int l = 0; l < 5 && ok; l++) {
+            publish();
+            if (t == 0) {
+                fence_after();
+                if (l == 0) {
+                    for (int k = 0; k < KG0 / 2; k++)
+                        mma(tmem + tt::ACC, sdesc(x0 + 2 * k * 2048, 2048, 128), sdesc(w0 + 2 * k * 1024, 1024, 128),
+                            idesc(64), k > 0);
+                } else if (l < 4) {
+                    const uint32_t a = hb + (l - 1) * tt::TILE64, w = w1 + (l - 1) * KGH * 8 * 128;
+                    for (int k = 0; k < KGH / 2; k++)
+                        mma(tmem + tt::ACC, sdesc(a + 2 * k * 2048, 2048, 128), sdesc(w + 2 * k * 1024, 1024, 128),
+                            idesc(64), k > 0);
+                } else {
+                    const uint32_t a = hb + 3 * tt::TILE64;
+                    for (int k = 0; k < KGH / 2; k++)
+                        mma(tmem + tt::ACC, sdesc(a + 2 * k * 2048, 2048, 128), sdesc(w4 + 2 * k * 256, 256, 128),
+                            idesc(16), k > 0);
                 }
-                if (v1) {
-                    *reinterpret_cast<uint32_t*>(q1) = A[k][1];
-                    *reinterpret_cast<uint32_t*>(q1 + 8) = A[k][3];
-                    *reinterpret_cast<uint32_t*>(h1) = m1;
-                    *reinterpret_cast<uint32_t*>(h1 + 8) = m3;
+                commit(b);
+            }
+            if (!(ok = sync_mma(50 + l, tile))) break;
+            float v[16];
+            if (l < 4) {
+                unsigned char* h = sm + tt::H + l * tt::TILE64;
+                mask[l][0] = mask[l][1] = 0u;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    ld16(lanes + tt::ACC + q * 16, v);
+                    ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        v[j] = fmaxf(v[j], 0.0f);
+                        if (v[j] > 0.0f) mask[l][q >> 1] |= 1u << ((q & 1) * 16 + j);
+                    }
+                    put8(h, 2 * q, (int)t, v);
+                    put8(h, 2 * q + 1, (int)t, v + 8);
+                }
+            } else {
+                ld16(lanes + tt::ACC, v);
+                ld_wait();
+                y[0] = v[0]; y[1] = v[1]; y[2] = v[2];
+            }
+        }
+        if (!ok) break;
+        // ---- output delta (relative L2), into DB ----
+        {
+            float d[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) d[j] = 0.0f;
+            if (valid) {
+#pragma unroll
+                for (int c = 0; c < NO; c++) {
+                    const float tv = target[(uint64_t)row * NO + c];
+                    const float den = y[c] * y[c] + 0.01f;
+                    const float res = y[c] - tv;
+                    lsum += res * res / den;
+                    d[c] = 2.0f * res / den * inv;
                 }
             }
-            if (l == 0) break;
-            // delta into h_l: delta_{l} * W_l, B = W_l^T [in][out]
-            layer<4>(A, sw + WT[3 - l], SH, acc, g, t);
+            put8(sm + tt::DB, 0, (int)t, d);
+            put8(sm + tt::DB, 1, (int)t, d + 8);
+        }
+        // ---- backward: stage s propagates through W_{4-s} and accumulates its gradient ----
+#pragma unroll
+        for (int s = 0; s < 5 && ok; s++) {
+            publish();
+            const uint32_t din = (s & 1) ? da : db;        // delta at the output of the layer
+            if (t == 0) {
+                fence_after();
+                const int l = 4 - s;                       // weight layer
+                if (s < 4) {
+                    // next delta (pre-mask) = din * W_l: B = W_l read MN-major (N = inputs, K = outputs)
+                    if (l == 4) {
+                        mma(tmem + tt::ACC, sdesc(din, 2048, 128), sdesc(w4, 128, 256), tt::idesc_t(64, false, true), 0u);
+                    } else {
+                        const uint32_t w = w1 + (l - 1) * KGH * 8 * 128;
+                        for (int k = 0; k < KGH / 2; k++)
+                            mma(tmem + tt::ACC, sdesc(din + 2 * k * 2048, 2048, 128), sdesc(w + 2 * k * 128, 128, 1024),
+                                tt::idesc_t(64, false, true), k > 0);
+                    }
+                }
+                // dW_l^T += input_l^T din: A = the layer's input tile, B = din, both MN-major, K = samples
+                const uint32_t nout = l == 4 ? 16u : 64u;
+                const uint32_t gcol = l == 4 ? tt::G4 : l == 3 ? tt::G3 : l == 2 ? tt::G2 : l == 1 ? tt::G1 : tt::G0A;
+                const uint32_t ain = l == 0 ? x0 : hb + (l - 1) * tt::TILE64;
+                const int parts = l == 0 ? 2 : 1;
+                for (int part = 0; part < parts; part++)
+                    for (int k = 0; k < 8; k++)
+                        mma(tmem + gcol + part * 64u, sdesc(ain + part * 16 * 2048 + 2 * k * 128, 128, 2048),
+                            sdesc(din + 2 * k * 128, 128, 2048), tt::idesc_t(nout, true, true), (acc_g | k) ? 1u : 0u);
+                commit(b);
+            }
+            if (!(ok = sync_mma(60 + s, tile))) break;
+            if (s == 4) break;
+            // mask with relu'(z) of the layer's input and store the next delta into the other tile
+            const int ml = 3 - s;                           // h_{ml+1} = input of W_{4-s}
+            unsigned char* dout = sm + ((s & 1) ? tt::DB : tt::DA);
+            float v[16];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ld16(lanes + tt::ACC + q * 16, v);
+                ld_wait();
+                const uint32_t m = mask[ml][q >> 1] >> ((q & 1) * 16);
+#pragma unroll
+                for (int j = 0; j < 16; j++) v[j] = ((m >> j) & 1u) && valid ? v[j] : 0.0f;
+                put8(dout, 2 * q, (int)t, v);
+                put8(dout, 2 * q + 1, (int)t, v + 8);
+            }
+        }
+        acc_g = 1u;
+    }
+    // ---- this CTA's gradient sums into its slice of the partial buffer ----
+    fence_before();
+    __syncthreads();
+    fence_after();
+    float* P = partial + (uint64_t)blockIdx.x * N_PARAMS;
+    {
+        float v[16];
+#pragma unroll 1
+        for (int blk = 0; blk < 6; blk++) {
+            const uint32_t col = blk == 0 ? tt::G0A : blk == 1 ? tt::G0B : blk == 2 ? tt::G1 : blk == 3 ? tt::G2
+                               : blk == 4 ? tt::G3 : tt::G4;
+            const int i = (blk == 1 ? 128 : 0) + (int)t;                  // layer input (TMEM row)
+            const int ni = blk < 2 ? NE : NH;
+            const int off = blk < 2 ? OFF_W0 : blk == 2 ? OFF_W1 : blk == 3 ? OFF_W2 : blk == 4 ? OFF_W3 : OFF_W4;
+            const int nq = blk == 5 ? 1 : 4;
+#pragma unroll 1
+            for (int q = 0; q < nq; q++) {
+                ld16(lanes + col + q * 16, v);
+                ld_wait();
+                if (i < ni) {
+                    const int no = blk == 5 ? NO : 16;
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (j < no) P[off + (q * 16 + j) * ni + i] = ok && acc_g ? v[j] : 0.0f;
+                }
+            }
         }
     }
-    // warp-reduce the loss
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if (lane == 0) atomicAdd(loss, lsum * inv);
-}
-
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
-{
-    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
-}
-
-// Weight gradients of all five layers in one launch: grad_l[o][i] +=
-// sum_s D_l[s][o] * X_l[s][i].  A CTA owns one 16 (o) x 64 (i) tile of one
-// layer and a range of 4 * chunk samples; each of its warps reduces `chunk`
-// samples on the tensor cores (ldmatrix.trans tiles of 16 samples), the four
-// partial tiles are summed in shared memory and added to the gradient with
-// FP32 atomics.
-struct WgradLayer
-{
-    const __nv_bfloat16* D;   // [s][ds], o < no real
-    const __nv_bfloat16* X;   // [s][xs], i < ni real
-    float* grad;              // [no][ni]
-    int ds, no, xs, ni;
-    int o_tiles, i_groups;
-    uint32_t first_cta;
-};
-struct WgradArgs
-{
-    WgradLayer l[5];
-    uint32_t n, chunk, ctas_per_tile;
-};
-
-__global__ void __launch_bounds__(128) k_mlp_wgrad(WgradArgs args)
-{
-    __shared__ __align__(16) __nv_bfloat16 sD[4][16][24];
-    __shared__ __align__(16) __nv_bfloat16 sX[4][16][72];
-    __shared__ float red[3][32][33];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
-    int li = 0;
-#pragma unroll
-    for (int k = 1; k < 5; k++)
-        if (blockIdx.x >= args.l[k].first_cta) li = k;
-    const WgradLayer& L = args.l[li];
-    const uint32_t local = blockIdx.x - L.first_cta;
-    const uint32_t tile = local / args.ctas_per_tile, part = local % args.ctas_per_tile;
-    const int ot = (int)(tile % L.o_tiles), ig = (int)(tile / L.o_tiles);
-    const uint32_t s_begin = (part * 4 + warp) * args.chunk;
-    const uint32_t s_end = min(args.n, s_begin + args.chunk);
-    float acc[8][4];
-#pragma unroll
-    for (int q = 0; q < 8; q++) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
-    for (uint32_t s0 = s_begin; s0 < s_end; s0 += 16) {
-        // stage 16 samples x 16 o of D and 16 samples x 64 i of X
-        __syncwarp();
-        for (int e = lane; e < 16 * 2; e += 32) {
-            const int r = e >> 1, h = e & 1;
-            const uint32_t s = s0 + r;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            const int oc = ot * 16 + h * 8;
-            if (s < s_end && oc < L.ds) v = *reinterpret_cast<const uint4*>(L.D + (uint64_t)s * L.ds + oc);
-            *reinterpret_cast<uint4*>(&sD[warp][r][h * 8]) = v;
-        }
-        for (int e = lane; e < 16 * 8; e += 32) {
-            const int r = e >> 3, h = e & 7;
-            const uint32_t s = s0 + r;
-            const int ic = ig * 64 + h * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (s < s_end && ic < L.xs) v = *reinterpret_cast<const uint4*>(L.X + (uint64_t)s * L.xs + ic);
-            *reinterpret_cast<uint4*>(&sX[warp][r][h * 8]) = v;
-        }
-        __syncwarp();
-        // A = D^T (16 o x 16 s): matrices (s0-7,o0-7), (s0-7,o8-15), (s8-15,o0-7), (s8-15,o8-15)
-        uint32_t a[4];
-        {
-            const int mtx = lane >> 3, r = lane & 7;
-            const int srow = (mtx & 2) ? 8 + r : r;
-            const int ocol = (mtx & 1) ? 8 : 0;
-            ldsm_x4_trans(a[0], a[1], a[2], a[3], &sD[warp][srow][ocol]);
-        }
-        // B = X (16 s x 8 i) per n-tile: matrices (s0-7, i), (s8-15, i) for two n-tiles per ldmatrix
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int mtx = lane >> 3, r = lane & 7;
-            const int srow = (mtx & 1) ? 8 + r : r;
-            const int icol = q * 16 + ((mtx & 2) ? 8 : 0);
-            uint32_t b0, b1, b2, b3;
-            ldsm_x4_trans(b0, b1, b2, b3, &sX[warp][srow][icol]);
-            mma16816(acc[2 * q], a, b0, b1);
-            mma16816(acc[2 * q + 1], a, b2, b3);
-        }
-    }
-    // sum the four warps' tiles in shared memory, then one atomic per element
-    if (warp > 0) {
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-#pragma unroll
-            for (int e = 0; e < 4; e++) red[warp - 1][lane][q * 4 + e] = acc[q][e];
-    }
+    if ((t & 31) == 0) atomicAdd(loss, lsum * inv);
+    if (!ok) wait(b, phase);   // let MMAs still in flight land (bounded) before the columns are freed
+    fence_before();
     __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-#pragma unroll
-            for (int e = 0; e < 4; e++) acc[q][e] += red[0][lane][q * 4 + e] + red[1][lane][q * 4 + e] + red[2][lane][q * 4 + e];
-        // C rows o = ot*16 + g (+8), cols i = ig*64 + q*8 + 2t (+1)
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int i = ig * 64 + q * 8 + 2 * t;
-            const int o0 = ot * 16 + g, o1 = o0 + 8;
-            if (o0 < L.no && i < L.ni) atomicAdd(&L.grad[o0 * L.ni + i], acc[q][0]);
-            if (o0 < L.no && i + 1 < L.ni) atomicAdd(&L.grad[o0 * L.ni + i + 1], acc[q][1]);
-            if (o1 < L.no && i < L.ni) atomicAdd(&L.grad[o1 * L.ni + i], acc[q][2]);
-            if (o1 < L.no && i + 1 < L.ni) atomicAdd(&L.grad[o1 * L.ni + i + 1], acc[q][3]);
-        }
-    }
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tt::TMEM_COLS) : "memory");
 }
 
-// bf16 image position of master parameter p (forward layout), and of its transpose (or -1)
-__device__ __forceinline__ void image_pos(int p, int& fwd, int& bwd)
+// Sum of the CTAs' gradient slices, in CTA order, added to the gradient.
+__global__ void __launch_bounds__(256) k_mlp_reduce(const float* __restrict__ partial, uint32_t n_parts,
+                                                   float* __restrict__ g)
 {
-    bwd = -1;
-    if (p < OFF_W1) { const int o = p / NE, i = p % NE; fwd = B_W0 + o * S0 + i; return; }
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N_PARAMS) return;
+    float s = 0.0f;
+    for (uint32_t c = 0; c < n_parts; c++) s += partial[(uint64_t)c * N_PARAMS + p];
+    g[p] += s;
+}
+
+// bf16 image position of master parameter p
+__device__ __forceinline__ int image_pos(int p)
+{
+    if (p < OFF_W1) return B_W0 + (p / NE) * S0 + p % NE;
     if (p < OFF_W4) {
-        const int l = (p - OFF_W1) / (NH * NH), r = (p - OFF_W1) % (NH * NH), o = r / NH, i = r % NH;
-        fwd = B_W1 + l * NH * SH + o * SH + i;
-        bwd = B_W1T + l * NH * SH + i * SH + o;
-        return;
+        const int l = (p - OFF_W1) / (NH * NH), r = (p - OFF_W1) % (NH * NH);
+        return B_W1 + l * NH * SH + (r / NH) * SH + r % NH;
     }
-    const int r = p - OFF_W4, o = r / NH, i = r % NH;
-    fwd = B_W4 + o * SH + i;
-    bwd = B_W4T + i * S4T + o;
+    const int r = p - OFF_W4;
+    return B_W4 + (r / NH) * SH + r % NH;
 }
 
 __global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
@@ -672,20 +622,14 @@ __global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ w, float* 
     v[p] = vp;
     const float wp = w[p] - lr * (mp / c1) / (sqrtf(vp / c2) + eps);
     w[p] = wp;
-    int f, b;
-    image_pos(p, f, b);
-    img[f] = __float2bfloat16_rn(wp);
-    if (b >= 0) img[b] = __float2bfloat16_rn(wp);
+    img[image_pos(p)] = __float2bfloat16_rn(wp);
 }
 
 __global__ void k_mlp_image(const float* __restrict__ w, __nv_bfloat16* __restrict__ img)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N_PARAMS) return;
-    int f, b;
-    image_pos(p, f, b);
-    img[f] = __float2bfloat16_rn(w[p]);
-    if (b >= 0) img[b] = __float2bfloat16_rn(w[p]);
+    img[image_pos(p)] = __float2bfloat16_rn(w[p]);
 }
 
 }  // namespace
@@ -790,8 +734,6 @@ extern "C" tgx_status tgx_cache_set_weights(tgx_ctx* c, tgx_cache* k, const floa
     return TGX_OK;
 }
 
-static int all_smem() { return B_TOTAL * 2; }
-
 // inference of n queries (min(n, *d_n) when d_n is given) on the tcgen05 kernel
 static tgx_status cache_forward(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t n, const float* d_x,
                                 float* d_rgb)
@@ -826,41 +768,17 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
 {
     static bool attr = false;
     if (!attr) {
-        TGX_CUDA(cudaFuncSetAttribute(k_mlp_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, all_smem()));
+        TGX_CUDA(cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tt::SMEM));
         attr = true;
     }
-    const uint64_t np = ((uint64_t)n + 15) / 16 * 16;
-    const size_t bytes = np * NEP * 2 + 4 * np * NH * 2 * 2 + np * 16 * 2;
-    TGX_TRY(devbuf_reserve(k->scratch, bytes));
-    __nv_bfloat16* enc = (__nv_bfloat16*)k->scratch.ptr;
-    __nv_bfloat16* act = enc + np * NEP;
-    __nv_bfloat16* dlt = act + 4 * np * NH;
-    __nv_bfloat16* dy = dlt + 4 * np * NH;
+    const uint32_t tiles = (n + 127) / 128;
+    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)c->num_sms);
+    TGX_TRY(devbuf_reserve(k->scratch, (size_t)grid * N_PARAMS * 4));
+    float* partial = (float*)k->scratch.ptr;
     TGX_CUDA(cudaMemsetAsync(k->loss, 0, 4, c->stream));
-    const uint32_t tiles = (uint32_t)(np / 16);
-    const uint32_t grid = std::min<uint32_t>((tiles + 3) / 4, (uint32_t)c->num_sms * 4);
-    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, 128, all_smem(), k_mlp_fwd_bwd, k->img, n, d_x, d_t, enc, act, dlt, dy, k->loss);
-    // weight gradients of all layers: D [s][o] against the layer input X [s][i]
-    WgradArgs a;
-    a.n = n;
-    a.chunk = 256;
-    a.ctas_per_tile = (n + 4 * a.chunk - 1) / (4 * a.chunk);
-    const WgradLayer ls[5] = {
-        {dlt + 0 * np * NH, enc, k->g + OFF_W0, NH, NH, NEP, NE, 0, 0, 0},
-        {dlt + 1 * np * NH, act + 0 * np * NH, k->g + OFF_W1, NH, NH, NH, NH, 0, 0, 0},
-        {dlt + 2 * np * NH, act + 1 * np * NH, k->g + OFF_W2, NH, NH, NH, NH, 0, 0, 0},
-        {dlt + 3 * np * NH, act + 2 * np * NH, k->g + OFF_W3, NH, NH, NH, NH, 0, 0, 0},
-        {dy, act + 3 * np * NH, k->g + OFF_W4, 16, NO, NH, NH, 0, 0, 0},
-    };
-    uint32_t ctas = 0;
-    for (int l = 0; l < 5; l++) {
-        a.l[l] = ls[l];
-        a.l[l].o_tiles = (ls[l].no + 15) / 16;
-        a.l[l].i_groups = (ls[l].ni + 63) / 64;
-        a.l[l].first_cta = ctas;
-        ctas += (uint32_t)(a.l[l].o_tiles * a.l[l].i_groups) * a.ctas_per_tile;
-    }
-    TGX_LAUNCH(c, TR_MLP_WGRAD, ctas, 128, 0, k_mlp_wgrad, a);
+    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, k->img, n, d_x, d_t, partial, k->loss,
+               c->d_status);
+    TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, partial, grid, k->g);
     return TGX_OK;
 }
 

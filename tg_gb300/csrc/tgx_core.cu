@@ -144,7 +144,7 @@ extern "C" void tgx_destroy(tgx_ctx* c)
 static const char* kTraceNames[TR_COUNT] = {
     "k_object_setup", "k_vis_cluster_setup", "k_vis_count", "k_vis_prefix", "k_vis_scan", "k_vis_bin_fill", "k_vis_tiles",
     "k_svo_candidates", "k_svo_alloc", "k_svo_voxelize", "k_svo_pyramid", "k_svo_trace", "k_gi_paths", "k_trace_queue", "k_mlp_forward",
-    "k_mlp_fwd_bwd", "k_mlp_wgrad", "k_mlp_adam"};
+    "k_mlp_train_tc", "k_mlp_reduce", "k_mlp_adam"};
 
 static cudaEvent_t trace_event(tgx_ctx* c)
 {
