@@ -842,7 +842,7 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
 #define VIS_TILES_ARGS w.records, w.rects, (const uint32_t*)w.bins, w.tile_off, w.tile_order, d_vc, n_views, \
                        s->d_bits, s->d_inv_rot, d_outs, w.counters, c->d_status
     if (threads == 64) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 16>), VIS_TILES_ARGS);
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), VIS_TILES_ARGS);
     } else if (threads == 128) {
         TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), VIS_TILES_ARGS);
     } else if (threads == 256) {
