@@ -570,38 +570,56 @@ __device__ __forceinline__ int slab_class(float ox, float oy, float oz, float dx
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Instantiated per block size (= tile pixels) so the register budget can be
-// bounded for the occupancy each size needs.
-template <int kThreads, int kMinBlocks>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRecord* __restrict__ records,
-                                                   const uint2* __restrict__ rects,
-                                                   const uint32_t* __restrict__ bins,
-                                                   const uint32_t* __restrict__ tile_off,
-                                                   const uint32_t* __restrict__ tile_order,
-                                                   const ViewConst* __restrict__ views, uint32_t n_views,
-                                                   const uint32_t* __restrict__ bits,
-                                                   const float* __restrict__ inv_rot,
-                                                   unsigned long long* const* __restrict__ outs,
-                                                   uint32_t* __restrict__ counters, tgx_dev_status* __restrict__ status)
+// One job's tile inputs: a scene's records and bins for its views.
+struct TileJob
 {
-    __shared__ VisRecord s_rec[kBatch];
-    __shared__ __align__(128) uint32_t s_bits[kBatch * 16];
-    __shared__ __align__(8) unsigned long long s_bar;
-    __shared__ uint32_t s_view;
-    __shared__ uint32_t s_n;
+    const VisRecord* records;
+    const uint2* rects;
+    const uint32_t* bins;
+    const uint32_t* tile_off;
+    const uint32_t* tile_order;
+    const ViewConst* views;
+    const uint32_t* bits;
+    const float* inv_rot;
+    unsigned long long* const* outs;
+    uint32_t* counters;
+    uint32_t n_views, n_tiles;
+    uint32_t first;              // the job's first item in a multi-job work queue
+};
 
-    const uint32_t tile = tile_order[blockIdx.x];
-    // bins overflowed this frame: walk every record and test its rectangle (slow, exact)
-    const bool scan_all = counters[C_OVERFLOW] != 0u;
+struct TileSmem
+{
+    VisRecord rec[kBatch];
+    __align__(128) uint32_t bits[kBatch * 16];
+    __align__(8) unsigned long long bar;
+    uint32_t view, n;
+};
+
+__device__ __forceinline__ void tile_smem_init(TileSmem& sm)
+{
     if (threadIdx.x == 0) {
-        uint32_t v = 0;
-        while (v + 1 < n_views && views[v + 1].tile_base <= tile) v++;
-        s_view = v;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&s_bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&sm.bar)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+}
+
+// Tile `slot` (in the job's heavy-first order) of one job: every pixel's
+// nearest packed word over the clusters binned to the tile.  `phase` is the
+// parity of the CTA's bulk-copy mbarrier, carried across tiles.
+__device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSmem& sm, uint32_t& phase,
+                                         tgx_dev_status* __restrict__ status)
+{
+    __syncthreads();   // the CTA's previous tile is done with the shared state
+    const uint32_t tile = J.tile_order[slot];
+    // bins overflowed this frame: walk every record and test its rectangle (slow, exact)
+    const bool scan_all = J.counters[C_OVERFLOW] != 0u;
+    if (threadIdx.x == 0) {
+        uint32_t v = 0;
+        while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
+        sm.view = v;
+    }
     __syncthreads();
-    const ViewConst& vc = views[s_view];
+    const ViewConst& vc = J.views[sm.view];
     const uint32_t lt = tile - vc.tile_base;
     const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
     const uint32_t px = tx * vc.tile_w + threadIdx.x % vc.tile_w;
@@ -623,49 +641,48 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRec
     uint32_t best_d24 = 0xffffffu;
     uint32_t cur_obj = 0xffffffffu;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
-    const uint32_t begin = scan_all ? 0u : tile_off[tile];
-    const uint32_t end = scan_all ? counters[C_RECORDS] : tile_off[tile + 1];
-    uint32_t phase = 0;
+    const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
+    const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
     for (uint32_t base = begin; base < end; base += kBatch) {
         uint32_t n = min(kBatch, end - base);
         __syncthreads();   // the previous batch is fully consumed
         if (!scan_all) {
-            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) s_rec[k] = records[bins[base + k]];
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) sm.rec[k] = J.records[J.bins[base + k]];
             __syncthreads();
             // every pixel already closer than the nearest bucket left: the tile is done
-            const uint32_t lo = bucket_lo(depth_bucket(s_rec[0].d24_lb));
+            const uint32_t lo = bucket_lo(depth_bucket(sm.rec[0].d24_lb));
             if (__syncthreads_and(!valid || best_d24 < lo)) break;
         } else {
             // keep the records of this view whose tile rectangle holds this tile
-            if (threadIdx.x == 0) s_n = 0;
+            if (threadIdx.x == 0) sm.n = 0;
             __syncthreads();
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-                const VisRecord r = records[base + k];
-                const uint2 q = rects[base + k];
-                if (r.view == s_view && tx >= (q.x & 0xffffu) && tx <= (q.y & 0xffffu) && ty >= (q.x >> 16) &&
+                const VisRecord r = J.records[base + k];
+                const uint2 q = J.rects[base + k];
+                if (r.view == sm.view && tx >= (q.x & 0xffffu) && tx <= (q.y & 0xffffu) && ty >= (q.x >> 16) &&
                     ty <= (q.y >> 16))
-                    s_rec[atomicAdd(&s_n, 1u)] = r;
+                    sm.rec[atomicAdd(&sm.n, 1u)] = r;
             }
             __syncthreads();
-            n = s_n;
+            n = sm.n;
             if (n == 0) continue;
         }
         // stage the n bitmasks (64 B each) with bulk async copies completing on the mbarrier
         if (threadIdx.x == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&s_bar)), "r"(n * 64u) : "memory");
-        // order this thread's earlier generic reads of s_bits before the async-proxy writes
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&sm.bar)), "r"(n * 64u) : "memory");
+        // order this thread's earlier generic reads of sm.bits before the async-proxy writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-            const uint32_t* src = bits + (uint64_t)s_rec[k].cluster_idx * 16u;
+            const uint32_t* src = J.bits + (uint64_t)sm.rec[k].cluster_idx * 16u;
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];"
-                         :: "r"(smem_addr(&s_bits[k * 16])), "l"(src), "r"(smem_addr(&s_bar)) : "memory");
+                         :: "r"(smem_addr(&sm.bits[k * 16])), "l"(src), "r"(smem_addr(&sm.bar)) : "memory");
         }
         // bounded wait on the barrier phase
         {
             uint32_t done = 0, polls = 0;
             while (!done) {
                 asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                             : "=r"(done) : "r"(smem_addr(&s_bar)), "r"(phase) : "memory");
+                             : "=r"(done) : "r"(smem_addr(&sm.bar)), "r"(phase) : "memory");
                 if (++polls >= kWaitLimit && !done) {
                     dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
                     break;
@@ -675,13 +692,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRec
         phase ^= 1u;
         if (!valid) continue;
         for (uint32_t k = 0; k < n; k++) {
-            const VisRecord& r = s_rec[k];
+            const VisRecord& r = sm.rec[k];
             if (best_d24 < r.d24_lb) continue;   // cannot produce a smaller word
             if (r.object_idx != cur_obj) {
                 // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
                 // object's shared linear part (see k_object_setup)
                 cur_obj = r.object_idx;
-                const float* L = inv_rot + 9u * cur_obj;
+                const float* L = J.inv_rot + 9u * cur_obj;
                 const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
                 const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
                 const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
@@ -693,12 +710,59 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(const VisRec
             }
             const int sc = slab_class(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz);
             if (sc == kMiss) continue;
-            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit, &s_bits[k * 16],
-                                                  r.cluster_pointer, vc.far_plane, &counters[C_DDA_OVERRUN]);
+            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit, &sm.bits[k * 16],
+                                                  r.cluster_pointer, vc.far_plane, &J.counters[C_DDA_OVERRUN]);
             if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
         }
     }
-    if (valid) outs[s_view][(size_t)py * vc.width + px] = best;
+    if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+}
+
+// Instantiated per block size (= tile pixels) so the register budget can be
+// bounded for the occupancy each size needs.  One CTA per tile of one job.
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
+{
+    __shared__ TileSmem sm;
+    tile_smem_init(sm);
+    uint32_t phase = 0;
+    vis_tile(J, blockIdx.x, sm, phase, status);
+}
+
+// Persistent form over several jobs (scenes, each with its views): CTAs take
+// tiles from one work queue in job order, each job's tiles heavy-first, until
+// all jobs' tiles are done.
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles_queue(const TileJob* __restrict__ jobs,
+                                                                          uint32_t n_jobs, uint32_t total,
+                                                                          uint32_t* __restrict__ queue,
+                                                                          tgx_dev_status* __restrict__ status)
+{
+    __shared__ TileSmem sm;
+    __shared__ TileJob s_job;
+    __shared__ uint32_t s_slot, s_jobidx;
+    tile_smem_init(sm);
+    if (threadIdx.x == 0) s_jobidx = 0xffffffffu;
+    uint32_t phase = 0;
+    for (;;) {
+        __syncthreads();   // the previous tile is done with s_job
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(queue, 1u);
+            s_slot = 0xffffffffu;
+            if (item < total) {
+                uint32_t lo = 0, hi = n_jobs - 1;   // the last job whose first item is <= item
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
+                }
+                if (lo != s_jobidx) { s_job = jobs[lo]; s_jobidx = lo; }
+                s_slot = item - s_job.first;
+            }
+        }
+        __syncthreads();
+        if (s_slot == 0xffffffffu) break;
+        vis_tile(s_job, s_slot, sm, phase, status);
+    }
 }
 
 }  // namespace
@@ -807,7 +871,27 @@ static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_of
     w.tile_order = w.tile_off + (n_tiles + 1);
 }
 
-enum VisPhase { VIS_ALL = 0, VIS_TO_SCAN = 1, VIS_FROM_BINS = 2 };
+enum VisPhase { VIS_ALL = 0, VIS_TO_SCAN = 1, VIS_FROM_BINS = 2, VIS_NO_TILES = 3 };
+
+static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs, uint32_t n_views,
+                        uint32_t n_tiles, const VisScratch& w)
+{
+    TileJob J;
+    J.records = w.records;
+    J.rects = w.rects;
+    J.bins = w.bins;
+    J.tile_off = w.tile_off;
+    J.tile_order = w.tile_order;
+    J.views = d_vc;
+    J.bits = s->d_bits;
+    J.inv_rot = s->d_inv_rot;
+    J.outs = d_outs;
+    J.counters = w.counters;
+    J.n_views = n_views;
+    J.n_tiles = n_tiles;
+    J.first = 0;
+    return J;
+}
 
 // The launches of one frame (n_views views of scene s, view table d_vc / d_outs
 // on the device): all of them, or the part up to the tile scan, or the rest.
@@ -838,19 +922,57 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
                w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
                n_tiles, w.bin_capacity, c->d_status);
+    if (phase == VIS_NO_TILES) return TGX_OK;
+    const TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
     const uint32_t threads = c->tile_w * c->tile_h;
-#define VIS_TILES_ARGS w.records, w.rects, (const uint32_t*)w.bins, w.tile_off, w.tile_order, d_vc, n_views, \
-                       s->d_bits, s->d_inv_rot, d_outs, w.counters, c->d_status
     if (threads == 64) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), VIS_TILES_ARGS);
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
     } else if (threads == 128) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), VIS_TILES_ARGS);
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), J, c->d_status);
     } else if (threads == 256) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), VIS_TILES_ARGS);
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), J, c->d_status);
     } else {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), VIS_TILES_ARGS);
+        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), J, c->d_status);
     }
-#undef VIS_TILES_ARGS
+    return TGX_OK;
+}
+
+// The tile stage of several jobs as one persistent launch over a work queue
+// (d_jobs: the jobs' TileJob records with their first queue items; d_queue
+// zeroed before the launch).
+// Resident CTAs of the persistent tile kernel for the context's tile size
+// (an occupancy query: call it outside stream capture).
+template <int kThreads, int kMinBlocks>
+static uint32_t vis_queue_ctas_t(tgx_ctx* c)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles_queue<kThreads, kMinBlocks>, kThreads, 0) !=
+            cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return (uint32_t)c->num_sms * (uint32_t)per_sm;
+}
+
+static uint32_t vis_queue_ctas(tgx_ctx* c)
+{
+    const uint32_t threads = c->tile_w * c->tile_h;
+    if (threads == 64) return vis_queue_ctas_t<64, 20>(c);
+    if (threads == 128) return vis_queue_ctas_t<128, 10>(c);
+    if (threads == 256) return vis_queue_ctas_t<256, 5>(c);
+    return vis_queue_ctas_t<1024, 1>(c);
+}
+
+static tgx_status vis_launch_queue(tgx_ctx* c, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total, uint32_t* d_queue,
+                                   uint32_t ctas)
+{
+    TGX_CUDA(cudaMemsetAsync(d_queue, 0, 4, c->stream));
+    const uint32_t threads = c->tile_w * c->tile_h;
+    const uint32_t grid = std::max(1u, std::min(ctas, total));
+#define QUEUE_ARGS d_jobs, n_jobs, total, d_queue, c->d_status
+    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, 64, 0, (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
+    else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, 128, 0, (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
+    else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, 256, 0, (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
+    else TGX_LAUNCH(c, TR_VIS_TILES, grid, 1024, 0, (k_vis_tiles_queue<1024, 1>), QUEUE_ARGS);
+#undef QUEUE_ARGS
     return TGX_OK;
 }
 
@@ -966,6 +1088,8 @@ struct tgx_frame_graph
         std::vector<uint64_t*> outs;
         size_t table_off, ptr_off;
         uint32_t n_tiles;
+        uint64_t rec_cap, bin_cap;               // this job's own scratch
+        size_t scratch_off;
     };
     std::vector<Job> jobs;
     uint32_t kernels = 0;
@@ -989,10 +1113,15 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     tgx_frame_graph* g = new (std::nothrow) tgx_frame_graph();
     if (!g) return TGX_ERR_OUT_OF_MEMORY;
     auto fail = [&](tgx_status st) { cudaStreamSynchronize(c->stream); frame_graph_free(g); return st; };
-    // sizes, and one uncaptured frame per job to size the bins
-    size_t table_bytes = 0, tile_bytes = 0, off_bytes = 0;
-    uint64_t rec_cap = 0, bin_cap = (size_t)1 << 20;
+    // sizes, and one uncaptured frame per job to size its bins
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t table_bytes = 0, scratch_bytes = 0;
+    uint32_t total_tiles = 0;
     std::vector<std::vector<unsigned char>> tables(n_jobs);
+    auto job_bytes = [&](const tgx_frame_graph::Job& job) {
+        return al((size_t)job.rec_cap * (sizeof(VisRecord) + sizeof(uint2))) + 256 + al(vis_tile_bytes(job.n_tiles)) +
+               al((size_t)(job.n_tiles + 1) * 4 * 2) + al((size_t)job.bin_cap * 4);
+    };
     for (uint32_t j = 0; j < n_jobs; j++) {
         const tgx_vis_job& jb = jobs[j];
         if (!jb.scene || !jb.views || !jb.d_visbuf || !jb.n_views) {
@@ -1009,20 +1138,20 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         job.outs.assign(jb.d_visbuf, jb.d_visbuf + jb.n_views);
         tables[j] = vis_view_table(c, jb.views, jb.n_views, jb.d_visbuf, job.n_tiles, job.ptr_off);
         job.table_off = table_bytes;
-        table_bytes += (tables[j].size() + 255) & ~(size_t)255;
-        tile_bytes = std::max(tile_bytes, vis_tile_bytes(job.n_tiles));
-        off_bytes = std::max(off_bytes, (size_t)(job.n_tiles + 1) * 4 * 2);
-        rec_cap = std::max<uint64_t>(rec_cap, (uint64_t)jb.scene->n_cluster_pointers * jb.n_views);
-        bin_cap = std::max<uint64_t>(bin_cap, std::max<uint64_t>((uint64_t)job.n_tiles * 64, (uint64_t)entries * 3 / 2));
+        table_bytes += al(tables[j].size());
+        job.rec_cap = (uint64_t)jb.scene->n_cluster_pointers * jb.n_views;
+        job.bin_cap = std::max<uint64_t>(1u << 16, std::max<uint64_t>((uint64_t)job.n_tiles * 64, (uint64_t)entries * 3 / 2));
+        if (job.rec_cap > 0xffffffffull || job.bin_cap > 0xffffffffull || (uint64_t)total_tiles + job.n_tiles > 0xffffffffull) {
+            tgx_set_error("tgx_frame_graph_create: job %u has too many (view, cluster) pairs or tiles", j);
+            return fail(TGX_ERR_CAPACITY);
+        }
+        total_tiles += job.n_tiles;
+        job.scratch_off = scratch_bytes;
+        scratch_bytes += job_bytes(job);
         g->jobs.push_back(std::move(job));
     }
-    if (rec_cap > 0xffffffffull || bin_cap > 0xffffffffull) {
-        tgx_set_error("tgx_frame_graph_create: a job has too many (view, cluster) pairs");
-        return fail(TGX_ERR_CAPACITY);
-    }
-    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t rec_bytes = al((size_t)rec_cap * (sizeof(VisRecord) + sizeof(uint2)));
-    const size_t total = table_bytes + rec_bytes + 256 + al(tile_bytes) + al(off_bytes) + al((size_t)bin_cap * 4);
+    const size_t jobs_off = table_bytes + scratch_bytes;
+    const size_t total = jobs_off + al((size_t)n_jobs * sizeof(TileJob)) + 256;
     if (cudaMalloc(&g->d_mem, total) != cudaSuccess) {
         cudaGetLastError();
         tgx_set_error("tgx_frame_graph_create: out of device memory (%zu bytes)", total);
@@ -1034,38 +1163,95 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
             tgx_set_error("tgx_frame_graph_create: view table upload failed");
             return fail(TGX_ERR_CUDA);
         }
-    VisScratch w;
-    char* p = base + table_bytes;
-    w.records = (VisRecord*)p;
-    w.rec_cap = (uint32_t)rec_cap;
-    w.rects = (uint2*)(w.records + rec_cap);
-    p += rec_bytes;
-    w.counters = (uint32_t*)p;
-    p += 256;
-    uint32_t* tile_cnt = (uint32_t*)p;
-    p += al(tile_bytes);
-    uint32_t* tile_off = (uint32_t*)p;
-    p += al(off_bytes);
-    w.bins = (uint32_t*)p;
-    w.bin_capacity = (uint32_t)bin_cap;
-    // capture (no trace events inside the graph)
+    // each job's own scratch, so the jobs' sorting passes can run side by side
+    std::vector<VisScratch> ws(n_jobs);
+    std::vector<TileJob> tjobs(n_jobs);
+    for (uint32_t j = 0; j < n_jobs; j++) {
+        const tgx_frame_graph::Job& job = g->jobs[j];
+        VisScratch& w = ws[j];
+        char* p = base + table_bytes + job.scratch_off;
+        w.records = (VisRecord*)p;
+        w.rec_cap = (uint32_t)job.rec_cap;
+        w.rects = (uint2*)(w.records + job.rec_cap);
+        p += al((size_t)job.rec_cap * (sizeof(VisRecord) + sizeof(uint2)));
+        w.counters = (uint32_t*)p;
+        p += 256;
+        uint32_t* tile_cnt = (uint32_t*)p;
+        p += al(vis_tile_bytes(job.n_tiles));
+        uint32_t* tile_off = (uint32_t*)p;
+        p += al((size_t)(job.n_tiles + 1) * 4 * 2);
+        w.bins = (uint32_t*)p;
+        w.bin_capacity = (uint32_t)job.bin_cap;
+        vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
+        const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
+        unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
+        tjobs[j] = tile_job(job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, w);
+        tjobs[j].first = j ? tjobs[j - 1].first + g->jobs[j - 1].n_tiles : 0u;
+    }
+    TileJob* d_jobs = (TileJob*)(base + jobs_off);
+    uint32_t* d_queue = (uint32_t*)(base + jobs_off + al((size_t)n_jobs * sizeof(TileJob)));
+    if (cudaMemcpy(d_jobs, tjobs.data(), n_jobs * sizeof(TileJob), cudaMemcpyHostToDevice) != cudaSuccess) {
+        tgx_set_error("tgx_frame_graph_create: job table upload failed");
+        return fail(TGX_ERR_CUDA);
+    }
+    const uint32_t queue_ctas = vis_queue_ctas(c);
+    // side streams and events for the fork and join inside the capture
+    const uint32_t n_side = std::min<uint32_t>(n_jobs, 8u);
+    std::vector<cudaStream_t> side(n_side, nullptr);
+    std::vector<cudaEvent_t> done(n_jobs, nullptr);
+    cudaEvent_t fork = nullptr;
+    auto release = [&]() {
+        for (cudaStream_t q : side) if (q) cudaStreamDestroy(q);
+        for (cudaEvent_t e : done) if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+    };
+    bool ok = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
+    for (uint32_t k = 0; k < n_side && ok; k++) ok = cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking) == cudaSuccess;
+    for (uint32_t j = 0; j < n_jobs && ok; j++) ok = cudaEventCreateWithFlags(&done[j], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        release();
+        tgx_set_error("tgx_frame_graph_create: stream or event creation failed");
+        return fail(TGX_ERR_CUDA);
+    }
+    // capture (no trace events inside the graph): every job's passes up to the
+    // bins on its side stream, then one persistent tile launch over all jobs
     const bool tracing = c->trace.enabled;
     c->trace.enabled = false;
     const uint64_t launches0 = c->launches;
-    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaStream_t main_stream = c->stream;
+    if (cudaStreamBeginCapture(main_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         c->trace.enabled = tracing;
+        release();
         tgx_set_error("tgx_frame_graph_create: stream capture refused (%s)", cudaGetErrorString(cudaGetLastError()));
         return fail(TGX_ERR_CUDA);
     }
     tgx_status st = TGX_OK;
-    for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++) {
-        const tgx_frame_graph::Job& job = g->jobs[j];
-        vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
+    if (n_jobs == 1) {
+        // one job: its passes and the one-CTA-per-tile launch, no fork
+        const tgx_frame_graph::Job& job = g->jobs[0];
         const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
         unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
-        st = vis_launch(c, job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, w);
+        st = vis_launch(c, job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, ws[0], VIS_ALL);
+        goto captured;
     }
+    if (cudaEventRecord(fork, main_stream) != cudaSuccess) st = TGX_ERR_CUDA;
+    for (uint32_t k = 0; k < n_side && st == TGX_OK; k++)
+        if (cudaStreamWaitEvent(side[k], fork, 0) != cudaSuccess) st = TGX_ERR_CUDA;
+    for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++) {
+        const tgx_frame_graph::Job& job = g->jobs[j];
+        c->stream = side[j % n_side];
+        const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
+        unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
+        st = vis_launch(c, job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, ws[j], VIS_NO_TILES);
+        if (st == TGX_OK && cudaEventRecord(done[j], c->stream) != cudaSuccess) st = TGX_ERR_CUDA;
+    }
+    c->stream = main_stream;
+    for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++)
+        if (cudaStreamWaitEvent(main_stream, done[j], 0) != cudaSuccess) st = TGX_ERR_CUDA;
+    if (st == TGX_OK) st = vis_launch_queue(c, d_jobs, n_jobs, total_tiles, d_queue, queue_ctas);
+captured:
     const cudaError_t ce = cudaStreamEndCapture(c->stream, &g->graph);
+    release();
     c->trace.enabled = tracing;
     g->kernels = (uint32_t)(c->launches - launches0);
     c->launches = launches0;
@@ -1329,8 +1515,21 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
     NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, bins,
               n_tiles, kNaBins, status);
-    NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), records, rects, bins, tile_off, tile_order, d_vc, 1u,
-              d_voxel_bits, inv_rot, d_outs, counters, status);
+    TileJob J;
+    J.records = records;
+    J.rects = rects;
+    J.bins = bins;
+    J.tile_off = tile_off;
+    J.tile_order = tile_order;
+    J.views = d_vc;
+    J.bits = d_voxel_bits;
+    J.inv_rot = inv_rot;
+    J.outs = d_outs;
+    J.counters = counters;
+    J.n_views = 1;
+    J.n_tiles = n_tiles;
+    J.first = 0;
+    NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), J, status);
     if (out_error) {
         tgx_dev_status hs;
         TGX_CUDA(cudaMemcpyAsync(&hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st));
