@@ -631,6 +631,9 @@ def main() -> None:
             if _ < 2:
                 svo.close()
         info = svo.info()
+        # the traversal's DDA steps per ray-queue round, tuned on this frame
+        from tg_gb300.autotune import tune_gi_traversal
+        trace_steps, trace_tuning = tune_gi_traversal(ctx, sc, svo, view, out, device=local, use_cache=False)
         # incremental update after 8 objects move (tgx_scene_set_objects + tgx_svo_update),
         # against the full builds above; the scene is moved back (untimed) for the GI frames
         rng = np.random.default_rng(7)
@@ -672,6 +675,8 @@ def main() -> None:
                     "pairs": int(info.n_pairs), "device_mb": round(info.device_bytes / 2**20, 1)},
             "gi_plain_frame_ms": gi_ms,
             "gi_config": "1 bounce, 4 spp, Philox seed 2, <=256 SVO steps, sun + sky",
+            "gi_trace_steps": trace_steps,
+            "gi_trace_autotune_ms": trace_tuning,
             "gi_bounce_rays_per_s": hits * 4 / (gi_ms * 1e-3),
             "gi_device_status": int(err.code),
         }

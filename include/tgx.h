@@ -128,6 +128,8 @@ typedef struct tgx_config
     uint32_t tile_w;           /* visibility tile width in pixels (0 = default 16) */
     uint32_t tile_h;           /* visibility tile height in pixels (0 = default 16) */
     uint32_t flags;            /* TGX_FLAG_* bits, 0 for defaults */
+    uint32_t trace_steps;      /* SVO traversal: DDA steps a lane runs between refills of the
+                                  ray queue (1..256, 0 = default 8); see tgx_set_trace_steps */
 } tgx_config;
 
 /* Keeps the visibility bin storage at its minimum (64 entries) so frames
@@ -154,6 +156,10 @@ const char* tgx_last_error_string(void);
 
 tgx_status  tgx_create(const tgx_config* config, tgx_ctx** out_ctx);
 void        tgx_destroy(tgx_ctx* ctx);
+/* The SVO traversal's DDA steps per lane between refills of its ray queue
+ * (1..256): fewer refill idle lanes sooner, more amortise the refill.  The
+ * autotuner (tg_gb300/autotune.py) picks it per scene; default 8. */
+tgx_status  tgx_set_trace_steps(tgx_ctx* ctx, uint32_t steps);
 /* The cudaStream_t the context launches on (as void*). */
 void*       tgx_stream(tgx_ctx* ctx);
 tgx_status  tgx_sync(tgx_ctx* ctx);

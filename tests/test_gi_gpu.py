@@ -209,3 +209,25 @@ def test_pixel_point_network_lowers_the_error(ctx):
         finally:
             cache.close()
     svo.close(); sc.close()
+
+
+def test_trace_steps_per_round_changes_no_result(ctx):
+    """tgx_set_trace_steps only reschedules the persistent traversal: GI is bit-equal for every setting."""
+    import torch
+    s, sc, svo, view, vis = _scene_setup(ctx, seed=29)
+    params = tg.gi_params(spp=2, bounces=2, seed=4)
+    outs = []
+    for k in (1, 3, 8, 64):
+        ctx.set_trace_steps(k)
+        rgb = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+        ctx.gi_render(sc, svo, view, vis, params, rgb)
+        outs.append(rgb)
+    ctx.set_trace_steps(8)
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    for o in outs[1:]:
+        assert torch.equal(outs[0], o)
+    for bad in (0, 257):
+        with pytest.raises(tg.TgxError):
+            ctx.set_trace_steps(bad)
+    svo.close(); sc.close()

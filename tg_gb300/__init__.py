@@ -100,7 +100,7 @@ class SceneDesc(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("tile_w", C.c_uint32),
-                ("tile_h", C.c_uint32), ("flags", C.c_uint32)]
+                ("tile_h", C.c_uint32), ("flags", C.c_uint32), ("trace_steps", C.c_uint32)]
 
 
 class DeviceError(C.Structure):
@@ -150,6 +150,7 @@ EXPORTS = [
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
+    "tgx_set_trace_steps",
 ]
 
 
@@ -181,6 +182,7 @@ def _load() -> C.CDLL:
         "tgx_scene_download": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "tgx_shade": (i32, [vp, vp, vp, vp, u32, vp]),
         "tgx_svo_update": (i32, [vp, vp, vp, C.POINTER(u32)]),
+        "tgx_set_trace_steps": (i32, [vp, u32]),
         "tgx_scene_set_objects": (i32, [vp, vp, u32, u32, vp]),
         "tgx_svo_destroy": (None, [vp, vp]),
         "tgx_svo_get_info": (i32, [vp, vp, C.POINTER(SvoInfo)]),
@@ -339,8 +341,10 @@ def decode(packed: int):
 class Context:
     """tgx_ctx: one device, one stream."""
 
-    def __init__(self, device: int = 0, stream: int | None = None, tile: tuple[int, int] = (16, 16), flags: int = 0):
-        cfg = Config(device=device, stream=stream or 0, tile_w=tile[0], tile_h=tile[1], flags=flags)
+    def __init__(self, device: int = 0, stream: int | None = None, tile: tuple[int, int] = (16, 16), flags: int = 0,
+                 trace_steps: int = 0):
+        cfg = Config(device=device, stream=stream or 0, tile_w=tile[0], tile_h=tile[1], flags=flags,
+                     trace_steps=trace_steps)
         h = C.c_void_p()
         check(lib.tgx_create(C.byref(cfg), C.byref(h)), "tgx_create")
         self.handle = h
@@ -368,6 +372,10 @@ class Context:
 
     def sync(self) -> None:
         check(lib.tgx_sync(self.handle), "tgx_sync")
+
+    def set_trace_steps(self, steps: int) -> None:
+        """tgx_set_trace_steps: DDA steps per lane between ray-queue refills."""
+        check(lib.tgx_set_trace_steps(self.handle, steps), "tgx_set_trace_steps")
 
     def launches(self) -> int:
         return int(lib.tgx_launch_count(self.handle))

@@ -80,6 +80,10 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
         tgx_set_error("tgx_create: tile %ux%u must hold 32..1024 pixels in whole warps", tw, th);
         return TGX_ERR_INVALID_ARGUMENT;
     }
+    if (cfg->trace_steps > 256) {
+        tgx_set_error("tgx_create: trace_steps %u outside 1..256", cfg->trace_steps);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
     TGX_CUDA(cudaSetDevice(cfg->device));
     tgx_ctx* c = new (std::nothrow) tgx_ctx();
     if (!c) return TGX_ERR_OUT_OF_MEMORY;
@@ -88,11 +92,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     c->tile_h = th;
     c->flags = cfg->flags;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
-    // tuning override of the traversal's steps per queue round (1..256)
-    if (const char* e = getenv("TGX_TRACE_STEPS_PER_ROUND")) {
-        const long v = strtol(e, nullptr, 10);
-        if (v >= 1 && v <= 256) c->trace_steps_per_round = (uint32_t)v;
-    }
+    if (cfg->trace_steps) c->trace_steps_per_round = cfg->trace_steps;
     if (cfg->stream) {
         c->stream = (cudaStream_t)cfg->stream;
     } else {
@@ -247,6 +247,16 @@ extern "C" tgx_status tgx_sync(tgx_ctx* c)
 {
     if (!c) return TGX_ERR_INVALID_ARGUMENT;
     TGX_CUDA(cudaStreamSynchronize(c->stream));
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_set_trace_steps(tgx_ctx* c, uint32_t steps)
+{
+    if (!c || steps < 1 || steps > 256) {
+        tgx_set_error("tgx_set_trace_steps: steps %u outside 1..256", steps);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    c->trace_steps_per_round = steps;
     return TGX_OK;
 }
 
