@@ -702,10 +702,16 @@ def main() -> None:
     algo_bytes = 8 * rays + 72 * n_vis + 96 * len(scene.objects)
     achieved = algo_bytes / (top_ms * 1e-3) / 1e9
 
-    traffic = None
+    traffic, limiter = None, None
     tf = ROOT / "profiles" / "vis_tiles_traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+        prof = json.loads(tf.read_text())
+        traffic = prof.get("dram_bytes_per_launch")
+        if "smsp__issue_active" in prof:
+            # the tile kernel's real ceiling is instruction issue, not HBM: its ncu issue-slot fraction
+            limiter = {"kind": "issue", "smsp__issue_active": prof["smsp__issue_active"],
+                       "threads_per_warp_instruction": prof.get("threads_per_warp_instruction"),
+                       "what": prof.get("limiter"), "source": "profiles/vis_tiles_1080p_512obj.md"}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
@@ -725,7 +731,8 @@ def main() -> None:
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "algorithmic_bytes": algo_bytes,
-                     "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback"},
+                     "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback",
+                     **({"limiter": limiter} if limiter else {})},
         "clocks": clocks.summary(),
         "hit_pixels": hits,
         **gi_report,
