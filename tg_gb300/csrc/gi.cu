@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __rest
                     empty = true;
                 } else {
                     const Ray ray = item < n_a ? ra[item] : rb[item - n_a];
-                    const int res = svo_trace_begin(s, ray.o, ray.d, r);
+                    const int res = svo_trace_begin(s, occ_off, ray.o, ray.d, max_steps, r);
                     if (res == kTraceRunning) have = true;
                     else write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
                 }

@@ -16,9 +16,10 @@
 //                   the weight gradients of 128-sample tiles in one kernel;
 //                   gradients summed in TMEM over a CTA's tiles, then written
 //                   to the CTA's slice of a partial buffer.
-//   k_mlp_reduce    adds the slices in a fixed order (deterministic).
-//   k_mlp_adam      Adam on the FP32 master weights; refreshes the BF16
+//   k_mlp_adam      sums the slices in a fixed order (deterministic), then
+//                   Adam on the FP32 master weights; refreshes the BF16
 //                   image the kernels stage from.
+//   k_mlp_reduce    the same sum into the gradient, for tgx_cache_gradient.
 
 #include "tgx_internal.cuh"
 
@@ -243,10 +244,26 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
     uint32_t phase = 0;
     bool ok = true;
     const uint32_t tiles = (n + M - 1) / M;
+    // this thread's query of the group's next tile, loaded one tile ahead so
+    // its HBM latency hides behind the current tile's layers
+    float xn[NI];
+    {
+        const uint32_t row = (blockIdx.x * 2 + g) * M + gt;
+#pragma unroll
+        for (int i = 0; i < NI; i++) xn[i] = row < n ? __ldg(&x[(uint64_t)row * NI + i]) : 0.0f;
+    }
     for (uint32_t tile = blockIdx.x * 2 + g; tile < tiles && ok; tile += gridDim.x * 2) {
         const uint32_t row = tile * M + gt;
+        float xc[NI];
 #pragma unroll
-        for (int i = 0; i < NI; i++) encode_input(ga + A0, i, (int)gt, row < n ? x[(uint64_t)row * NI + i] : 0.0f);
+        for (int i = 0; i < NI; i++) xc[i] = xn[i];
+        {
+            const uint32_t next = (tile + gridDim.x * 2) * M + gt;
+#pragma unroll
+            for (int i = 0; i < NI; i++) xn[i] = next < n ? __ldg(&x[(uint64_t)next * NI + i]) : 0.0f;
+        }
+#pragma unroll
+        for (int i = 0; i < NI; i++) encode_input(ga + A0, i, (int)gt, xc[i]);
         {
             const float z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             put8(ga + A0, KG0 - 1, (int)gt, z);   // features 216..223
@@ -608,13 +625,18 @@ __device__ __forceinline__ int image_pos(int p)
     return B_W4 + (r / NH) * SH + r % NH;
 }
 
+// The gradient is g plus the n_parts slices of `partial` (the training
+// kernel's per-CTA sums) added in CTA order, as k_mlp_reduce adds them.
 __global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                                                 float* __restrict__ g, float lr, float b1, float b2, float eps,
+                                                 float* __restrict__ g, const float* __restrict__ partial,
+                                                 uint32_t n_parts, float lr, float b1, float b2, float eps,
                                                  float c1, float c2, __nv_bfloat16* __restrict__ img)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N_PARAMS) return;
-    const float gp = g[p];
+    float sum = 0.0f;
+    for (uint32_t c = 0; c < n_parts; c++) sum += partial[(uint64_t)c * N_PARAMS + p];
+    const float gp = g[p] + sum;
     g[p] = 0.0f;
     const float mp = b1 * m[p] + (1.0f - b1) * gp;
     const float vp = b2 * v[p] + (1.0f - b2) * gp * gp;
@@ -764,7 +786,10 @@ tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, ui
 }
 
 // Computes the batch gradient into the accumulator (no update); returns the loss if out_loss.
-static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t)
+// The fused training kernel over n samples; leaves the per-CTA gradient
+// slices in k->scratch (*parts of them).
+static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t,
+                                   uint32_t* parts)
 {
     static bool attr = false;
     if (!attr) {
@@ -778,7 +803,16 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
     TGX_CUDA(cudaMemsetAsync(k->loss, 0, 4, c->stream));
     TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, k->img, n, d_x, d_t, partial, k->loss,
                c->d_status);
-    TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, partial, grid, k->g);
+    *parts = grid;
+    return TGX_OK;
+}
+
+// ... and their sum added to the gradient
+static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t)
+{
+    uint32_t parts = 0;
+    TGX_TRY(cache_grad_parts(c, k, n, d_x, d_t, &parts));
+    TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, (const float*)k->scratch.ptr, parts, k->g);
     return TGX_OK;
 }
 
@@ -799,12 +833,13 @@ extern "C" tgx_status tgx_cache_train_step(tgx_ctx* c, tgx_cache* k, uint32_t n,
                                            float lr)
 {
     if (!c || !k || !n || !d_x || !d_t) return TGX_ERR_INVALID_ARGUMENT;
-    TGX_TRY(cache_grad(c, k, n, d_x, d_t));
+    uint32_t parts = 0;
+    TGX_TRY(cache_grad_parts(c, k, n, d_x, d_t, &parts));
     k->step++;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
     const float c1 = (float)(1.0 - pow((double)b1, (double)k->step)), c2 = (float)(1.0 - pow((double)b2, (double)k->step));
-    TGX_LAUNCH(c, TR_MLP_ADAM, (N_PARAMS + 255) / 256, 256, 0, k_mlp_adam, k->w, k->m, k->v, k->g, lr, b1, b2, eps, c1, c2,
-               k->img);
+    TGX_LAUNCH(c, TR_MLP_ADAM, (N_PARAMS + 255) / 256, 256, 0, k_mlp_adam, k->w, k->m, k->v, k->g,
+               (const float*)k->scratch.ptr, parts, lr, b1, b2, eps, c1, c2, k->img);
     return TGX_OK;
 }
 

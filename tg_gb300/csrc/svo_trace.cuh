@@ -88,9 +88,34 @@ struct RayState
 
 constexpr int kTraceRunning = -2;
 
+// Occupancy bit of cell c (grid coordinates at log2 size g); tv is the slot +
+// 1 of the 32^3 block holding c, needed below the block level (g < 5).
+__device__ __forceinline__ bool svo_occupied(const SvoDev& s, const uint32_t* occ_off, uint32_t g, const int32_t c[3],
+                                             uint32_t tv)
+{
+    const bool sub = g < 5u;
+    const uint32_t m = sub ? (32u >> g) : (s.B >> (g - 5u));
+    const uint32_t mk = sub ? m - 1u : 0xffffffffu;
+    const uint32_t v = (((uint32_t)c[2] & mk) * m + ((uint32_t)c[1] & mk)) * m + ((uint32_t)c[0] & mk);
+    const uint32_t* base = !sub ? s.occ + occ_off[(g - 5u) & 15u]
+                         : g == 0 ? s.pool + (uint64_t)(tv - 1u) * 1024u
+                                  : s.sub + (uint64_t)(tv - 1u) * 32u + (g == 3 ? 16u : 0u);
+    return (__ldg(&base[v >> 5]) >> (v & 31u)) & 1u;
+}
+
 // Sets up a ray.  Returns kTraceRunning when the DDA has to run, else the
-// result (0: the ray misses the SVO cube or has no direction).
-__device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const float o[3], const float d[3], RayState& r)
+// result (0: the ray misses the SVO cube or has no direction; 1: the entry
+// voxel is set).
+//
+// The DDA starts where the top-down descent from the root would first find an
+// empty cell, found bottom-up instead: the entry point's voxel, then its
+// ancestors (the cell of every level that holds the point is the voxel's
+// coordinates shifted right, with the same boundary rule) until an occupied
+// one.  The descent's iterations are counted into r.steps as if they had
+// run, so every result and the step budget stay those of the top-down walk.
+// occ_off: the pyramid level offsets (shared memory in the persistent kernel).
+__device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* occ_off, const float o[3],
+                                               const float d[3], uint32_t max_steps, RayState& r)
 {
     const float E = (float)(1u << s.L);
 #pragma unroll
@@ -123,10 +148,41 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const float o[3]
     r.li = s.NL - 1;
     r.g = s.L - 1u;
     r.tv = 0;
-    const float isz = __int_as_float((int)((127u - r.g) << 23));
-    const int32_t hi = (1 << (s.L - r.g)) - 1;
+    if (max_steps < s.NL) {   // the budget could run out inside the descent: run it
+        const float isz = __int_as_float((int)((127u - r.g) << 23));
+        const int32_t hi = (1 << (s.L - r.g)) - 1;
 #pragma unroll
-    for (int a = 0; a < 3; a++) r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], 0, hi);
+        for (int a = 0; a < 3; a++) r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], 0, hi);
+        return kTraceRunning;
+    }
+    int32_t cv[3];
+    const int32_t vhi = (1 << s.L) - 1;
+#pragma unroll
+    for (int a = 0; a < 3; a++) cv[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), 1.0f, r.st[a], 0, vhi);
+    const uint32_t tv = __ldg(&s.table[((uint64_t)(cv[2] >> 5) * s.B + (uint64_t)(cv[1] >> 5)) * s.B + (uint64_t)(cv[0] >> 5)]);
+    // coarsest empty level holding the point (-1: the voxel itself is set)
+    int32_t e = -1;
+    for (uint32_t li = 0; li < s.NL; li++) {
+        const uint32_t g = svo_level_log2(s.L, li);
+        const int32_t c[3] = {cv[0] >> g, cv[1] >> g, cv[2] >> g};
+        const bool occ = g < 5u && tv == 0u ? false : svo_occupied(s, occ_off, g, c, tv);
+        if (occ) break;
+        e = (int32_t)li;
+    }
+    if (e < 0) {   // the descent reaches the voxel: NL iterations, a hit
+        r.steps = s.NL;
+        r.li = 0;
+        r.g = 0;
+        r.tv = tv;
+        r.c[0] = cv[0]; r.c[1] = cv[1]; r.c[2] = cv[2];
+        return 1;
+    }
+    r.li = (uint32_t)e;
+    r.g = svo_level_log2(s.L, (uint32_t)e);
+    r.tv = r.g < 5u ? tv : 0u;
+    r.steps = s.NL - 1u - (uint32_t)e;
+#pragma unroll
+    for (int a = 0; a < 3; a++) r.c[a] = cv[a] >> r.g;
     return kTraceRunning;
 }
 
@@ -212,7 +268,7 @@ static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d
                                 int32_t out_c[3], int32_t& out_axis, uint32_t& out_steps)
 {
     RayState r;
-    int res = svo_trace_begin(s, o, d, r);
+    int res = svo_trace_begin(s, s.occ_off, o, d, max_steps, r);
     if (res == kTraceRunning) res = svo_trace_run(s, s.occ_off, r, max_steps, 0xffffffffu);
     out_steps = r.steps;
     if (res == 1) {
