@@ -12,10 +12,11 @@
 //      whose whole path passes becomes a (cluster, block) pair; the block is
 //      marked in the dense block table.
 //   2. k_svo_alloc       gives every marked block a slot in the block pool.
-//   3. k_svo_voxelize    one warp per pair: the leaf voxelisation of
+//   3. k_svo_voxelize    the pairs grouped by block (count, scan, place),
+//      then one CTA per block, one warp per pair: the leaf voxelisation of
 //      tg__construct_leaf_node (:102-317) -- corner lerp, [0,8)^3 test, bit
-//      fetch -- into a warp-private 4 KiB block image in shared memory, then
-//      coalesced atomicOr of its non-zero words into the pool.
+//      fetch -- into the block's image (and material grid) in shared
+//      memory, written out whole and coalesced, with no global atomics.
 //   4. k_svo_pyramid     bottom-up occupancy: one bit per non-empty block and
 //      per non-empty node of every coarser level, and inside each block one
 //      bit per non-empty 4^3 and 8^3 cell (the sub-block levels the
@@ -36,7 +37,7 @@ namespace {
 constexpr uint32_t kBlockSide = 32;
 constexpr uint32_t kBlockWords = 1024;
 constexpr uint32_t kMark = 0xffffffffu;
-constexpr uint32_t kWarpsPerVoxCta = 4;
+constexpr uint32_t kWarpsPerVoxCta = 16;
 
 struct SvoPair
 {
@@ -281,11 +282,11 @@ __global__ void __launch_bounds__(256) k_svo_alloc(uint32_t* __restrict__ table,
 
 __device__ __forceinline__ uint32_t trim_u32(float v) { return v > 0.0f ? (uint32_t)v : 0u; }
 
-// max of a 16-bit code in place (CAS on the containing aligned word)
-__device__ __forceinline__ void atomic_max_u16(uint16_t* addr, uint32_t val)
+// max of a 16-bit code in place in shared memory (CAS on the containing word)
+__device__ __forceinline__ void smem_max_u16(uint32_t* words, uint32_t idx, uint32_t val)
 {
-    uint32_t* base = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(addr) & ~(uintptr_t)3);
-    const uint32_t shift = (reinterpret_cast<uintptr_t>(addr) & 2) ? 16u : 0u;
+    uint32_t* base = words + (idx >> 1);
+    const uint32_t shift = (idx & 1u) ? 16u : 0u;
     uint32_t old = *base;
     for (int guard = 0; guard < 1 << 20; guard++) {
         if (((old >> shift) & 0xffffu) >= val) return;
@@ -296,22 +297,82 @@ __device__ __forceinline__ void atomic_max_u16(uint16_t* addr, uint32_t val)
     }
 }
 
+// 3a. pairs grouped by their block's slot: counts, one scan, placement
+__global__ void __launch_bounds__(256) k_svo_pair_count(const SvoPair* __restrict__ pairs,
+                                                       const uint32_t* __restrict__ counters, uint32_t pair_capacity,
+                                                       const uint32_t* __restrict__ table, uint32_t* __restrict__ cnt)
+{
+    const uint32_t n = min(counters[S_PAIRS], pair_capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t tv = table[pairs[i].block];
+        if (tv) atomicAdd(&cnt[tv - 1u], 1u);
+    }
+}
+
+// exclusive scan of cnt[0, n) into off[0, n] (off[n] = total): one CTA, each
+// thread a contiguous run
+__global__ void __launch_bounds__(1024) k_svo_pair_scan(const uint32_t* __restrict__ cnt, uint32_t n,
+                                                       uint32_t* __restrict__ off)
+{
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x, per = (n + 1023u) / 1024u;
+    const uint32_t b = min(n, t * per), e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += cnt[i];
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t o = 1; o < 1024u; o <<= 1) {
+        const uint32_t v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = t ? part[t - 1u] : 0u;
+    for (uint32_t i = b; i < e; i++) {
+        off[i] = run;
+        run += cnt[i];
+    }
+    if (t == 1023u) off[n] = part[1023];
+}
+
+__global__ void __launch_bounds__(256) k_svo_pair_fill(const SvoPair* __restrict__ pairs,
+                                                      const uint32_t* __restrict__ counters, uint32_t pair_capacity,
+                                                      const uint32_t* __restrict__ table, const uint32_t* __restrict__ off,
+                                                      uint32_t* __restrict__ cursor, SvoPair* __restrict__ sorted)
+{
+    const uint32_t n = min(counters[S_PAIRS], pair_capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const SvoPair pr = pairs[i];
+        const uint32_t tv = table[pr.block];
+        if (tv) sorted[off[tv - 1u] + atomicAdd(&cursor[tv - 1u], 1u)] = pr;
+    }
+}
+
+// 3b. voxelisation: one CTA per block slot.  Its warps take the block's
+// (cluster, block) pairs; every set voxel goes into the CTA's shared image of
+// the block (and the material codes' maximum into its shared material grid),
+// then the block is written out whole, coalesced, with no global atomics.
+template <bool kMat>
 __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
-    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, const SvoPair* __restrict__ pairs,
-    const uint32_t* __restrict__ counters, uint32_t pair_capacity, const uint32_t* __restrict__ table,
-    uint32_t* __restrict__ pool, const uint8_t* __restrict__ material, uint16_t* __restrict__ mat_pool,
-    float mnx, float mny, float mnz, uint32_t B)
+    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, const SvoPair* __restrict__ sorted,
+    const uint32_t* __restrict__ off, uint32_t* __restrict__ pool, const uint8_t* __restrict__ material,
+    uint16_t* __restrict__ mat_pool, float mnx, float mny, float mnz, uint32_t B)
 {
-    __shared__ uint32_t s_img[kWarpsPerVoxCta][kBlockWords];
+    extern __shared__ __align__(16) uint32_t s_blk[];   // 1024 bit words, then 16384 words of u16 codes
+    __shared__ uint32_t s_cw[kWarpsPerVoxCta][16];       // each warp's current cluster bits
+    uint32_t* img = s_blk;
+    uint32_t* smat = s_blk + kBlockWords;
+    const uint32_t slot = blockIdx.x;
+    const uint32_t pb = off[slot], pe = off[slot + 1];
+    if (pb == pe) return;
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    uint32_t* img = s_img[wid];
-    const uint32_t n_pairs = min(counters[S_PAIRS], pair_capacity);
-    for (uint32_t pi = blockIdx.x * kWarpsPerVoxCta + wid; pi < n_pairs; pi += gridDim.x * kWarpsPerVoxCta) {
-        const SvoPair pr = pairs[pi];
-        const uint32_t tv = table[pr.block];
-        if (tv == 0u) continue;   // allocation failed (recorded in the status word)
-        const uint32_t slot = tv - 1u;
+    const uint32_t words = kBlockWords + (kMat ? 16384u : 0u);
+    for (uint32_t k = threadIdx.x; k < words / 4u; k += blockDim.x)
+        reinterpret_cast<uint4*>(s_blk)[k] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    for (uint32_t pi = pb + wid; pi < pe; pi += kWarpsPerVoxCta) {
+        const SvoPair pr = sorted[pi];
         const uint32_t cp = pr.cluster_pointer;
         const uint32_t ci = cluster_pointers[cp];
         const tgx_object& od = objects[c2o[ci]];
@@ -347,21 +408,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
         const uint32_t x1 = trim_u32(xsub(tmax.x, pmin.x)), y1 = trim_u32(xsub(tmax.y, pmin.y)), z1 = trim_u32(xsub(tmax.z, pmin.z));
         if (x0 >= x1 || y0 >= y1 || z0 >= z1) continue;
 
-        for (uint32_t k = lane; k < kBlockWords; k += 32) img[k] = 0u;
-        __syncwarp();
         const uint32_t nx = x1 - x0, ny = y1 - y0, nz = z1 - z0;
         const uint32_t total = nx * ny * nz;
-        const uint32_t* cb = bits + (uint64_t)ci * 16u;
-        uint32_t cw16[16];
-#pragma unroll
-        for (int k = 0; k < 16; k++) cw16[k] = cb[k];
+        // the block side is exactly 32 unless min is so large that min + extent rounds
+        const bool p32 = pext.x == 32.0f && pext.y == 32.0f && pext.z == 32.0f;
+        // the cluster's 16 bit words, one shared-memory lookup per voxel
+        __syncwarp();
+        if (lane < 16) s_cw[wid][lane] = bits[(uint64_t)ci * 16u + lane];
+        __syncwarp();
+        // t -> (ix, iy, iz) without integer division: t < 2^15 and nx, ny <= 32,
+        // so (t + 0.5) / n lies at least 0.5 / n from an integer while the
+        // float product's error stays below 2^15 / n * 2^-23; truncation is exact
+        const float rnx = 1.0f / (float)nx, rny = 1.0f / (float)ny;
         for (uint32_t t = lane; t < total; t += 32) {
-            const uint32_t ix = x0 + t % nx, iy = y0 + (t / nx) % ny, iz = z0 + t / (nx * ny);
-            const float tz = xdiv(xadd((float)iz, 0.5f), pext.z);
+            const uint32_t q1 = (uint32_t)(((float)t + 0.5f) * rnx);
+            const uint32_t q2 = (uint32_t)(((float)q1 + 0.5f) * rny);
+            const uint32_t ix = x0 + (t - q1 * nx), iy = y0 + (q1 - q2 * ny), iz = z0 + q2;
+            // (i + 0.5) / 32 is an exact scaling: the reciprocal multiply gives the same bits
+            const float tz = p32 ? xmul(xadd((float)iz, 0.5f), 0.03125f) : xdiv(xadd((float)iz, 0.5f), pext.z);
             const float omtz = xsub(1.0f, tz);
-            const float ty = xdiv(xadd((float)iy, 0.5f), pext.y);
+            const float ty = p32 ? xmul(xadd((float)iy, 0.5f), 0.03125f) : xdiv(xadd((float)iy, 0.5f), pext.y);
             const float omty = xsub(1.0f, ty);
-            const float tx = xdiv(xadd((float)ix, 0.5f), pext.x);
+            const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
             const float omtx = xsub(1.0f, tx);
 #define LZ(i, j, comp) xadd(xmul(omtz, bc[i].comp), xmul(tz, bc[j].comp))
             const float pz0x = LZ(0, 4, x), pz0y = LZ(0, 4, y), pz0z = LZ(0, 4, z);
@@ -382,25 +450,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
             const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
             if (cz < 0.0f || cz >= 8.0f) continue;
             const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
-            uint32_t word = 0;
-#pragma unroll
-            for (int k = 0; k < 16; k++) word = (rvi >> 5) == (uint32_t)k ? cw16[k] : word;
+            const uint32_t word = s_cw[wid][rvi >> 5];
             if (word & (1u << (rvi & 31u))) {
                 const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy)),
                                                     (float)ix);
                 atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
-                if (mat_pool)
-                    atomic_max_u16(mat_pool + (uint64_t)slot * 32768u + bvi,
-                                   ((od.lut_idx << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
+                if (kMat) smem_max_u16(smat, bvi, ((od.lut_idx << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
             }
         }
-        __syncwarp();
-        uint32_t* dst = pool + (uint64_t)slot * kBlockWords;
-        for (uint32_t k = lane; k < kBlockWords; k += 32) {
-            const uint32_t v = img[k];
-            if (v) atomicOr(&dst[k], v);
-        }
-        __syncwarp();
+    }
+    __syncthreads();
+    uint4* dst = reinterpret_cast<uint4*>(pool + (uint64_t)slot * kBlockWords);
+    for (uint32_t k = threadIdx.x; k < kBlockWords / 4u; k += blockDim.x) dst[k] = reinterpret_cast<const uint4*>(img)[k];
+    if (kMat) {
+        uint4* md = reinterpret_cast<uint4*>(mat_pool + (uint64_t)slot * 32768u);
+        for (uint32_t k = threadIdx.x; k < 16384u / 4u; k += blockDim.x) md[k] = reinterpret_cast<const uint4*>(smat)[k];
     }
 }
 
@@ -622,8 +686,9 @@ static uint64_t svo_device_bytes(const tgx_svo* s)
 }
 
 // Per-slot arrays (pool, sub masks, non-empty flags, free list, materials)
-// sized for `cap` slots; the first `keep` slots are carried over, the rest
-// start zero.
+// sized for `cap` slots; the first `keep` slots are carried over.  The rest
+// of the small arrays start zero; pool and material slots are written whole
+// by the voxeliser before anything reads them.
 static tgx_status svo_resize_slots(tgx_ctx* c, tgx_svo* s, uint32_t cap, uint32_t keep, bool materials)
 {
     struct Arr { void** p; uint64_t per_slot; };
@@ -642,7 +707,7 @@ static tgx_status svo_resize_slots(tgx_ctx* c, tgx_svo* s, uint32_t cap, uint32_
     for (int a = 0; a < n_arr; a++) {
         const uint64_t kept = (uint64_t)keep * arrs[a].per_slot, total = (uint64_t)cap * arrs[a].per_slot;
         if (kept) TGX_CUDA(cudaMemcpyAsync(fresh[a], *arrs[a].p, kept, cudaMemcpyDeviceToDevice, c->stream));
-        TGX_CUDA(cudaMemsetAsync((char*)fresh[a] + kept, 0, total - kept, c->stream));
+        if (a != 0 && a != 4) TGX_CUDA(cudaMemsetAsync((char*)fresh[a] + kept, 0, total - kept, c->stream));
     }
     TGX_CUDA(cudaStreamSynchronize(c->stream));
     for (int a = 0; a < n_arr; a++) {
@@ -696,12 +761,37 @@ static tgx_status svo_fill(tgx_ctx* c, tgx_svo* s, const tgx_scene* sc, uint32_t
     TGX_CUDA(cudaMemsetAsync(s->d_occ, 0, s->occ_words * 4, c->stream));
     TGX_LAUNCH(c, TR_SVO_ALLOC, grid, 256, 0, k_svo_alloc, s->d_table, n_table, counters, s->d_free, n_free, next_slot,
                s->pool_cap, c->d_status);
-    const uint32_t vgrid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((s->n_pairs + kWarpsPerVoxCta - 1) / kWarpsPerVoxCta,
-                                                                              (uint64_t)c->num_sms * 16));
-    TGX_LAUNCH(c, TR_SVO_VOXELIZE, vgrid, 32 * kWarpsPerVoxCta, 0, k_svo_voxelize, sc->d_objects, sc->d_cluster_pointers,
-               sc->d_c2o, sc->d_bits, (const SvoPair*)c->svo_pairs.ptr, counters,
-               (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair)), s->d_table, s->d_pool, s->d_mat ? sc->d_material : nullptr,
-               s->d_mat, s->mn[0], s->mn[1], s->mn[2], s->B);
+    // group the pairs by block slot: counts, offsets, placement
+    const uint32_t cap = (uint32_t)(c->svo_pairs.bytes / sizeof(SvoPair));
+    const uint64_t n_slots = s->pool_cap;
+    const size_t sort_bytes = (size_t)(n_slots + 1) * 4 * 2 + (size_t)std::max<uint64_t>(s->n_pairs, 1) * sizeof(SvoPair) + 64;
+    TGX_TRY(devbuf_reserve(c->svo_sort, sort_bytes));
+    uint32_t* cnt = (uint32_t*)c->svo_sort.ptr;
+    uint32_t* off = cnt + (n_slots + 1);
+    SvoPair* sorted = (SvoPair*)(((uintptr_t)(off + n_slots + 1) + 15) & ~(uintptr_t)15);
+    const uint32_t pgrid_pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((s->n_pairs + 255) / 256, (uint64_t)c->num_sms * 16));
+    TGX_CUDA(cudaMemsetAsync(cnt, 0, n_slots * 4, c->stream));
+    TGX_LAUNCH(c, TR_SVO_VOXELIZE, pgrid_pairs, 256, 0, k_svo_pair_count, (const SvoPair*)c->svo_pairs.ptr, counters, cap,
+               s->d_table, cnt);
+    TGX_LAUNCH(c, TR_SVO_VOXELIZE, 1, 1024, 0, k_svo_pair_scan, cnt, (uint32_t)n_slots, off);
+    TGX_CUDA(cudaMemsetAsync(cnt, 0, n_slots * 4, c->stream));
+    TGX_LAUNCH(c, TR_SVO_VOXELIZE, pgrid_pairs, 256, 0, k_svo_pair_fill, (const SvoPair*)c->svo_pairs.ptr, counters, cap,
+               s->d_table, off, cnt, sorted);
+    // one CTA per slot: the block's image and material grid in shared memory
+    static bool attr = false;
+    if (!attr) {
+        TGX_CUDA(cudaFuncSetAttribute(k_svo_voxelize<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (kBlockWords + 16384) * 4));
+        attr = true;
+    }
+    if (s->d_mat)
+        TGX_LAUNCH(c, TR_SVO_VOXELIZE, (uint32_t)n_slots, 32 * kWarpsPerVoxCta, (kBlockWords + 16384) * 4,
+                   k_svo_voxelize<true>, sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, sorted, off,
+                   s->d_pool, sc->d_material, s->d_mat, s->mn[0], s->mn[1], s->mn[2], s->B);
+    else
+        TGX_LAUNCH(c, TR_SVO_VOXELIZE, (uint32_t)n_slots, 32 * kWarpsPerVoxCta, kBlockWords * 4, k_svo_voxelize<false>,
+                   sc->d_objects, sc->d_cluster_pointers, sc->d_c2o, sc->d_bits, sorted, off, s->d_pool,
+                   (const uint8_t*)nullptr, (uint16_t*)nullptr, s->mn[0], s->mn[1], s->mn[2], s->B);
     const uint32_t pgrid = (uint32_t)std::min<uint64_t>((n_table * 32 + 255) / 256, (uint64_t)c->num_sms * 32);
     TGX_LAUNCH(c, TR_SVO_PYRAMID, pgrid, 256, 0, k_svo_pyramid, s->d_table, n_table, s->d_pool, s->d_nonempty, s->d_sub,
                s->d_occ, (const uint64_t*)((char*)s->d_occ + svo_occ_off_bytes(s->occ_words)), s->n_levels, s->B, counters);

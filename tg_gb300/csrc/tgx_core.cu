@@ -128,6 +128,8 @@ extern "C" void tgx_destroy(tgx_ctx* c)
     devbuf_free(c->vis_views);
     devbuf_free(c->svo_counters);
     devbuf_free(c->svo_pairs);
+    devbuf_free(c->svo_scratch);
+    devbuf_free(c->svo_sort);
     devbuf_free(c->gi_scratch);
     devbuf_free(c->host_stage);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);

@@ -128,7 +128,8 @@ struct tgx_ctx
     DevBuf svo_counters;   // SVO build counters
     DevBuf svo_pairs;      // (cluster, block) voxelisation pairs
     DevBuf gi_scratch;     // learned-cache GI queries, hits, training batch
-    DevBuf svo_scratch;    // SVO update: dirty-block marks, old object records
+    DevBuf svo_scratch;    // SVO update: dirty-block marks
+    DevBuf svo_sort;       // SVO build: pairs grouped by block slot, per-slot counts and offsets
     uint32_t vis_last_tiles = 0;
     uint64_t vis_last_pairs = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters
