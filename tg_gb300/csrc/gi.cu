@@ -243,14 +243,26 @@ __device__ __forceinline__ void write_hit(RayHit* h, int res, const RayState& r)
 // Persistent traversal of two ray lists: a (n * mul_a rays) then b (n * mul_b
 // rays), n read from the device.  No CTA waits on another: a CTA that starts
 // after the queue is drained exits at once.
-__global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __restrict__ ra, RayHit* __restrict__ ha,
-                                                     uint32_t mul_a, const Ray* __restrict__ rb,
-                                                     RayHit* __restrict__ hb, uint32_t mul_b,
-                                                     const uint32_t* __restrict__ n_dev, uint32_t max_steps,
-                                                     uint32_t steps_per_round, uint32_t* __restrict__ queue,
-                                                     uint32_t* __restrict__ exhausted)
+//
+// A warp sets rays up 32 at a time, one per lane, and parks the ones whose
+// DDA has to run in a per-warp ring of 64 states in shared memory; a lane
+// whose ray ended takes the next parked state.  The set-up (entry slab, the
+// bottom-up start) then runs on full warps instead of on the few lanes that
+// happen to need a ray at a refill.
+constexpr uint32_t kTraceWarps = 4;     // 128 threads
+constexpr uint32_t kRing = 64;          // parked states per warp
+
+__global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, const Ray* __restrict__ ra,
+                                                                  RayHit* __restrict__ ha, uint32_t mul_a,
+                                                                  const Ray* __restrict__ rb, RayHit* __restrict__ hb,
+                                                                  uint32_t mul_b, const uint32_t* __restrict__ n_dev,
+                                                                  uint32_t max_steps, uint32_t steps_per_round,
+                                                                  uint32_t* __restrict__ queue,
+                                                                  uint32_t* __restrict__ exhausted)
 {
     __shared__ uint32_t occ_off[16];
+    __shared__ RayState ring[kTraceWarps][kRing];
+    __shared__ uint32_t ring_item[kTraceWarps][kRing];
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int i = 0; i < 16; i++) occ_off[i] = s.occ_off[i];
@@ -258,31 +270,55 @@ __global__ void __launch_bounds__(128) k_trace_queue(SvoDev s, const Ray* __rest
     __syncthreads();
     const uint32_t n = *n_dev;
     const uint32_t n_a = n * mul_a, n_tot = n_a + n * mul_b;
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     RayState r;
     uint32_t item = 0;
-    bool have = false, empty = false;
+    bool have = false;
+    uint32_t head = 0, count = 0;   // the warp's ring (warp-uniform)
+    bool drained = false;           // the ray queue is exhausted (warp-uniform)
     for (;;) {
-        const bool need = !have && !empty;
-        const uint32_t mask = __ballot_sync(0xffffffffu, need);
-        if (mask) {
-            const uint32_t leader = __ffs(mask) - 1u;
+        const uint32_t need_mask = __ballot_sync(0xffffffffu, !have);
+        const uint32_t n_need = (uint32_t)__popc(need_mask);
+        // set up rays, 32 at a time, until the ring can serve every idle lane
+        while (n_need && count < n_need && !drained) {
             uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(mask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-                item = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
-                if (item >= n_tot) {
-                    empty = true;
-                } else {
-                    const Ray ray = item < n_a ? ra[item] : rb[item - n_a];
-                    const int res = svo_trace_begin(s, occ_off, ray.o, ray.d, max_steps, r);
-                    if (res == kTraceRunning) have = true;
-                    else write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
-                }
+            if (lane == 0) base = atomicAdd(queue, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + 32u >= n_tot) drained = true;
+            const uint32_t it = base + lane;
+            bool running = false;
+            RayState rs;
+            if (it < n_tot) {
+                const Ray ray = it < n_a ? ra[it] : rb[it - n_a];
+                const int res = svo_trace_begin(s, occ_off, ray.o, ray.d, max_steps, rs);
+                if (res == kTraceRunning) running = true;
+                else write_hit(it < n_a ? &ha[it] : &hb[it - n_a], res, rs);
+            }
+            const uint32_t run_mask = __ballot_sync(0xffffffffu, running);
+            if (running) {
+                const uint32_t slot = (head + count + (uint32_t)__popc(run_mask & lt_mask)) & (kRing - 1u);
+                ring[w][slot] = rs;
+                ring_item[w][slot] = it;
+            }
+            count += (uint32_t)__popc(run_mask);
+            __syncwarp();
+        }
+        // idle lanes take parked states in lane order
+        const uint32_t take = min(n_need, count);
+        if (!have) {
+            const uint32_t rank = (uint32_t)__popc(need_mask & lt_mask);
+            if (rank < take) {
+                const uint32_t slot = (head + rank) & (kRing - 1u);
+                r = ring[w][slot];
+                item = ring_item[w][slot];
+                have = true;
             }
         }
-        if (__all_sync(0xffffffffu, empty)) break;
+        head = (head + take) & (kRing - 1u);
+        count -= take;
+        __syncwarp();
+        if (!__any_sync(0xffffffffu, have) && drained && count == 0) break;
         if (have) {
             const int res = svo_trace_run(s, occ_off, r, max_steps, steps_per_round);
             if (res != kTraceRunning) {
