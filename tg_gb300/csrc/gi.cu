@@ -941,13 +941,10 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_resolve, b.roots, &counters[CC_ROOTS], p,
                b.root_hits, qidx, qrgb, hits, q.primary_weight > 0.0f ? pqrgb : nullptr, q.primary_weight,
                primary ? pmean : nullptr, d_rgb);
-    if (primary && q.n_train_primary && cp->train_steps) {
+    const bool train_primary = primary && q.n_train_primary && cp->train_steps;
+    if (train_primary)
         TGX_LAUNCH(c, TR_GI, (q.n_train_primary + 255) / 256, 256, 0, k_gi_primary_batch, p, q, &counters[CC_ROOTS], pqx,
                    pmean, ptx, ptt);
-        const uint32_t per = q.n_train_primary / cp->train_steps;
-        for (uint32_t k = 0; k < cp->train_steps && per; k++)
-            TGX_TRY(tgx_cache_train_step(c, pnet, per, ptx + 9ull * per * k, ptt + 3ull * per * k, cp->lr));
-    }
     if (train) {
         TGX_LAUNCH(c, TR_GI, (q.n_train + 255) / 256, 256, 0, k_gi_target_roots, p, q, hits, counters,
                    (uint32_t)capacity, b.roots, tx, tt);
@@ -956,9 +953,18 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         pp.frame = p.frame | 0x800000u;   // decorrelated from the pixel streams
         TGX_TRY(run_paths(c, s, sc->d_luts, pp, b, &counters[CC_TRAIN_ROOTS], q.n_train, q.train_spp,
                           &counters[CC_QUEUE], exhausted, tt));
-        const uint32_t per = q.n_train / cp->train_steps;
-        for (uint32_t k = 0; k < cp->train_steps && per; k++)
-            TGX_TRY(tgx_cache_train_step(c, cache, per, tx + 9ull * per * k, tt + 3ull * per * k, cp->lr));
+    }
+    // the two networks' Adam steps, side by side in shared launches
+    const uint32_t per = train ? q.n_train / cp->train_steps : 0u;
+    const uint32_t pper = train_primary ? q.n_train_primary / cp->train_steps : 0u;
+    for (uint32_t k = 0; k < cp->train_steps && (per || pper); k++) {
+        tgx_cache* nets[2];
+        uint32_t ns[2];
+        const float *xs[2], *ts[2];
+        uint32_t m = 0;
+        if (per) { nets[m] = cache; ns[m] = per; xs[m] = tx + 9ull * per * k; ts[m] = tt + 3ull * per * k; m++; }
+        if (pper) { nets[m] = pnet; ns[m] = pper; xs[m] = ptx + 9ull * pper * k; ts[m] = ptt + 3ull * pper * k; m++; }
+        TGX_TRY(cache_train_pair(c, nets, ns, xs, ts, m, cp->lr));
     }
     return TGX_OK;
 }

@@ -382,14 +382,36 @@ __host__ __device__ constexpr uint32_t idesc_t(uint32_t n, bool ta, bool tb)
 
 }  // namespace tt
 
-__global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ wimg, uint32_t n,
-                                                                const float* __restrict__ x,
-                                                                const float* __restrict__ target,
-                                                                float* __restrict__ partial, float* __restrict__ loss,
-                                                                tgx_dev_status* __restrict__ status)
+// One network's training batch in a launch that may carry two networks
+// (the cache's two networks train side by side): CTAs first_cta ..
+// first_cta + n_ctas - 1 of the grid work on it.
+struct TrainJob
+{
+    const __nv_bfloat16* wimg;
+    const float* x;
+    const float* target;
+    float* partial;
+    float* loss;
+    uint32_t n, first_cta, n_ctas;
+};
+struct TrainJobs
+{
+    TrainJob j[2];
+};
+
+__global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs, tgx_dev_status* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     using namespace tc;
+    const bool second = blockIdx.x >= jobs.j[1].first_cta;   // field by field: no local copy of the table
+    const __nv_bfloat16* wimg = second ? jobs.j[1].wimg : jobs.j[0].wimg;
+    const float* x = second ? jobs.j[1].x : jobs.j[0].x;
+    const float* target = second ? jobs.j[1].target : jobs.j[0].target;
+    float* partial = second ? jobs.j[1].partial : jobs.j[0].partial;
+    float* loss = second ? jobs.j[1].loss : jobs.j[0].loss;
+    const uint32_t n = second ? jobs.j[1].n : jobs.j[0].n;
+    const uint32_t cta = blockIdx.x - (second ? jobs.j[1].first_cta : jobs.j[0].first_cta);
+    const uint32_t n_ctas = second ? jobs.j[1].n_ctas : jobs.j[0].n_ctas;
     const uint32_t t = threadIdx.x, warp = t >> 5;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tt::BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + tt::BAR + 16);
@@ -438,7 +460,7 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(const __nv_bflo
         fence_before();
         __syncthreads();
     };
-    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    for (uint32_t tile = cta; tile < tiles && ok; tile += n_ctas) {
         const uint32_t row = tile * 128 + t;
         const bool valid = row < n;
 #pragma unroll
@@ -567,7 +589,7 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(const __nv_bflo
     fence_before();
     __syncthreads();
     fence_after();
-    float* P = partial + (uint64_t)blockIdx.x * N_PARAMS;
+    float* P = partial + (uint64_t)cta * N_PARAMS;
     {
         float v[16];
 #pragma unroll 1
@@ -625,15 +647,40 @@ __device__ __forceinline__ int image_pos(int p)
     return B_W4 + (r / NH) * SH + r % NH;
 }
 
-// The gradient is g plus the n_parts slices of `partial` (the training
-// kernel's per-CTA sums) added in CTA order, as k_mlp_reduce adds them.
-__global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                                                 float* __restrict__ g, const float* __restrict__ partial,
-                                                 uint32_t n_parts, float lr, float b1, float b2, float eps,
-                                                 float c1, float c2, __nv_bfloat16* __restrict__ img)
+// Adam for up to two networks (blockIdx.y).  The gradient is g plus the
+// n_parts slices of `partial` (the training kernel's per-CTA sums) added in
+// CTA order, as k_mlp_reduce adds them.
+struct AdamJob
+{
+    float* w;
+    float* m;
+    float* v;
+    float* g;
+    const float* partial;
+    __nv_bfloat16* img;
+    uint32_t n_parts;
+    float c1, c2;
+};
+struct AdamJobs
+{
+    AdamJob j[2];
+};
+
+__global__ void __launch_bounds__(256) k_mlp_adam(AdamJobs jobs, float lr, float b1, float b2, float eps)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N_PARAMS) return;
+    const AdamJob& J = jobs.j[0];
+    const AdamJob& K = jobs.j[1];
+    const bool second = blockIdx.y != 0;
+    float* w = second ? K.w : J.w;
+    float* m = second ? K.m : J.m;
+    float* v = second ? K.v : J.v;
+    float* g = second ? K.g : J.g;
+    const float* partial = second ? K.partial : J.partial;
+    const uint32_t n_parts = second ? K.n_parts : J.n_parts;
+    const float c1 = second ? K.c1 : J.c1, c2 = second ? K.c2 : J.c2;
+    __nv_bfloat16* img = second ? K.img : J.img;
     float sum = 0.0f;
     for (uint32_t c = 0; c < n_parts; c++) sum += partial[(uint64_t)c * N_PARAMS + p];
     const float gp = g[p] + sum;
@@ -786,24 +833,42 @@ tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, ui
 }
 
 // Computes the batch gradient into the accumulator (no update); returns the loss if out_loss.
-// The fused training kernel over n samples; leaves the per-CTA gradient
-// slices in k->scratch (*parts of them).
-static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t,
-                                   uint32_t* parts)
+// The fused training kernel over one network's n samples, or over two
+// networks' batches side by side in one launch; leaves each network's per-CTA
+// gradient slices in its scratch (parts[i] of them).
+static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, const float* const* d_x,
+                                   const float* const* d_t, uint32_t n_nets, uint32_t* parts)
 {
     static bool attr = false;
     if (!attr) {
         TGX_CUDA(cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tt::SMEM));
         attr = true;
     }
-    const uint32_t tiles = (n + 127) / 128;
-    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)c->num_sms);
-    TGX_TRY(devbuf_reserve(k->scratch, (size_t)grid * N_PARAMS * 4));
-    float* partial = (float*)k->scratch.ptr;
-    TGX_CUDA(cudaMemsetAsync(k->loss, 0, 4, c->stream));
-    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, k->img, n, d_x, d_t, partial, k->loss,
-               c->d_status);
-    *parts = grid;
+    TrainJobs jobs;
+    uint32_t grid = 0;
+    for (uint32_t i = 0; i < 2; i++) {
+        TrainJob& J = jobs.j[i];
+        if (i >= n_nets) {   // an empty second job past the end of the grid
+            J = jobs.j[0];
+            J.first_cta = 0xffffffffu;
+            continue;
+        }
+        const uint32_t tiles = (n[i] + 127) / 128;
+        const uint32_t ctas = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)c->num_sms));
+        TGX_TRY(devbuf_reserve(k[i]->scratch, (size_t)ctas * N_PARAMS * 4));
+        TGX_CUDA(cudaMemsetAsync(k[i]->loss, 0, 4, c->stream));
+        J.wimg = k[i]->img;
+        J.x = d_x[i];
+        J.target = d_t[i];
+        J.partial = (float*)k[i]->scratch.ptr;
+        J.loss = k[i]->loss;
+        J.n = n[i];
+        J.first_cta = grid;
+        J.n_ctas = ctas;
+        parts[i] = ctas;
+        grid += ctas;
+    }
+    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, jobs, c->d_status);
     return TGX_OK;
 }
 
@@ -811,7 +876,7 @@ static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* k, uint32_t n, const f
 static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t)
 {
     uint32_t parts = 0;
-    TGX_TRY(cache_grad_parts(c, k, n, d_x, d_t, &parts));
+    TGX_TRY(cache_grad_parts(c, &k, &n, &d_x, &d_t, 1, &parts));
     TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, (const float*)k->scratch.ptr, parts, k->g);
     return TGX_OK;
 }
@@ -829,18 +894,35 @@ extern "C" tgx_status tgx_cache_gradient(tgx_ctx* c, tgx_cache* k, uint32_t n, c
     return TGX_OK;
 }
 
+// One Adam step of one network, or of two networks side by side (shared
+// training and Adam launches); n[i] samples each.
+tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, const float* const* d_x,
+                            const float* const* d_t, uint32_t n_nets, float lr)
+{
+    uint32_t parts[2] = {0, 0};
+    TGX_TRY(cache_grad_parts(c, k, n, d_x, d_t, n_nets, parts));
+    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
+    AdamJobs jobs;
+    for (uint32_t i = 0; i < n_nets; i++) {
+        k[i]->step++;
+        AdamJob& J = jobs.j[i];
+        J.w = k[i]->w; J.m = k[i]->m; J.v = k[i]->v; J.g = k[i]->g;
+        J.partial = (const float*)k[i]->scratch.ptr;
+        J.img = k[i]->img;
+        J.n_parts = parts[i];
+        J.c1 = (float)(1.0 - pow((double)b1, (double)k[i]->step));
+        J.c2 = (float)(1.0 - pow((double)b2, (double)k[i]->step));
+    }
+    if (n_nets < 2) jobs.j[1] = jobs.j[0];
+    TGX_LAUNCH(c, TR_MLP_ADAM, dim3((N_PARAMS + 255) / 256, n_nets), 256, 0, k_mlp_adam, jobs, lr, b1, b2, eps);
+    return TGX_OK;
+}
+
 extern "C" tgx_status tgx_cache_train_step(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* d_x, const float* d_t,
                                            float lr)
 {
     if (!c || !k || !n || !d_x || !d_t) return TGX_ERR_INVALID_ARGUMENT;
-    uint32_t parts = 0;
-    TGX_TRY(cache_grad_parts(c, k, n, d_x, d_t, &parts));
-    k->step++;
-    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
-    const float c1 = (float)(1.0 - pow((double)b1, (double)k->step)), c2 = (float)(1.0 - pow((double)b2, (double)k->step));
-    TGX_LAUNCH(c, TR_MLP_ADAM, (N_PARAMS + 255) / 256, 256, 0, k_mlp_adam, k->w, k->m, k->v, k->g,
-               (const float*)k->scratch.ptr, parts, lr, b1, b2, eps, c1, c2, k->img);
-    return TGX_OK;
+    return cache_train_pair(c, &k, &n, &d_x, &d_t, 1, lr);
 }
 
 extern "C" tgx_status tgx_cache_last_loss(tgx_ctx* c, const tgx_cache* k, float* out_loss)

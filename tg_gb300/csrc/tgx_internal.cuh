@@ -341,6 +341,8 @@ void trace_free(tgx_ctx* ctx);
 
 // cache inference over min(max_n, *d_n) inputs (mlp.cu)
 tgx_status cache_primary(tgx_ctx* c, tgx_cache* k, tgx_cache** out);
+tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, const float* const* d_x,
+                            const float* const* d_t, uint32_t n_nets, float lr);
 tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
                                float* d_rgb);
 
