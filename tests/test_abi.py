@@ -98,3 +98,60 @@ def test_decode_matches_get_hovered_voxel_layout():
     assert hit and ptr == 7777 and vox == 300 and abs(depth - 123456 / 16777215) < 1e-7
     hit, depth, ptr, vox = tg.decode(tg.VIS_EMPTY)
     assert not hit and depth == 1.0 and ptr == 0xFFFFFFFF
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "tgx.h"
+int main(void)
+{
+    tgx_view v;
+    const float pos[3] = {0.0f, 0.0f, 0.0f};
+    if (tgx_abi_version() != TGX_ABI_VERSION) return 2;
+    if (tgx_make_view(pos, 0.0f, 3.14159265f, 1.0471976f, 64, 48, 0.1f, 256.0f, &v) != TGX_OK) return 3;
+    printf("tgx_object %zu\n", sizeof(tgx_object));
+    printf("tgx_view %zu\n", sizeof(tgx_view));
+    printf("tgx_material %zu\n", sizeof(tgx_material));
+    printf("tgx_scene_desc %zu\n", sizeof(tgx_scene_desc));
+    printf("tgx_config %zu\n", sizeof(tgx_config));
+    printf("tgx_device_error %zu\n", sizeof(tgx_device_error));
+    printf("tgx_vis_stats %zu\n", sizeof(tgx_vis_stats));
+    printf("tgx_svo_info %zu\n", sizeof(tgx_svo_info));
+    printf("tgx_gi_params %zu\n", sizeof(tgx_gi_params));
+    printf("tgx_cache_gi_params %zu\n", sizeof(tgx_cache_gi_params));
+    printf("tgx_gen_params %zu\n", sizeof(tgx_gen_params));
+    printf("view_width %u\n", v.width);
+    return 0;
+}
+"""
+
+
+def test_header_compiles_as_c99_and_layouts_match_the_binding(tmp_path):
+    """An engine's C translation unit: the header compiles as strict C99,
+    links against the library, and every struct has the size the Python
+    binding assumes."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "engine.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "engine"
+    lib_dir = tg.LIB_PATH.parent
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", str(ROOT / "include"), str(src),
+                    "-L", str(lib_dir), "-ltgx", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    sizes = {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
+    assert sizes["view_width"] == 64
+    assert sizes["tgx_object"] == tg.OBJECT_DTYPE.itemsize
+    assert sizes["tgx_view"] == tg.VIEW_DTYPE.itemsize
+    assert sizes["tgx_material"] == tg.MATERIAL_DTYPE.itemsize
+    assert sizes["tgx_scene_desc"] == C.sizeof(tg.SceneDesc)
+    assert sizes["tgx_config"] == C.sizeof(tg.Config)
+    assert sizes["tgx_device_error"] == C.sizeof(tg.DeviceError)
+    assert sizes["tgx_vis_stats"] == C.sizeof(tg.VisStats)
+    assert sizes["tgx_svo_info"] == C.sizeof(tg.SvoInfo)
+    assert sizes["tgx_gi_params"] == tg.GI_PARAMS_DTYPE.itemsize
+    assert sizes["tgx_cache_gi_params"] == tg.CACHE_GI_DTYPE.itemsize
+    assert sizes["tgx_gen_params"] == C.sizeof(tg.GenParams)
