@@ -458,6 +458,8 @@ typedef struct tgx_cache_gi_params
     float    primary_weight;    /* 0..1: largest share of a pixel's incoming light taken from the
                                    cache's pixel-point network instead of its samples (0: off) */
     uint32_t n_train_primary;   /* training samples of the pixel-point network per frame (0) */
+    float    primary_variance_scale; /* multiplies the samples' variance v in the shrinkage weight
+                                   (0 = the default, 2) */
 } tgx_cache_gi_params;
 
 /*
@@ -472,9 +474,11 @@ typedef struct tgx_cache_gi_params
  * It is trained (n_train_primary random pixels per frame, no extra paths) on
  * each pixel's sample mean m of incoming light.  With primary_weight w > 0 a
  * pixel's incoming light becomes m + k (P - m), P the network's prediction
- * and k = min(w, v / max(|P - m|^2, v)) with v the variance of m estimated
- * from the pixel's samples: the prediction counts where it agrees with the
- * samples within their noise.  Asynchronous; all buffers DEVICE memory.
+ * and k = min(w, s v / max(|P - m|^2, s v + t)) with v the variance of m
+ * estimated from the pixel's samples, s = primary_variance_scale and t the
+ * network's error variance over the frame (mean |P - m|^2 - mean v): the
+ * prediction counts where it agrees with the samples within their noise and
+ * the network is accurate enough over the frame.  Asynchronous; all buffers DEVICE memory.
  */
 tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, tgx_cache* cache,
                                  const tgx_view* view, const uint64_t* d_visbuf, const tgx_gi_params* params,

@@ -59,15 +59,18 @@ assert GI_PARAMS_DTYPE.itemsize == 64
 
 CACHE_GI_DTYPE = np.dtype([("n_train", np.uint32), ("train_spp", np.uint32), ("train_steps", np.uint32),
                            ("lr", np.float32), ("box_min", np.float32, 3), ("box_max", np.float32, 3),
-                           ("primary_weight", np.float32), ("n_train_primary", np.uint32)])
+                           ("primary_weight", np.float32), ("n_train_primary", np.uint32),
+                           ("primary_variance_scale", np.float32)])
 
 
 def cache_gi_params(box_min, box_max, n_train: int = 65536, train_spp: int = 16, train_steps: int = 4,
-                    lr: float = 1e-2, primary_weight: float = 0.0, n_train_primary: int = 0) -> np.ndarray:
+                    lr: float = 1e-2, primary_weight: float = 0.0, n_train_primary: int = 0,
+                    primary_variance_scale: float = 0.0) -> np.ndarray:
     p = np.zeros(1, CACHE_GI_DTYPE)
     p["n_train"], p["train_spp"], p["train_steps"], p["lr"] = n_train, train_spp, train_steps, lr
     p["box_min"], p["box_max"] = box_min, box_max
     p["primary_weight"], p["n_train_primary"] = primary_weight, n_train_primary
+    p["primary_variance_scale"] = primary_variance_scale
     return p
 
 

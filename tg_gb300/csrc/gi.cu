@@ -43,6 +43,7 @@ namespace {
 constexpr float kInvPi = 0.318309886f;
 constexpr uint32_t kMaxBounces = 4;
 constexpr uint64_t kMaxPathsPerChunk = 16ull << 20;   // paths in flight per wavefront chunk
+constexpr bool kShrinkFrameStats = true;              // empirical-Bayes blend with the frame's statistics
 
 struct GiParams
 {
@@ -509,6 +510,7 @@ struct CacheGiConst
     uint32_t n_train, train_spp;
     uint32_t n_train_primary;   // training samples of the pixel-point network per frame
     float primary_weight;
+    float primary_variance_scale;
 };
 
 enum CacheCounter { CC_ROOTS = 0, CC_QUERIES = 1, CC_TRAIN_ROOTS = 2, CC_QUEUE = 3 };
@@ -602,8 +604,9 @@ __global__ void __launch_bounds__(256) k_gi_primary_batch(GiParams p, CacheGiCon
 // pixel = direct + albedo * mean(sky, or hit albedo * cache prediction)
 // With the pixel-point network (prim_rgb), the incoming light is shrunk from
 // the sample mean m toward the network's prediction P at the pixel's point:
-// e = m + k (P - m) with k = min(w, v / max(|P - m|^2, v)), v the variance of
-// the mean estimated from the pixel's own samples (k = w with one sample).
+// e = m + k (P - m) with k = min(w, s v / max(|P - m|^2, s v)), v the variance
+// of the mean estimated from the pixel's own samples and s its scale (k = w
+// with one sample).
 // A prediction within the samples' noise is taken up to the weight w; one far
 // outside it (where the network is wrong) is mostly ignored.  The sample mean
 // is kept (pmean) as that network's training target.
@@ -614,9 +617,12 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
                                                          const float* __restrict__ qrgb,
                                                          const CacheHit* __restrict__ hits,
                                                          const float* __restrict__ prim_rgb, float primary_weight,
-                                                         float* __restrict__ pmean, float* __restrict__ out)
+                                                         float variance_scale, float* __restrict__ pmean,
+                                                         float* __restrict__ pvar, float* __restrict__ stats,
+                                                         float* __restrict__ out)
 {
     const uint32_t n = *n_dev;
+    float s_d2 = 0.0f, s_v = 0.0f;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const PathRoot& rt = roots[r];
         float acc[3] = {0.0f, 0.0f, 0.0f}, sq = 0.0f;
@@ -650,9 +656,17 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
             }
             kw = primary_weight;
             if (p.spp > 1) {
-                const float n = (float)p.spp;
-                const float v = fmaxf(sq - n * m2, 0.0f) / ((n - 1.0f) * n);   // variance of the mean, summed over channels
-                if (d2 > v) kw = fminf(kw, v / d2);
+                const float ns = (float)p.spp;
+                // variance of the mean, summed over channels
+                const float v = fmaxf(sq - ns * m2, 0.0f) / ((ns - 1.0f) * ns);
+                if (pvar) {   // the blend waits for the frame's statistics (k_gi_cache_blend)
+                    pvar[r] = v;
+                    s_d2 += d2;
+                    s_v += v;
+                    continue;
+                }
+                const float vs = variance_scale * v;
+                if (d2 > vs) kw = fminf(kw, vs / d2);
             }
         }
 #pragma unroll
@@ -660,6 +674,53 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
             const float e = prim_rgb ? m[i] + kw * (pr[i] - m[i]) : m[i];
             out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], e));
         }
+    }
+    if (stats) {   // the frame's sums of |P - m|^2 and v
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s_d2 += __shfl_xor_sync(0xffffffffu, s_d2, o);
+            s_v += __shfl_xor_sync(0xffffffffu, s_v, o);
+        }
+        if ((threadIdx.x & 31u) == 0) {
+            atomicAdd(&stats[0], s_d2);
+            atomicAdd(&stats[1], s_v);
+        }
+    }
+}
+
+// Blend with the frame's statistics: the network's error variance tau^2 =
+// mean |P - m|^2 - mean v over the pixels, and per pixel
+// k = min(w, s v / max(|P - m|^2, s v + tau^2)): a pixel's prediction is
+// trusted as far as its samples' (scaled) noise outweighs the network's
+// typical error over the frame, and never beyond what the pixel's own
+// disagreement allows.
+__global__ void __launch_bounds__(256) k_gi_cache_blend(const PathRoot* __restrict__ roots,
+                                                       const uint32_t* __restrict__ n_dev, GiParams p,
+                                                       const RayHit* __restrict__ root_hits,
+                                                       const float* __restrict__ pmean, const float* __restrict__ prim_rgb,
+                                                       const float* __restrict__ pvar, const float* __restrict__ stats,
+                                                       float primary_weight, float variance_scale,
+                                                       float* __restrict__ out)
+{
+    const uint32_t n = *n_dev;
+    const float inv_n = n ? 1.0f / (float)n : 0.0f;
+    const float tau2 = fmaxf(stats[0] * inv_n - stats[1] * inv_n, 1e-12f);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const PathRoot& rt = roots[r];
+        float L[3] = {0.0f, 0.0f, 0.0f};
+        const float ndl = sun_cos(rt.n, p);
+        if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
+        float m[3], pr[3], d2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            m[i] = pmean[3ull * r + i];
+            pr[i] = fmaxf(prim_rgb[3ull * r + i], 0.0f);
+            d2 += (pr[i] - m[i]) * (pr[i] - m[i]);
+        }
+        const float v = variance_scale * pvar[r];
+        const float kw = fminf(primary_weight, v / fmaxf(fmaxf(d2, v + tau2), 1e-30f));
+#pragma unroll
+        for (int i = 0; i < 3; i++) out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], m[i] + kw * (pr[i] - m[i])));
     }
 }
 
@@ -872,6 +933,11 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         return TGX_ERR_INVALID_ARGUMENT;
     }
     q.primary_weight = cp->primary_weight;
+    if (!(cp->primary_variance_scale >= 0.0f)) {
+        tgx_set_error("tgx_gi_render_cached: primary_variance_scale must be >= 0");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    q.primary_variance_scale = cp->primary_variance_scale > 0.0f ? cp->primary_variance_scale : 2.0f;
     q.n_train_primary = cp->n_train_primary;
     const bool primary = q.primary_weight > 0.0f || (q.n_train_primary && cp->train_steps);
     tgx_cache* pnet = nullptr;
@@ -888,7 +954,7 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     const uint64_t n_prim = primary ? n_pix : 0;
     auto layout = [&](Carver& cv, uint32_t*& counters, PathBufs& b, int32_t*& qidx, float*& qx, float*& qrgb,
                       CacheHit*& hits, float*& tx, float*& tt, float*& pqx, float*& pqrgb, float*& pmean,
-                      float*& ptx, float*& ptt) {
+                      float*& pvar, float*& pstats, float*& ptx, float*& ptt) {
         counters = cv.take<uint32_t>(64);
         carve_paths(cv, b, max_roots, max_paths);
         qidx = cv.take<int32_t>(capacity);
@@ -900,16 +966,18 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         pqx = cv.take<float>(n_prim * 9);
         pqrgb = cv.take<float>(n_prim * 3);
         pmean = cv.take<float>(n_prim * 3);
+        pvar = cv.take<float>(n_prim);
+        pstats = cv.take<float>(primary ? 2 : 0);
         ptx = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 9);
         ptt = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 3);
     };
     uint32_t* counters; PathBufs b; int32_t* qidx; CacheHit* hits;
-    float *qx, *qrgb, *tx, *tt, *pqx, *pqrgb, *pmean, *ptx, *ptt;
+    float *qx, *qrgb, *tx, *tt, *pqx, *pqrgb, *pmean, *pvar, *pstats, *ptx, *ptt;
     Carver size{nullptr};
-    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, ptx, ptt);
+    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pvar, pstats, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->gi_scratch, size.off + 256));
     Carver cv{(char*)c->gi_scratch.ptr};
-    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, ptx, ptt);
+    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pvar, pstats, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
     uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
     TGX_CUDA(cudaMemsetAsync(counters, 0, 64 * 4, c->stream));
@@ -938,9 +1006,16 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         if (q.primary_weight > 0.0f)
             TGX_TRY(cache_infer_counted(c, pnet, &counters[CC_ROOTS], (uint32_t)n_pix, pqx, pqrgb));
     }
+    // the frame-statistics blend needs more than one sample per pixel
+    const bool blend = q.primary_weight > 0.0f && p.spp > 1 && kShrinkFrameStats;
+    if (blend) TGX_CUDA(cudaMemsetAsync(pstats, 0, 2 * sizeof(float), c->stream));
     TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_resolve, b.roots, &counters[CC_ROOTS], p,
                b.root_hits, qidx, qrgb, hits, q.primary_weight > 0.0f ? pqrgb : nullptr, q.primary_weight,
-               primary ? pmean : nullptr, d_rgb);
+               q.primary_variance_scale, primary ? pmean : nullptr, blend ? pvar : nullptr, blend ? pstats : nullptr,
+               d_rgb);
+    if (blend)
+        TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_blend, b.roots, &counters[CC_ROOTS], p,
+                   b.root_hits, pmean, pqrgb, pvar, pstats, q.primary_weight, q.primary_variance_scale, d_rgb);
     const bool train_primary = primary && q.n_train_primary && cp->train_steps;
     if (train_primary)
         TGX_LAUNCH(c, TR_GI, (q.n_train_primary + 255) / 256, 256, 0, k_gi_primary_batch, p, q, &counters[CC_ROOTS], pqx,
