@@ -459,7 +459,7 @@ typedef struct tgx_cache_gi_params
                                    cache's pixel-point network instead of its samples (0: off) */
     uint32_t n_train_primary;   /* training samples of the pixel-point network per frame (0) */
     float    primary_variance_scale; /* multiplies the samples' variance v in the shrinkage weight
-                                   (0 = the default, 2) */
+                                   (0 = the default, 0.5) */
 } tgx_cache_gi_params;
 
 /*
@@ -473,12 +473,14 @@ typedef struct tgx_cache_gi_params
  * The cache also holds a second network for the pixels' own surface points.
  * It is trained (n_train_primary random pixels per frame, no extra paths) on
  * each pixel's sample mean m of incoming light.  With primary_weight w > 0 a
- * pixel's incoming light becomes m + k (P - m), P the network's prediction
- * and k = min(w, s v / max(|P - m|^2, s v + t)) with v the variance of m
- * estimated from the pixel's samples, s = primary_variance_scale and t the
- * network's error variance over the frame (mean |P - m|^2 - mean v): the
- * prediction counts where it agrees with the samples within their noise and
- * the network is accurate enough over the frame.  Asynchronous; all buffers DEVICE memory.
+ * pixel's incoming light becomes m + k (P - m), P the network's prediction.
+ * With one sample k = w.  With spp > 1, k = min(w, s v / (s v + b)): b is
+ * the network's squared error over the pixel's 9x9 neighbourhood (mean
+ * |P - m|^2 less mean variance of m), v the variance of m, its own estimate
+ * mixed with the neighbourhood's as (spp - 1) : 1, and s =
+ * primary_variance_scale; both relative to the pixel's predicted brightness.
+ * The prediction counts where the network is accurate around the pixel and
+ * the pixel's samples are noisy.  Asynchronous; all buffers DEVICE memory.
  */
 tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx_svo* svo, tgx_cache* cache,
                                  const tgx_view* view, const uint64_t* d_visbuf, const tgx_gi_params* params,

@@ -182,8 +182,8 @@ def test_pixel_point_network_lowers_the_error(ctx):
     """The cache's second network, trained on the pixels' own sample means,
     lowers the error of 4-spp cached GI against a 256-spp plain render.  With
     weight 0 it trains but leaves every pixel bit-equal to cached GI without
-    it (bounce network frozen: its training sums gradients with atomics, so
-    two trained runs differ in the last bits)."""
+    it (bounce network frozen: its training batch comes from hits appended in
+    arbitrary order, so two trained runs differ in the last bits)."""
     import torch
     s, sc, svo, view, vis = _scene_setup(ctx, seed=23)
     ref = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
@@ -209,6 +209,42 @@ def test_pixel_point_network_lowers_the_error(ctx):
         finally:
             cache.close()
     svo.close(); sc.close()
+
+
+def test_shrinkage_is_one_weight_per_pixel_between_samples_and_network(ctx):
+    """With both networks frozen, a 3-spp cached pixel is its samples' mean m
+    moved toward the pixel-point network's prediction P by one weight k in
+    [0, w] for all three channels: out - out(w=0) = k (out(P) - out(w=0)),
+    where out(P) is the 1-spp render with w = 1 (P alone).  Direct light and
+    albedo are the same in all three renders."""
+    import torch
+    s, sc, svo, view, vis = _scene_setup(ctx, seed=31)
+    box = ((-40.0,) * 3, (40.0,) * 3)
+    cache = tg.Cache(ctx, seed=3)
+    out = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+    train = tg.cache_gi_params(*box, n_train=8192, train_spp=8, train_steps=4, primary_weight=1.0,
+                               n_train_primary=4096)
+    for f in range(40):
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=f), train, out)
+    w = 0.8
+    renders = {}
+    for name, spp, weight in (("m", 3, 0.0), ("P", 1, 1.0), ("blend", 3, w)):
+        cp = tg.cache_gi_params(*box, n_train=0, train_steps=0, primary_weight=weight)
+        o = torch.empty_like(out)
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=9), cp, o)
+        renders[name] = o
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    cache.close()
+    hit = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
+    m, p_, b = (renders[k].cpu().numpy().reshape(-1, 3)[hit].astype(np.float64) for k in ("m", "P", "blend"))
+    d, e = p_ - m, b - m
+    big = np.abs(d).max(axis=1) > 1e-2
+    assert big.sum() > 200
+    k = (e[big] * d[big]).sum(1) / (d[big] * d[big]).sum(1)
+    assert np.abs(e[big] - k[:, None] * d[big]).max() < 1e-5
+    assert k.min() > -1e-5 and k.max() < w + 1e-5
+    assert np.ptp(k) > 0.05   # the weight varies over the pixels
 
 
 def test_trace_steps_per_round_changes_no_result(ctx):

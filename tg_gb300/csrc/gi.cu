@@ -43,7 +43,6 @@ namespace {
 constexpr float kInvPi = 0.318309886f;
 constexpr uint32_t kMaxBounces = 4;
 constexpr uint64_t kMaxPathsPerChunk = 16ull << 20;   // paths in flight per wavefront chunk
-constexpr bool kShrinkFrameStats = true;              // empirical-Bayes blend with the frame's statistics
 
 struct GiParams
 {
@@ -604,12 +603,12 @@ __global__ void __launch_bounds__(256) k_gi_primary_batch(GiParams p, CacheGiCon
 // pixel = direct + albedo * mean(sky, or hit albedo * cache prediction)
 // With the pixel-point network (prim_rgb), the incoming light is shrunk from
 // the sample mean m toward the network's prediction P at the pixel's point:
-// e = m + k (P - m) with k = min(w, s v / max(|P - m|^2, s v)), v the variance
-// of the mean estimated from the pixel's own samples and s its scale (k = w
-// with one sample).
-// A prediction within the samples' noise is taken up to the weight w; one far
-// outside it (where the network is wrong) is mostly ignored.  The sample mean
-// is kept (pmean) as that network's training target.
+// e = m + k (P - m).  With one sample k = w; with more, this pass stores the
+// pixel's statistics for k_gi_cache_blend: the variance v of its mean and its
+// disagreement d2 = |P - m|^2, both as they reach the output (times the
+// albedo) and relative to the predicted pixel (|direct + albedo P|^2 + 0.03,
+// the relMSE weight).  The sample mean is kept (pmean) as that network's
+// training target.
 __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __restrict__ roots,
                                                          const uint32_t* __restrict__ n_dev, GiParams p,
                                                          const RayHit* __restrict__ root_hits,
@@ -617,15 +616,13 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
                                                          const float* __restrict__ qrgb,
                                                          const CacheHit* __restrict__ hits,
                                                          const float* __restrict__ prim_rgb, float primary_weight,
-                                                         float variance_scale, float* __restrict__ pmean,
-                                                         float* __restrict__ pvar, float* __restrict__ stats,
+                                                         float* __restrict__ pmean, float2* __restrict__ pstat,
                                                          float* __restrict__ out)
 {
     const uint32_t n = *n_dev;
-    float s_d2 = 0.0f, s_v = 0.0f;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const PathRoot& rt = roots[r];
-        float acc[3] = {0.0f, 0.0f, 0.0f}, sq = 0.0f;
+        float acc[3] = {0.0f, 0.0f, 0.0f}, sq[3] = {0.0f, 0.0f, 0.0f};
         for (uint32_t k = 0; k < p.spp; k++) {
             const int32_t qv = qidx[(uint64_t)r * p.spp + k];
 #pragma unroll
@@ -633,94 +630,90 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
                 const float f = qv >= 0 ? xmul(hits[qv].a[i], fmaxf(qrgb[3ull * qv + i], 0.0f))
                                         : (qv == -1 ? p.sky_radiance[i] : 0.0f);
                 acc[i] = xadd(acc[i], f);
-                if (prim_rgb) sq += f * f;
+                sq[i] += f * f;
             }
         }
         float L[3] = {0.0f, 0.0f, 0.0f};
         const float ndl = sun_cos(rt.n, p);
         if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
         const float inv_spp = xdiv(1.0f, (float)(p.spp ? p.spp : 1u));
-        float m[3], pr[3], kw = 0.0f;
+        float m[3], pr[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             m[i] = xmul(acc[i], inv_spp);
             if (pmean) pmean[3ull * r + i] = m[i];
         }
         if (prim_rgb) {
-            float d2 = 0.0f, m2 = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 3; i++) {
-                pr[i] = fmaxf(prim_rgb[3ull * r + i], 0.0f);
-                d2 += (pr[i] - m[i]) * (pr[i] - m[i]);
-                m2 += m[i] * m[i];
-            }
-            kw = primary_weight;
-            if (p.spp > 1) {
+            for (int i = 0; i < 3; i++) pr[i] = fmaxf(prim_rgb[3ull * r + i], 0.0f);
+            if (pstat) {   // the blend waits for the neighbourhood's statistics (k_gi_cache_blend)
                 const float ns = (float)p.spp;
-                // variance of the mean, summed over channels
-                const float v = fmaxf(sq - ns * m2, 0.0f) / ((ns - 1.0f) * ns);
-                if (pvar) {   // the blend waits for the frame's statistics (k_gi_cache_blend)
-                    pvar[r] = v;
-                    s_d2 += d2;
-                    s_v += v;
-                    continue;
+                float v = 0.0f, d2 = 0.0f, nrm = 0.03f;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const float a2 = rt.a[i] * rt.a[i];
+                    v += a2 * fmaxf(sq[i] - ns * m[i] * m[i], 0.0f);
+                    d2 += a2 * (pr[i] - m[i]) * (pr[i] - m[i]);
+                    const float y = L[i] + rt.a[i] * pr[i];
+                    nrm += y * y;
                 }
-                const float vs = variance_scale * v;
-                if (d2 > vs) kw = fminf(kw, vs / d2);
+                v /= (ns - 1.0f) * ns;
+                pstat[rt.key] = make_float2(v / nrm, d2 / nrm);
+                continue;
             }
         }
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const float e = prim_rgb ? m[i] + kw * (pr[i] - m[i]) : m[i];
+            const float e = prim_rgb ? m[i] + primary_weight * (pr[i] - m[i]) : m[i];
             out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], e));
-        }
-    }
-    if (stats) {   // the frame's sums of |P - m|^2 and v
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s_d2 += __shfl_xor_sync(0xffffffffu, s_d2, o);
-            s_v += __shfl_xor_sync(0xffffffffu, s_v, o);
-        }
-        if ((threadIdx.x & 31u) == 0) {
-            atomicAdd(&stats[0], s_d2);
-            atomicAdd(&stats[1], s_v);
         }
     }
 }
 
-// Blend with the frame's statistics: the network's error variance tau^2 =
-// mean |P - m|^2 - mean v over the pixels, and per pixel
-// k = min(w, s v / max(|P - m|^2, s v + tau^2)): a pixel's prediction is
-// trusted as far as its samples' (scaled) noise outweighs the network's
-// typical error over the frame, and never beyond what the pixel's own
-// disagreement allows.
+// The shrinkage weight.  Over the geometry pixels of the (2R+1)^2 window the
+// mean relative variance vn and mean relative disagreement dn give the
+// network's local squared error b2 = max(dn - vn, 0); the pixel's variance is
+// its own estimate v mixed with vn by their degrees of freedom,
+// vm = a v + (1 - a) vn with a = (spp - 1) / spp, so that a pixel whose few
+// samples spread far apart leans toward the network.  Then
+// k = min(w, s vm / (s vm + b2)), s the variance scale: the k that minimises
+// the expected error of m + k (P - m) for noise vm and network error b2.
+constexpr int kBlendRadius = 4;
+
 __global__ void __launch_bounds__(256) k_gi_cache_blend(const PathRoot* __restrict__ roots,
                                                        const uint32_t* __restrict__ n_dev, GiParams p,
                                                        const RayHit* __restrict__ root_hits,
                                                        const float* __restrict__ pmean, const float* __restrict__ prim_rgb,
-                                                       const float* __restrict__ pvar, const float* __restrict__ stats,
+                                                       const float2* __restrict__ pstat, uint32_t width, uint32_t height,
                                                        float primary_weight, float variance_scale,
                                                        float* __restrict__ out)
 {
     const uint32_t n = *n_dev;
-    const float inv_n = n ? 1.0f / (float)n : 0.0f;
-    const float tau2 = fmaxf(stats[0] * inv_n - stats[1] * inv_n, 1e-12f);
+    const float a = (float)(p.spp - 1) / (float)p.spp;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const PathRoot& rt = roots[r];
+        const int x = (int)(rt.key % width), y = (int)(rt.key / width);
+        const int x0 = max(x - kBlendRadius, 0), x1 = min(x + kBlendRadius, (int)width - 1);
+        const int y0 = max(y - kBlendRadius, 0), y1 = min(y + kBlendRadius, (int)height - 1);
+        float sv = 0.0f, sd = 0.0f, cnt = 0.0f;
+        for (int yy = y0; yy <= y1; yy++) {
+            const float2* row = pstat + (size_t)yy * width;
+            for (int xx = x0; xx <= x1; xx++) {
+                const float2 t = __ldg(row + xx);
+                if (t.x == t.x) { sv += t.x; sd += t.y; cnt += 1.0f; }   // NaN: no geometry there
+            }
+        }
+        const float vn = sv / cnt, b2 = fmaxf(sd - sv, 0.0f) / cnt;   // cnt >= 1: the pixel itself
+        const float vm = variance_scale * (a * pstat[rt.key].x + (1.0f - a) * vn);
+        const float kw = vm > 0.0f ? fminf(primary_weight, vm / (vm + b2)) : 0.0f;
         float L[3] = {0.0f, 0.0f, 0.0f};
         const float ndl = sun_cos(rt.n, p);
         if (ndl > 0.0f && root_hits[r].res != 1) sun_term(rt.a, ndl, p, L);
-        float m[3], pr[3], d2 = 0.0f;
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            m[i] = pmean[3ull * r + i];
-            pr[i] = fmaxf(prim_rgb[3ull * r + i], 0.0f);
-            d2 += (pr[i] - m[i]) * (pr[i] - m[i]);
+            const float m = pmean[3ull * r + i], pr = fmaxf(prim_rgb[3ull * r + i], 0.0f);
+            out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], m + kw * (pr - m)));
         }
-        const float v = variance_scale * pvar[r];
-        const float kw = fminf(primary_weight, v / fmaxf(fmaxf(d2, v + tau2), 1e-30f));
-#pragma unroll
-        for (int i = 0; i < 3; i++) out[3ull * rt.key + i] = xadd(L[i], xmul(rt.a[i], m[i] + kw * (pr[i] - m[i])));
     }
 }
 
@@ -937,7 +930,7 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         tgx_set_error("tgx_gi_render_cached: primary_variance_scale must be >= 0");
         return TGX_ERR_INVALID_ARGUMENT;
     }
-    q.primary_variance_scale = cp->primary_variance_scale > 0.0f ? cp->primary_variance_scale : 2.0f;
+    q.primary_variance_scale = cp->primary_variance_scale > 0.0f ? cp->primary_variance_scale : 0.5f;
     q.n_train_primary = cp->n_train_primary;
     const bool primary = q.primary_weight > 0.0f || (q.n_train_primary && cp->train_steps);
     tgx_cache* pnet = nullptr;
@@ -952,9 +945,11 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
     const uint64_t max_paths = std::max<uint64_t>(n_pix * cs, (uint64_t)q.n_train * cs_t);
 
     const uint64_t n_prim = primary ? n_pix : 0;
+    // the blend needs more than one sample per pixel
+    const bool blend = q.primary_weight > 0.0f && p.spp > 1;
     auto layout = [&](Carver& cv, uint32_t*& counters, PathBufs& b, int32_t*& qidx, float*& qx, float*& qrgb,
                       CacheHit*& hits, float*& tx, float*& tt, float*& pqx, float*& pqrgb, float*& pmean,
-                      float*& pvar, float*& pstats, float*& ptx, float*& ptt) {
+                      float2*& pstat, float*& ptx, float*& ptt) {
         counters = cv.take<uint32_t>(64);
         carve_paths(cv, b, max_roots, max_paths);
         qidx = cv.take<int32_t>(capacity);
@@ -966,18 +961,18 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         pqx = cv.take<float>(n_prim * 9);
         pqrgb = cv.take<float>(n_prim * 3);
         pmean = cv.take<float>(n_prim * 3);
-        pvar = cv.take<float>(n_prim);
-        pstats = cv.take<float>(primary ? 2 : 0);
+        pstat = cv.take<float2>(blend ? n_pix : 0);   // per pixel of the view
         ptx = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 9);
         ptt = cv.take<float>((uint64_t)(primary ? q.n_train_primary : 0u) * 3);
     };
     uint32_t* counters; PathBufs b; int32_t* qidx; CacheHit* hits;
-    float *qx, *qrgb, *tx, *tt, *pqx, *pqrgb, *pmean, *pvar, *pstats, *ptx, *ptt;
+    float *qx, *qrgb, *tx, *tt, *pqx, *pqrgb, *pmean, *ptx, *ptt;
+    float2* pstat;
     Carver size{nullptr};
-    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pvar, pstats, ptx, ptt);
+    layout(size, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pstat, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->gi_scratch, size.off + 256));
     Carver cv{(char*)c->gi_scratch.ptr};
-    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pvar, pstats, ptx, ptt);
+    layout(cv, counters, b, qidx, qx, qrgb, hits, tx, tt, pqx, pqrgb, pmean, pstat, ptx, ptt);
     TGX_TRY(devbuf_reserve(c->svo_counters, 4 * 4 + 64));
     uint32_t* exhausted = (uint32_t*)c->svo_counters.ptr + 8;
     TGX_CUDA(cudaMemsetAsync(counters, 0, 64 * 4, c->stream));
@@ -1006,16 +1001,15 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         if (q.primary_weight > 0.0f)
             TGX_TRY(cache_infer_counted(c, pnet, &counters[CC_ROOTS], (uint32_t)n_pix, pqx, pqrgb));
     }
-    // the frame-statistics blend needs more than one sample per pixel
-    const bool blend = q.primary_weight > 0.0f && p.spp > 1 && kShrinkFrameStats;
-    if (blend) TGX_CUDA(cudaMemsetAsync(pstats, 0, 2 * sizeof(float), c->stream));
+    // pixels without geometry keep NaN statistics (all bytes 0xff)
+    if (blend) TGX_CUDA(cudaMemsetAsync(pstat, 0xff, n_pix * sizeof(float2), c->stream));
     TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_resolve, b.roots, &counters[CC_ROOTS], p,
                b.root_hits, qidx, qrgb, hits, q.primary_weight > 0.0f ? pqrgb : nullptr, q.primary_weight,
-               q.primary_variance_scale, primary ? pmean : nullptr, blend ? pvar : nullptr, blend ? pstats : nullptr,
-               d_rgb);
+               primary ? pmean : nullptr, blend ? pstat : nullptr, d_rgb);
     if (blend)
         TGX_LAUNCH(c, TR_GI, stride_grid(c, n_pix, 256), 256, 0, k_gi_cache_blend, b.roots, &counters[CC_ROOTS], p,
-                   b.root_hits, pmean, pqrgb, pvar, pstats, q.primary_weight, q.primary_variance_scale, d_rgb);
+                   b.root_hits, pmean, pqrgb, pstat, view->width, view->height, q.primary_weight,
+                   q.primary_variance_scale, d_rgb);
     const bool train_primary = primary && q.n_train_primary && cp->train_steps;
     if (train_primary)
         TGX_LAUNCH(c, TR_GI, (q.n_train_primary + 255) / 256, 256, 0, k_gi_primary_batch, p, q, &counters[CC_ROOTS], pqx,

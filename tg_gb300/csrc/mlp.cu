@@ -846,6 +846,12 @@ static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* const* k, const uint32
     }
     TrainJobs jobs;
     uint32_t grid = 0;
+    // One wave of CTAs (one per SM: the kernel holds most of an SM's shared
+    // memory) shared between the jobs in proportion to their 128-sample tiles,
+    // so that every CTA loops over about as many tiles.
+    const uint32_t sms = (uint32_t)c->num_sms;
+    uint32_t total = 0;
+    for (uint32_t i = 0; i < n_nets; i++) total += (n[i] + 127) / 128;
     for (uint32_t i = 0; i < 2; i++) {
         TrainJob& J = jobs.j[i];
         if (i >= n_nets) {   // an empty second job past the end of the grid
@@ -854,7 +860,8 @@ static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* const* k, const uint32
             continue;
         }
         const uint32_t tiles = (n[i] + 127) / 128;
-        const uint32_t ctas = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)c->num_sms));
+        const uint32_t share = total <= sms ? tiles : (uint32_t)((uint64_t)tiles * sms / total);
+        const uint32_t ctas = std::max(1u, std::min(tiles, share));
         TGX_TRY(devbuf_reserve(k[i]->scratch, (size_t)ctas * N_PARAMS * 4));
         TGX_CUDA(cudaMemsetAsync(k[i]->loss, 0, 4, c->stream));
         J.wimg = k[i]->img;
