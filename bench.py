@@ -375,9 +375,10 @@ def bench_large(local: int):
     """Config 5: 2^24 clusters (4096 objects of 16^3 clusters, Bernoulli(0.3) bits as
     in config 1, uniform rotations, translations in an 8192^3 box; 1 GiB of bits,
     8 GiB of material bytes), 8 views of uneven resolution up to 3840x2160 in one
-    tgx_vis_render call, the 16384^3 SVO (without its per-voxel material grid),
-    and 2-bounce GI at 8 spp on the 3840x2160 view: learned cache and the plain
-    fallback, both scored by relMSE against a 64-spp plain render."""
+    tgx_vis_render call, the 16384^3 SVO (with its per-voxel material grid where
+    it fits), and 2-bounce GI at 8 spp on the 3840x2160 view: learned cache
+    (configured training, 60 warm-up frames) and the plain fallback, both scored
+    by relMSE against a 64-spp plain render."""
     import torch
     import tg_gb300 as tg
 
@@ -413,16 +414,22 @@ def bench_large(local: int):
     res.update({"views": len(sizes), "pixels": pixels, "vis_frame_ms": round(vis_ms, 3),
                 "vis_grays_per_s": pixels / (vis_ms * 1e-3) / 1e9})
     mn = (-8192.0, -8192.0, -8192.0)
-    svo = ctx.svo_build(sc, mn, 14, materials=False)
+    # with the per-voxel material grid (64 KiB per block) when it fits, else grey albedo
+    try:
+        svo = ctx.svo_build(sc, mn, 14, materials=True)
+        materials = True
+    except tg.TgxError:
+        svo = ctx.svo_build(sc, mn, 14, materials=False)
+        materials = False
     ctx.sync()
     svo.close()
     t0 = time.perf_counter()
-    svo = ctx.svo_build(sc, mn, 14, materials=False)
+    svo = ctx.svo_build(sc, mn, 14, materials=materials)
     ctx.sync()
     res["svo_build_ms"] = round((time.perf_counter() - t0) * 1e3, 1)
     info = svo.info()
     res["svo"] = {"extent": 16384, "blocks": int(info.n_blocks), "nonempty_blocks": int(info.n_nonempty_blocks),
-                  "device_gib": round(info.device_bytes / 2**30, 2)}
+                  "device_gib": round(info.device_bytes / 2**30, 2), "materials": materials}
     # GI on the 3840x2160 view
     v0, vis0 = views[0:1], outs[0]
     n = 3840 * 2160 * 3
@@ -445,20 +452,24 @@ def bench_large(local: int):
             ctx.sync()
             return e0.elapsed_time(e1) / frames
 
-        plain_ms = timed(lambda f: ctx.gi_render(sc, svo, v0, vis0, tg.gi_params(spp=8, bounces=2, seed=2, frame=f),
-                                                 out))
-        plain_err = rel_mse(out.cpu().numpy(), r, mask)
+        plain = {}
+        for spp in (4, 8):
+            ms = timed(lambda f: ctx.gi_render(sc, svo, v0, vis0, tg.gi_params(spp=spp, bounces=2, seed=2, frame=f),
+                                               out))
+            plain[spp] = {"frame_ms": round(ms, 2), "relmse": rel_mse(out.cpu().numpy(), r, mask)}
         cache = tg.Cache(ctx, seed=7)
-        cp = tg.cache_gi_params(box[0], box[1])
-        for f in range(20):
+        cp = tg.cache_gi_params(box[0], box[1], **CACHE_VARIANTS["configured_training"])
+        for f in range(60):
             ctx.gi_render_cached(sc, svo, cache, v0, vis0, tg.gi_params(spp=1, bounces=2, seed=2, frame=f), cp, out)
-        cached_ms = timed(lambda f: ctx.gi_render_cached(sc, svo, cache, v0, vis0,
-                                                          tg.gi_params(spp=8, bounces=2, seed=2, frame=40 + f), cp, out))
-        cached_err = rel_mse(out.cpu().numpy(), r, mask)
+        cached = {}
+        for spp in (2, 4, 8):
+            ms = timed(lambda f: ctx.gi_render_cached(sc, svo, cache, v0, vis0,
+                                                      tg.gi_params(spp=spp, bounces=2, seed=2, frame=60 + 10 * spp + f),
+                                                      cp, out))
+            cached[spp] = {"frame_ms": round(ms, 2), "relmse": rel_mse(out.cpu().numpy(), r, mask)}
         cache.close()
     res["gi_4k"] = {"geometry_pixels": int(mask.sum()), "judge": "plain 2-bounce GI, 64 spp",
-                    "plain_8spp": {"frame_ms": round(plain_ms, 2), "relmse": plain_err},
-                    "cached_8spp": {"frame_ms": round(cached_ms, 2), "relmse": cached_err}}
+                    "plain": plain, "cached_configured_training": cached}
     res["device_gib_used"] = round((free0 - torch.cuda.mem_get_info()[0]) / 2**30, 2)
     res["device_status"] = int(ctx.device_error().code)
     svo.close()
