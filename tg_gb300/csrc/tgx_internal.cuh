@@ -339,6 +339,39 @@ void trace_free(tgx_ctx* ctx);
         (ctx)->launches++;                                                        \
     } while (0)
 
+// The same launch as a programmatic dependent of the stream's previous
+// kernel: its CTAs may be scheduled while that kernel drains, and each waits
+// in pdl_wait() until the previous kernel has completed and its writes are
+// visible.  Every kernel launched this way calls pdl_wait() before its first
+// access to global memory that an earlier kernel of the stream touches.
+#define TGX_LAUNCH_PDL(ctx, slot, grid, block, smem, kernel, ...)                  \
+    do {                                                                          \
+        trace_begin((ctx), (slot));                                               \
+        cudaLaunchConfig_t cfg_ = {};                                             \
+        cfg_.gridDim = dim3(grid);                                                \
+        cfg_.blockDim = dim3(block);                                              \
+        cfg_.dynamicSmemBytes = (smem);                                           \
+        cfg_.stream = (ctx)->stream;                                              \
+        cudaLaunchAttribute attr_[1];                                             \
+        attr_[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;         \
+        attr_[0].val.programmaticStreamSerializationAllowed = 1;                  \
+        cfg_.attrs = attr_;                                                       \
+        cfg_.numAttrs = 1;                                                        \
+        cudaError_t le_ = cudaLaunchKernelEx(&cfg_, kernel, __VA_ARGS__);         \
+        trace_end((ctx), (slot));                                                 \
+        if (le_ != cudaSuccess) {                                                 \
+            tgx_set_error("launch of %s failed: %s", #kernel, cudaGetErrorString(le_)); \
+            return TGX_ERR_CUDA;                                                  \
+        }                                                                         \
+        (ctx)->launches++;                                                        \
+    } while (0)
+
+// griddepcontrol (PTX ISA 7.8, sm_90+): a kernel's wait for the kernel it
+// depends on, and its signal that its dependents may be scheduled.  Both are
+// no-ops in a kernel launched without the programmatic attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // cache inference over min(max_n, *d_n) inputs (mlp.cu)
 tgx_status cache_primary(tgx_ctx* c, tgx_cache* k, tgx_cache** out);
 tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, const float* const* d_x,

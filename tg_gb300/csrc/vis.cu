@@ -9,9 +9,9 @@
 //      sphere, then box corners) and empty clusters, computes a conservative
 //      screen-tile rectangle and a lower bound of the packed depth, and
 //      appends a 32-byte record.
-//   1b. k_vis_record_origin one thread per record: the ws2ms matrix and the
-//      camera position in cluster space exactly as the shader does.
-//   2. k_vis_count          one warp per record: counts it per (tile, depth bucket).
+//   2. k_vis_count          per record: the ws2ms matrix and the camera
+//      position in cluster space exactly as the shader does (one thread per
+//      record), and its counts per (tile, depth bucket) (one warp per record).
 //   3. k_vis_prefix         per tile: offsets of its 16 depth buckets; per
 //                           256 tiles: their sum and class histogram.
 //   4. k_vis_scan           one CTA: bases of the 256-tile groups and the
@@ -90,9 +90,13 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
     const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp,
     const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
     uint2* __restrict__ rects, uint32_t record_capacity, uint32_t* __restrict__ counters,
-    tgx_dev_status* __restrict__ status)
+    uint32_t* __restrict__ zero, uint32_t n_zero, tgx_dev_status* __restrict__ status)
 {
+    pdl_wait();
+    pdl_trigger();
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // the (tile, bucket) counts start at zero; k_vis_count runs after this kernel
+    for (uint64_t i = gid; i < n_zero; i += (uint64_t)gridDim.x * blockDim.x) zero[i] = 0u;
     const uint32_t v = (uint32_t)(gid / n_cp);
     const uint32_t cp = (uint32_t)(gid % n_cp);
     bool keep = false;
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
                 }
             }
             if (keep) {
-                // the exact cluster-space origin is computed by k_vis_record_origin
+                // the exact cluster-space origin is computed by k_vis_count
                 rec.cluster_idx = ci;
                 rec.cluster_pointer = cp;
                 rec.object_idx = oi;
@@ -217,16 +221,20 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
 }
 
 // ---------------------------------------------------------------------------
-// 1b. exact ws2ms and ray origin of every kept record (visibility.frag:57-66);
-//     kept apart from the cull so the cull runs at high occupancy
+// 2. per record: the exact ws2ms and ray origin (visibility.frag:57-66), one
+//    thread per record; then its per-(tile, bucket) counts, one warp per
+//    record with the lanes over its tiles.  The two loops write different
+//    fields and buffers; the cull kept apart runs at high occupancy.
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) k_vis_record_origin(VisRecord* __restrict__ records,
-                                                          const uint32_t* __restrict__ counters,
-                                                          uint32_t record_capacity,
-                                                          const tgx_object* __restrict__ objects,
-                                                          const ViewConst* __restrict__ views)
+__global__ void __launch_bounds__(256) k_vis_count(VisRecord* __restrict__ records, const uint2* __restrict__ rects,
+                                                  const uint32_t* __restrict__ counters, uint32_t record_capacity,
+                                                  const tgx_object* __restrict__ objects,
+                                                  const ViewConst* __restrict__ views,
+                                                  uint32_t* __restrict__ bucket_cnt, uint32_t n_tiles)
 {
+    pdl_wait();
+    pdl_trigger();
     const uint32_t n = min(counters[C_RECORDS], record_capacity);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         VisRecord& rec = records[i];
@@ -252,24 +260,12 @@ __global__ void __launch_bounds__(128) k_vis_record_origin(VisRecord* __restrict
         dm4_mulv4(ws2ms, vc.cam[0], vc.cam[1], vc.cam[2], 1.0f, o);
         rec.ox = o[0]; rec.oy = o[1]; rec.oz = o[2];
     }
-}
-
-// ---------------------------------------------------------------------------
-// 2. per-(tile, bucket) counts: one warp per record, lanes over its tiles
-// ---------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(256) k_vis_count(const VisRecord* __restrict__ records, const uint2* __restrict__ rects,
-                                                  const uint32_t* __restrict__ counters,
-                                                  const ViewConst* __restrict__ views,
-                                                  uint32_t* __restrict__ bucket_cnt, uint32_t n_tiles)
-{
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t n = counters[C_RECORDS];
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
         const uint2 r = rects[i];
-        const VisRecord& rec = records[i];
-        const ViewConst& vc = views[rec.view];
-        const uint32_t b = depth_bucket(rec.d24_lb);
+        const uint32_t view = records[i].view;
+        const ViewConst& vc = views[view];
+        const uint32_t b = depth_bucket(records[i].d24_lb);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
         for (uint32_t k = lane; k < cnt; k += 32) {
@@ -297,6 +293,8 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_prefix(uint32_t* __restrict_
     __shared__ uint32_t cls[kOrderClasses];
     __shared__ uint32_t wsum[kScanTiles / 32];
     if (threadIdx.x < kOrderClasses) cls[threadIdx.x] = 0;
+    pdl_wait();
+    pdl_trigger();
     __syncthreads();
     const uint32_t t = blockIdx.x * kScanTiles + threadIdx.x;
     uint32_t run = 0;
@@ -344,6 +342,8 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_au
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
     uint32_t* cls_cnt = cta_aux + n_ctas;
+    pdl_wait();
+    pdl_trigger();
     // CTA bases
     uint32_t carry = 0;
     for (uint32_t base = 0; base < n_ctas; base += 1024) {
@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_au
     }
     // class totals (warp c sums class c over the CTAs)
     uint32_t tot = 0;
+#pragma unroll 4
     for (uint32_t b = lane; b < n_ctas; b += 32) tot += cls_cnt[b * kOrderClasses + wid];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
@@ -391,17 +392,25 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_au
     __syncthreads();
     // per-(CTA, class) cursors: warp c scans class c over the CTAs
     uint32_t run = cls_base[wid];
-    for (uint32_t b0 = 0; b0 < n_ctas; b0 += 32) {
-        const uint32_t b = b0 + lane;
-        const uint32_t x = b < n_ctas ? cls_cnt[b * kOrderClasses + wid] : 0u;
-        uint32_t incl = x;
+    for (uint32_t b0 = 0; b0 < n_ctas; b0 += 128) {   // four chunks of 32 CTAs: loads first
+        uint32_t x[4];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((int)lane >= o) incl += y;
+        for (int j = 0; j < 4; j++) {
+            const uint32_t b = b0 + 32u * j + lane;
+            x[j] = b < n_ctas ? cls_cnt[b * kOrderClasses + wid] : 0u;
         }
-        if (b < n_ctas) cls_cnt[b * kOrderClasses + wid] = run + incl - x;
-        run += __shfl_sync(0xffffffffu, incl, 31);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t b = b0 + 32u * j + lane;
+            uint32_t incl = x[j];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += y;
+            }
+            if (b < n_ctas) cls_cnt[b * kOrderClasses + wid] = run + incl - x[j];
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
     }
 }
 
@@ -418,6 +427,8 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize(const uint32_t* __r
     __shared__ uint32_t cur[kOrderClasses];
     __shared__ uint32_t wsum[kScanTiles / 32];
     const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    pdl_wait();
+    pdl_trigger();
     if (threadIdx.x < kOrderClasses) cur[threadIdx.x] = cta_aux[n_ctas + blockIdx.x * kOrderClasses + threadIdx.x];
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t t = blockIdx.x * kScanTiles + threadIdx.x;
@@ -453,6 +464,8 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
                                                      uint32_t n_tiles, uint32_t bin_capacity,
                                                      tgx_dev_status* __restrict__ status)
 {
+    pdl_wait();
+    pdl_trigger();
     if (counters[C_OVERFLOW]) return;   // the tile kernel scans all records instead
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = counters[C_RECORDS];
@@ -725,6 +738,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, t
 {
     __shared__ TileSmem sm;
     tile_smem_init(sm);
+    pdl_wait();
     uint32_t phase = 0;
     vis_tile(J, blockIdx.x, sm, phase, status);
 }
@@ -903,36 +917,35 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
     if (phase != VIS_FROM_BINS) {
         TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
-        TGX_CUDA(cudaMemsetAsync(w.bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, c->stream));
         const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
         TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
                    s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-                   w.records, w.rects, w.rec_cap, w.counters, c->d_status);
-        TGX_LAUNCH(c, TR_VIS_SETUP, (uint32_t)c->num_sms * 4, 128, 0, k_vis_record_origin, w.records, w.counters,
-                   w.rec_cap, s->d_objects, d_vc);
-        TGX_LAUNCH(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, d_vc, w.bucket_cnt,
-                   n_tiles);
-        TGX_LAUNCH(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off, w.tile_total,
-                   n_tiles, w.cta_aux);
-        TGX_LAUNCH(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity, w.counters);
-        TGX_LAUNCH(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux,
-                   w.tile_off, w.tile_order);
+                   w.records, w.rects, w.rec_cap, w.counters, w.bucket_cnt, n_tiles * kBuckets, c->d_status);
+        // each later pass is a programmatic dependent of the one before
+        TGX_LAUNCH_PDL(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, w.rec_cap,
+                       s->d_objects, d_vc, w.bucket_cnt, n_tiles);
+        TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off,
+                       w.tile_total, n_tiles, w.cta_aux);
+        TGX_LAUNCH_PDL(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity,
+                       w.counters);
+        TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux,
+                       w.tile_off, w.tile_order);
     }
     if (phase == VIS_TO_SCAN) return TGX_OK;
-    TGX_LAUNCH(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
-               w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
-               n_tiles, w.bin_capacity, c->d_status);
+    TGX_LAUNCH_PDL(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
+                   w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
+                   n_tiles, w.bin_capacity, c->d_status);
     if (phase == VIS_NO_TILES) return TGX_OK;
     const TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
     const uint32_t threads = c->tile_w * c->tile_h;
     if (threads == 64) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
     } else if (threads == 128) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), J, c->d_status);
     } else if (threads == 256) {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), J, c->d_status);
     } else {
-        TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), J, c->d_status);
     }
     return TGX_OK;
 }
@@ -1493,7 +1506,6 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     // what must start at zero; everything else is written before it is read
     TGX_CUDA(cudaMemsetAsync(counters, 0, 256, st));
     TGX_CUDA(cudaMemsetAsync(status, 0, sizeof(tgx_dev_status), st));
-    TGX_CUDA(cudaMemsetAsync(bucket_cnt, 0, (size_t)n_tiles * kBuckets * 4, st));
     unsigned char stage[sizeof(ViewConst) + 32];
     const size_t ptr_off = (sizeof(ViewConst) + 15) & ~(size_t)15;
     memcpy(stage, &vc, sizeof(ViewConst));
@@ -1506,9 +1518,9 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     NA_LAUNCH((n_objects + 127) / 128, 128, k_vis_noalloc_inv_rot, d_objects, n_objects, inv_rot);
     NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
               d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
-              kNaMaxClusterPointers, counters, status);
-    NA_LAUNCH((uint32_t)sms * 4, 128, k_vis_record_origin, records, counters, kNaMaxClusterPointers, d_objects, d_vc);
-    NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, d_vc, bucket_cnt, n_tiles);
+              kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kBuckets, status);
+    NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, kNaMaxClusterPointers, d_objects, d_vc, bucket_cnt,
+              n_tiles);
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
     NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
     NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
