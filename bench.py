@@ -604,6 +604,7 @@ def main() -> None:
             pass
         for _ in range(2):
             ctx.vis_render_host(sc, view, [host_out])
+        # one blocking call per frame (latency): the L2 flush between calls is outside the clock
         e2e_ms = []
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
@@ -611,7 +612,26 @@ def main() -> None:
             t0 = time.perf_counter()
             ctx.vis_render_host(sc, view, [host_out])
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        e2e = statistics.mean(e2e_ms)
+        e2e_blocking = statistics.mean(e2e_ms)
+        # pipelined frame loop (throughput): the host issues frame i+1 while frame i renders into
+        # its pinned host buffer; the L2 flush runs before every render on the render stream,
+        # inside the clock
+        host_bufs = [host_out, np.empty_like(host_out)]
+        try:
+            host_bufs[1] = torch.empty(W * H, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        except Exception:
+            pass
+        for i in range(2):
+            ctx.vis_render_host_async(sc, view, [host_bufs[i & 1]])
+        ctx.vis_host_wait(0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ctx.vis_render_host_async(sc, view, [host_bufs[i & 1]])
+            ctx.vis_host_wait(1)
+        ctx.vis_host_wait(0)
+        e2e = (time.perf_counter() - t0) * 1e3 / args.steps
         err = ctx.device_error()
         if err.code:
             raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
@@ -731,9 +751,14 @@ def main() -> None:
         "config": {**CONFIG, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "tile": f"{tile[0]}x{tile[1]}",
                    "autotune_ms": {f"{t[0]}x{t[1]}": round(v, 4) for t, v in tuning.items()}},
-        "e2e": {"value": rays * world / (e2e * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
-                "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e,
-                "path": "tgx_vis_render_host (views from host, visibility buffer back to pinned host memory)"},
+        "e2e": {"value": rays * world / (e2e_blocking * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
+                "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e_blocking,
+                "path": "tgx_vis_render_host, one blocking call per frame: views from the host, the visibility "
+                        "buffer written into pinned host memory by the render itself (the L2 flush between "
+                        "calls is outside the clock, as for the device-timed value)",
+                "pipelined": {"value": rays * world / (e2e * 1e-3) / 1e9, "ms_per_step": e2e,
+                              "path": "tgx_vis_render_host_async + tgx_vis_host_wait(1) per frame, the L2 flush "
+                                      "before every render inside the clock"}},
         "gpu_launches": int(launches),
         "launch": ("one CUDA graph replay per frame (tgx_frame_graph), same kernels as tgx_vis_render"
                    if args.launch == "graph" else "separate launches per frame (tgx_vis_render)"),

@@ -203,9 +203,27 @@ tgx_status  tgx_vis_render(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view*
                            uint64_t* const* d_visbuf);
 
 /* Same as tgx_vis_render but h_visbuf[i] are HOST pointers; the call copies
- * the views in and the buffers out and returns when they are on the host. */
+ * the views in and returns when the buffers are on the host.  A buffer in
+ * pinned (page-locked) host memory is written by the render directly over the
+ * CPU-GPU link, with no device copy; any other goes through a device buffer
+ * and a copy. */
 tgx_status  tgx_vis_render_host(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                                 uint64_t* const* h_visbuf);
+
+/* Pipelined form of tgx_vis_render_host for frame loops that read every
+ * frame back: enqueues the frame and returns without waiting.  Pinned host
+ * buffers are written by the render directly.  Other buffers are copied on a
+ * second stream, so frame k's copy overlaps frame k+1's render; the library
+ * keeps two device copies of them and holds a render back until the copy two
+ * frames before it has finished.  A frame's host buffers must not be touched
+ * until tgx_vis_host_wait says the frame is done.  Errors of the call come
+ * back from it; device errors from tgx_last_device_error. */
+tgx_status  tgx_vis_render_host_async(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
+                                      uint64_t* const* h_visbuf);
+/* Waits until at most `max_in_flight` frames of tgx_vis_render_host_async are
+ * still being rendered or copied (0: all of them are on the host).  Frames
+ * complete in issue order. */
+tgx_status  tgx_vis_host_wait(tgx_ctx* ctx, uint32_t max_in_flight);
 
 /*
  * Visibility render that allocates nothing.  No counterpart in the reference:

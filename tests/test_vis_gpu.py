@@ -84,6 +84,32 @@ def test_tile_shapes_agree(oracle, tile):
     assert_same(g, oracle.vis_render(s, v, mode=1))
 
 
+def test_pipelined_host_buffers_equal_the_oracle(ctx, oracle):
+    """tgx_vis_render_host_async: five frames of different cameras issued back
+    to back into pinned and pageable host buffers, waited for with at most
+    one frame in flight and then all; every buffer equals the oracle's render
+    of its own camera.  The blocking call into a pinned buffer, too."""
+    import torch
+    s = cfg1_scene()
+    sc = ctx.upload(s)
+    views = [cfg1_view(72, 40 + 8 * k) for k in range(5)]
+    # pinned buffers (written by the render) and pageable ones (device copy, then a copy out)
+    outs = [torch.zeros(72 * (40 + 8 * k), dtype=torch.int64, pin_memory=k % 2 == 0).numpy().view(np.uint64)
+            for k in range(5)]
+    for k, (v, o) in enumerate(zip(views, outs)):
+        ctx.vis_render_host_async(sc, v, [o])
+        if k == 2:
+            ctx.vis_host_wait(1)
+    ctx.vis_host_wait(0)
+    assert ctx.device_error().code == 0
+    for v, o in zip(views, outs):
+        assert_same(o, oracle.vis_render(s, v, mode=1))
+    pinned = torch.zeros(72 * 40, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    ctx.vis_render_host(sc, views[0], [pinned])
+    assert_same(pinned, oracle.vis_render(s, views[0], mode=1))
+    sc.close()
+
+
 def test_host_buffers_and_pick(ctx, oracle):
     s, v = cfg1_scene(), cfg1_view(64, 64)
     sc = ctx.upload(s)

@@ -153,7 +153,7 @@ EXPORTS = [
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
-    "tgx_set_trace_steps",
+    "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait",
 ]
 
 
@@ -176,6 +176,8 @@ def _load() -> C.CDLL:
         "tgx_scene_destroy": (None, [vp, vp]),
         "tgx_vis_render": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
         "tgx_vis_render_host": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_vis_render_host_async": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "tgx_vis_host_wait": (i32, [vp, u32]),
         "tgx_vis_decode": (i32, [u64, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32)]),
         "tgx_pick": (i32, [vp, vp, u32, u32, u32, u32, C.POINTER(C.c_float), C.POINTER(u32), C.POINTER(u32), C.POINTER(i32)]),
         "tgx_svo_build": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
@@ -422,6 +424,19 @@ class Context:
         ptrs = (C.c_void_p * len(views))(*[_ptr(o) for o in outs])
         check(lib.tgx_vis_render_host(self.handle, scene.handle, _ptr(views), len(views), ptrs),
               "tgx_vis_render_host")
+
+    def vis_render_host_async(self, scene: "Scene", views: np.ndarray, outs) -> None:
+        """Pipelined host outputs (tgx_vis_render_host_async): returns before
+        the buffers are filled; `outs` (uint64 arrays, pinned for overlap) are
+        ready after vis_host_wait."""
+        views = np.ascontiguousarray(views, dtype=VIEW_DTYPE)
+        ptrs = (C.c_void_p * len(views))(*[_ptr(o) for o in outs])
+        check(lib.tgx_vis_render_host_async(self.handle, scene.handle, _ptr(views), len(views), ptrs),
+              "tgx_vis_render_host_async")
+
+    def vis_host_wait(self, max_in_flight: int = 0) -> None:
+        """Waits until at most `max_in_flight` pipelined host renders are pending."""
+        check(lib.tgx_vis_host_wait(self.handle, max_in_flight), "tgx_vis_host_wait")
 
     def generate_scene(self, kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, **kw) -> "Scene":
         """The generate_scene scene built in device memory (tgx_generate_scene_device)."""

@@ -136,6 +136,15 @@ extern "C" void tgx_destroy(tgx_ctx* c)
     if (c->h_counter) cudaFreeHost(c->h_counter);
     if (c->h_vis_counters) cudaFreeHost(c->h_vis_counters);
     if (c->vis_done) cudaEventDestroy(c->vis_done);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    for (int i = 0; i < 2; i++) {
+        devbuf_free(c->host_slot[i]);
+        if (c->host_rendered[i]) cudaEventDestroy(c->host_rendered[i]);
+        if (c->host_copied[i]) cudaEventDestroy(c->host_copied[i]);
+    }
     if (c->d_status) cudaFree(c->d_status);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

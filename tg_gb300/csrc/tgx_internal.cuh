@@ -139,6 +139,13 @@ struct tgx_ctx
     size_t h_pinned_bytes = 0;
     uint64_t* h_counter = nullptr;   // pinned u64 readback slot
     uint32_t trace_steps_per_round = 8;   // DDA steps a traversal lane runs between queue refills
+    // pipelined host-buffer renders (tgx_vis_render_host_async): two device
+    // copies of the buffers, the copy stream and per-copy events
+    cudaStream_t copy_stream = nullptr;
+    DevBuf host_slot[2];
+    cudaEvent_t host_rendered[2] = {nullptr, nullptr};
+    cudaEvent_t host_copied[2] = {nullptr, nullptr};
+    uint64_t host_issued = 0, host_done = 0;
 };
 
 struct tgx_scene

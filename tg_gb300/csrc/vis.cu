@@ -1320,26 +1320,109 @@ extern "C" tgx_status tgx_vis_render(tgx_ctx* c, const tgx_scene* s, const tgx_v
     return vis_render_device(c, s, views, n_views, d_visbuf);
 }
 
+// The device address of pinned (page-locked, mapped) host memory, or null for
+// any other pointer.  The tile kernel stores each pixel once, so it can write
+// a pinned host buffer directly over the CPU-GPU link, hidden under its own
+// work, instead of through a device buffer and a copy.
+static uint64_t* mapped_host(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer ? (uint64_t*)a.devicePointer : nullptr;
+}
+
+// Output pointers of a host-buffer render: pinned buffers directly, the rest
+// in `stage` (device memory, `staged` entries) for a copy afterwards.
+static tgx_status host_outputs(tgx_ctx* c, const tgx_view* views, uint32_t n_views, uint64_t* const* h_visbuf,
+                               DevBuf& stage, std::vector<uint64_t*>& dptr, std::vector<bool>& staged, const char* who)
+{
+    size_t total = 0;
+    std::vector<size_t> offs(n_views);
+    dptr.assign(n_views, nullptr);
+    staged.assign(n_views, false);
+    for (uint32_t i = 0; i < n_views; i++) {
+        if (!h_visbuf[i]) { tgx_set_error("%s: output %u is NULL", who, i); return TGX_ERR_INVALID_ARGUMENT; }
+        dptr[i] = mapped_host(h_visbuf[i]);
+        if (dptr[i]) continue;
+        staged[i] = true;
+        offs[i] = total;
+        total += (size_t)views[i].width * views[i].height;
+    }
+    if (total) TGX_TRY(devbuf_reserve(stage, total * 8));
+    for (uint32_t i = 0; i < n_views; i++)
+        if (staged[i]) dptr[i] = (uint64_t*)stage.ptr + offs[i];
+    return TGX_OK;
+}
+
 extern "C" tgx_status tgx_vis_render_host(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
                                           uint64_t* const* h_visbuf)
 {
     if (!c || !s || !h_visbuf) { tgx_set_error("tgx_vis_render_host: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
     TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
-    size_t total = 0;
-    std::vector<size_t> offs(n_views);
-    for (uint32_t i = 0; i < n_views; i++) {
-        if (!h_visbuf[i]) { tgx_set_error("tgx_vis_render_host: output %u is NULL", i); return TGX_ERR_INVALID_ARGUMENT; }
-        offs[i] = total;
-        total += (size_t)views[i].width * views[i].height;
-    }
-    TGX_TRY(devbuf_reserve(c->host_stage, total * 8));
-    std::vector<uint64_t*> dptr(n_views);
-    for (uint32_t i = 0; i < n_views; i++) dptr[i] = (uint64_t*)c->host_stage.ptr + offs[i];
+    TGX_CUDA(cudaSetDevice(c->device));
+    std::vector<uint64_t*> dptr;
+    std::vector<bool> staged;
+    TGX_TRY(host_outputs(c, views, n_views, h_visbuf, c->host_stage, dptr, staged, "tgx_vis_render_host"));
     TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data()));
     for (uint32_t i = 0; i < n_views; i++)
-        TGX_CUDA(cudaMemcpyAsync(h_visbuf[i], dptr[i], (size_t)views[i].width * views[i].height * 8,
-                                 cudaMemcpyDeviceToHost, c->stream));
+        if (staged[i])
+            TGX_CUDA(cudaMemcpyAsync(h_visbuf[i], dptr[i], (size_t)views[i].width * views[i].height * 8,
+                                     cudaMemcpyDeviceToHost, c->stream));
     TGX_CUDA(cudaStreamSynchronize(c->stream));
+    return TGX_OK;
+}
+
+// Pinned host buffers are written by the render itself.  Other buffers go
+// through two device copies that alternate between frames: frame k renders
+// into copy k % 2 on the context stream once frame k-2's copy out of it is
+// done (an event wait on the device, not the host), then the copy stream
+// takes it to the host while frame k+1 renders into the other copy.
+extern "C" tgx_status tgx_vis_render_host_async(tgx_ctx* c, const tgx_scene* s, const tgx_view* views,
+                                                uint32_t n_views, uint64_t* const* h_visbuf)
+{
+    if (!c || !s || !h_visbuf) {
+        tgx_set_error("tgx_vis_render_host_async: NULL argument");
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
+    TGX_CUDA(cudaSetDevice(c->device));
+    if (!c->copy_stream) {
+        TGX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++) {
+            TGX_CUDA(cudaEventCreateWithFlags(&c->host_rendered[i], cudaEventDisableTiming));
+            TGX_CUDA(cudaEventCreateWithFlags(&c->host_copied[i], cudaEventDisableTiming));
+        }
+    }
+    const uint32_t slot = (uint32_t)(c->host_issued & 1u);
+    // the copy two frames back reads this slot: the render waits for it on the device
+    TGX_CUDA(cudaStreamWaitEvent(c->stream, c->host_copied[slot], 0));
+    std::vector<uint64_t*> dptr;
+    std::vector<bool> staged;
+    TGX_TRY(host_outputs(c, views, n_views, h_visbuf, c->host_slot[slot], dptr, staged, "tgx_vis_render_host_async"));
+    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data()));
+    TGX_CUDA(cudaEventRecord(c->host_rendered[slot], c->stream));
+    TGX_CUDA(cudaStreamWaitEvent(c->copy_stream, c->host_rendered[slot], 0));
+    for (uint32_t i = 0; i < n_views; i++)
+        if (staged[i])
+            TGX_CUDA(cudaMemcpyAsync(h_visbuf[i], dptr[i], (size_t)views[i].width * views[i].height * 8,
+                                     cudaMemcpyDeviceToHost, c->copy_stream));
+    // marks the frame done: after its copies, or after its render when it wrote the host directly
+    TGX_CUDA(cudaEventRecord(c->host_copied[slot], c->copy_stream));
+    c->host_issued++;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_vis_host_wait(tgx_ctx* c, uint32_t max_in_flight)
+{
+    if (!c) { tgx_set_error("tgx_vis_host_wait: NULL context"); return TGX_ERR_INVALID_ARGUMENT; }
+    while (c->host_issued - c->host_done > max_in_flight) {
+        // copies complete in issue order; the slot's event is that of its latest frame
+        TGX_CUDA(cudaEventSynchronize(c->host_copied[c->host_done & 1u]));
+        c->host_done++;
+    }
     return TGX_OK;
 }
 
