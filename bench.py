@@ -478,6 +478,81 @@ def bench_large(local: int):
     return res
 
 
+def run_case(case: str, variant: str, spp: int, local: int) -> None:
+    """One small workload for a profiler: the launches of interest come last
+    and are few.  Prints one JSON line with the launch counts an ncu skip
+    (-s) needs.
+
+    svo-build     two 4096^3 SVO builds of the 512-object scene (profile the second)
+    train-step    cache training steps of 32,768 synthetic samples (3 warm-up, 20 timed)
+    cached-frame  60 warm-up cached-GI frames, then one more (profile the last)"""
+    import torch
+    import tg_gb300 as tg
+
+    torch.cuda.set_device(local)
+    ctx = tg.Context(local, tile=(8, 8))
+    res = {"case": case}
+    if case == "svo-build":
+        sc = ctx.upload(make_scene())
+        for k in range(2):
+            n0 = ctx.launches()
+            t0 = time.perf_counter()
+            svo = ctx.svo_build(sc, (-2048.0, -2048.0, -2048.0), 12)
+            ctx.sync()
+            res[f"build{k}_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+            res[f"build{k}_launches"] = [n0, ctx.launches() - n0]
+            info = svo.info()
+            res["blocks"], res["pairs"] = int(info.n_blocks), int(info.n_pairs)
+            if k == 0:
+                svo.close()
+    elif case == "train-step":
+        n = 32768
+        rng = np.random.default_rng(3)
+        x = np.concatenate([rng.uniform(0, 1, (n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3))], axis=1)
+        x[:, 3:6] /= np.linalg.norm(x[:, 3:6], axis=1, keepdims=True)
+        x[:, 6:9] /= np.linalg.norm(x[:, 6:9], axis=1, keepdims=True)
+        t = (0.3 + 0.2 * np.sin(4 * x[:, :3]) + 0.1 * x[:, 3:6] ** 2).astype(np.float32)
+        cache = tg.Cache(ctx, seed=1)
+        dx, dt = torch.from_numpy(x.astype(np.float32)).cuda(), torch.from_numpy(t).cuda()
+        for _ in range(3):
+            cache.train_step(dx, dt, 1e-2)
+        ctx.sync()
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(20):
+            cache.train_step(dx, dt, 1e-2)
+        e1.record(stream)
+        ctx.sync()
+        res["train_step_us"] = round(e0.elapsed_time(e1) / 20 * 1e3, 1)
+        res["loss"] = cache.last_loss()
+        cache.close()
+    else:
+        sc = ctx.upload(make_scene())
+        view = make_view()
+        vis = torch.empty(W * H, dtype=torch.int64, device="cuda")
+        ctx.vis_render(sc, view, [vis])
+        svo = ctx.svo_build(sc, (-2048.0, -2048.0, -2048.0), 12)
+        out = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+        box = ((-1100.0,) * 3, (1100.0,) * 3)
+        cache = tg.Cache(ctx, seed=7)
+        cp = tg.cache_gi_params(box[0], box[1], **CACHE_VARIANTS[variant])
+        for f in range(60):
+            ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=f), cp, out)
+        ctx.sync()
+        n1 = ctx.launches()
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=spp, bounces=2, seed=2, frame=60), cp, out)
+        ctx.sync()
+        res.update({"variant": variant, "spp": spp, "launches_before_frame": n1,
+                    "frame_launches": ctx.launches() - n1})
+        cache.close()
+    err = ctx.device_error()
+    if err.code:
+        raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
+    ctx.close()
+    print(json.dumps(res), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -494,8 +569,15 @@ def main() -> None:
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
     ap.add_argument("--launch", choices=["graph", "calls"], default="graph",
                     help="time the frame as one CUDA graph replay (tgx_frame_graph) or as separate launches")
+    ap.add_argument("--case", choices=["svo-build", "train-step", "cached-frame"],
+                    help="run only one small workload for a profiler (see run_case) and exit")
+    ap.add_argument("--case-variant", default="configured_training", choices=sorted(CACHE_VARIANTS))
+    ap.add_argument("--case-spp", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        run_case(args.case, args.case_variant, args.case_spp, int(os.environ.get("LOCAL_RANK", "0")))
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
