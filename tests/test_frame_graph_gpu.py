@@ -33,9 +33,10 @@ def test_frame_graph_equals_individual_calls(ctx):
         ctx.vis_render(sc, v, o)
     outs = [[torch.full((w * h,), 7, dtype=torch.int64, device="cuda") for w, h in s] for s in sizes]
     g = ctx.frame_graph([(sc, v, o) for sc, v, o in zip(scenes, views, outs)])
-    # per job: cull, record origins with counts, prefix, scan, finalize, bin
-    # fill; then one persistent tile launch over both jobs' tiles
-    assert g.kernels == 2 * 6 + 1
+    # per job: cull, record origins with counts, prefix, finalize with the
+    # group scan (small frames), bin fill; then one persistent tile launch
+    # over both jobs' tiles
+    assert g.kernels == 2 * 5 + 1
     for o in outs:
         for t in o:
             t.fill_(7)

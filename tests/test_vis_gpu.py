@@ -110,6 +110,21 @@ def test_pipelined_host_buffers_equal_the_oracle(ctx, oracle):
     sc.close()
 
 
+def test_large_frame_scan_path_equals_small_frames():
+    """More than 512 groups of 256 tiles (here two 2048x1088 views in 8x4 tiles,
+    139,264 tiles) take the one-CTA scan + finalize; each view alone (272
+    groups) takes the direct finalize.  Both give the same buffers."""
+    s = fuzz_scene(41, n_objects=12, box=50.0, max_cpa=5)
+    views = [tg.make_view((0.0, 5.0, -90.0), 0.05, float(np.pi), 1.1, 2048, 1088, 0.1, 300.0),
+             tg.make_view((20.0, -5.0, 80.0), -0.1, 0.2, 0.9, 2048, 1088, 0.1, 300.0)]
+    with tg.Context(0, tile=(8, 4)) as c:
+        together = render(c, s, np.concatenate(views))
+        alone = [render(c, s, v)[0] for v in views]
+    for a, b in zip(together, alone):
+        assert_same(a, b)
+        assert (a != EMPTY).sum() > 10000
+
+
 def test_host_buffers_and_pick(ctx, oracle):
     s, v = cfg1_scene(), cfg1_view(64, 64)
     sc = ctx.upload(s)

@@ -17,6 +17,8 @@
 //   4. k_vis_scan           one CTA: bases of the 256-tile groups and the
 //      k_vis_finalize       cursors of the launch order (heaviest class
 //                           first); then per group: tile offsets and order.
+//                           Up to 512 groups, k_vis_finalize_direct does both:
+//                           each CTA reads all groups' sums and histograms.
 //   5. k_vis_bin_fill       one warp per record: scatters it into the
 //                           (tile, bucket) bins, so every tile's list runs
 //                           near to far.
@@ -446,6 +448,95 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize(const uint32_t* __r
     for (uint32_t w = 0; w < wid; w++) before += wsum[w];
     if (valid) {
         tile_off[t] = before + incl - x;
+        tile_order[atomicAdd(&cur[tile_class(x)], 1u)] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4'. frames of at most kDirectGroups groups skip the one-CTA scan: every
+//     CTA of the finalize derives its own group base and class cursors from
+//     all groups' sums and class histograms (read from L2; 127 x 33 words at
+//     1080p), then places its tiles as k_vis_finalize does.  Same offsets,
+//     order and counters as k_vis_scan + k_vis_finalize.
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t kDirectGroups = 512;
+
+__global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32_t* __restrict__ tile_total,
+                                                                   uint32_t n_tiles,
+                                                                   const uint32_t* __restrict__ cta_aux,
+                                                                   uint32_t* __restrict__ tile_off,
+                                                                   uint32_t* __restrict__ tile_order,
+                                                                   uint32_t bin_capacity,
+                                                                   uint32_t* __restrict__ counters)
+{
+    constexpr uint32_t kWarps = kScanTiles / 32;
+    __shared__ uint32_t cur[kOrderClasses];
+    __shared__ uint32_t part_tot[kWarps][kOrderClasses], part_pre[kWarps][kOrderClasses];
+    __shared__ uint32_t red_pre[kWarps], red_all[kWarps], wsum[kWarps];
+    const uint32_t n_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
+    const uint32_t g = blockIdx.x, lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    pdl_wait();
+    pdl_trigger();
+    // this group's base (the sums of the groups before it) and the frame's total
+    uint32_t pre = 0, all = 0;
+    for (uint32_t i = threadIdx.x; i < n_ctas; i += kScanTiles) {
+        const uint32_t v = cta_aux[i];
+        all += v;
+        pre += i < g ? v : 0u;
+    }
+    // per class (lane): its count over all groups and over the groups before this one
+    const uint32_t* cls_cnt = cta_aux + n_ctas;
+    uint32_t ct = 0, cp = 0;
+    for (uint32_t b = wid; b < n_ctas; b += kWarps) {
+        const uint32_t v = cls_cnt[b * kOrderClasses + lane];
+        ct += v;
+        cp += b < g ? v : 0u;
+    }
+    part_tot[wid][lane] = ct;
+    part_pre[wid][lane] = cp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pre += __shfl_xor_sync(0xffffffffu, pre, o);
+        all += __shfl_xor_sync(0xffffffffu, all, o);
+    }
+    if (lane == 0) { red_pre[wid] = pre; red_all[wid] = all; }
+    // the tiles' totals, scanned within each warp
+    const uint32_t t = g * kScanTiles + threadIdx.x;
+    const bool valid = t < n_tiles;
+    const uint32_t x = valid ? tile_total[t] : 0u;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {   // class bases, heaviest class first, plus this group's share before it
+        uint32_t tot = 0, before = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; w++) { tot += part_tot[w][lane]; before += part_pre[w][lane]; }
+        uint32_t suffix = tot;   // classes lane .. 31
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_down_sync(0xffffffffu, suffix, o);
+            if (lane + o < 32) suffix += y;
+        }
+        cur[lane] = suffix - tot + before;
+    }
+    __syncthreads();
+    uint32_t base = 0, total = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kWarps; w++) { base += red_pre[w]; total += red_all[w]; }
+    if (g == 0 && threadIdx.x == 0) {
+        tile_off[n_tiles] = total;
+        counters[C_ENTRIES] = total;
+        counters[C_OVERFLOW] = total > bin_capacity ? 1u : 0u;
+    }
+    for (uint32_t w = 0; w < wid; w++) base += wsum[w];
+    if (valid) {
+        tile_off[t] = base + incl - x;
         tile_order[atomicAdd(&cur[tile_class(x)], 1u)] = t;
     }
 }
@@ -926,10 +1017,15 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
                        s->d_objects, d_vc, w.bucket_cnt, n_tiles);
         TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off,
                        w.tile_total, n_tiles, w.cta_aux);
-        TGX_LAUNCH_PDL(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity,
-                       w.counters);
-        TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles, w.cta_aux,
-                       w.tile_off, w.tile_order);
+        if (n_scan_ctas <= kDirectGroups) {
+            TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize_direct, w.tile_total, n_tiles,
+                           w.cta_aux, w.tile_off, w.tile_order, w.bin_capacity, w.counters);
+        } else {
+            TGX_LAUNCH_PDL(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity,
+                           w.counters);
+            TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles,
+                           w.cta_aux, w.tile_off, w.tile_order);
+        }
     }
     if (phase == VIS_TO_SCAN) return TGX_OK;
     TGX_LAUNCH_PDL(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
@@ -1606,8 +1702,13 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
               n_tiles);
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
     NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
-    NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
-    NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
+    if (n_scan_ctas <= kDirectGroups) {
+        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize_direct, tile_total, n_tiles, cta_aux, tile_off, tile_order,
+                  kNaBins, counters);
+    } else {
+        NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
+        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
+    }
     NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, bins,
               n_tiles, kNaBins, status);
     TileJob J;
