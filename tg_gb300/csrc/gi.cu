@@ -717,27 +717,38 @@ __global__ void __launch_bounds__(256) k_gi_cache_blend(const PathRoot* __restri
     }
 }
 
-// Training roots: n_train bounce hits of this frame picked at random; the
-// target at each is the demodulated radiance (direct / albedo + mean
-// incoming) toward where its ray came from, estimated by the path passes.
-__global__ void __launch_bounds__(256) k_gi_target_roots(GiParams p, CacheGiConst q, const CacheHit* __restrict__ hits,
+// Training roots: n_train bounce hits of this frame, one picked at random
+// from each of n_train equal strata of the hit list (so every hit is
+// equally likely, and neighbouring roots come from neighbouring pixels and
+// trace together).  Root i's sample goes to batch slot key(i), which deals
+// the strata round-robin over the `steps` Adam steps: each step sees the
+// whole frame.  The target at each is the demodulated radiance (direct /
+// albedo + mean incoming) toward where its ray came from, estimated by the
+// path passes.
+__global__ void __launch_bounds__(256) k_gi_target_roots(GiParams p, CacheGiConst q, uint32_t steps,
+                                                        const CacheHit* __restrict__ hits,
                                                         uint32_t* __restrict__ counters, uint32_t capacity,
                                                         PathRoot* __restrict__ roots, float* __restrict__ tx,
                                                         float* __restrict__ tt)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= q.n_train) return;
+    const uint32_t per = steps ? q.n_train / steps : 0u;
+    const uint32_t key = i < per * steps ? (i % steps) * per + i / steps : i;
     const uint32_t n_hits = min(counters[CC_QUERIES], capacity);
     if (i == 0) counters[CC_TRAIN_ROOTS] = n_hits ? q.n_train : 0u;
     if (n_hits == 0) {
 #pragma unroll
-        for (int k = 0; k < 9; k++) tx[9ull * i + k] = 0.0f;
-        tt[3ull * i] = tt[3ull * i + 1] = tt[3ull * i + 2] = 0.0f;
+        for (int k = 0; k < 9; k++) tx[9ull * key + k] = 0.0f;
+        tt[3ull * key] = tt[3ull * key + 1] = tt[3ull * key + 2] = 0.0f;
         return;
     }
     uint32_t ctr[4] = {i, 0x7fffffffu, p.frame, 0x5eedu};
     philox(ctr, (uint32_t)p.seed ^ 0xA5A5A5A5u, (uint32_t)(p.seed >> 32));
-    const CacheHit h = hits[ctr[0] % n_hits];
+    const uint32_t lo = (uint32_t)((uint64_t)i * n_hits / q.n_train);
+    const uint32_t hi = (uint32_t)((uint64_t)(i + 1) * n_hits / q.n_train);
+    const uint32_t pick = hi > lo ? lo + ctr[0] % (hi - lo) : min(lo, n_hits - 1u);
+    const CacheHit h = hits[pick];
     PathRoot rt;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -745,9 +756,9 @@ __global__ void __launch_bounds__(256) k_gi_target_roots(GiParams p, CacheGiCons
         rt.n[k] = h.n[k];
         rt.a[k] = 1.0f;
     }
-    rt.key = i;
+    rt.key = key;
     roots[i] = rt;
-    cache_input(q, h.p, h.n, h.w, tx + 9ull * i);
+    cache_input(q, h.p, h.n, h.w, tx + 9ull * key);
 }
 
 }  // namespace
@@ -1015,8 +1026,8 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         TGX_LAUNCH(c, TR_GI, (q.n_train_primary + 255) / 256, 256, 0, k_gi_primary_batch, p, q, &counters[CC_ROOTS], pqx,
                    pmean, ptx, ptt);
     if (train) {
-        TGX_LAUNCH(c, TR_GI, (q.n_train + 255) / 256, 256, 0, k_gi_target_roots, p, q, hits, counters,
-                   (uint32_t)capacity, b.roots, tx, tt);
+        TGX_LAUNCH(c, TR_GI, (q.n_train + 255) / 256, 256, 0, k_gi_target_roots, p, q, cp->train_steps, hits,
+                   counters, (uint32_t)capacity, b.roots, tx, tt);
         GiParams pp = p;
         pp.bounces = p.bounces - 1;
         pp.frame = p.frame | 0x800000u;   // decorrelated from the pixel streams
