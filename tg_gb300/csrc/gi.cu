@@ -368,9 +368,10 @@ __global__ void __launch_bounds__(256) k_gi_emit(const PathRoot* __restrict__ ro
     const uint64_t n_items = n_paths + (root_rays ? n : 0u);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += (uint64_t)gridDim.x * blockDim.x) {
         if (i < n_paths) {
-            const PathRoot& rt = roots[i / cs];
+            const uint32_t r = (uint32_t)i / cs;   // paths in flight < 2^32: 32-bit division
+            const PathRoot& rt = roots[r];
             float w[3];
-            sample_cosine(rt.n, rt.key, s0 + (uint32_t)(i % cs), 0, p, w);
+            sample_cosine(rt.n, rt.key, s0 + ((uint32_t)i - r * cs), 0, p, w);
             set_ray(rays[i], rt.o, w);
             if (!st) continue;   // first-bounce queries keep no path state
             PathState ps;
@@ -432,7 +433,8 @@ __global__ void __launch_bounds__(256) k_gi_shade(SvoDev s, const tgx_material* 
                 if (ps.ndl > 0.0f) set_ray(ns, o3, p.sun_dir);
                 if (k + 1 < p.bounces) {
                     float w2[3];
-                    sample_cosine(n2, roots[i / cs].key, s0 + (uint32_t)(i % cs), k + 1, p, w2);
+                    const uint32_t r = (uint32_t)i / cs;
+                    sample_cosine(n2, roots[r].key, s0 + ((uint32_t)i - r * cs), k + 1, p, w2);
                     set_ray(nb, o3, w2);
                 } else {
                     ps.flags &= ~P_ALIVE;
@@ -536,7 +538,8 @@ __global__ void __launch_bounds__(256) k_gi_query_shade(SvoDev s, const tgx_mate
     const uint64_t n_paths = (uint64_t)(*n_dev) * cs;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_paths; i += (uint64_t)gridDim.x * blockDim.x) {
         const RayHit h = hb[i];
-        int32_t* qi = qidx + (i / cs) * spp + s0 + (i % cs);
+        const uint32_t r = (uint32_t)i / cs;   // paths in flight < 2^32: 32-bit division
+        int32_t* qi = qidx + (uint64_t)r * spp + s0 + ((uint32_t)i - r * cs);
         const bool hit = h.res == 1;
         const uint32_t slot = warp_append(&counters[CC_QUERIES], hit);
         if (!hit) { *qi = -1; continue; }
