@@ -624,15 +624,37 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tt::TMEM_COLS) : "memory");
 }
 
-// Sum of the CTAs' gradient slices, in CTA order, added to the gradient.
+// Sum of the CTAs' gradient slices of parameter p in a fixed order: eight
+// running sums over the slices c = j mod 8 of the first 8 * floor(n / 8)
+// (eight loads in flight instead of one chain), added 0 + 1 + ... + 7, then
+// the rest in order.  Deterministic; k_mlp_reduce and k_mlp_adam share it,
+// so both see the same gradient bits.
+__device__ __forceinline__ float sum_slices(const float* __restrict__ partial, uint32_t n_parts, int p)
+{
+    float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t c = 0;
+    for (; c + 8 <= n_parts; c += 8) {
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[j] = partial[(uint64_t)(c + j) * N_PARAMS + p];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[j] += x[j];
+    }
+    float tail = 0.0f;   // the last n_parts mod 8 slices
+    for (; c < n_parts; c++) tail += partial[(uint64_t)c * N_PARAMS + p];
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += acc[j];
+    return s + tail;
+}
+
+// The slices' sum added to the gradient.
 __global__ void __launch_bounds__(256) k_mlp_reduce(const float* __restrict__ partial, uint32_t n_parts,
                                                    float* __restrict__ g)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N_PARAMS) return;
-    float s = 0.0f;
-    for (uint32_t c = 0; c < n_parts; c++) s += partial[(uint64_t)c * N_PARAMS + p];
-    g[p] += s;
+    g[p] += sum_slices(partial, n_parts, p);
 }
 
 // bf16 image position of master parameter p
@@ -648,8 +670,8 @@ __device__ __forceinline__ int image_pos(int p)
 }
 
 // Adam for up to two networks (blockIdx.y).  The gradient is g plus the
-// n_parts slices of `partial` (the training kernel's per-CTA sums) added in
-// CTA order, as k_mlp_reduce adds them.
+// n_parts slices of `partial` (the training kernel's per-CTA sums) added as
+// k_mlp_reduce adds them (sum_slices).
 struct AdamJob
 {
     float* w;
@@ -681,9 +703,7 @@ __global__ void __launch_bounds__(256) k_mlp_adam(AdamJobs jobs, float lr, float
     const uint32_t n_parts = second ? K.n_parts : J.n_parts;
     const float c1 = second ? K.c1 : J.c1, c2 = second ? K.c2 : J.c2;
     __nv_bfloat16* img = second ? K.img : J.img;
-    float sum = 0.0f;
-    for (uint32_t c = 0; c < n_parts; c++) sum += partial[(uint64_t)c * N_PARAMS + p];
-    const float gp = g[p] + sum;
+    const float gp = g[p] + sum_slices(partial, n_parts, p);
     g[p] = 0.0f;
     const float mp = b1 * m[p] + (1.0f - b1) * gp;
     const float vp = b2 * v[p] + (1.0f - b2) * gp * gp;
