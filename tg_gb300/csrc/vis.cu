@@ -119,17 +119,26 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
             const float ohx = xmul(half, (float)od.n_cluster_pointers_per_dim[0]);
             const float ohy = xmul(half, (float)od.n_cluster_pointers_per_dim[1]);
             const float ohz = xmul(half, (float)od.n_cluster_pointers_per_dim[2]);
-            float rot[16];
+            // the box's corner 0 relative to the camera and its three edges (8 voxels
+            // along each rotated axis); corner k = base + (k&1) ex + (k&2) ey + (k&4) ez.
+            // Rounding differs from a per-corner transform by ulps, far inside the
+            // cull's slack (0.05 + 1e-5 |p|) and the rectangle's 2-pixel margin.
+            float base[3], ex[3], ey[3], ez[3];
+            {
+                const float lx = offx - ohx, ly = offy - ohy, lz = offz - ohz;
 #pragma unroll
-            for (int k = 0; k < 16; k++) rot[k] = od.rotation[k];
+                for (int r = 0; r < 3; r++) {
+                    const float r0 = od.rotation[r], r1 = od.rotation[4 + r], r2 = od.rotation[8 + r];
+                    base[r] = r0 * lx + r1 * ly + r2 * lz + od.translation[r] - vc.cam[r];
+                    ex[r] = 8.0f * r0; ey[r] = 8.0f * r1; ez[r] = 8.0f * r2;
+                }
+            }
 
             // ---- bounding-sphere cull against the side planes and the far plane ----
             {
-                const float lx = offx + 4.0f - ohx, ly = offy + 4.0f - ohy, lz = offz + 4.0f - ohz;
                 float q[3];
 #pragma unroll
-                for (int r = 0; r < 3; r++)
-                    q[r] = DM(rot, r, 0) * lx + DM(rot, r, 1) * ly + DM(rot, r, 2) * lz + od.translation[r] - vc.cam[r];
+                for (int r = 0; r < 3; r++) q[r] = base[r] + 0.5f * (ex[r] + ey[r] + ez[r]);
                 const float rad = 6.9283f + 0.05f + 1e-5f * (fabsf(q[0]) + fabsf(q[1]) + fabsf(q[2]));
                 const float dist = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
                 bool out = dist - rad > vc.far_plane * 1.0001f;
@@ -153,13 +162,10 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
             float cxw = 0.0f, cyw = 0.0f, czw = 0.0f;
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                const float lx = offx + ((k & 1) ? 8.0f : 0.0f) - ohx;
-                const float ly = offy + ((k & 2) ? 8.0f : 0.0f) - ohy;
-                const float lz = offz + ((k & 4) ? 8.0f : 0.0f) - ohz;
                 float p[3];
 #pragma unroll
                 for (int r = 0; r < 3; r++)
-                    p[r] = DM(rot, r, 0) * lx + DM(rot, r, 1) * ly + DM(rot, r, 2) * lz + od.translation[r] - vc.cam[r];
+                    p[r] = base[r] + ((k & 1) ? ex[r] : 0.0f) + ((k & 2) ? ey[r] : 0.0f) + ((k & 4) ? ez[r] : 0.0f);
                 cxw += p[0]; cyw += p[1]; czw += p[2];
                 const float depth = p[0] * vc.fwd[0] + p[1] * vc.fwd[1] + p[2] * vc.fwd[2];
                 if (depth > -0.5f) any_front = true;
