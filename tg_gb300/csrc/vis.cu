@@ -11,7 +11,7 @@
 //      appends a 32-byte record.
 //   2. k_vis_count          per record: the ws2ms matrix and the camera
 //      position in cluster space exactly as the shader does (one thread per
-//      record), and its counts per (tile, depth bucket) (one warp per record).
+//      record), and its counts per (tile, depth bucket) (a half-warp per record).
 //   3. k_vis_prefix         per tile: offsets of its 16 depth buckets; per
 //                           256 tiles: their sum and class histogram.
 //   4. k_vis_scan           one CTA: bases of the 256-tile groups and the
@@ -19,7 +19,7 @@
 //                           first); then per group: tile offsets and order.
 //                           Up to 512 groups, k_vis_finalize_direct does both:
 //                           each CTA reads all groups' sums and histograms.
-//   5. k_vis_bin_fill       one warp per record: scatters it into the
+//   5. k_vis_bin_fill       a half-warp per record: scatters it into the
 //                           (tile, bucket) bins, so every tile's list runs
 //                           near to far.
 //   6. k_vis_tiles          one CTA per screen tile, one thread per pixel:
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
 
 // ---------------------------------------------------------------------------
 // 2. per record: the exact ws2ms and ray origin (visibility.frag:57-66), one
-//    thread per record; then its per-(tile, bucket) counts, one warp per
+//    thread per record; then its per-(tile, bucket) counts, a half-warp per
 //    record with the lanes over its tiles.  The two loops write different
 //    fields and buffers; the cull kept apart runs at high occupancy.
 // ---------------------------------------------------------------------------
@@ -268,15 +268,15 @@ __global__ void __launch_bounds__(256) k_vis_count(VisRecord* __restrict__ recor
         dm4_mulv4(ws2ms, vc.cam[0], vc.cam[1], vc.cam[2], 1.0f, o);
         rec.ox = o[0]; rec.oy = o[1]; rec.oz = o[2];
     }
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t lane = threadIdx.x & 15u;   // a half-warp per record: records span ~17 tiles on average
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; i < n; i += (gridDim.x * blockDim.x) >> 4) {
         const uint2 r = rects[i];
         const uint32_t view = records[i].view;
         const ViewConst& vc = views[view];
         const uint32_t b = depth_bucket(records[i].d24_lb);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
-        for (uint32_t k = lane; k < cnt; k += 32) {
+        for (uint32_t k = lane; k < cnt; k += 16) {
             const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
             atomicAdd(&bucket_cnt[b * n_tiles + t], 1u);
         }
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
 }
 
 // ---------------------------------------------------------------------------
-// 5. bin fill: one warp per record, lanes over its tiles
+// 5. bin fill: a half-warp per record, lanes over its tiles
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restrict__ records,
@@ -564,16 +564,16 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
     pdl_wait();
     pdl_trigger();
     if (counters[C_OVERFLOW]) return;   // the tile kernel scans all records instead
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 15u;   // a half-warp per record, as in k_vis_count
     const uint32_t n = counters[C_RECORDS];
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; i < n; i += (gridDim.x * blockDim.x) >> 4) {
         const uint2 r = rects[i];
         const VisRecord& rec = records[i];
         const ViewConst& vc = views[rec.view];
         const uint32_t b = depth_bucket(rec.d24_lb);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
-        for (uint32_t k = lane; k < cnt; k += 32) {
+        for (uint32_t k = lane; k < cnt; k += 16) {
             const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
             const uint32_t pos = tile_off[t] + bucket_off[b * n_tiles + t] + atomicAdd(&cursor[b * n_tiles + t], 1u);
             if (pos < bin_capacity) bins[pos] = i;
