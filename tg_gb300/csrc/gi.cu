@@ -52,12 +52,14 @@ struct GiParams
 };
 static_assert(sizeof(GiParams) == sizeof(tgx_gi_params), "GI parameter layout");
 
-struct Ray
+// Records of the wavefront passes, aligned so that a thread moves each with
+// vector loads and stores (8 or 16 bytes) instead of one word at a time.
+struct __align__(8) Ray
 {
     float o[3], d[3];   // d = 0: no ray
 };
 
-struct RayHit
+struct __align__(8) RayHit
 {
     float t;
     int32_t c[3];
@@ -65,7 +67,7 @@ struct RayHit
     int32_t res;        // 1 hit, 0 miss, -1 step budget ran out
 };
 
-struct PathRoot
+struct __align__(8) PathRoot
 {
     float o[3];         // offset surface point
     float n[3];         // normal
@@ -73,7 +75,7 @@ struct PathRoot
     uint32_t key;       // Philox key and output index (pixel, or training sample)
 };
 
-struct PathState
+struct __align__(16) PathState
 {
     float v[3];         // radiance gathered so far
     float T[3];         // throughput
@@ -83,6 +85,8 @@ struct PathState
     uint32_t pad;
 };
 enum : uint32_t { P_ALIVE = 1u, P_SHADOW = 2u };
+static_assert(sizeof(Ray) == 24 && sizeof(RayHit) == 24 && sizeof(PathRoot) == 40 && sizeof(PathState) == 48,
+              "record sizes: the alignment adds no padding");
 
 __device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
 {
@@ -193,14 +197,16 @@ __device__ __forceinline__ void sun_term(const float a[3], float ndl, const GiPa
 
 __device__ __forceinline__ void set_ray(Ray& r, const float o[3], const float d[3])
 {
-    r.o[0] = o[0]; r.o[1] = o[1]; r.o[2] = o[2];
-    r.d[0] = d[0]; r.d[1] = d[1]; r.d[2] = d[2];
+    float2* q = reinterpret_cast<float2*>(&r);   // three 8-byte stores
+    q[0] = make_float2(o[0], o[1]);
+    q[1] = make_float2(o[2], d[0]);
+    q[2] = make_float2(d[1], d[2]);
 }
 
 __device__ __forceinline__ void null_ray(Ray& r)
 {
-    r.o[0] = r.o[1] = r.o[2] = 0.0f;
-    r.d[0] = r.d[1] = r.d[2] = 0.0f;
+    float2* q = reinterpret_cast<float2*>(&r);
+    q[0] = q[1] = q[2] = make_float2(0.0f, 0.0f);
 }
 
 // face normal of an SVO hit: the face crossed, or the dominant axis when the
