@@ -493,9 +493,9 @@ typedef struct tgx_cache_gi_params
  * each pixel's sample mean m of incoming light.  With primary_weight w > 0 a
  * pixel's incoming light becomes m + k (P - m), P the network's prediction.
  * With one sample k = w.  With spp > 1, k = min(w, s v / (s v + b)): b is
- * the network's squared error over the pixel's 9x9 neighbourhood (mean
+ * the network's squared error over the pixel's 13x13 neighbourhood (mean
  * |P - m|^2 less mean variance of m), v the variance of m, its own estimate
- * mixed with the neighbourhood's as (spp - 1) : 1, and s =
+ * mixed with the neighbourhood's as (spp - 1) : 1/2, and s =
  * primary_variance_scale; both relative to the pixel's predicted brightness.
  * The prediction counts where the network is accurate around the pixel and
  * the pixel's samples are noisy.  Asynchronous; all buffers DEVICE memory.

@@ -682,12 +682,12 @@ __global__ void __launch_bounds__(256) k_gi_cache_resolve(const PathRoot* __rest
 // The shrinkage weight.  Over the geometry pixels of the (2R+1)^2 window the
 // mean relative variance vn and mean relative disagreement dn give the
 // network's local squared error b2 = max(dn - vn, 0); the pixel's variance is
-// its own estimate v mixed with vn by their degrees of freedom,
-// vm = a v + (1 - a) vn with a = (spp - 1) / spp, so that a pixel whose few
+// its own estimate v mixed with vn, vm = a v + (1 - a) vn with
+// a = (spp - 1) / (spp - 1/2) (0.67 at 2 spp, 0.8 at 3), so that a pixel whose few
 // samples spread far apart leans toward the network.  Then
 // k = min(w, s vm / (s vm + b2)), s the variance scale: the k that minimises
 // the expected error of m + k (P - m) for noise vm and network error b2.
-constexpr int kBlendRadius = 4;
+constexpr int kBlendRadius = 6;   // a 13x13 window
 
 __global__ void __launch_bounds__(256) k_gi_cache_blend(const PathRoot* __restrict__ roots,
                                                        const uint32_t* __restrict__ n_dev, GiParams p,
@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(256) k_gi_cache_blend(const PathRoot* __restri
                                                        float* __restrict__ out)
 {
     const uint32_t n = *n_dev;
-    const float a = (float)(p.spp - 1) / (float)p.spp;
+    const float a = (float)(p.spp - 1) / ((float)p.spp - 0.5f);
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const PathRoot& rt = roots[r];
         const int x = (int)(rt.key % width), y = (int)(rt.key / width);
