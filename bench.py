@@ -42,15 +42,21 @@ CONFIG = {
 }
 
 
+# the 512-object scene and its 1080p view (generator arguments of tgx_generate_scene / tgx_make_view)
+SCENE_ARGS = (1, 512, 2, 16, 1)
+SCENE_KW = dict(noise_period=64.0, noise_threshold=0.5, box_min=(-1024.0, -1024.0, -1024.0),
+                box_max=(1024.0, 1024.0, 1024.0), n_luts=32)
+VIEW_ARGS = ((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), W, H, 0.1, 4096.0)
+
+
 def make_scene():
     import tg_gb300 as tg
-    return tg.generate_scene(1, 512, 2, 16, seed=1, noise_period=64.0, noise_threshold=0.5,
-                             box_min=(-1024.0, -1024.0, -1024.0), box_max=(1024.0, 1024.0, 1024.0), n_luts=32)
+    return tg.generate_scene(*SCENE_ARGS, **SCENE_KW)
 
 
 def make_view():
     import tg_gb300 as tg
-    return tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), W, H, 0.1, 4096.0)
+    return tg.make_view(*VIEW_ARGS)
 
 
 class ClockSampler:
@@ -108,31 +114,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference(budget_s: float = 12.0, rows_per_chunk: int = 32):
-    """The oracle (CPU transcription of visibility.frag) on bands of rows of the
-    same frame, all host threads, until about budget_s seconds are spent."""
+def cpu_reference(budget_s: float = 12.0, scene=None, view=None):
+    """The oracle (CPU transcription of visibility.frag) rendering whole frames
+    of the same workload on all host threads until about budget_s seconds are
+    spent.  Without a scene it builds the scene and view with the oracle's own
+    generator (byte-equal to the product's), so the product library is never
+    loaded."""
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle_lib import Oracle
 
-    scene, view = make_scene(), make_view()
     o = Oracle()
+    if scene is None:
+        scene = o.generate_scene(*SCENE_ARGS, **SCENE_KW)
+        view = o.make_view(*VIEW_ARGS)
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    rows = 0
-    y = 0
-    # spread the sampled bands over the frame so the sample sees the same mix of sky and geometry
-    order = list(range(0, H, rows_per_chunk))
-    rng = np.random.default_rng(0)
-    rng.shuffle(order)
-    for y in order:
-        o.vis_render(scene, view, mode=1, rows=(y, min(H, y + rows_per_chunk)), threads=cores)
-        rows += min(H, y + rows_per_chunk) - y
-        if time.perf_counter() - t0 > budget_s:
+    frames = 0
+    while True:
+        o.vis_render(scene, view, mode=1, threads=cores)
+        frames += 1
+        dt = time.perf_counter() - t0
+        if dt > budget_s:
             break
-    dt = time.perf_counter() - t0
-    value = rows * W / dt / 1e9
+    value = frames * W * H / dt / 1e9
     return {"value": value, "unit": "Grays/s", "cores": cores, "kind": "port",
-            "sample": f"{rows} of {H} rows of the 1920x1080 frame ({rows * W} primary rays) in {dt:.1f} s"}
+            "sample": f"{frames} whole 1920x1080 frames ({frames * W * H} primary rays) in {dt:.1f} s"}
 
 
 def run_reference(args, rank: int) -> None:
@@ -141,8 +147,13 @@ def run_reference(args, rank: int) -> None:
     steps = []
     cb = None
     per_step = max(2.0, min(10.0, 150.0 / (args.warmup + args.steps)))
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import Oracle
+    o = Oracle()
+    scene = o.generate_scene(*SCENE_ARGS, **SCENE_KW)
+    view = o.make_view(*VIEW_ARGS)
     for i in range(args.warmup + args.steps):
-        r = cpu_reference(budget_s=per_step / 2 if i < args.warmup else per_step)
+        r = cpu_reference(budget_s=per_step / 2 if i < args.warmup else per_step, scene=scene, view=view)
         if i >= args.warmup:
             steps.append(r)
         cb = r
@@ -830,8 +841,9 @@ def main() -> None:
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": {**CONFIG, "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "tile": f"{tile[0]}x{tile[1]}",
+        "config": CONFIG,
+        "parallelism": "replicas" if world > 1 else "single-gpu",
+        "tuning": {"tile": f"{tile[0]}x{tile[1]}",
                    "autotune_ms": {f"{t[0]}x{t[1]}": round(v, 4) for t, v in tuning.items()}},
         "e2e": {"value": rays * world / (e2e_blocking * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
                 "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e_blocking,
@@ -861,7 +873,7 @@ def main() -> None:
         "wall_s_timed": t_wall,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_reference(budget_s=12.0)
+        line["cpu_baseline"] = cpu_reference(budget_s=12.0, scene=scene, view=view)
     if rank == 0:
         print(json.dumps(line), flush=True)
     sc.close()

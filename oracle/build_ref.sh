@@ -9,9 +9,13 @@
 # tg_math.c carries MSVC integer suffixes (tg_math.c:695-696,749-750: `1ui32`)
 # that gcc rejects, so a suffix-stripped copy is made in a temporary directory
 # that is deleted afterwards; only the .so lands in oracle/_ref/.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: $TGX_REFERENCE_ROOT)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${TGX_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "no reference root given (argument or TGX_REFERENCE_ROOT); skipping" >&2
+    exit 0
+fi
 SRC="$REF/tg/src"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"

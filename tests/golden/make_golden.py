@@ -2,7 +2,7 @@
 own CPU code (oracle/_ref/libtgref.so, built by oracle/build_ref.sh from the
 reference sources).  Run from the repository root:
 
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh <reference checkout root> && python tests/golden/make_golden.py
 
 Fixtures:
   ref_primitives.npz   tgm_m4_angle_axis, tgm_m4_inverse, tgm_m4_mul,

@@ -37,9 +37,86 @@ def load_ref() -> C.CDLL | None:
     return lib
 
 
+# numpy layouts of include/tgx.h's records, kept here so that this module
+# never loads the product library (bench.py's CPU reference arm uses it alone)
+OBJECT_DTYPE = np.dtype([
+    ("n_cluster_pointers_per_dim", np.uint32, 3), ("first_cluster_pointer", np.uint32),
+    ("translation", np.float32, 3), ("lut_idx", np.uint32), ("rotation", np.float32, 16),
+])
+VIEW_DTYPE = np.dtype([
+    ("camera", np.float32, 4), ("ray_bl", np.float32, 4), ("ray_br", np.float32, 4),
+    ("ray_tr", np.float32, 4), ("ray_tl", np.float32, 4), ("near_plane", np.float32),
+    ("far_plane", np.float32), ("width", np.uint32), ("height", np.uint32),
+])
+MATERIAL_DTYPE = np.dtype([("albedo", np.float32, 3), ("roughness", np.float32)])
+assert OBJECT_DTYPE.itemsize == 96 and VIEW_DTYPE.itemsize == 96
+
+
+class _GenParams(C.Structure):
+    """tgx_gen_params (include/tgx.h)."""
+    _fields_ = [
+        ("kind", C.c_uint32), ("n_objects", C.c_uint32), ("min_clusters_per_axis", C.c_uint32),
+        ("max_clusters_per_axis", C.c_uint32), ("bernoulli_p", C.c_float), ("noise_period", C.c_float),
+        ("noise_threshold", C.c_float), ("seed", C.c_uint64), ("box_min", C.c_float * 3),
+        ("box_max", C.c_float * 3), ("fixed_translation", C.c_float * 3), ("n_luts", C.c_uint32),
+        ("threads", C.c_uint32),
+    ]
+
+
+class OracleScene:
+    """A scene store in numpy arrays with the fields the oracle reads."""
+
+    def __init__(self, objects, cluster_pointers, cluster_idx_to_object_idx, voxel_bits, material_idx, luts):
+        self.objects = objects
+        self.cluster_pointers = cluster_pointers
+        self.cluster_idx_to_object_idx = cluster_idx_to_object_idx
+        self.voxel_bits = voxel_bits
+        self.material_idx = material_idx
+        self.luts = luts
+
+
 class Oracle:
     def __init__(self):
         self.lib = load_oracle()
+        lib = self.lib
+        vp = C.c_void_p
+        lib.oracle_gen_objects.restype = C.c_uint64
+        lib.oracle_gen_objects.argtypes = [vp, vp]
+        lib.oracle_gen_fill.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, vp, vp]
+        lib.oracle_make_view.restype = C.c_int
+        lib.oracle_make_view.argtypes = [vp, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32, C.c_float,
+                                         C.c_float, vp]
+
+    def generate_scene(self, kind: int, n_objects: int, min_cpa: int, max_cpa: int, seed: int, *,
+                       bernoulli_p: float = 0.3, noise_period: float = 64.0, noise_threshold: float = 0.5,
+                       box_min=(0.0, 0.0, 0.0), box_max=(0.0, 0.0, 0.0), translation=(0.0, 0.0, 0.0),
+                       n_luts: int = 1, threads: int = 0) -> OracleScene:
+        """The seeded synthetic scene, from the oracle's own generator (oracle_scene.c);
+        the arguments mean what they mean for the product's tgx_generate_scene."""
+        p = _GenParams(kind=kind, n_objects=n_objects, min_clusters_per_axis=min_cpa,
+                       max_clusters_per_axis=max_cpa, bernoulli_p=bernoulli_p, noise_period=noise_period,
+                       noise_threshold=noise_threshold, seed=seed, n_luts=n_luts, threads=threads)
+        p.box_min[:] = box_min
+        p.box_max[:] = box_max
+        p.fixed_translation[:] = translation
+        objects = np.zeros(n_objects, OBJECT_DTYPE)
+        n = int(self.lib.oracle_gen_objects(C.byref(p), _p(objects)))
+        assert n > 0, "scene too large"
+        cp = np.zeros(n, np.uint32)
+        c2o = np.zeros(n, np.uint32)
+        bits = np.zeros((n, 16), np.uint32)
+        mats = np.zeros((n, 512), np.uint8)
+        luts = np.zeros(max(1, n_luts) * 256, MATERIAL_DTYPE)
+        self.lib.oracle_gen_fill(C.byref(p), _p(objects), n, _p(cp), _p(c2o), _p(bits), _p(mats), _p(luts))
+        return OracleScene(objects, cp, c2o, bits, mats, luts)
+
+    def make_view(self, position, pitch: float, yaw: float, fov_y: float, width: int, height: int,
+                  near: float = 0.1, far: float = 256.0) -> np.ndarray:
+        """tg's pinhole view (oracle_make_view) as a one-record array."""
+        v = np.zeros(1, VIEW_DTYPE)
+        pos = np.asarray(position, np.float32)
+        assert self.lib.oracle_make_view(_p(pos), pitch, yaw, fov_y, width, height, near, far, _p(v)) == 0
+        return v
 
     def vis_render(self, scene, view, mode: int = 1, rows=None, threads: int = 0) -> np.ndarray:
         v = np.ascontiguousarray(view).reshape(1)
