@@ -135,6 +135,13 @@ typedef struct tgx_config
 /* Keeps the visibility bin storage at its minimum (64 entries) so frames
  * overflow it and take the exact record-scan path; for testing that path. */
 #define TGX_FLAG_MIN_BIN_CAPACITY       1u
+/* Test of the device-side timeout path: the first bitmask batch of every
+ * visibility tile waits for 64 bytes more than it copies, so its bounded wait
+ * (about one second) runs out.  The tile then stops staging, the frame's
+ * pixels are incomplete, and tgx_last_device_error reports TGX_ERR_TIMEOUT
+ * (where = 5).  Nothing faults; the context stays usable.  Never set it
+ * outside such a test. */
+#define TGX_FLAG_TEST_LOST_COPY         2u
 
 typedef struct tgx_device_error
 {
@@ -241,13 +248,20 @@ tgx_status  tgx_vis_host_wait(tgx_ctx* ctx, uint32_t max_in_flight);
  * which every GPU that loads the library holds until the process exits.
  * Limits: at most 65,536 objects, 524,288 cluster pointers and 32,768 screen
  * tiles of 16x16 pixels (3840x2160 fits); larger inputs are rejected with
- * TGX_ERR_CAPACITY and a message.  The first call on a device looks up the
- * array's device address, so make that first call before any stream capture.
- * Every call shares the one array and reuses what the previous call left in
- * it, so calls whose work overlaps on the GPU (other streams, other host
- * threads) race; serialise them.  Runs on `stream` (a cudaStream_t, or NULL
- * for the legacy default stream) and returns without waiting, unless
- * out_error is non-NULL: then it waits and reports the device status word.
+ * TGX_ERR_CAPACITY and a message.  The tile bins hold 1,048,576 (cluster,
+ * tile) entries; a frame that needs more is still rendered exactly, but every
+ * tile then tests every visible cluster's screen rectangle, which is much
+ * slower (tgx_vis_render grows its bins instead).  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress, once per device,
+ * with that device current), so make that first call before any stream
+ * capture.  The view and the output pointer are handed to the GPU by value in
+ * a kernel's arguments: no host buffer is read after the call returns.  Every
+ * call shares the one array and reuses what the previous call left in it
+ * (what must start at zero is cleared by each call), so calls whose work
+ * overlaps on the GPU (other streams, other host threads) race; serialise
+ * them.  Runs on `stream` (a cudaStream_t, or NULL for the legacy default
+ * stream) and returns without waiting, unless out_error is non-NULL: then it
+ * synchronises the stream and reports the device status word.
  */
 tgx_status  tgx_vis_render_noalloc(void* stream, const tgx_object* d_objects, uint32_t n_objects,
                                    const uint32_t* d_cluster_pointers, uint32_t n_cluster_pointers,

@@ -267,3 +267,50 @@ def test_trace_steps_per_round_changes_no_result(ctx):
         with pytest.raises(tg.TgxError):
             ctx.set_trace_steps(bad)
     svo.close(); sc.close()
+
+
+@pytest.fixture(scope="module")
+def bench_scene(oracle):
+    """The benchmarked GI frame's inputs: the 512-object scene, its 4096^3 SVO
+    around the camera as the oracle builds it (with materials), the 1080p view."""
+    s = tg.generate_scene(1, 512, 2, 16, seed=1, noise_period=64.0, noise_threshold=0.5,
+                          box_min=(-1024, -1024, -1024), box_max=(1024, 1024, 1024), n_luts=32)
+    mn, L = [-2048.0] * 3, 12
+    blocks, words, mats = svo_build_with_materials(oracle, s, mn, L, capacity=1 << 15)
+    osvo = OracleSvo(oracle, blocks, words, mats, mn, L)
+    view = tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), 1920, 1080, 0.1, 4096.0)
+    yield s, mn, L, osvo, view, len(blocks)
+    osvo.close()
+
+
+@pytest.mark.parametrize("bounces,spp", [(1, 4), (2, 2)])
+def test_gi_benchmark_frame_bands_bit_exact(ctx, oracle, bench_scene, bounces, spp):
+    """Plain GI of the benchmarked frame (512 objects, 4096^3 SVO, 1920x1080,
+    Philox seed 2, <= 256 SVO steps) against the oracle bit for bit on three
+    bands of 16 rows spread over the frame (92,160 pixels); the SVO itself
+    equals the oracle's block for block."""
+    import torch
+    s, mn, L, osvo, view, n_oracle_blocks = bench_scene
+    sc = ctx.upload(s)
+    svo = ctx.svo_build(sc, mn, L)
+    assert svo.info().n_nonempty_blocks == n_oracle_blocks
+    vis = torch.empty(1920 * 1080, dtype=torch.int64, device="cuda")
+    ctx.vis_render(sc, view, [vis])
+    params = tg.gi_params(spp=spp, bounces=bounces, seed=2, max_steps=256)
+    rgb = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
+    ctx.gi_render(sc, svo, view, vis, params, rgb)
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    g = rgb.cpu().numpy().reshape(-1, 3)
+    visb = vis.cpu().numpy().view(np.uint64)
+    n_geo = 0
+    for r0 in (200, 532, 900):
+        rows = (r0, r0 + 16)
+        ref = gi_render(oracle, osvo, s, view, params, visb, rows=rows)
+        sl = slice(rows[0] * 1920, rows[1] * 1920)
+        bad = np.nonzero((g[sl].view(np.uint32) != ref[sl].view(np.uint32)).any(axis=1))[0]
+        assert len(bad) == 0, (rows, len(bad), bad[:5], g[sl][bad[:3]], ref[sl][bad[:3]])
+        n_geo += int((visb[sl] != np.uint64(tg.VIS_EMPTY)).sum())
+    assert n_geo > 5000
+    svo.close()
+    sc.close()

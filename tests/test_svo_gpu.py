@@ -52,6 +52,38 @@ def test_matches_oracle_other_extents(ctx, oracle, seed, L):
     assert np.array_equal(words, owords)
 
 
+def test_benchmark_scene_4096_matches_oracle(ctx, oracle):
+    """The benchmarked SVO: the 512-object scene in the 4096^3 cube around the
+    camera (15,856 non-empty blocks), block for block against the oracle."""
+    s = tg.generate_scene(1, 512, 2, 16, seed=1, noise_period=64.0, noise_threshold=0.5,
+                          box_min=(-1024, -1024, -1024), box_max=(1024, 1024, 1024), n_luts=32)
+    mn = [-2048.0] * 3
+    xyz, words, info = build(ctx, s, mn, 12)
+    oxyz, owords, _ = oracle.svo_build(s, mn, 12, capacity=1 << 15)
+    assert len(oxyz) > 10000
+    assert np.array_equal(xyz, oxyz)
+    assert np.array_equal(words, owords)
+
+
+@pytest.mark.parametrize("L", [13, 14])
+def test_largest_extents_match_oracle(ctx, oracle, L):
+    """Side lengths 8192 and 16384 (the large configuration's SVO): a small
+    scene placed near the cube's far corner, at the origin and near its near
+    corner, so block coordinates reach the top of the block table."""
+    half = 2.0 ** (L - 1)
+    s = permute_clusters(fuzz_scene(40 + L, n_objects=9, box=60.0, max_cpa=4), L)
+    objs = s.objects.copy()
+    for i, c in enumerate((half - 90.0, 0.0, -half + 90.0)):
+        objs["translation"][3 * i:3 * i + 3] += np.float32(c)
+    s = tg.HostScene(objs, s.cluster_pointers, s.cluster_idx_to_object_idx, s.voxel_bits, s.material_idx, s.luts)
+    mn = [-half] * 3
+    xyz, words, info = build(ctx, s, mn, L)
+    oxyz, owords, _ = oracle.svo_build(s, mn, L)
+    assert len(oxyz) > 0 and xyz.max() > half - 200 and xyz.min() < -half + 200
+    assert np.array_equal(xyz, oxyz)
+    assert np.array_equal(words, owords)
+
+
 def test_offset_extent_and_clusters_outside(ctx, oracle):
     # objects partly outside the cube: only the inside voxels are built
     s = fuzz_scene(7, n_objects=6, box=120.0, max_cpa=5)

@@ -28,6 +28,7 @@ STATUS_NAMES = {
 }
 VIS_EMPTY = 0xFFFFFFFFFFFFFFFF
 FLAG_MIN_BIN_CAPACITY = 1
+FLAG_TEST_LOST_COPY = 2
 
 # numpy views of the C structs -------------------------------------------------
 

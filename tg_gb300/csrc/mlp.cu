@@ -85,7 +85,6 @@ constexpr int GROUP_BYTES = A1 + KGH * 16 * 128;
 constexpr int BAR = GROUP + 2 * GROUP_BYTES;            // 2 mbarriers, TMEM address
 constexpr int SMEM = BAR + 64;
 constexpr uint32_t TMEM_COLS = 128;                     // 64 per group
-constexpr uint32_t kWaitLimit = 1u << 22;
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
 __host__ __device__ constexpr uint32_t idesc(uint32_t n)
@@ -114,17 +113,8 @@ __device__ __forceinline__ void commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
 }
 
-// bounded wait for mbarrier phase `parity`; false when the limit ran out
-__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity)
-{
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
-        uint32_t done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
+// bounded wait for mbarrier phase `parity` (about a second); false when the limit ran out
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity) { return mbar_wait_bounded(bar, parity); }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }

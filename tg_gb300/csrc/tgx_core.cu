@@ -71,7 +71,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
     }
     tgx_config def = {};
     if (!cfg) cfg = &def;
-    if (cfg->device < 0 || cfg->device >= n || (cfg->flags & ~TGX_FLAG_MIN_BIN_CAPACITY) != 0) {
+    if (cfg->device < 0 || cfg->device >= n || (cfg->flags & ~(TGX_FLAG_MIN_BIN_CAPACITY | TGX_FLAG_TEST_LOST_COPY)) != 0) {
         tgx_set_error("tgx_create: bad device %d or flags %u", cfg->device, cfg->flags);
         return TGX_ERR_INVALID_ARGUMENT;
     }

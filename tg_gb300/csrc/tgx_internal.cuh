@@ -379,6 +379,29 @@ void trace_free(tgx_ctx* ctx);
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// Bounded wait for phase `parity` of the mbarrier at shared address `bar`:
+// true once the phase has completed, false when about `limit_ns` nanoseconds
+// of the GPU's global timer went by first.  The timer is read only when the
+// first test fails, so a wait that is already over costs one instruction.
+constexpr unsigned long long kMbarWaitNs = 1000000000ull;   // one second
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
+                                                  unsigned long long limit_ns = kMbarWaitNs)
+{
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (done) return true;
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) return false;
+    }
+}
+
 // cache inference over min(max_n, *d_n) inputs (mlp.cu)
 tgx_status cache_primary(tgx_ctx* c, tgx_cache* k, tgx_cache** out);
 tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, const float* const* d_x,

@@ -47,7 +47,6 @@ constexpr uint32_t kCluster = 8;
 constexpr uint32_t kBatch = 64;            // records staged per shared-memory batch
 constexpr uint32_t kMaxDdaSteps = 64;      // the 8^3 DDA needs at most 22
 constexpr uint32_t kBuckets = 16;          // depth buckets per tile
-constexpr uint32_t kWaitLimit = 1u << 20;  // mbarrier polls before a copy is declared lost
 
 struct alignas(16) VisRecord
 {
@@ -695,6 +694,8 @@ struct TileJob
     uint32_t* counters;
     uint32_t n_views, n_tiles;
     uint32_t first;              // the job's first item in a multi-job work queue
+    uint32_t extra_tx;           // bytes the first batch's barrier expects beyond its copies: 0, or 64
+                                 // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
 
 struct TileSmem
@@ -715,8 +716,12 @@ __device__ __forceinline__ void tile_smem_init(TileSmem& sm)
 
 // Tile `slot` (in the job's heavy-first order) of one job: every pixel's
 // nearest packed word over the clusters binned to the tile.  `phase` is the
-// parity of the CTA's bulk-copy mbarrier, carried across tiles.
-__device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSmem& sm, uint32_t& phase,
+// parity of the CTA's bulk-copy mbarrier, carried across tiles.  Returns
+// false (the same in every thread) when a batch's copies did not complete in
+// time: the status word then holds TGX_ERR_TIMEOUT, the CTA has issued no
+// further copies, has waited once more (bounded) for the ones in flight and
+// has written its pixels' words so far; it must not stage another tile.
+__device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSmem& sm, uint32_t& phase,
                                          tgx_dev_status* __restrict__ status)
 {
     __syncthreads();   // the CTA's previous tile is done with the shared state
@@ -753,9 +758,12 @@ __device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSm
     float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
     const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
     const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
+    bool lost = false;      // this thread's wait for a batch's copies ran out
+    uint32_t extra = J.extra_tx;
     for (uint32_t base = begin; base < end; base += kBatch) {
         uint32_t n = min(kBatch, end - base);
-        __syncthreads();   // the previous batch is fully consumed
+        // the previous batch is fully consumed; after a lost copy no thread stages another
+        if (__syncthreads_or(lost)) break;
         if (!scan_all) {
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) sm.rec[k] = J.records[J.bins[base + k]];
             __syncthreads();
@@ -779,7 +787,8 @@ __device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSm
         }
         // stage the n bitmasks (64 B each) with bulk async copies completing on the mbarrier
         if (threadIdx.x == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&sm.bar)), "r"(n * 64u) : "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&sm.bar)), "r"(n * 64u + extra) : "memory");
+        extra = 0;
         // order this thread's earlier generic reads of sm.bits before the async-proxy writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
@@ -788,19 +797,9 @@ __device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSm
                          :: "r"(smem_addr(&sm.bits[k * 16])), "l"(src), "r"(smem_addr(&sm.bar)) : "memory");
         }
         // bounded wait on the barrier phase
-        {
-            uint32_t done = 0, polls = 0;
-            while (!done) {
-                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                             : "=r"(done) : "r"(smem_addr(&sm.bar)), "r"(phase) : "memory");
-                if (++polls >= kWaitLimit && !done) {
-                    dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
-                    break;
-                }
-            }
-        }
+        lost = !mbar_wait_bounded(smem_addr(&sm.bar), phase);
         phase ^= 1u;
-        if (!valid) continue;
+        if (!valid || lost) continue;
         for (uint32_t k = 0; k < n; k++) {
             const VisRecord& r = sm.rec[k];
             if (best_d24 < r.d24_lb) continue;   // cannot produce a smaller word
@@ -825,7 +824,20 @@ __device__ __forceinline__ void vis_tile(const TileJob& J, uint32_t slot, TileSm
             if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
         }
     }
+    if (__syncthreads_or(lost)) {
+        // a batch's copies did not complete: report it, give the copies still in
+        // flight one more bounded wait so none lands after the CTA is gone, and
+        // write the words found so far
+        if (threadIdx.x == 0) {
+            dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
+            mbar_wait_bounded(smem_addr(&sm.bar), phase ^ 1u);
+        }
+        __syncthreads();
+        if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+        return false;
+    }
     if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+    return true;
 }
 
 // Instantiated per block size (= tile pixels) so the register budget can be
@@ -872,7 +884,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles_queue(const 
         }
         __syncthreads();
         if (s_slot == 0xffffffffu) break;
-        vis_tile(s_job, s_slot, sm, phase, status);
+        if (!vis_tile(s_job, s_slot, sm, phase, status)) break;   // its shared bitmask staging is not reusable
     }
 }
 
@@ -1001,6 +1013,7 @@ static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long
     J.n_views = n_views;
     J.n_tiles = n_tiles;
     J.first = 0;
+    J.extra_tx = 0;
     return J;
 }
 
@@ -1038,7 +1051,8 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
                    w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
                    n_tiles, w.bin_capacity, c->d_status);
     if (phase == VIS_NO_TILES) return TGX_OK;
-    const TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
+    TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
+    if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
     const uint32_t threads = c->tile_w * c->tile_h;
     if (threads == 64) {
         TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
@@ -1585,10 +1599,29 @@ constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * 4);   // abo
 // device address is taken with cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_vis_noalloc_scratch[kNaBytes];
 
-// per-object 3x3 of inverse(rotation), as k_object_setup computes it at upload
-__global__ void __launch_bounds__(128) k_vis_noalloc_inv_rot(const tgx_object* __restrict__ objs, uint32_t n,
-                                                            float* __restrict__ inv_rot)
+// The call's set-up on the device, so that no host buffer is read after the
+// call returns: the first CTA writes the view constants and the output
+// pointer (both passed by value) and zeroes the counters and the status
+// word; every thread writes one object's 3x3 of inverse(rotation), as
+// k_object_setup computes it at upload.
+__global__ void __launch_bounds__(128) k_vis_noalloc_setup(ViewConst vc, unsigned long long* visbuf,
+                                                          ViewConst* __restrict__ d_vc,
+                                                          unsigned long long** __restrict__ d_outs,
+                                                          uint32_t* __restrict__ counters,
+                                                          tgx_dev_status* __restrict__ status,
+                                                          const tgx_object* __restrict__ objs, uint32_t n,
+                                                          float* __restrict__ inv_rot)
 {
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) {
+            *d_vc = vc;
+            *d_outs = visbuf;
+            status->code = 0u;
+            status->where = 0u;
+            status->detail = 0ull;
+        }
+        if (threadIdx.x < 64) counters[threadIdx.x] = 0u;
+    }
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float rot[16], inv[16];
@@ -1688,19 +1721,13 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     uint32_t* tile_order = (uint32_t*)(base + kNaTileOrder);
     uint32_t* bins = (uint32_t*)(base + kNaBinsOff);
 
-    // what must start at zero; everything else is written before it is read
-    TGX_CUDA(cudaMemsetAsync(counters, 0, 256, st));
-    TGX_CUDA(cudaMemsetAsync(status, 0, sizeof(tgx_dev_status), st));
-    unsigned char stage[sizeof(ViewConst) + 32];
-    const size_t ptr_off = (sizeof(ViewConst) + 15) & ~(size_t)15;
-    memcpy(stage, &vc, sizeof(ViewConst));
-    memcpy(stage + ptr_off, &d_visbuf, sizeof(void*));
-    TGX_CUDA(cudaMemcpyAsync(d_vc, stage, ptr_off + sizeof(void*), cudaMemcpyHostToDevice, st));
-
     int sms = 0;
     TGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const uint32_t warp_grid = (uint32_t)sms * 8;
-    NA_LAUNCH((n_objects + 127) / 128, 128, k_vis_noalloc_inv_rot, d_objects, n_objects, inv_rot);
+    // what must start at zero (counters, status) is cleared by the set-up kernel;
+    // everything else is written before it is read
+    NA_LAUNCH((n_objects + 127) / 128, 128, k_vis_noalloc_setup, vc, (unsigned long long*)d_visbuf, d_vc, d_outs,
+              counters, status, d_objects, n_objects, inv_rot);
     NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
               d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
               kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kBuckets, status);
@@ -1731,6 +1758,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.n_views = 1;
     J.n_tiles = n_tiles;
     J.first = 0;
+    J.extra_tx = 0;
     NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), J, status);
     if (out_error) {
         tgx_dev_status hs;
