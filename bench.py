@@ -686,6 +686,11 @@ def main() -> None:
             call()
         trace = ctx.trace_read()
         ctx.trace(False)
+        # ---- the tile kernel's own work counts of one frame (its counting variant, untimed) ----
+        ctx.vis_count_work(True)
+        call()
+        work = ctx.vis_work().as_dict()
+        ctx.vis_count_work(False)
 
         # ---- end to end through the host-buffer entry point ----
         host_out = np.empty(W * H, np.uint64)
@@ -836,6 +841,22 @@ def main() -> None:
             limiter = {"kind": "issue", "smsp__issue_active": prof["smsp__issue_active"],
                        "threads_per_warp_instruction": prof.get("threads_per_warp_instruction"),
                        "what": prof.get("limiter"), "source": "profiles/vis_tiles_1080p_512obj.md"}
+    # the pass's FP32 work model (12 ops per DDA step + 60 ops of set-up per evaluated pair), from
+    # the kernel's own counts, against one FP32 op per lane per clock at the sampled SM clock
+    clk = clocks.summary()
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    tile_ms = trace["k_vis_tiles"][0] / max(trace["k_vis_tiles"][1], 1) if "k_vis_tiles" in trace else top_ms
+    fp32_ops = 12 * work["dda_steps"] + 60 * work["pairs"]
+    fp32_peak = n_sms * 128 * sm_mhz * 1e6
+    fp32 = {"model": "12 FP32 ops per DDA step + 60 per evaluated (pixel, cluster) pair, counted by the kernel",
+            "ops_per_frame": fp32_ops, "achieved_ops_per_s": fp32_ops / (tile_ms * 1e-3),
+            "peak_ops_per_s": fp32_peak, "frac": fp32_ops / (tile_ms * 1e-3) / fp32_peak,
+            "peak_note": f"{n_sms} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (median sampled SM clock)"}
+    limiter = {**(limiter or {"kind": "issue"}), "fp32": fp32}
+    vis_work = {**work, "frame": "one 1920x1080 frame of the workload (counting variant of the tile kernel)",
+                "pairs_per_s": work["pairs"] / (ms * 1e-3), "dda_steps_per_s": work["dda_steps"] / (ms * 1e-3),
+                "rates_over": "ms_per_step (the whole frame)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
@@ -863,8 +884,9 @@ def main() -> None:
                      "algorithmic_bytes": algo_bytes,
                      "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback",
                      **({"limiter": limiter} if limiter else {})},
-        "clocks": clocks.summary(),
+        "clocks": clk,
         "hit_pixels": hits,
+        "vis_work": vis_work,
         **gi_report,
         **({"batched_frame": batched} if batched else {}),
         **({"large_config": large} if large else {}),

@@ -279,6 +279,29 @@ typedef struct tgx_vis_stats
 
 tgx_status  tgx_vis_get_stats(tgx_ctx* ctx, tgx_vis_stats* out_stats);
 
+/* Work done by the visibility tile kernel, counted by the kernel itself.  No
+ * counterpart in the reference (its GPU work is counted by nobody).  After
+ * tgx_vis_count_work(ctx, 1) every tgx_vis_render on the context runs a
+ * counting variant of the tile kernel (same results, a little slower) and
+ * overwrites these totals; tgx_vis_get_work reads them (blocking).  A
+ * (pixel, cluster) pair is one binned cluster evaluated for one pixel. */
+typedef struct tgx_vis_work
+{
+    uint64_t pairs;               /* pairs evaluated: past the per-pixel depth skip */
+    uint64_t depth_skips;         /* pairs skipped: the pixel already holds a nearer word */
+    uint64_t dir_setups;          /* cluster-space ray directions computed (per pixel and object) */
+    uint64_t slab_misses;         /* pairs the conservative slab test rejects */
+    uint64_t sure_hits;           /* pairs whose box entry is certain (entry distance only) */
+    uint64_t exact_tests;         /* pairs that run the shader's full ray/box test */
+    uint64_t ddas;                /* pairs that run the voxel DDA */
+    uint64_t dda_steps;           /* voxels visited by those DDAs */
+    uint64_t hits;                /* DDAs that found a set voxel */
+    uint64_t batches;             /* (pixel, staged batch) visits */
+} tgx_vis_work;
+
+tgx_status  tgx_vis_count_work(tgx_ctx* ctx, int enable);
+tgx_status  tgx_vis_get_work(tgx_ctx* ctx, tgx_vis_work* out_work);
+
 /* Decodes one visibility-buffer word like tg_raytracer_get_hovered_voxel
  * (tgvk_raytracer.c:1639-1653): returns 1 on hit.  Host-only, no device work. */
 int         tgx_vis_decode(uint64_t packed, float* out_depth, uint32_t* out_cluster_pointer, uint32_t* out_voxel_idx);

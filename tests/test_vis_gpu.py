@@ -233,3 +233,27 @@ def test_lost_bitmask_copy_times_out_and_the_context_stays_usable(oracle):
     ref = oracle.vis_render(s, v, mode=1)
     assert_same(g, ref)
     assert (ref != EMPTY).sum() > 20
+
+
+def test_work_counting_variant_gives_the_same_buffer_and_consistent_counts(oracle):
+    """tgx_vis_count_work: the tile kernel's counting variant renders the same
+    buffer, and its counters add up (every evaluated pair is a slab miss, a
+    sure hit or an exact test; DDAs and hits only come from those)."""
+    s = fuzz_scene(61, n_objects=8, box=40.0, max_cpa=4)
+    v = tg.make_view((0.0, 0.0, -70.0), 0.05, float(np.pi), 1.1, 200, 120, 0.1, 256.0)
+    ref = oracle.vis_render(s, v, mode=1)
+    with tg.Context(0, tile=(8, 8)) as c:
+        c.vis_count_work(True)
+        (g,) = render(c, s, v)
+        w = c.vis_work().as_dict()
+        c.vis_count_work(False)
+        (g2,) = render(c, s, v)
+    assert_same(g, ref)
+    assert_same(g2, ref)
+    n_hit = int((ref != EMPTY).sum())
+    assert w["pairs"] == w["slab_misses"] + w["sure_hits"] + w["exact_tests"], w
+    assert w["ddas"] <= w["sure_hits"] + w["exact_tests"]
+    assert w["ddas"] >= w["sure_hits"]
+    assert n_hit <= w["hits"] <= w["ddas"] <= w["dda_steps"] <= 22 * w["ddas"]
+    assert 0 < w["dir_setups"] <= w["pairs"] + w["depth_skips"]
+    assert w["batches"] > 0

@@ -134,6 +134,15 @@ class VisStats(C.Structure):
                 ("dda_overruns", C.c_uint32)]
 
 
+class VisWork(C.Structure):
+    """tgx_vis_work: the visibility tile kernel's own work counts."""
+    _fields_ = [(n, C.c_uint64) for n in ("pairs", "depth_skips", "dir_setups", "slab_misses", "sure_hits",
+                                          "exact_tests", "ddas", "dda_steps", "hits", "batches")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
 class SvoInfo(C.Structure):
     _fields_ = [("min", C.c_float * 3), ("extent_log2", C.c_uint32), ("blocks_per_axis", C.c_uint32),
                 ("n_blocks", C.c_uint32), ("n_nonempty_blocks", C.c_uint32), ("n_pairs", C.c_uint32),
@@ -154,7 +163,8 @@ EXPORTS = [
     "tgx_gi_render_cached", "tgx_frame_graph_create", "tgx_frame_graph_launch", "tgx_frame_graph_set_views",
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
-    "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait",
+    "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait", "tgx_vis_count_work",
+    "tgx_vis_get_work",
 ]
 
 
@@ -199,6 +209,8 @@ def _load() -> C.CDLL:
         "tgx_make_view": (i32, [vp, C.c_float, C.c_float, C.c_float, u32, u32, C.c_float, C.c_float, vp]),
         "tgx_trace_enable": (i32, [vp, i32]),
         "tgx_vis_get_stats": (i32, [vp, C.POINTER(VisStats)]),
+        "tgx_vis_count_work": (i32, [vp, i32]),
+        "tgx_vis_get_work": (i32, [vp, C.POINTER(VisWork)]),
         "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "tgx_cache_n_params": (u32, []),
         "tgx_gi_render_cached": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -483,6 +495,16 @@ class Context:
         st = VisStats()
         check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
         return st
+
+    def vis_count_work(self, enable: bool) -> None:
+        """tgx_vis_count_work: later renders run the tile kernel's counting variant."""
+        check(lib.tgx_vis_count_work(self.handle, int(enable)), "tgx_vis_count_work")
+
+    def vis_work(self) -> VisWork:
+        """tgx_vis_get_work: the last counted render's work totals (blocking)."""
+        w = VisWork()
+        check(lib.tgx_vis_get_work(self.handle, C.byref(w)), "tgx_vis_get_work")
+        return w
 
     def pick(self, d_visbuf, w: int, h: int, x: int, y: int):
         d, cp, vx, hit = C.c_float(), C.c_uint32(), C.c_uint32(), C.c_int()

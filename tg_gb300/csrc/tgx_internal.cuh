@@ -130,6 +130,8 @@ struct tgx_ctx
     DevBuf gi_scratch;     // learned-cache GI queries, hits, training batch
     DevBuf svo_scratch;    // SVO update: dirty-block marks
     DevBuf svo_sort;       // SVO build: pairs grouped by block slot, per-slot counts and offsets
+    DevBuf vis_work;       // work counters of the tile kernel's counting variant
+    bool   vis_count_work = false;
     uint32_t vis_last_tiles = 0;
     uint64_t vis_last_pairs = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters

@@ -60,6 +60,9 @@ struct alignas(16) VisRecord
 static_assert(sizeof(VisRecord) == 32, "record layout");
 
 enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_COUNT = 8 };
+// work counters of the tile kernel's counting variant (tgx_vis_work, same order)
+enum Work { W_PAIRS = 0, W_DEPTH_SKIPS, W_DIR_SETUPS, W_SLAB_MISSES, W_SURE_HITS, W_EXACT_TESTS, W_DDAS, W_DDA_STEPS,
+            W_HITS, W_BATCHES, W_COUNT };
 constexpr uint32_t kOrderClasses = 32;     // tiles are launched heaviest class (log2 of bin count) first
 
 // bucket of a depth key: one per power of two of the 24-bit depth, keys < 512 share bucket 0
@@ -590,10 +593,11 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
 // direction components and the cluster's 16 bit words.  Returns the packed
 // word or ~0.  The DDA's per-axis steps 1/|d| are |ix| etc. exactly: a
 // correctly rounded 1/(-d) is the negated 1/d.
+template <bool kCount = false>
 __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float oz, float dx, float dy, float dz,
                                                        float ix, float iy, float iz, bool sure_hit,
                                                        const uint32_t* __restrict__ w, uint32_t cluster_pointer,
-                                                       float far_plane, uint32_t* overrun)
+                                                       float far_plane, uint32_t* overrun, uint32_t* work = nullptr)
 {
     float enter;
     if (sure_hit) {
@@ -611,6 +615,7 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
             (dz == 0.0f && (oz < 0.0f || oz > 8.0f)))
             return ULLONG_MAX;
     }
+    if (kCount) work[W_DDAS]++;
     const bool ent = enter > 0.0f;
     const float hx = ent ? xadd(ox, xmul(enter, dx)) : ox;
     const float hy = ent ? xadd(oy, xmul(enter, dy)) : oy;
@@ -629,7 +634,9 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = -iz; }
     for (uint32_t step = 0; step < kMaxDdaSteps; step++) {
         const uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
+        if (kCount) work[W_DDA_STEPS]++;
         if (w[rvi >> 5] & (1u << (rvi & 31u))) {
+            if (kCount) work[W_HITS]++;
             // entry distance of the voxel box (visibility.frag:155): only the near-plane
             // quotient of each axis can be the maximum, since (vmin-o)/d <= (vmax-o)/d for d>0
             const float nx = dx > 0.0f ? xdiv(xsub((float)x, ox), dx) : dx < 0.0f ? xdiv(xsub((float)(x + 1), ox), dx) : F32_MIN_TG;
@@ -694,6 +701,7 @@ struct TileJob
     uint32_t* counters;
     uint32_t n_views, n_tiles;
     uint32_t first;              // the job's first item in a multi-job work queue
+    unsigned long long* work;    // W_COUNT work counters (counting variant of the tile kernel only)
     uint32_t extra_tx;           // bytes the first batch's barrier expects beyond its copies: 0, or 64
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
@@ -721,9 +729,15 @@ __device__ __forceinline__ void tile_smem_init(TileSmem& sm)
 // time: the status word then holds TGX_ERR_TIMEOUT, the CTA has issued no
 // further copies, has waited once more (bounded) for the ones in flight and
 // has written its pixels' words so far; it must not stage another tile.
+template <bool kCount = false>
 __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSmem& sm, uint32_t& phase,
                                          tgx_dev_status* __restrict__ status)
 {
+    uint32_t work[W_COUNT];
+    if (kCount) {
+#pragma unroll
+        for (int i = 0; i < W_COUNT; i++) work[i] = 0u;
+    }
     __syncthreads();   // the CTA's previous tile is done with the shared state
     const uint32_t tile = J.tile_order[slot];
     // bins overflowed this frame: walk every record and test its rectangle (slow, exact)
@@ -800,10 +814,16 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
         lost = !mbar_wait_bounded(smem_addr(&sm.bar), phase);
         phase ^= 1u;
         if (!valid || lost) continue;
+        if (kCount) work[W_BATCHES]++;
         for (uint32_t k = 0; k < n; k++) {
             const VisRecord& r = sm.rec[k];
-            if (best_d24 < r.d24_lb) continue;   // cannot produce a smaller word
+            if (best_d24 < r.d24_lb) {   // cannot produce a smaller word
+                if (kCount) work[W_DEPTH_SKIPS]++;
+                continue;
+            }
+            if (kCount) work[W_PAIRS]++;
             if (r.object_idx != cur_obj) {
+                if (kCount) work[W_DIR_SETUPS]++;
                 // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
                 // object's shared linear part (see k_object_setup)
                 cur_obj = r.object_idx;
@@ -818,9 +838,14 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
                 iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
             }
             const int sc = slab_class(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz);
-            if (sc == kMiss) continue;
-            const unsigned long long p = vis_pair(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit, &sm.bits[k * 16],
-                                                  r.cluster_pointer, vc.far_plane, &J.counters[C_DDA_OVERRUN]);
+            if (sc == kMiss) {
+                if (kCount) work[W_SLAB_MISSES]++;
+                continue;
+            }
+            if (kCount) work[sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
+            const unsigned long long p = vis_pair<kCount>(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit,
+                                                          &sm.bits[k * 16], r.cluster_pointer, vc.far_plane,
+                                                          &J.counters[C_DDA_OVERRUN], work);
             if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
         }
     }
@@ -837,19 +862,29 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
         return false;
     }
     if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+    if (kCount) {
+        // per warp: sum the lanes' counters, one 64-bit atomic each
+#pragma unroll
+        for (int i = 0; i < W_COUNT; i++) {
+            unsigned long long v = work[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31u) == 0u && v) atomicAdd(&J.work[i], v);
+        }
+    }
     return true;
 }
 
 // Instantiated per block size (= tile pixels) so the register budget can be
 // bounded for the occupancy each size needs.  One CTA per tile of one job.
-template <int kThreads, int kMinBlocks>
+template <int kThreads, int kMinBlocks, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
 {
     __shared__ TileSmem sm;
     tile_smem_init(sm);
     pdl_wait();
     uint32_t phase = 0;
-    vis_tile(J, blockIdx.x, sm, phase, status);
+    vis_tile<kCount>(J, blockIdx.x, sm, phase, status);
 }
 
 // Persistent form over several jobs (scenes, each with its views): CTAs take
@@ -1013,6 +1048,7 @@ static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long
     J.n_views = n_views;
     J.n_tiles = n_tiles;
     J.first = 0;
+    J.work = nullptr;
     J.extra_tx = 0;
     return J;
 }
@@ -1054,6 +1090,17 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
     if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
     const uint32_t threads = c->tile_w * c->tile_h;
+    if (c->vis_count_work) {
+        // the counting variant (tgx_vis_count_work): same results, plus the work counters
+        TGX_TRY(devbuf_reserve(c->vis_work, W_COUNT * sizeof(unsigned long long)));
+        J.work = (unsigned long long*)c->vis_work.ptr;
+        TGX_CUDA(cudaMemsetAsync(J.work, 0, W_COUNT * sizeof(unsigned long long), c->stream));
+        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20, true>), J, c->d_status);
+        else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10, true>), J, c->d_status);
+        else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5, true>), J, c->d_status);
+        else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1, true>), J, c->d_status);
+        return TGX_OK;
+    }
     if (threads == 64) {
         TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
     } else if (threads == 128) {
@@ -1558,6 +1605,23 @@ extern "C" tgx_status tgx_vis_get_stats(tgx_ctx* c, tgx_vis_stats* out)
     return TGX_OK;
 }
 
+extern "C" tgx_status tgx_vis_count_work(tgx_ctx* c, int enable)
+{
+    if (!c) return TGX_ERR_INVALID_ARGUMENT;
+    c->vis_count_work = enable != 0;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_vis_get_work(tgx_ctx* c, tgx_vis_work* out)
+{
+    if (!c || !out) return TGX_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    if (!c->vis_work.ptr) return TGX_OK;
+    static_assert(sizeof(tgx_vis_work) == W_COUNT * sizeof(uint64_t), "tgx_vis_work layout");
+    TGX_CUDA(cudaMemcpy(out, c->vis_work.ptr, sizeof(*out), cudaMemcpyDeviceToHost));
+    return TGX_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Visibility render without any allocation (tgx_vis_render_noalloc).
 //
@@ -1758,6 +1822,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.n_views = 1;
     J.n_tiles = n_tiles;
     J.first = 0;
+    J.work = nullptr;
     J.extra_tx = 0;
     NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), J, status);
     if (out_error) {
