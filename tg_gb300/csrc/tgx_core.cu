@@ -110,6 +110,10 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
         tgx_destroy(c);
         return TGX_ERR_OUT_OF_MEMORY;
     }
+    if (const tgx_status st = vis_prepare_device(); st != TGX_OK) {
+        tgx_destroy(c);
+        return st;
+    }
     *out = c;
     return TGX_OK;
 }

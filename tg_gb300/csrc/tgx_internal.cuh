@@ -411,5 +411,6 @@ tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, 
 tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, uint32_t max_n, const float* d_x,
                                float* d_rgb);
 
+tgx_status vis_prepare_device();
 tgx_status vis_render_device(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                              uint64_t* const* d_visbuf);

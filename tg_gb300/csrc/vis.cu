@@ -706,20 +706,64 @@ struct TileJob
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
 
-struct TileSmem
+// Shared memory of a tile CTA (dynamic, sized by its thread count):
+//   the staged batch: kBatch records as arrays (the pair lanes index them by
+//   record) and their 64-byte bitmasks, filled by cp.async.bulk;
+//   every pixel's best packed word so far (the pair lanes' atomicMin target);
+//   per warp, a ring of kQueue live (pixel, record) pairs waiting for a lane:
+//   the pixel's cluster-space direction and reciprocals and the packed
+//   lane | record << 5 | sure_hit << 11.
+constexpr uint32_t kQueue = 64;                      // ring entries per warp (a record adds at most 32)
+constexpr uint32_t kSmBar = 0, kSmView = 8, kSmN = 12;
+constexpr uint32_t kSmBits = 128;                    // 16-byte aligned bulk-copy targets
+constexpr uint32_t kSmRec = kSmBits + kBatch * 64;   // 7 arrays of kBatch words
+enum RecField { R_OX = 0, R_OY, R_OZ, R_CP, R_OBJ, R_LB, R_CI, R_FIELDS };
+constexpr uint32_t kSmBest = kSmRec + R_FIELDS * kBatch * 4;
+constexpr uint32_t kQueueWords = 7 * kQueue;        // per warp: 6 float arrays + the packed word
+__host__ __device__ constexpr uint32_t tile_smem_bytes(uint32_t threads)
 {
-    VisRecord rec[kBatch];
-    __align__(128) uint32_t bits[kBatch * 16];
-    __align__(8) unsigned long long bar;
-    uint32_t view, n;
+    return kSmBest + 8u * threads + (threads / 32u) * kQueueWords * 4u;
+}
+
+struct TileSm
+{
+    unsigned char* p;
+    __device__ __forceinline__ unsigned long long* bar() const { return (unsigned long long*)(p + kSmBar); }
+    __device__ __forceinline__ uint32_t& view() const { return *(uint32_t*)(p + kSmView); }
+    __device__ __forceinline__ uint32_t& n() const { return *(uint32_t*)(p + kSmN); }
+    __device__ __forceinline__ uint32_t* bits() const { return (uint32_t*)(p + kSmBits); }
+    __device__ __forceinline__ uint32_t* rec(int f) const { return (uint32_t*)(p + kSmRec) + f * kBatch; }
+    __device__ __forceinline__ float* recf(int f) const { return (float*)(p + kSmRec) + f * kBatch; }
+    __device__ __forceinline__ unsigned long long* best() const { return (unsigned long long*)(p + kSmBest); }
+    __device__ __forceinline__ uint32_t* queue(uint32_t warp) const
+    {
+        return (uint32_t*)(p + kSmBest + 8u * blockDim.x) + warp * kQueueWords;
+    }
 };
 
-__device__ __forceinline__ void tile_smem_init(TileSmem& sm)
+__device__ __forceinline__ TileSm tile_sm()
+{
+    extern __shared__ __align__(128) unsigned char tile_dyn_smem[];
+    return TileSm{tile_dyn_smem};
+}
+
+__device__ __forceinline__ void tile_smem_init(const TileSm& sm)
 {
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&sm.bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(sm.bar())));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+}
+
+__device__ __forceinline__ void stage_record(const TileSm& sm, uint32_t k, const VisRecord& r)
+{
+    sm.recf(R_OX)[k] = r.ox;
+    sm.recf(R_OY)[k] = r.oy;
+    sm.recf(R_OZ)[k] = r.oz;
+    sm.rec(R_CP)[k] = r.cluster_pointer;
+    sm.rec(R_OBJ)[k] = r.object_idx;
+    sm.rec(R_LB)[k] = r.d24_lb;
+    sm.rec(R_CI)[k] = r.cluster_idx;
 }
 
 // Tile `slot` (in the job's heavy-first order) of one job: every pixel's
@@ -729,8 +773,18 @@ __device__ __forceinline__ void tile_smem_init(TileSmem& sm)
 // time: the status word then holds TGX_ERR_TIMEOUT, the CTA has issued no
 // further copies, has waited once more (bounded) for the ones in flight and
 // has written its pixels' words so far; it must not stage another tile.
+//
+// Per staged batch every lane walks the records for its own pixel: the depth
+// skip, the cluster-space direction (once per object), and the conservative
+// slab test.  The pairs that survive are compacted by warp ballot into the
+// warp's ring; whenever it holds 32, all 32 lanes take one pair each and run
+// the exact entry test and the voxel DDA (vis_pair), folding the result into
+// the pixel's word with a shared-memory atomicMin.  The ring is drained at
+// the end of each batch.  The minimum over a pixel's pairs does not depend on
+// the order they are evaluated in (every word is distinct), so the buffer is
+// the same bits as one DDA per pair in record order.
 template <bool kCount = false>
-__device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSmem& sm, uint32_t& phase,
+__device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const TileSm& sm, uint32_t& phase,
                                          tgx_dev_status* __restrict__ status)
 {
     uint32_t work[W_COUNT];
@@ -745,15 +799,21 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
     if (threadIdx.x == 0) {
         uint32_t v = 0;
         while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
-        sm.view = v;
+        sm.view() = v;
     }
+    sm.best()[threadIdx.x] = ULLONG_MAX;
     __syncthreads();
-    const ViewConst& vc = J.views[sm.view];
+    const uint32_t view = sm.view();
+    const ViewConst& vc = J.views[view];
     const uint32_t lt = tile - vc.tile_base;
     const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
     const uint32_t px = tx * vc.tile_w + threadIdx.x % vc.tile_w;
     const uint32_t py = ty * vc.tile_h + threadIdx.x / vc.tile_w;
     const bool valid = px < vc.width && py < vc.height;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t* const q = sm.queue(warp);
+    float* const qf = (float*)q;
+    const float far_plane = vc.far_plane;
 
     // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
     const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
@@ -766,102 +826,133 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
         dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
     }
 
-    unsigned long long best = ULLONG_MAX;
     uint32_t best_d24 = 0xffffffu;
     uint32_t cur_obj = 0xffffffffu;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
     const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
     const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
-    bool lost = false;      // this thread's wait for a batch's copies ran out
+    bool lost = false;      // a wait for a batch's copies ran out (the same in every lane of a warp)
     uint32_t extra = J.extra_tx;
+    uint32_t qh = 0;        // the warp's ring: first pending entry (warp-uniform)
     for (uint32_t base = begin; base < end; base += kBatch) {
         uint32_t n = min(kBatch, end - base);
         // the previous batch is fully consumed; after a lost copy no thread stages another
         if (__syncthreads_or(lost)) break;
         if (!scan_all) {
-            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) sm.rec[k] = J.records[J.bins[base + k]];
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) stage_record(sm, k, J.records[J.bins[base + k]]);
             __syncthreads();
             // every pixel already closer than the nearest bucket left: the tile is done
-            const uint32_t lo = bucket_lo(depth_bucket(sm.rec[0].d24_lb));
+            const uint32_t lo = bucket_lo(depth_bucket(sm.rec(R_LB)[0]));
             if (__syncthreads_and(!valid || best_d24 < lo)) break;
         } else {
             // keep the records of this view whose tile rectangle holds this tile
-            if (threadIdx.x == 0) sm.n = 0;
+            if (threadIdx.x == 0) sm.n() = 0;
             __syncthreads();
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
                 const VisRecord r = J.records[base + k];
-                const uint2 q = J.rects[base + k];
-                if (r.view == sm.view && tx >= (q.x & 0xffffu) && tx <= (q.y & 0xffffu) && ty >= (q.x >> 16) &&
-                    ty <= (q.y >> 16))
-                    sm.rec[atomicAdd(&sm.n, 1u)] = r;
+                const uint2 qr = J.rects[base + k];
+                if (r.view == view && tx >= (qr.x & 0xffffu) && tx <= (qr.y & 0xffffu) && ty >= (qr.x >> 16) &&
+                    ty <= (qr.y >> 16))
+                    stage_record(sm, atomicAdd(&sm.n(), 1u), r);
             }
             __syncthreads();
-            n = sm.n;
+            n = sm.n();
             if (n == 0) continue;
         }
         // stage the n bitmasks (64 B each) with bulk async copies completing on the mbarrier
         if (threadIdx.x == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(&sm.bar)), "r"(n * 64u + extra) : "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(sm.bar())), "r"(n * 64u + extra) : "memory");
         extra = 0;
-        // order this thread's earlier generic reads of sm.bits before the async-proxy writes
+        // order this thread's earlier generic reads of the bitmasks before the async-proxy writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-            const uint32_t* src = J.bits + (uint64_t)sm.rec[k].cluster_idx * 16u;
+            const uint32_t* src = J.bits + (uint64_t)sm.rec(R_CI)[k] * 16u;
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];"
-                         :: "r"(smem_addr(&sm.bits[k * 16])), "l"(src), "r"(smem_addr(&sm.bar)) : "memory");
+                         :: "r"(smem_addr(sm.bits() + k * 16)), "l"(src), "r"(smem_addr(sm.bar())) : "memory");
         }
         // bounded wait on the barrier phase
-        lost = !mbar_wait_bounded(smem_addr(&sm.bar), phase);
+        lost = __any_sync(0xffffffffu, !mbar_wait_bounded(smem_addr(sm.bar()), phase));
         phase ^= 1u;
-        if (!valid || lost) continue;
-        if (kCount) work[W_BATCHES]++;
-        for (uint32_t k = 0; k < n; k++) {
-            const VisRecord& r = sm.rec[k];
-            if (best_d24 < r.d24_lb) {   // cannot produce a smaller word
-                if (kCount) work[W_DEPTH_SKIPS]++;
-                continue;
+        if (lost) continue;
+        if (kCount && valid) work[W_BATCHES]++;
+        // produce live pairs record by record; drain the ring 32 at a time, and what is left at the end
+        uint32_t qn = 0;     // pending entries (warp-uniform)
+        for (uint32_t k = 0;;) {
+            if (k < n) {
+                bool live = false, sure = false;
+                if (valid) {
+                    if (best_d24 < sm.rec(R_LB)[k]) {   // cannot produce a smaller word
+                        if (kCount) work[W_DEPTH_SKIPS]++;
+                    } else {
+                        if (kCount) work[W_PAIRS]++;
+                        const uint32_t obj = sm.rec(R_OBJ)[k];
+                        if (obj != cur_obj) {
+                            // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
+                            // object's shared linear part (see k_object_setup)
+                            if (kCount) work[W_DIR_SETUPS]++;
+                            cur_obj = obj;
+                            const float* L = J.inv_rot + 9u * obj;
+                            const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
+                            const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
+                            const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
+                            const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
+                            dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
+                            ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
+                            iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
+                            iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                        }
+                        const int sc = slab_class(sm.recf(R_OX)[k], sm.recf(R_OY)[k], sm.recf(R_OZ)[k], dx, dy, dz,
+                                                  ix, iy, iz);
+                        live = sc != kMiss;
+                        sure = sc == kHit;
+                        if (kCount) work[sc == kMiss ? W_SLAB_MISSES : sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
+                    }
+                }
+                const uint32_t m = __ballot_sync(0xffffffffu, live);
+                if (live) {
+                    const uint32_t e = (qh + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1u);
+                    qf[0 * kQueue + e] = dx; qf[1 * kQueue + e] = dy; qf[2 * kQueue + e] = dz;
+                    qf[3 * kQueue + e] = ix; qf[4 * kQueue + e] = iy; qf[5 * kQueue + e] = iz;
+                    q[6 * kQueue + e] = lane | (k << 5) | ((uint32_t)sure << 11);
+                }
+                qn += __popc(m);
+                k++;
+                if (qn < 32u && k < n) continue;
             }
-            if (kCount) work[W_PAIRS]++;
-            if (r.object_idx != cur_obj) {
-                if (kCount) work[W_DIR_SETUPS]++;
-                // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
-                // object's shared linear part (see k_object_setup)
-                cur_obj = r.object_idx;
-                const float* L = J.inv_rot + 9u * cur_obj;
-                const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
-                const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
-                const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
-                const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
-                dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
-                ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
-                iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
-                iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+            if (qn == 0u) break;   // k == n and nothing pending
+            // one pair per lane: the exact test and the DDA; the word goes to its pixel
+            const uint32_t take = min(qn, 32u);
+            __syncwarp();
+            if (lane < take) {
+                const uint32_t e = (qh + lane) & (kQueue - 1u);
+                const uint32_t pk = q[6 * kQueue + e];
+                const uint32_t kk = (pk >> 5) & (kBatch - 1u);
+                const unsigned long long w = vis_pair<kCount>(
+                    sm.recf(R_OX)[kk], sm.recf(R_OY)[kk], sm.recf(R_OZ)[kk], qf[0 * kQueue + e], qf[1 * kQueue + e],
+                    qf[2 * kQueue + e], qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u,
+                    sm.bits() + kk * 16u, sm.rec(R_CP)[kk], far_plane, &J.counters[C_DDA_OVERRUN], work);
+                if (w != ULLONG_MAX) atomicMin(&sm.best()[(warp << 5) | (pk & 31u)], w);
             }
-            const int sc = slab_class(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz);
-            if (sc == kMiss) {
-                if (kCount) work[W_SLAB_MISSES]++;
-                continue;
-            }
-            if (kCount) work[sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
-            const unsigned long long p = vis_pair<kCount>(r.ox, r.oy, r.oz, dx, dy, dz, ix, iy, iz, sc == kHit,
-                                                          &sm.bits[k * 16], r.cluster_pointer, vc.far_plane,
-                                                          &J.counters[C_DDA_OVERRUN], work);
-            if (p < best) { best = p; best_d24 = (uint32_t)(p >> 40); }
+            qh = (qh + take) & (kQueue - 1u);
+            qn -= take;
+            __syncwarp();
+            best_d24 = (uint32_t)(sm.best()[threadIdx.x] >> 40);
         }
     }
+    const unsigned long long best = sm.best()[threadIdx.x];
     if (__syncthreads_or(lost)) {
         // a batch's copies did not complete: report it, give the copies still in
         // flight one more bounded wait so none lands after the CTA is gone, and
         // write the words found so far
         if (threadIdx.x == 0) {
             dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
-            mbar_wait_bounded(smem_addr(&sm.bar), phase ^ 1u);
+            mbar_wait_bounded(smem_addr(sm.bar()), phase ^ 1u);
         }
         __syncthreads();
-        if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+        if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
         return false;
     }
-    if (valid) J.outs[sm.view][(size_t)py * vc.width + px] = best;
+    if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
     if (kCount) {
         // per warp: sum the lanes' counters, one 64-bit atomic each
 #pragma unroll
@@ -869,18 +960,19 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, TileSm
             unsigned long long v = work[i];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if ((threadIdx.x & 31u) == 0u && v) atomicAdd(&J.work[i], v);
+            if (lane == 0u && v) atomicAdd(&J.work[i], v);
         }
     }
     return true;
 }
 
 // Instantiated per block size (= tile pixels) so the register budget can be
-// bounded for the occupancy each size needs.  One CTA per tile of one job.
+// bounded for the occupancy each size needs.  One CTA per tile of one job;
+// tile_smem_bytes(blockDim.x) of dynamic shared memory.
 template <int kThreads, int kMinBlocks, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
 {
-    __shared__ TileSmem sm;
+    const TileSm sm = tile_sm();
     tile_smem_init(sm);
     pdl_wait();
     uint32_t phase = 0;
@@ -896,7 +988,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles_queue(const 
                                                                           uint32_t* __restrict__ queue,
                                                                           tgx_dev_status* __restrict__ status)
 {
-    __shared__ TileSmem sm;
+    const TileSm sm = tile_sm();
     __shared__ TileJob s_job;
     __shared__ uint32_t s_slot, s_jobidx;
     tile_smem_init(sm);
@@ -1095,21 +1187,32 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
         TGX_TRY(devbuf_reserve(c->vis_work, W_COUNT * sizeof(unsigned long long)));
         J.work = (unsigned long long*)c->vis_work.ptr;
         TGX_CUDA(cudaMemsetAsync(J.work, 0, W_COUNT * sizeof(unsigned long long), c->stream));
-        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20, true>), J, c->d_status);
-        else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10, true>), J, c->d_status);
-        else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5, true>), J, c->d_status);
-        else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1, true>), J, c->d_status);
+        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<64, 20, true>), J, c->d_status);
+        else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<128, 10, true>), J, c->d_status);
+        else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<256, 5, true>), J, c->d_status);
+        else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<1024, 1, true>), J, c->d_status);
         return TGX_OK;
     }
     if (threads == 64) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<64, 20>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<64, 20>), J, c->d_status);
     } else if (threads == 128) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<128, 10>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<128, 10>), J, c->d_status);
     } else if (threads == 256) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<256, 5>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<256, 5>), J, c->d_status);
     } else {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, 0, (k_vis_tiles<1024, 1>), J, c->d_status);
+        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<1024, 1>), J, c->d_status);
     }
+    return TGX_OK;
+}
+
+// Opt-in to the dynamic shared memory the largest tile kernels need (more
+// than the 48 KB default); called once per context with its device current.
+tgx_status vis_prepare_device()
+{
+    const int big = (int)tile_smem_bytes(1024);
+    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles<1024, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles_queue<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return TGX_OK;
 }
 
@@ -1122,7 +1225,8 @@ template <int kThreads, int kMinBlocks>
 static uint32_t vis_queue_ctas_t(tgx_ctx* c)
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles_queue<kThreads, kMinBlocks>, kThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles_queue<kThreads, kMinBlocks>, kThreads,
+                                                      tile_smem_bytes(kThreads)) !=
             cudaSuccess || per_sm < 1)
         per_sm = 1;
     return (uint32_t)c->num_sms * (uint32_t)per_sm;
@@ -1144,10 +1248,10 @@ static tgx_status vis_launch_queue(tgx_ctx* c, const TileJob* d_jobs, uint32_t n
     const uint32_t threads = c->tile_w * c->tile_h;
     const uint32_t grid = std::max(1u, std::min(ctas, total));
 #define QUEUE_ARGS d_jobs, n_jobs, total, d_queue, c->d_status
-    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, 64, 0, (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
-    else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, 128, 0, (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
-    else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, 256, 0, (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
-    else TGX_LAUNCH(c, TR_VIS_TILES, grid, 1024, 0, (k_vis_tiles_queue<1024, 1>), QUEUE_ARGS);
+    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, 64, tile_smem_bytes(64), (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
+    else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, 128, tile_smem_bytes(128), (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
+    else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, 256, tile_smem_bytes(256), (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
+    else TGX_LAUNCH(c, TR_VIS_TILES, grid, 1024, tile_smem_bytes(1024), (k_vis_tiles_queue<1024, 1>), QUEUE_ARGS);
 #undef QUEUE_ARGS
     return TGX_OK;
 }
@@ -1618,7 +1722,8 @@ extern "C" tgx_status tgx_vis_get_work(tgx_ctx* c, tgx_vis_work* out)
     memset(out, 0, sizeof(*out));
     if (!c->vis_work.ptr) return TGX_OK;
     static_assert(sizeof(tgx_vis_work) == W_COUNT * sizeof(uint64_t), "tgx_vis_work layout");
-    TGX_CUDA(cudaMemcpy(out, c->vis_work.ptr, sizeof(*out), cudaMemcpyDeviceToHost));
+    TGX_CUDA(cudaMemcpyAsync(out, c->vis_work.ptr, sizeof(*out), cudaMemcpyDeviceToHost, c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
     return TGX_OK;
 }
 
@@ -1824,7 +1929,11 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
-    NA_LAUNCH(n_tiles, kNaTile * kNaTile, (k_vis_tiles<256, 5>), J, status);
+    k_vis_tiles<256, 5><<<n_tiles, kNaTile * kNaTile, tile_smem_bytes(kNaTile * kNaTile), st>>>(J, status);
+    if (const cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
+        tgx_set_error("tgx_vis_render_noalloc: launch of k_vis_tiles failed: %s", cudaGetErrorString(le));
+        return TGX_ERR_CUDA;
+    }
     if (out_error) {
         tgx_dev_status hs;
         TGX_CUDA(cudaMemcpyAsync(&hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st));
