@@ -125,8 +125,8 @@ typedef struct tgx_config
 {
     int      device;           /* CUDA device ordinal */
     void*    stream;           /* cudaStream_t to run on, or NULL for a context-owned stream */
-    uint32_t tile_w;           /* visibility tile width in pixels (0 = default 16) */
-    uint32_t tile_h;           /* visibility tile height in pixels (0 = default 16) */
+    uint32_t tile_w;           /* visibility tile width in pixels (0 = default 16); */
+    uint32_t tile_h;           /* and height (0 = 16): 32..512 pixels, a whole number of warps */
     uint32_t flags;            /* TGX_FLAG_* bits, 0 for defaults */
     uint32_t trace_steps;      /* SVO traversal: DDA steps a lane runs between refills of the
                                   ray queue (1..256, 0 = default 8); see tgx_set_trace_steps */
@@ -244,11 +244,11 @@ tgx_status  tgx_vis_host_wait(tgx_ctx* ctx, uint32_t max_in_flight);
  * (objects, cluster pointers, cluster->object map, voxel bits; indices are
  * trusted, not validated), the view on the host, and a DEVICE output of
  * width*height u64.  The result equals tgx_vis_render's bit for bit.  All
- * scratch lives in one fixed device array of about 31 MiB inside the library,
+ * scratch lives in one fixed device array of about 51 MiB inside the library,
  * which every GPU that loads the library holds until the process exits.
  * Limits: at most 65,536 objects, 524,288 cluster pointers and 32,768 screen
  * tiles of 16x16 pixels (3840x2160 fits); larger inputs are rejected with
- * TGX_ERR_CAPACITY and a message.  The tile bins hold 1,048,576 (cluster,
+ * TGX_ERR_CAPACITY and a message.  The tile bins hold 262,144 (cluster,
  * tile) entries; a frame that needs more is still rendered exactly, but every
  * tile then tests every visible cluster's screen rectangle, which is much
  * slower (tgx_vis_render grows its bins instead).  The first call on a device

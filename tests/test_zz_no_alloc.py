@@ -23,7 +23,7 @@ import tg_gb300 as tg
 
 pytestmark = pytest.mark.gpu
 
-NA_BINS = 1 << 20   # the fixed bins of the entry point (include/tgx.h)
+NA_BINS = 1 << 18   # the fixed bins of the entry point (include/tgx.h)
 
 
 def _bind():

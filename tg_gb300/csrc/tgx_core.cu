@@ -76,8 +76,8 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
         return TGX_ERR_INVALID_ARGUMENT;
     }
     const uint32_t tw = cfg->tile_w ? cfg->tile_w : 16, th = cfg->tile_h ? cfg->tile_h : 16;
-    if (tw * th > 1024 || tw * th < 32 || (tw * th) % 32 != 0) {
-        tgx_set_error("tgx_create: tile %ux%u must hold 32..1024 pixels in whole warps", tw, th);
+    if (tw * th > 512 || tw * th < 32 || (tw * th) % 32 != 0) {
+        tgx_set_error("tgx_create: tile %ux%u must hold 32..512 pixels in whole warps", tw, th);
         return TGX_ERR_INVALID_ARGUMENT;
     }
     if (cfg->trace_steps > 256) {
@@ -110,7 +110,7 @@ extern "C" tgx_status tgx_create(const tgx_config* cfg, tgx_ctx** out)
         tgx_destroy(c);
         return TGX_ERR_OUT_OF_MEMORY;
     }
-    if (const tgx_status st = vis_prepare_device(); st != TGX_OK) {
+    if (const tgx_status st = vis_prepare_device(c); st != TGX_OK) {
         tgx_destroy(c);
         return st;
     }

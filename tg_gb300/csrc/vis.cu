@@ -19,17 +19,20 @@
 //                           first); then per group: tile offsets and order.
 //                           Up to 512 groups, k_vis_finalize_direct does both:
 //                           each CTA reads all groups' sums and histograms.
-//   5. k_vis_bin_fill       a half-warp per record: scatters it into the
-//                           (tile, bucket) bins, so every tile's list runs
-//                           near to far.
-//   6. k_vis_tiles          one CTA per screen tile, one thread per pixel:
-//      stages batches of records in shared memory and their 64-byte
-//      bitmasks with cp.async.bulk (TMA) on an mbarrier; per pixel skips
-//      clusters whose depth bound cannot beat its current word, rejects clear
-//      misses with a conservative reciprocal slab test, runs the shader's
-//      exact ray/box test and DDA for the rest and keeps the minimum packed
-//      depth|pointer|voxel word; stops when every pixel of the tile is closer
-//      than the next depth bucket; writes every pixel once (fused clear).
+//   5. k_vis_bin_fill       a warp per record: writes it, with its cluster's
+//                           64-byte bitmask, as a 96-byte entry into each of its
+//                           (tile, bucket) bins, so every tile's entries are
+//                           contiguous and run near to far.
+//   6. k_vis_tiles          persistent, warp-specialised: per CTA a producer
+//      warp takes tiles from a queue (heaviest first) and bulk-copies batches
+//      of their entries into a two-stage shared-memory ring (cp.async.bulk on
+//      mbarriers); the tile's pixel warps, one thread per pixel, skip entries
+//      whose depth bound cannot beat the pixel's word, reject clear misses
+//      with a conservative reciprocal slab test, compact the surviving
+//      (pixel, cluster) pairs by warp ballot, and run the shader's exact
+//      ray/box test and DDA on full warps of pairs, keeping each pixel's
+//      minimum packed depth|pointer|voxel word (shared atomicMin); every
+//      pixel is written once (fused clear).
 //
 // Every pair evaluates the same binary32 operations in the same order as the
 // CPU oracle's transcription of visibility.frag, so the buffer is bit-exact.
@@ -44,7 +47,6 @@
 namespace {
 
 constexpr uint32_t kCluster = 8;
-constexpr uint32_t kBatch = 64;            // records staged per shared-memory batch
 constexpr uint32_t kMaxDdaSteps = 64;      // the 8^3 DDA needs at most 22
 constexpr uint32_t kBuckets = 16;          // depth buckets per tile
 
@@ -59,7 +61,22 @@ struct alignas(16) VisRecord
 };
 static_assert(sizeof(VisRecord) == 32, "record layout");
 
-enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_COUNT = 8 };
+enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_TILE_QUEUE = 4, C_COUNT = 8 };
+
+// One binned (tile, cluster) entry as the tile kernel stages it: the record's
+// fields the DDA needs and the cluster's 64-byte bitmask, so a batch of a
+// tile's entries is one contiguous bulk copy.
+struct alignas(16) TileEntry
+{
+    float    ox, oy, oz;        // camera position in cluster space
+    uint32_t cluster_pointer;
+    uint32_t object_idx;
+    uint32_t d24_lb;
+    uint32_t pad[2];
+    uint32_t bits[16];
+};
+static_assert(sizeof(TileEntry) == 96, "entry layout");
+constexpr uint32_t kEntryWords = sizeof(TileEntry) / 4;
 // work counters of the tile kernel's counting variant (tgx_vis_work, same order)
 enum Work { W_PAIRS = 0, W_DEPTH_SKIPS, W_DIR_SETUPS, W_SLAB_MISSES, W_SURE_HITS, W_EXACT_TESTS, W_DDAS, W_DDA_STEPS,
             W_HITS, W_BATCHES, W_COUNT };
@@ -550,7 +567,8 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
 }
 
 // ---------------------------------------------------------------------------
-// 5. bin fill: a half-warp per record, lanes over its tiles
+// 5. bin fill: a warp per record; its lanes take the record's tiles' slots
+//    (32 at a time), then 24 lanes write the 96-byte entry into each slot
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restrict__ records,
@@ -559,27 +577,43 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
                                                      const ViewConst* __restrict__ views,
                                                      const uint32_t* __restrict__ tile_off,
                                                      const uint32_t* __restrict__ bucket_off,
-                                                     uint32_t* __restrict__ cursor, uint32_t* __restrict__ bins,
+                                                     uint32_t* __restrict__ cursor, TileEntry* __restrict__ entries,
+                                                     const uint32_t* __restrict__ bits,
                                                      uint32_t n_tiles, uint32_t bin_capacity,
                                                      tgx_dev_status* __restrict__ status)
 {
     pdl_wait();
     pdl_trigger();
     if (counters[C_OVERFLOW]) return;   // the tile kernel scans all records instead
-    const uint32_t lane = threadIdx.x & 15u;   // a half-warp per record, as in k_vis_count
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t n = counters[C_RECORDS];
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 4; i < n; i += (gridDim.x * blockDim.x) >> 4) {
+    uint32_t* const ew = reinterpret_cast<uint32_t*>(entries);
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
         const uint2 r = rects[i];
+        const uint32_t* rw = reinterpret_cast<const uint32_t*>(records + i);
+        // entry word `lane`: ox oy oz pointer object lb 0 0 | 16 bitmask words
+        uint32_t word = 0u;
+        if (lane < 3u) word = rw[lane];
+        else if (lane < 6u) word = rw[lane + 1u];
+        else if (lane >= 8u && lane < kEntryWords) word = bits[(uint64_t)rw[3] * 16u + (lane - 8u)];
         const VisRecord& rec = records[i];
         const ViewConst& vc = views[rec.view];
         const uint32_t b = depth_bucket(rec.d24_lb);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
-        for (uint32_t k = lane; k < cnt; k += 16) {
-            const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
-            const uint32_t pos = tile_off[t] + bucket_off[b * n_tiles + t] + atomicAdd(&cursor[b * n_tiles + t], 1u);
-            if (pos < bin_capacity) bins[pos] = i;
-            else dev_error(status, TGX_ERR_DEVICE_FAULT, 3, pos);
+        for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
+            uint32_t pos = 0xffffffffu;
+            const uint32_t k = k0 + lane;
+            if (k < cnt) {
+                const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
+                pos = tile_off[t] + bucket_off[b * n_tiles + t] + atomicAdd(&cursor[b * n_tiles + t], 1u);
+                if (pos >= bin_capacity) { dev_error(status, TGX_ERR_DEVICE_FAULT, 3, pos); pos = 0xffffffffu; }
+            }
+            const uint32_t m = min(32u, cnt - k0);
+            for (uint32_t q = 0; q < m; q++) {
+                const uint32_t pq = __shfl_sync(0xffffffffu, pos, q);
+                if (pq != 0xffffffffu && lane < kEntryWords) ew[(uint64_t)pq * kEntryWords + lane] = word;
+            }
         }
     }
 }
@@ -691,7 +725,7 @@ struct TileJob
 {
     const VisRecord* records;
     const uint2* rects;
-    const uint32_t* bins;
+    const TileEntry* entries;
     const uint32_t* tile_off;
     const uint32_t* tile_order;
     const ViewConst* views;
@@ -706,255 +740,346 @@ struct TileJob
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
 
-// Shared memory of a tile CTA (dynamic, sized by its thread count):
-//   the staged batch: kBatch records as arrays (the pair lanes index them by
-//   record) and their 64-byte bitmasks, filled by cp.async.bulk;
-//   every pixel's best packed word so far (the pair lanes' atomicMin target);
-//   per warp, a ring of kQueue live (pixel, record) pairs waiting for a lane:
-//   the pixel's cluster-space direction and reciprocals and the packed
-//   lane | record << 5 | sure_hit << 11.
-constexpr uint32_t kQueue = 64;                      // ring entries per warp (a record adds at most 32)
-constexpr uint32_t kSmBar = 0, kSmView = 8, kSmN = 12;
-constexpr uint32_t kSmBits = 128;                    // 16-byte aligned bulk-copy targets
-constexpr uint32_t kSmRec = kSmBits + kBatch * 64;   // 7 arrays of kBatch words
-enum RecField { R_OX = 0, R_OY, R_OZ, R_CP, R_OBJ, R_LB, R_CI, R_FIELDS };
-constexpr uint32_t kSmBest = kSmRec + R_FIELDS * kBatch * 4;
-constexpr uint32_t kQueueWords = 7 * kQueue;        // per warp: 6 float arrays + the packed word
-__host__ __device__ constexpr uint32_t tile_smem_bytes(uint32_t threads)
+// The tile kernel is persistent and warp-specialised.  A CTA has the tile's
+// pixel warps ("compute warps", one thread per pixel) plus one producer warp.
+// The producer takes tiles from an atomic queue in heavy-first order and, per
+// batch of at most kStageEntries of a tile's entries, issues one cp.async.bulk of
+// the contiguous 96-byte entries into a stage of a kStages-deep ring; the
+// stage's "full" mbarrier completes when the bytes land.  Tiles without
+// entries never reach a stage: the producer writes their pixels itself.  The
+// compute warps take the stages in order, evaluate the batch (below) and
+// release the stage on its "empty" mbarrier.  So the next batch's global
+// round trips (queue, tile order, offsets, the copy) overlap this batch's
+// arithmetic.
+//
+// Shared memory (dynamic, tile_smem_bytes(compute threads)):
+//   full[kStages], empty[kStages] mbarriers; per stage a 16-byte descriptor
+//   (tile, view, n | flags, job); the stages' entries; every pixel's best
+//   packed word so far; per compute warp a ring of kQueue live (pixel,
+//   entry) pairs: the pixel's cluster-space direction and reciprocals and
+//   lane | entry << 5 | sure_hit << 11.
+constexpr uint32_t kStages = 2;
+constexpr uint32_t kStageEntries = 32;               // entries per batch
+constexpr uint32_t kQueue = 64;                      // ring entries per compute warp (an entry adds at most 32)
+constexpr uint32_t kQueueWords = 7 * kQueue;         // 6 float arrays + the packed word
+constexpr uint32_t kSmFull = 0, kSmEmpty = 8 * kStages, kSmMeta = 16 * kStages, kSmAbort = kSmMeta + 16 * kStages;
+constexpr uint32_t kSmStages = 128;
+constexpr uint32_t kStageBytes = kStageEntries * sizeof(TileEntry);
+constexpr uint32_t kSmBest = kSmStages + kStages * kStageBytes;
+static_assert(kSmAbort + 4 <= kSmStages, "header");
+constexpr uint32_t kMetaFirst = 1u << 16, kMetaLast = 1u << 17, kMetaEnd = 1u << 18, kMetaUnsorted = 1u << 19;
+__host__ __device__ constexpr uint32_t tile_smem_bytes(uint32_t compute_threads)
 {
-    return kSmBest + 8u * threads + (threads / 32u) * kQueueWords * 4u;
+    return kSmBest + 8u * compute_threads + (compute_threads / 32u) * kQueueWords * 4u;
 }
 
 struct TileSm
 {
     unsigned char* p;
-    __device__ __forceinline__ unsigned long long* bar() const { return (unsigned long long*)(p + kSmBar); }
-    __device__ __forceinline__ uint32_t& view() const { return *(uint32_t*)(p + kSmView); }
-    __device__ __forceinline__ uint32_t& n() const { return *(uint32_t*)(p + kSmN); }
-    __device__ __forceinline__ uint32_t* bits() const { return (uint32_t*)(p + kSmBits); }
-    __device__ __forceinline__ uint32_t* rec(int f) const { return (uint32_t*)(p + kSmRec) + f * kBatch; }
-    __device__ __forceinline__ float* recf(int f) const { return (float*)(p + kSmRec) + f * kBatch; }
+    uint32_t n_compute;
+    __device__ __forceinline__ uint32_t full(uint32_t s) const { return smem_addr(p + kSmFull + 8 * s); }
+    __device__ __forceinline__ uint32_t empty(uint32_t s) const { return smem_addr(p + kSmEmpty + 8 * s); }
+    __device__ __forceinline__ uint4* meta(uint32_t s) const { return (uint4*)(p + kSmMeta) + s; }
+    __device__ __forceinline__ volatile uint32_t* abort_flag() const { return (volatile uint32_t*)(p + kSmAbort); }
+    __device__ __forceinline__ TileEntry* stage(uint32_t s) const { return (TileEntry*)(p + kSmStages + s * kStageBytes); }
     __device__ __forceinline__ unsigned long long* best() const { return (unsigned long long*)(p + kSmBest); }
     __device__ __forceinline__ uint32_t* queue(uint32_t warp) const
     {
-        return (uint32_t*)(p + kSmBest + 8u * blockDim.x) + warp * kQueueWords;
+        return (uint32_t*)(p + kSmBest + 8u * n_compute) + warp * kQueueWords;
     }
 };
 
-__device__ __forceinline__ TileSm tile_sm()
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
-    extern __shared__ __align__(128) unsigned char tile_dyn_smem[];
-    return TileSm{tile_dyn_smem};
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void tile_smem_init(const TileSm& sm)
+// Everything one tile job needs (a scene with its views and scratch); the
+// multi-job form reads them from a table in global memory.
+template <bool kMulti>
+__device__ __forceinline__ const TileJob& job_of(const TileJob& single, const TileJob* jobs, uint32_t j)
 {
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(sm.bar())));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    return kMulti ? jobs[j] : single;
+}
+
+// ---- producer warp ----
+template <bool kMulti>
+__device__ void tile_producer(const TileJob& J0, const TileJob* __restrict__ jobs, uint32_t n_jobs, uint32_t total,
+                              uint32_t* __restrict__ queue, const TileSm& sm, tgx_dev_status* __restrict__ status)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t it = 0;              // batches published so far (stage it % kStages, its use it / kStages)
+    bool failed = false;
+    uint32_t extra = 0;
+    auto acquire = [&](uint32_t s) -> bool {   // wait until the compute warps released stage s
+        const uint32_t use = it / kStages;
+        if (use == 0u) return true;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(sm.empty(s), (use - 1u) & 1u));
+        if (!ok && lane == 0) { dev_error(status, TGX_ERR_TIMEOUT, 6, it); *sm.abort_flag() = 1u; }
+        return ok;
+    };
+    for (;;) {
+        if (*sm.abort_flag()) { failed = true; break; }
+        uint32_t item = 0;
+        if (lane == 0) item = atomicAdd(queue, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        uint32_t j = 0;
+        if (kMulti) {   // the last job whose first item is <= item
+            uint32_t lo = 0, hi = n_jobs - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
+            }
+            j = lo;
+        }
+        const TileJob& J = job_of<kMulti>(J0, jobs, j);
+        if (!kMulti || j == 0) extra = (item == 0u) ? J.extra_tx : 0u;
+        const uint32_t tile = J.tile_order[item - J.first];
+        uint32_t view = 0;
+        while (view + 1 < J.n_views && J.views[view + 1].tile_base <= tile) view++;
+        const bool scan_all = J.counters[C_OVERFLOW] != 0u;
+        const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
+        const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
+        const ViewConst& vc = J.views[view];
+        const uint32_t lt = tile - vc.tile_base;
+        const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
+        bool any = false;
+        for (uint32_t base = begin; base < end;) {
+            const uint32_t s = it % kStages;
+            if (!acquire(s)) { failed = true; break; }
+            TileEntry* st = sm.stage(s);
+            uint32_t n = 0, next = end;
+            if (!scan_all) {
+                n = min(kStageEntries, end - base);
+                next = base + n;
+                if (lane == 0) {
+                    *sm.meta(s) = make_uint4(tile, view, n | (base == begin ? kMetaFirst : 0u) | (next == end ? kMetaLast : 0u), j);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                 :: "r"(sm.full(s)), "r"(n * (uint32_t)sizeof(TileEntry) + extra) : "memory");
+                    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                                 :: "r"(smem_addr(st)), "l"(J.entries + base), "r"(n * (uint32_t)sizeof(TileEntry)),
+                                    "r"(sm.full(s)) : "memory");
+                }
+                extra = 0;
+            } else {
+                // bins overflowed this frame: gather the records whose tile rectangle holds
+                // this tile (slow, exact), copying each into the stage in record order
+                uint32_t* sw = reinterpret_cast<uint32_t*>(st);
+                for (next = base; next < end && n < kStageEntries;) {
+                    const uint32_t k0 = next, k = k0 + lane;
+                    bool keep = false;
+                    if (k < end) {
+                        const uint2 qr = J.rects[k];
+                        keep = J.records[k].view == view && tx >= (qr.x & 0xffffu) && tx <= (qr.y & 0xffffu) &&
+                               ty >= (qr.x >> 16) && ty <= (qr.y >> 16);
+                    }
+                    uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    uint32_t used = min(32u, end - k0);        // records examined
+                    const uint32_t room = kStageEntries - n;
+                    if ((uint32_t)__popc(m) > room) {          // keep the first `room`; rescan after the last kept
+                        uint32_t rest = m, last = 0;
+                        for (uint32_t r = 0; r < room; r++) { last = (uint32_t)__ffs(rest) - 1u; rest &= rest - 1u; }
+                        m ^= rest;
+                        used = last + 1u;
+                    }
+                    next = k0 + used;
+                    while (m) {
+                        const uint32_t kk = k0 + (uint32_t)__ffs(m) - 1u;
+                        m &= m - 1u;
+                        const uint32_t* rw = reinterpret_cast<const uint32_t*>(J.records + kk);
+                        uint32_t word = 0u;
+                        if (lane < 3u) word = rw[lane];
+                        else if (lane < 6u) word = rw[lane + 1u];
+                        else if (lane >= 8u && lane < kEntryWords) word = J.bits[(uint64_t)rw[3] * 16u + (lane - 8u)];
+                        if (lane < kEntryWords) sw[n * kEntryWords + lane] = word;
+                        n++;
+                    }
+                }
+                if (n == 0u && !any) break;   // no record holds this tile (no stage used)
+                const bool last = next >= end;
+                __syncwarp();
+                if (lane == 0) {
+                    *sm.meta(s) = make_uint4(tile, view, n | kMetaUnsorted | (!any ? kMetaFirst : 0u) | (last ? kMetaLast : 0u), j);
+                    mbar_arrive(sm.full(s));
+                }
+            }
+            any = true;
+            it++;
+            base = next;
+        }
+        if (failed) break;
+        if (!any) {
+            // no entries: the tile's pixels see no cluster
+            const uint32_t npx = vc.tile_w * vc.tile_h;
+            for (uint32_t q = lane; q < npx; q += 32u) {
+                const uint32_t px = tx * vc.tile_w + q % vc.tile_w, py = ty * vc.tile_h + q / vc.tile_w;
+                if (px < vc.width && py < vc.height) J.outs[view][(size_t)py * vc.width + px] = ULLONG_MAX;
+            }
+        }
+    }
+    if (!failed) {
+        // tell the compute warps there is no more work
+        const uint32_t s = it % kStages;
+        if (acquire(s)) {
+            if (lane == 0) {
+                *sm.meta(s) = make_uint4(0u, 0u, kMetaEnd, 0u);
+                mbar_arrive(sm.full(s));
+            }
+            it++;
+        } else {
+            failed = true;
+        }
+    }
+    if (failed && lane == 0) {
+        // copies still in flight land before the CTA leaves (bounded waits)
+        for (uint32_t s = 0; s < kStages; s++) {
+            const uint32_t last_use = it > s ? (it - 1u - s) / kStages : 0xffffffffu;
+            if (last_use != 0xffffffffu) mbar_wait_bounded(sm.full(s), last_use & 1u);
+        }
     }
 }
 
-__device__ __forceinline__ void stage_record(const TileSm& sm, uint32_t k, const VisRecord& r)
-{
-    sm.recf(R_OX)[k] = r.ox;
-    sm.recf(R_OY)[k] = r.oy;
-    sm.recf(R_OZ)[k] = r.oz;
-    sm.rec(R_CP)[k] = r.cluster_pointer;
-    sm.rec(R_OBJ)[k] = r.object_idx;
-    sm.rec(R_LB)[k] = r.d24_lb;
-    sm.rec(R_CI)[k] = r.cluster_idx;
-}
-
-// Tile `slot` (in the job's heavy-first order) of one job: every pixel's
-// nearest packed word over the clusters binned to the tile.  `phase` is the
-// parity of the CTA's bulk-copy mbarrier, carried across tiles.  Returns
-// false (the same in every thread) when a batch's copies did not complete in
-// time: the status word then holds TGX_ERR_TIMEOUT, the CTA has issued no
-// further copies, has waited once more (bounded) for the ones in flight and
-// has written its pixels' words so far; it must not stage another tile.
-//
-// Per staged batch every lane walks the records for its own pixel: the depth
-// skip, the cluster-space direction (once per object), and the conservative
-// slab test.  The pairs that survive are compacted by warp ballot into the
-// warp's ring; whenever it holds 32, all 32 lanes take one pair each and run
-// the exact entry test and the voxel DDA (vis_pair), folding the result into
-// the pixel's word with a shared-memory atomicMin.  The ring is drained at
-// the end of each batch.  The minimum over a pixel's pairs does not depend on
-// the order they are evaluated in (every word is distinct), so the buffer is
-// the same bits as one DDA per pair in record order.
-template <bool kCount = false>
-__device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const TileSm& sm, uint32_t& phase,
-                                         tgx_dev_status* __restrict__ status)
+// ---- compute warps ----
+// Per batch every lane walks the entries for its own pixel: the depth skip,
+// the cluster-space direction (once per object), and the conservative slab
+// test.  The pairs that survive are compacted by warp ballot into the warp's
+// ring; whenever it holds 32, all 32 lanes take one pair each and run the
+// exact entry test and the voxel DDA (vis_pair), folding the result into the
+// pixel's word with a shared-memory atomicMin.  The ring is drained at the end
+// of each batch.  The minimum over a pixel's pairs does not depend on the
+// order they are evaluated in (every word is distinct), so the buffer is the
+// same bits as one DDA per pair in entry order.  A warp whose pixels are all
+// nearer than the rest of the tile's (depth-sorted) entries skips them.
+template <bool kCount, bool kMulti>
+__device__ void tile_compute(const TileJob& J0, const TileJob* __restrict__ jobs, const TileSm& sm,
+                             tgx_dev_status* __restrict__ status)
 {
     uint32_t work[W_COUNT];
     if (kCount) {
 #pragma unroll
         for (int i = 0; i < W_COUNT; i++) work[i] = 0u;
     }
-    __syncthreads();   // the CTA's previous tile is done with the shared state
-    const uint32_t tile = J.tile_order[slot];
-    // bins overflowed this frame: walk every record and test its rectangle (slow, exact)
-    const bool scan_all = J.counters[C_OVERFLOW] != 0u;
-    if (threadIdx.x == 0) {
-        uint32_t v = 0;
-        while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
-        sm.view() = v;
-    }
-    sm.best()[threadIdx.x] = ULLONG_MAX;
-    __syncthreads();
-    const uint32_t view = sm.view();
-    const ViewConst& vc = J.views[view];
-    const uint32_t lt = tile - vc.tile_base;
-    const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
-    const uint32_t px = tx * vc.tile_w + threadIdx.x % vc.tile_w;
-    const uint32_t py = ty * vc.tile_h + threadIdx.x / vc.tile_w;
-    const bool valid = px < vc.width && py < vc.height;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t* const q = sm.queue(warp);
     float* const qf = (float*)q;
-    const float far_plane = vc.far_plane;
-
-    // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
-    const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
-    const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)vc.height));
-    float dws[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const float a = xadd(xmul(vc.bl[i], xsub(1.0f, fy)), xmul(vc.tl[i], fy));
-        const float b = xadd(xmul(vc.br[i], xsub(1.0f, fy)), xmul(vc.tr[i], fy));
-        dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
-    }
-
-    uint32_t best_d24 = 0xffffffu;
-    uint32_t cur_obj = 0xffffffffu;
+    unsigned long long* const best_p = sm.best() + threadIdx.x;
+    uint32_t tile = 0, view = 0, j = 0, px = 0, py = 0;
+    bool valid = false, skip = false;
+    uint32_t best_d24 = 0xffffffu, cur_obj = 0xffffffffu;
+    float dws[3] = {0.0f, 0.0f, 0.0f};
     float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
-    const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
-    const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
-    bool lost = false;      // a wait for a batch's copies ran out (the same in every lane of a warp)
-    uint32_t extra = J.extra_tx;
-    uint32_t qh = 0;        // the warp's ring: first pending entry (warp-uniform)
-    for (uint32_t base = begin; base < end; base += kBatch) {
-        uint32_t n = min(kBatch, end - base);
-        // the previous batch is fully consumed; after a lost copy no thread stages another
-        if (__syncthreads_or(lost)) break;
-        if (!scan_all) {
-            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) stage_record(sm, k, J.records[J.bins[base + k]]);
-            __syncthreads();
-            // every pixel already closer than the nearest bucket left: the tile is done
-            const uint32_t lo = bucket_lo(depth_bucket(sm.rec(R_LB)[0]));
-            if (__syncthreads_and(!valid || best_d24 < lo)) break;
-        } else {
-            // keep the records of this view whose tile rectangle holds this tile
-            if (threadIdx.x == 0) sm.n() = 0;
-            __syncthreads();
-            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-                const VisRecord r = J.records[base + k];
-                const uint2 qr = J.rects[base + k];
-                if (r.view == view && tx >= (qr.x & 0xffffu) && tx <= (qr.y & 0xffffu) && ty >= (qr.x >> 16) &&
-                    ty <= (qr.y >> 16))
-                    stage_record(sm, atomicAdd(&sm.n(), 1u), r);
+    for (uint32_t it = 0;; it++) {
+        const uint32_t s = it % kStages;
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(sm.full(s), (it / kStages) & 1u))) {
+            if (lane == 0) { dev_error(status, TGX_ERR_TIMEOUT, 5, sm.meta(s)->x); *sm.abort_flag() = 1u; }
+            break;
+        }
+        const uint4 meta = *sm.meta(s);
+        if (meta.z & kMetaEnd) break;
+        const TileJob& J = job_of<kMulti>(J0, jobs, meta.w);
+        const ViewConst& vc = J.views[meta.y];
+        if (meta.z & kMetaFirst) {
+            tile = meta.x; view = meta.y; j = meta.w;
+            const uint32_t lt = tile - vc.tile_base;
+            px = (lt % vc.tiles_x) * vc.tile_w + threadIdx.x % vc.tile_w;
+            py = (lt / vc.tiles_x) * vc.tile_h + threadIdx.x / vc.tile_w;
+            valid = px < vc.width && py < vc.height;
+            // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
+            const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
+            const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)vc.height));
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const float a = xadd(xmul(vc.bl[i], xsub(1.0f, fy)), xmul(vc.tl[i], fy));
+                const float b = xadd(xmul(vc.br[i], xsub(1.0f, fy)), xmul(vc.tr[i], fy));
+                dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
             }
-            __syncthreads();
-            n = sm.n();
-            if (n == 0) continue;
+            *best_p = ULLONG_MAX;
+            best_d24 = 0xffffffu;
+            cur_obj = 0xffffffffu;
+            skip = false;
         }
-        // stage the n bitmasks (64 B each) with bulk async copies completing on the mbarrier
-        if (threadIdx.x == 0)
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(sm.bar())), "r"(n * 64u + extra) : "memory");
-        extra = 0;
-        // order this thread's earlier generic reads of the bitmasks before the async-proxy writes
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-            const uint32_t* src = J.bits + (uint64_t)sm.rec(R_CI)[k] * 16u;
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];"
-                         :: "r"(smem_addr(sm.bits() + k * 16)), "l"(src), "r"(smem_addr(sm.bar())) : "memory");
-        }
-        // bounded wait on the barrier phase
-        lost = __any_sync(0xffffffffu, !mbar_wait_bounded(smem_addr(sm.bar()), phase));
-        phase ^= 1u;
-        if (lost) continue;
-        if (kCount && valid) work[W_BATCHES]++;
-        // produce live pairs record by record; drain the ring 32 at a time, and what is left at the end
-        uint32_t qn = 0;     // pending entries (warp-uniform)
-        for (uint32_t k = 0;;) {
-            if (k < n) {
-                bool live = false, sure = false;
-                if (valid) {
-                    if (best_d24 < sm.rec(R_LB)[k]) {   // cannot produce a smaller word
-                        if (kCount) work[W_DEPTH_SKIPS]++;
-                    } else {
-                        if (kCount) work[W_PAIRS]++;
-                        const uint32_t obj = sm.rec(R_OBJ)[k];
-                        if (obj != cur_obj) {
-                            // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
-                            // object's shared linear part (see k_object_setup)
-                            if (kCount) work[W_DIR_SETUPS]++;
-                            cur_obj = obj;
-                            const float* L = J.inv_rot + 9u * obj;
-                            const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
-                            const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
-                            const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
-                            const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
-                            dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
-                            ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
-                            iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
-                            iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+        const uint32_t n = meta.z & 0xffffu;
+        const TileEntry* E = sm.stage(s);
+        if (!skip && n > 0u) {
+            if (kCount && valid) work[W_BATCHES]++;
+            uint32_t qh = 0, qn = 0;   // the warp's ring (warp-uniform)
+            for (uint32_t k = 0;;) {
+                if (k < n) {
+                    bool live = false, sure = false;
+                    if (valid) {
+                        if (best_d24 < E[k].d24_lb) {   // cannot produce a smaller word
+                            if (kCount) work[W_DEPTH_SKIPS]++;
+                        } else {
+                            if (kCount) work[W_PAIRS]++;
+                            const uint32_t obj = E[k].object_idx;
+                            if (obj != cur_obj) {
+                                // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
+                                // object's shared linear part (see k_object_setup)
+                                if (kCount) work[W_DIR_SETUPS]++;
+                                cur_obj = obj;
+                                const float* L = J.inv_rot + 9u * obj;
+                                const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
+                                const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
+                                const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
+                                const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
+                                dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
+                                ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
+                                iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
+                                iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                            }
+                            const int sc = slab_class(E[k].ox, E[k].oy, E[k].oz, dx, dy, dz, ix, iy, iz);
+                            live = sc != kMiss;
+                            sure = sc == kHit;
+                            if (kCount) work[sc == kMiss ? W_SLAB_MISSES : sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
                         }
-                        const int sc = slab_class(sm.recf(R_OX)[k], sm.recf(R_OY)[k], sm.recf(R_OZ)[k], dx, dy, dz,
-                                                  ix, iy, iz);
-                        live = sc != kMiss;
-                        sure = sc == kHit;
-                        if (kCount) work[sc == kMiss ? W_SLAB_MISSES : sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
                     }
+                    const uint32_t m = __ballot_sync(0xffffffffu, live);
+                    if (live) {
+                        const uint32_t e = (qh + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1u);
+                        qf[0 * kQueue + e] = dx; qf[1 * kQueue + e] = dy; qf[2 * kQueue + e] = dz;
+                        qf[3 * kQueue + e] = ix; qf[4 * kQueue + e] = iy; qf[5 * kQueue + e] = iz;
+                        q[6 * kQueue + e] = lane | (k << 5) | ((uint32_t)sure << 11);
+                    }
+                    qn += __popc(m);
+                    k++;
+                    if (qn < 32u && k < n) continue;
                 }
-                const uint32_t m = __ballot_sync(0xffffffffu, live);
-                if (live) {
-                    const uint32_t e = (qh + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1u);
-                    qf[0 * kQueue + e] = dx; qf[1 * kQueue + e] = dy; qf[2 * kQueue + e] = dz;
-                    qf[3 * kQueue + e] = ix; qf[4 * kQueue + e] = iy; qf[5 * kQueue + e] = iz;
-                    q[6 * kQueue + e] = lane | (k << 5) | ((uint32_t)sure << 11);
+                if (qn == 0u) break;   // k == n and nothing pending
+                // one pair per lane: the exact test and the DDA; the word goes to its pixel
+                const uint32_t take = min(qn, 32u);
+                __syncwarp();
+                if (lane < take) {
+                    const uint32_t e = (qh + lane) & (kQueue - 1u);
+                    const uint32_t pk = q[6 * kQueue + e];
+                    const TileEntry& te = E[(pk >> 5) & (kStageEntries - 1u)];
+                    const unsigned long long w = vis_pair<kCount>(
+                        te.ox, te.oy, te.oz, qf[0 * kQueue + e], qf[1 * kQueue + e], qf[2 * kQueue + e],
+                        qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u, te.bits,
+                        te.cluster_pointer, vc.far_plane, &J.counters[C_DDA_OVERRUN], work);
+                    if (w != ULLONG_MAX) atomicMin(sm.best() + ((warp << 5) | (pk & 31u)), w);
                 }
-                qn += __popc(m);
-                k++;
-                if (qn < 32u && k < n) continue;
+                qh = (qh + take) & (kQueue - 1u);
+                qn -= take;
+                __syncwarp();
+                best_d24 = (uint32_t)(*best_p >> 40);
             }
-            if (qn == 0u) break;   // k == n and nothing pending
-            // one pair per lane: the exact test and the DDA; the word goes to its pixel
-            const uint32_t take = min(qn, 32u);
-            __syncwarp();
-            if (lane < take) {
-                const uint32_t e = (qh + lane) & (kQueue - 1u);
-                const uint32_t pk = q[6 * kQueue + e];
-                const uint32_t kk = (pk >> 5) & (kBatch - 1u);
-                const unsigned long long w = vis_pair<kCount>(
-                    sm.recf(R_OX)[kk], sm.recf(R_OY)[kk], sm.recf(R_OZ)[kk], qf[0 * kQueue + e], qf[1 * kQueue + e],
-                    qf[2 * kQueue + e], qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u,
-                    sm.bits() + kk * 16u, sm.rec(R_CP)[kk], far_plane, &J.counters[C_DDA_OVERRUN], work);
-                if (w != ULLONG_MAX) atomicMin(&sm.best()[(warp << 5) | (pk & 31u)], w);
+            // the later entries of this tile (bucket-sorted) are no nearer than this batch's last bucket
+            if (!(meta.z & kMetaUnsorted)) {
+                const uint32_t lo = bucket_lo(depth_bucket(E[n - 1].d24_lb));
+                skip = __all_sync(0xffffffffu, !valid || best_d24 < lo);
             }
-            qh = (qh + take) & (kQueue - 1u);
-            qn -= take;
-            __syncwarp();
-            best_d24 = (uint32_t)(sm.best()[threadIdx.x] >> 40);
         }
-    }
-    const unsigned long long best = sm.best()[threadIdx.x];
-    if (__syncthreads_or(lost)) {
-        // a batch's copies did not complete: report it, give the copies still in
-        // flight one more bounded wait so none lands after the CTA is gone, and
-        // write the words found so far
-        if (threadIdx.x == 0) {
-            dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
-            mbar_wait_bounded(smem_addr(sm.bar()), phase ^ 1u);
+        if (meta.z & kMetaLast) {
+            if (valid) J.outs[view][(size_t)py * vc.width + px] = *best_p;
         }
-        __syncthreads();
-        if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
-        return false;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(sm.empty(s));
     }
-    if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
     if (kCount) {
         // per warp: sum the lanes' counters, one 64-bit atomic each
+        const TileJob& J = job_of<kMulti>(J0, jobs, j);
 #pragma unroll
         for (int i = 0; i < W_COUNT; i++) {
             unsigned long long v = work[i];
@@ -963,56 +1088,34 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
             if (lane == 0u && v) atomicAdd(&J.work[i], v);
         }
     }
-    return true;
 }
 
-// Instantiated per block size (= tile pixels) so the register budget can be
-// bounded for the occupancy each size needs.  One CTA per tile of one job;
-// tile_smem_bytes(blockDim.x) of dynamic shared memory.
-template <int kThreads, int kMinBlocks, bool kCount = false>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
+// One launch of the tile stage: kCompute pixel threads (the tile) plus the
+// producer warp per CTA, as many CTAs as fit on the GPU.  The single-job form
+// takes its job by value and its tiles from counters[C_TILE_QUEUE] (zeroed
+// with the frame's counters); the multi-job form takes a job table whose
+// tiles form one queue, heavy-first within each job.
+template <int kCompute, int kMinBlocks, bool kCount, bool kMulti>
+__global__ void __launch_bounds__(kCompute + 32, kMinBlocks) k_vis_tiles(TileJob J0, const TileJob* __restrict__ jobs,
+                                                                         uint32_t n_jobs, uint32_t total,
+                                                                         uint32_t* __restrict__ queue,
+                                                                         tgx_dev_status* __restrict__ status)
 {
-    const TileSm sm = tile_sm();
-    tile_smem_init(sm);
-    pdl_wait();
-    uint32_t phase = 0;
-    vis_tile<kCount>(J, blockIdx.x, sm, phase, status);
-}
-
-// Persistent form over several jobs (scenes, each with its views): CTAs take
-// tiles from one work queue in job order, each job's tiles heavy-first, until
-// all jobs' tiles are done.
-template <int kThreads, int kMinBlocks>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles_queue(const TileJob* __restrict__ jobs,
-                                                                          uint32_t n_jobs, uint32_t total,
-                                                                          uint32_t* __restrict__ queue,
-                                                                          tgx_dev_status* __restrict__ status)
-{
-    const TileSm sm = tile_sm();
-    __shared__ TileJob s_job;
-    __shared__ uint32_t s_slot, s_jobidx;
-    tile_smem_init(sm);
-    if (threadIdx.x == 0) s_jobidx = 0xffffffffu;
-    uint32_t phase = 0;
-    for (;;) {
-        __syncthreads();   // the previous tile is done with s_job
-        if (threadIdx.x == 0) {
-            const uint32_t item = atomicAdd(queue, 1u);
-            s_slot = 0xffffffffu;
-            if (item < total) {
-                uint32_t lo = 0, hi = n_jobs - 1;   // the last job whose first item is <= item
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1) >> 1;
-                    if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
-                }
-                if (lo != s_jobidx) { s_job = jobs[lo]; s_jobidx = lo; }
-                s_slot = item - s_job.first;
-            }
+    extern __shared__ __align__(128) unsigned char tile_dyn_smem[];
+    const uint32_t n_compute = blockDim.x - 32u;
+    const TileSm sm{tile_dyn_smem, n_compute};
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < kStages; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(sm.full(s)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(sm.empty(s)), "r"(n_compute / 32u));
         }
-        __syncthreads();
-        if (s_slot == 0xffffffffu) break;
-        if (!vis_tile(s_job, s_slot, sm, phase, status)) break;   // its shared bitmask staging is not reusable
+        *sm.abort_flag() = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncthreads();
+    pdl_wait();
+    if (threadIdx.x >= n_compute) tile_producer<kMulti>(J0, jobs, n_jobs, total, kMulti ? queue : &J0.counters[C_TILE_QUEUE], sm, status);
+    else tile_compute<kCount, kMulti>(J0, jobs, sm, status);
 }
 
 }  // namespace
@@ -1100,8 +1203,8 @@ struct VisScratch
     uint32_t* cta_aux;
     uint32_t* tile_off;
     uint32_t* tile_order;
-    uint32_t* bins;
-    uint32_t bin_capacity;
+    TileEntry* entries;
+    uint32_t bin_capacity;     // entries
 };
 
 // bytes of the tile-sized part of the scratch
@@ -1129,7 +1232,7 @@ static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long
     TileJob J;
     J.records = w.records;
     J.rects = w.rects;
-    J.bins = w.bins;
+    J.entries = w.entries;
     J.tile_off = w.tile_off;
     J.tile_order = w.tile_order;
     J.views = d_vc;
@@ -1144,6 +1247,9 @@ static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long
     J.extra_tx = 0;
     return J;
 }
+
+static tgx_status vis_launch_tiles(tgx_ctx* c, const TileJob& J, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total,
+                                   uint32_t* d_queue, bool count, bool pdl);
 
 // The launches of one frame (n_views views of scene s, view table d_vc / d_outs
 // on the device): all of them, or the part up to the tile scan, or the rest.
@@ -1176,83 +1282,77 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     }
     if (phase == VIS_TO_SCAN) return TGX_OK;
     TGX_LAUNCH_PDL(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
-                   w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.bins,
-                   n_tiles, w.bin_capacity, c->d_status);
+                   w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.entries,
+                   s->d_bits, n_tiles, w.bin_capacity, c->d_status);
     if (phase == VIS_NO_TILES) return TGX_OK;
     TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
     if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
-    const uint32_t threads = c->tile_w * c->tile_h;
     if (c->vis_count_work) {
         // the counting variant (tgx_vis_count_work): same results, plus the work counters
         TGX_TRY(devbuf_reserve(c->vis_work, W_COUNT * sizeof(unsigned long long)));
         J.work = (unsigned long long*)c->vis_work.ptr;
         TGX_CUDA(cudaMemsetAsync(J.work, 0, W_COUNT * sizeof(unsigned long long), c->stream));
-        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<64, 20, true>), J, c->d_status);
-        else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<128, 10, true>), J, c->d_status);
-        else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<256, 5, true>), J, c->d_status);
-        else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<1024, 1, true>), J, c->d_status);
-        return TGX_OK;
+        return vis_launch_tiles(c, J, nullptr, 1, n_tiles, nullptr, true, false);
     }
-    if (threads == 64) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<64, 20>), J, c->d_status);
-    } else if (threads == 128) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<128, 10>), J, c->d_status);
-    } else if (threads == 256) {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<256, 5>), J, c->d_status);
-    } else {
-        TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, tile_smem_bytes(threads), (k_vis_tiles<1024, 1>), J, c->d_status);
-    }
-    return TGX_OK;
+    return vis_launch_tiles(c, J, nullptr, 1, n_tiles, nullptr, false, true);
 }
 
-// Opt-in to the dynamic shared memory the largest tile kernels need (more
-// than the 48 KB default); called once per context with its device current.
-tgx_status vis_prepare_device()
-{
-    const int big = (int)tile_smem_bytes(1024);
-    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles<1024, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    TGX_CUDA(cudaFuncSetAttribute(k_vis_tiles_queue<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    return TGX_OK;
-}
-
-// The tile stage of several jobs as one persistent launch over a work queue
-// (d_jobs: the jobs' TileJob records with their first queue items; d_queue
-// zeroed before the launch).
-// Resident CTAs of the persistent tile kernel for the context's tile size
-// (an occupancy query: call it outside stream capture).
-template <int kThreads, int kMinBlocks>
-static uint32_t vis_queue_ctas_t(tgx_ctx* c)
+// Resident CTAs per SM of the tile kernel for `compute` pixel threads (an
+// occupancy query: call it outside stream capture).
+template <int kCompute, int kMinBlocks>
+static uint32_t vis_tile_per_sm()
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles_queue<kThreads, kMinBlocks>, kThreads,
-                                                      tile_smem_bytes(kThreads)) !=
-            cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles<kCompute, kMinBlocks, false, false>,
+                                                      kCompute + 32, tile_smem_bytes(kCompute)) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
         per_sm = 1;
-    return (uint32_t)c->num_sms * (uint32_t)per_sm;
+    }
+    return (uint32_t)per_sm;
 }
 
-static uint32_t vis_queue_ctas(tgx_ctx* c)
+uint32_t vis_tile_ctas_per_sm(uint32_t compute)
 {
-    const uint32_t threads = c->tile_w * c->tile_h;
-    if (threads == 64) return vis_queue_ctas_t<64, 20>(c);
-    if (threads == 128) return vis_queue_ctas_t<128, 10>(c);
-    if (threads == 256) return vis_queue_ctas_t<256, 5>(c);
-    return vis_queue_ctas_t<1024, 1>(c);
+    if (compute == 64) return vis_tile_per_sm<64, 13>();
+    if (compute == 128) return vis_tile_per_sm<128, 8>();
+    if (compute == 256) return vis_tile_per_sm<256, 4>();
+    return vis_tile_per_sm<512, 1>();
 }
 
-static tgx_status vis_launch_queue(tgx_ctx* c, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total, uint32_t* d_queue,
-                                   uint32_t ctas)
+// Once per context, with its device current: the tile kernel's resident CTAs
+// per SM for the context's tile size.
+tgx_status vis_prepare_device(tgx_ctx* c)
 {
-    TGX_CUDA(cudaMemsetAsync(d_queue, 0, 4, c->stream));
-    const uint32_t threads = c->tile_w * c->tile_h;
-    const uint32_t grid = std::max(1u, std::min(ctas, total));
-#define QUEUE_ARGS d_jobs, n_jobs, total, d_queue, c->d_status
-    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, 64, tile_smem_bytes(64), (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
-    else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, 128, tile_smem_bytes(128), (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
-    else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, 256, tile_smem_bytes(256), (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
-    else TGX_LAUNCH(c, TR_VIS_TILES, grid, 1024, tile_smem_bytes(1024), (k_vis_tiles_queue<1024, 1>), QUEUE_ARGS);
-#undef QUEUE_ARGS
+    c->vis_tile_ctas = (uint32_t)c->num_sms * vis_tile_ctas_per_sm(c->tile_w * c->tile_h);
+    return TGX_OK;
+}
+
+// One launch of the tile stage: the single job J (by value, its tiles from its
+// counters' queue) or the n_jobs of the device table d_jobs (their `total`
+// tiles from d_queue, zeroed here).  Persistent: at most as many CTAs as fit.
+static tgx_status vis_launch_tiles(tgx_ctx* c, const TileJob& J, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total,
+                                   uint32_t* d_queue, bool count, bool pdl)
+{
+    const uint32_t compute = c->tile_w * c->tile_h;
+    const uint32_t grid = std::max(1u, std::min(c->vis_tile_ctas, total));
+    const uint32_t threads = compute + 32, smem = tile_smem_bytes(compute);
+    const bool multi = d_jobs != nullptr;
+    if (multi) TGX_CUDA(cudaMemsetAsync(d_queue, 0, 4, c->stream));
+#define TILE_ARGS J, d_jobs, n_jobs, total, d_queue, c->d_status
+#define TILE_VARIANT(C, B)                                                                                       \
+    do {                                                                                                         \
+        if (multi) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, true>), TILE_ARGS); \
+        else if (count) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, true, false>), TILE_ARGS); \
+        else if (pdl) TGX_LAUNCH_PDL(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, false>), TILE_ARGS); \
+        else TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, false>), TILE_ARGS);     \
+    } while (0)
+    if (compute == 64) TILE_VARIANT(64, 13);
+    else if (compute == 128) TILE_VARIANT(128, 8);
+    else if (compute == 256) TILE_VARIANT(256, 4);
+    else TILE_VARIANT(512, 1);
+#undef TILE_VARIANT
+#undef TILE_ARGS
     return TGX_OK;
 }
 
@@ -1304,19 +1404,21 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     if (n_pairs > 0xffffffffull) { tgx_set_error("too many (view, cluster) pairs"); return TGX_ERR_CAPACITY; }
     VisScratch w;
     bool exact = false;
+    constexpr size_t kEntry = sizeof(TileEntry);
     if (c->flags & TGX_FLAG_MIN_BIN_CAPACITY) {
-        TGX_TRY(devbuf_reserve(c->vis_bins, 64 * 4));
+        TGX_TRY(devbuf_reserve(c->vis_bins, 64 * kEntry));
         w.bin_capacity = 64;
     } else {
         exact = c->vis_last_tiles == 0 || n_tiles > c->vis_last_tiles || n_pairs > c->vis_last_pairs;
         if (c->vis_done && cudaEventQuery(c->vis_done) == cudaSuccess) {
             const uint32_t* hc = (const uint32_t*)c->h_vis_counters;
             if (hc[C_OVERFLOW]) exact = true;
-            if ((size_t)hc[C_ENTRIES] * 2 > c->vis_bins.bytes / 4) TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)hc[C_ENTRIES] * 2 * 4));
+            if ((size_t)hc[C_ENTRIES] * 2 > c->vis_bins.bytes / kEntry)
+                TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)hc[C_ENTRIES] * 2 * kEntry));
         }
         cudaGetLastError();
-        TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 64, (size_t)1 << 20) * 4));
-        w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
+        TGX_TRY(devbuf_reserve(c->vis_bins, std::max<size_t>((size_t)n_tiles * 16, (size_t)1 << 18) * kEntry));
+        w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / kEntry, 0xffffffffu);
     }
     w.rec_cap = (uint32_t)n_pairs;
     TGX_TRY(devbuf_reserve(c->vis_records, (size_t)w.rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
@@ -1326,7 +1428,7 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     w.records = (VisRecord*)c->vis_records.ptr;
     w.rects = (uint2*)(w.records + w.rec_cap);
     w.counters = (uint32_t*)c->vis_counters.ptr;
-    w.bins = (uint32_t*)c->vis_bins.ptr;
+    w.entries = (TileEntry*)c->vis_bins.ptr;
     vis_carve_tiles(w, (uint32_t*)c->vis_tile_cnt.ptr, (uint32_t*)c->vis_tile_off.ptr, n_tiles);
     if (!exact) {
         TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w));
@@ -1336,9 +1438,9 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
         TGX_CUDA(cudaStreamSynchronize(c->stream));
         const uint32_t entries = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
         if (entries > w.bin_capacity) {
-            TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)entries * 4));
-            w.bins = (uint32_t*)c->vis_bins.ptr;
-            w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / 4, 0xffffffffu);
+            TGX_TRY(devbuf_reserve(c->vis_bins, (size_t)entries * kEntry));
+            w.entries = (TileEntry*)c->vis_bins.ptr;
+            w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / kEntry, 0xffffffffu);
             if (entries <= w.bin_capacity) TGX_CUDA(cudaMemsetAsync(w.counters + C_OVERFLOW, 0, 4, c->stream));
         }
         TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_FROM_BINS));
@@ -1400,7 +1502,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     std::vector<std::vector<unsigned char>> tables(n_jobs);
     auto job_bytes = [&](const tgx_frame_graph::Job& job) {
         return al((size_t)job.rec_cap * (sizeof(VisRecord) + sizeof(uint2))) + 256 + al(vis_tile_bytes(job.n_tiles)) +
-               al((size_t)(job.n_tiles + 1) * 4 * 2) + al((size_t)job.bin_cap * 4);
+               al((size_t)(job.n_tiles + 1) * 4 * 2) + al((size_t)job.bin_cap * sizeof(TileEntry));
     };
     for (uint32_t j = 0; j < n_jobs; j++) {
         const tgx_vis_job& jb = jobs[j];
@@ -1420,7 +1522,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         job.table_off = table_bytes;
         table_bytes += al(tables[j].size());
         job.rec_cap = (uint64_t)jb.scene->n_cluster_pointers * jb.n_views;
-        job.bin_cap = std::max<uint64_t>(1u << 16, std::max<uint64_t>((uint64_t)job.n_tiles * 64, (uint64_t)entries * 3 / 2));
+        job.bin_cap = std::max<uint64_t>(1u << 14, std::max<uint64_t>((uint64_t)job.n_tiles * 4, (uint64_t)entries * 3 / 2));
         if (job.rec_cap > 0xffffffffull || job.bin_cap > 0xffffffffull || (uint64_t)total_tiles + job.n_tiles > 0xffffffffull) {
             tgx_set_error("tgx_frame_graph_create: job %u has too many (view, cluster) pairs or tiles", j);
             return fail(TGX_ERR_CAPACITY);
@@ -1460,7 +1562,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         p += al(vis_tile_bytes(job.n_tiles));
         uint32_t* tile_off = (uint32_t*)p;
         p += al((size_t)(job.n_tiles + 1) * 4 * 2);
-        w.bins = (uint32_t*)p;
+        w.entries = (TileEntry*)p;
         w.bin_capacity = (uint32_t)job.bin_cap;
         vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
         const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
@@ -1474,7 +1576,6 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         tgx_set_error("tgx_frame_graph_create: job table upload failed");
         return fail(TGX_ERR_CUDA);
     }
-    const uint32_t queue_ctas = vis_queue_ctas(c);
     // side streams and events for the fork and join inside the capture
     const uint32_t n_side = std::min<uint32_t>(n_jobs, 8u);
     std::vector<cudaStream_t> side(n_side, nullptr);
@@ -1507,7 +1608,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     }
     tgx_status st = TGX_OK;
     if (n_jobs == 1) {
-        // one job: its passes and the one-CTA-per-tile launch, no fork
+        // one job: its passes and its own tile launch, no fork
         const tgx_frame_graph::Job& job = g->jobs[0];
         const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
         unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
@@ -1528,7 +1629,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     c->stream = main_stream;
     for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++)
         if (cudaStreamWaitEvent(main_stream, done[j], 0) != cudaSuccess) st = TGX_ERR_CUDA;
-    if (st == TGX_OK) st = vis_launch_queue(c, d_jobs, n_jobs, total_tiles, d_queue, queue_ctas);
+    if (st == TGX_OK) st = vis_launch_tiles(c, TileJob{}, d_jobs, n_jobs, total_tiles, d_queue, false, false);
 captured:
     const cudaError_t ce = cudaStreamEndCapture(c->stream, &g->graph);
     release();
@@ -1745,7 +1846,7 @@ namespace {
 constexpr uint32_t kNaMaxObjects = 65536;
 constexpr uint32_t kNaMaxClusterPointers = 1u << 19;
 constexpr uint32_t kNaMaxTiles = 32768;      // 16x16 tiles: up to 3840x2160
-constexpr uint32_t kNaBins = 1u << 20;       // more entries take the exact record-scan path
+constexpr uint32_t kNaBins = 1u << 18;       // (tile, cluster) entries; more take the exact record-scan path
 constexpr uint32_t kNaTile = 16;
 
 constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -1762,7 +1863,7 @@ constexpr size_t kNaScanAux = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
 constexpr size_t kNaTileOff = kNaScanAux + na_align(((size_t)kNaMaxTiles / kScanTiles + 1) * (1 + kOrderClasses) * 4);
 constexpr size_t kNaTileOrder = kNaTileOff + na_align(((size_t)kNaMaxTiles + 1) * 4);
 constexpr size_t kNaBinsOff = kNaTileOrder + na_align((size_t)kNaMaxTiles * 4);
-constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * 4);   // about 31 MiB
+constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * sizeof(TileEntry));   // about 51 MiB
 
 // The scratch.  In host code this name is only a host-side stand-in: its
 // device address is taken with cudaGetSymbolAddress below.
@@ -1806,6 +1907,7 @@ __global__ void __launch_bounds__(128) k_vis_noalloc_setup(ViewConst vc, unsigne
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mutex;
 void* g_na_ptr[kNaMaxDevices] = {};
+uint32_t g_na_ctas[kNaMaxDevices] = {};   // resident tile CTAs on the device (16x16 tiles)
 
 // Device address of the scratch on the current device, looked up once per device.
 tgx_status na_scratch(int device, unsigned char** out)
@@ -1822,6 +1924,12 @@ tgx_status na_scratch(int device, unsigned char** out)
             tgx_set_error("tgx_vis_render_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return TGX_ERR_CUDA;
         }
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
+            tgx_set_error("tgx_vis_render_noalloc: no multiprocessor count for device %d", device);
+            return TGX_ERR_CUDA;
+        }
+        g_na_ctas[device] = (uint32_t)sms * vis_tile_ctas_per_sm(kNaTile * kNaTile);
         g_na_ptr[device] = p;
     }
     *out = (unsigned char*)g_na_ptr[device];
@@ -1888,7 +1996,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     uint32_t* cta_aux = (uint32_t*)(base + kNaScanAux);
     uint32_t* tile_off = (uint32_t*)(base + kNaTileOff);
     uint32_t* tile_order = (uint32_t*)(base + kNaTileOrder);
-    uint32_t* bins = (uint32_t*)(base + kNaBinsOff);
+    TileEntry* entries = (TileEntry*)(base + kNaBinsOff);
 
     int sms = 0;
     TGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -1911,12 +2019,12 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
         NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
         NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
     }
-    NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, bins,
-              n_tiles, kNaBins, status);
+    NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, entries,
+              d_voxel_bits, n_tiles, kNaBins, status);
     TileJob J;
     J.records = records;
     J.rects = rects;
-    J.bins = bins;
+    J.entries = entries;
     J.tile_off = tile_off;
     J.tile_order = tile_order;
     J.views = d_vc;
@@ -1929,7 +2037,11 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
-    k_vis_tiles<256, 5><<<n_tiles, kNaTile * kNaTile, tile_smem_bytes(kNaTile * kNaTile), st>>>(J, status);
+    {
+        const uint32_t grid = std::max(1u, std::min(g_na_ctas[device], n_tiles));
+        k_vis_tiles<256, 4, false, false><<<grid, kNaTile * kNaTile + 32, tile_smem_bytes(kNaTile * kNaTile), st>>>(
+            J, nullptr, 1u, n_tiles, nullptr, status);
+    }
     if (const cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         tgx_set_error("tgx_vis_render_noalloc: launch of k_vis_tiles failed: %s", cudaGetErrorString(le));
         return TGX_ERR_CUDA;
