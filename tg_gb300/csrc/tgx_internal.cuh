@@ -131,7 +131,7 @@ struct tgx_ctx
     DevBuf svo_scratch;    // SVO update: dirty-block marks
     DevBuf svo_sort;       // SVO build: pairs grouped by block slot, per-slot counts and offsets
     DevBuf vis_work;       // work counters of the tile kernel's counting variant
-    uint32_t vis_tile_ctas = 0;        // resident CTAs of the persistent tile kernel on this device
+    uint32_t vis_tile_ctas = 0;        // resident CTAs of the persistent (batched-frame) tile kernel
     bool   vis_count_work = false;
     uint32_t vis_last_tiles = 0;
     uint64_t vis_last_pairs = 0;
@@ -413,6 +413,5 @@ tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, ui
                                float* d_rgb);
 
 tgx_status vis_prepare_device(tgx_ctx* c);
-uint32_t   vis_tile_ctas_per_sm(uint32_t compute_threads);
 tgx_status vis_render_device(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                              uint64_t* const* d_visbuf);

@@ -740,346 +740,265 @@ struct TileJob
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
 
-// The tile kernel is persistent and warp-specialised.  A CTA has the tile's
-// pixel warps ("compute warps", one thread per pixel) plus one producer warp.
-// The producer takes tiles from an atomic queue in heavy-first order and, per
-// batch of at most kStageEntries of a tile's entries, issues one cp.async.bulk of
-// the contiguous 96-byte entries into a stage of a kStages-deep ring; the
-// stage's "full" mbarrier completes when the bytes land.  Tiles without
-// entries never reach a stage: the producer writes their pixels itself.  The
-// compute warps take the stages in order, evaluate the batch (below) and
-// release the stage on its "empty" mbarrier.  So the next batch's global
-// round trips (queue, tile order, offsets, the copy) overlap this batch's
-// arithmetic.
-//
-// Shared memory (dynamic, tile_smem_bytes(compute threads)):
-//   full[kStages], empty[kStages] mbarriers; per stage a 16-byte descriptor
-//   (tile, view, n | flags, job); the stages' entries; every pixel's best
-//   packed word so far; per compute warp a ring of kQueue live (pixel,
-//   entry) pairs: the pixel's cluster-space direction and reciprocals and
+// Shared memory of a tile CTA (dynamic, tile_smem_bytes(threads)):
+//   the mbarrier of the bulk copies, the tile's view and a gather count;
+//   the staged batch: up to kBatch of the tile's 96-byte entries;
+//   every pixel's best packed word so far (the pair lanes' atomicMin target);
+//   per warp, a ring of kQueue live (pixel, entry) pairs waiting for a lane:
+//   the pixel's cluster-space direction and reciprocals and the packed
 //   lane | entry << 5 | sure_hit << 11.
-constexpr uint32_t kStages = 2;
-constexpr uint32_t kStageEntries = 32;               // entries per batch
-constexpr uint32_t kQueue = 64;                      // ring entries per compute warp (an entry adds at most 32)
+constexpr uint32_t kBatch = 48;                      // entries per staged batch (k < 64 fits the packed word)
+constexpr uint32_t kQueue = 64;                      // ring entries per warp (an entry adds at most 32)
 constexpr uint32_t kQueueWords = 7 * kQueue;         // 6 float arrays + the packed word
-constexpr uint32_t kSmFull = 0, kSmEmpty = 8 * kStages, kSmMeta = 16 * kStages, kSmAbort = kSmMeta + 16 * kStages;
-constexpr uint32_t kSmStages = 128;
-constexpr uint32_t kStageBytes = kStageEntries * sizeof(TileEntry);
-constexpr uint32_t kSmBest = kSmStages + kStages * kStageBytes;
-static_assert(kSmAbort + 4 <= kSmStages, "header");
-constexpr uint32_t kMetaFirst = 1u << 16, kMetaLast = 1u << 17, kMetaEnd = 1u << 18, kMetaUnsorted = 1u << 19;
-__host__ __device__ constexpr uint32_t tile_smem_bytes(uint32_t compute_threads)
+constexpr uint32_t kSmBar = 0, kSmView = 8, kSmN = 12;
+constexpr uint32_t kSmStage = 128;                   // 16-byte aligned bulk-copy target
+constexpr uint32_t kSmBest = kSmStage + kBatch * sizeof(TileEntry);
+__host__ __device__ constexpr uint32_t tile_smem_bytes(uint32_t threads)
 {
-    return kSmBest + 8u * compute_threads + (compute_threads / 32u) * kQueueWords * 4u;
+    return kSmBest + 8u * threads + (threads / 32u) * kQueueWords * 4u;
 }
 
 struct TileSm
 {
     unsigned char* p;
-    uint32_t n_compute;
-    __device__ __forceinline__ uint32_t full(uint32_t s) const { return smem_addr(p + kSmFull + 8 * s); }
-    __device__ __forceinline__ uint32_t empty(uint32_t s) const { return smem_addr(p + kSmEmpty + 8 * s); }
-    __device__ __forceinline__ uint4* meta(uint32_t s) const { return (uint4*)(p + kSmMeta) + s; }
-    __device__ __forceinline__ volatile uint32_t* abort_flag() const { return (volatile uint32_t*)(p + kSmAbort); }
-    __device__ __forceinline__ TileEntry* stage(uint32_t s) const { return (TileEntry*)(p + kSmStages + s * kStageBytes); }
+    __device__ __forceinline__ uint32_t bar() const { return smem_addr(p + kSmBar); }
+    __device__ __forceinline__ uint32_t& view() const { return *(uint32_t*)(p + kSmView); }
+    __device__ __forceinline__ uint32_t& n() const { return *(uint32_t*)(p + kSmN); }
+    __device__ __forceinline__ TileEntry* stage() const { return (TileEntry*)(p + kSmStage); }
     __device__ __forceinline__ unsigned long long* best() const { return (unsigned long long*)(p + kSmBest); }
     __device__ __forceinline__ uint32_t* queue(uint32_t warp) const
     {
-        return (uint32_t*)(p + kSmBest + 8u * n_compute) + warp * kQueueWords;
+        return (uint32_t*)(p + kSmBest + 8u * blockDim.x) + warp * kQueueWords;
     }
 };
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+__device__ __forceinline__ TileSm tile_sm()
 {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+    extern __shared__ __align__(128) unsigned char tile_dyn_smem[];
+    return TileSm{tile_dyn_smem};
 }
 
-// Everything one tile job needs (a scene with its views and scratch); the
-// multi-job form reads them from a table in global memory.
-template <bool kMulti>
-__device__ __forceinline__ const TileJob& job_of(const TileJob& single, const TileJob* jobs, uint32_t j)
+__device__ __forceinline__ void tile_smem_init(const TileSm& sm)
 {
-    return kMulti ? jobs[j] : single;
-}
-
-// ---- producer warp ----
-template <bool kMulti>
-__device__ void tile_producer(const TileJob& J0, const TileJob* __restrict__ jobs, uint32_t n_jobs, uint32_t total,
-                              uint32_t* __restrict__ queue, const TileSm& sm, tgx_dev_status* __restrict__ status)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t it = 0;              // batches published so far (stage it % kStages, its use it / kStages)
-    bool failed = false;
-    uint32_t extra = 0;
-    auto acquire = [&](uint32_t s) -> bool {   // wait until the compute warps released stage s
-        const uint32_t use = it / kStages;
-        if (use == 0u) return true;
-        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(sm.empty(s), (use - 1u) & 1u));
-        if (!ok && lane == 0) { dev_error(status, TGX_ERR_TIMEOUT, 6, it); *sm.abort_flag() = 1u; }
-        return ok;
-    };
-    for (;;) {
-        if (*sm.abort_flag()) { failed = true; break; }
-        uint32_t item = 0;
-        if (lane == 0) item = atomicAdd(queue, 1u);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total) break;
-        uint32_t j = 0;
-        if (kMulti) {   // the last job whose first item is <= item
-            uint32_t lo = 0, hi = n_jobs - 1;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
-            }
-            j = lo;
-        }
-        const TileJob& J = job_of<kMulti>(J0, jobs, j);
-        if (!kMulti || j == 0) extra = (item == 0u) ? J.extra_tx : 0u;
-        const uint32_t tile = J.tile_order[item - J.first];
-        uint32_t view = 0;
-        while (view + 1 < J.n_views && J.views[view + 1].tile_base <= tile) view++;
-        const bool scan_all = J.counters[C_OVERFLOW] != 0u;
-        const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
-        const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
-        const ViewConst& vc = J.views[view];
-        const uint32_t lt = tile - vc.tile_base;
-        const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
-        bool any = false;
-        for (uint32_t base = begin; base < end;) {
-            const uint32_t s = it % kStages;
-            if (!acquire(s)) { failed = true; break; }
-            TileEntry* st = sm.stage(s);
-            uint32_t n = 0, next = end;
-            if (!scan_all) {
-                n = min(kStageEntries, end - base);
-                next = base + n;
-                if (lane == 0) {
-                    *sm.meta(s) = make_uint4(tile, view, n | (base == begin ? kMetaFirst : 0u) | (next == end ? kMetaLast : 0u), j);
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                                 :: "r"(sm.full(s)), "r"(n * (uint32_t)sizeof(TileEntry) + extra) : "memory");
-                    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                                 :: "r"(smem_addr(st)), "l"(J.entries + base), "r"(n * (uint32_t)sizeof(TileEntry)),
-                                    "r"(sm.full(s)) : "memory");
-                }
-                extra = 0;
-            } else {
-                // bins overflowed this frame: gather the records whose tile rectangle holds
-                // this tile (slow, exact), copying each into the stage in record order
-                uint32_t* sw = reinterpret_cast<uint32_t*>(st);
-                for (next = base; next < end && n < kStageEntries;) {
-                    const uint32_t k0 = next, k = k0 + lane;
-                    bool keep = false;
-                    if (k < end) {
-                        const uint2 qr = J.rects[k];
-                        keep = J.records[k].view == view && tx >= (qr.x & 0xffffu) && tx <= (qr.y & 0xffffu) &&
-                               ty >= (qr.x >> 16) && ty <= (qr.y >> 16);
-                    }
-                    uint32_t m = __ballot_sync(0xffffffffu, keep);
-                    uint32_t used = min(32u, end - k0);        // records examined
-                    const uint32_t room = kStageEntries - n;
-                    if ((uint32_t)__popc(m) > room) {          // keep the first `room`; rescan after the last kept
-                        uint32_t rest = m, last = 0;
-                        for (uint32_t r = 0; r < room; r++) { last = (uint32_t)__ffs(rest) - 1u; rest &= rest - 1u; }
-                        m ^= rest;
-                        used = last + 1u;
-                    }
-                    next = k0 + used;
-                    while (m) {
-                        const uint32_t kk = k0 + (uint32_t)__ffs(m) - 1u;
-                        m &= m - 1u;
-                        const uint32_t* rw = reinterpret_cast<const uint32_t*>(J.records + kk);
-                        uint32_t word = 0u;
-                        if (lane < 3u) word = rw[lane];
-                        else if (lane < 6u) word = rw[lane + 1u];
-                        else if (lane >= 8u && lane < kEntryWords) word = J.bits[(uint64_t)rw[3] * 16u + (lane - 8u)];
-                        if (lane < kEntryWords) sw[n * kEntryWords + lane] = word;
-                        n++;
-                    }
-                }
-                if (n == 0u && !any) break;   // no record holds this tile (no stage used)
-                const bool last = next >= end;
-                __syncwarp();
-                if (lane == 0) {
-                    *sm.meta(s) = make_uint4(tile, view, n | kMetaUnsorted | (!any ? kMetaFirst : 0u) | (last ? kMetaLast : 0u), j);
-                    mbar_arrive(sm.full(s));
-                }
-            }
-            any = true;
-            it++;
-            base = next;
-        }
-        if (failed) break;
-        if (!any) {
-            // no entries: the tile's pixels see no cluster
-            const uint32_t npx = vc.tile_w * vc.tile_h;
-            for (uint32_t q = lane; q < npx; q += 32u) {
-                const uint32_t px = tx * vc.tile_w + q % vc.tile_w, py = ty * vc.tile_h + q / vc.tile_w;
-                if (px < vc.width && py < vc.height) J.outs[view][(size_t)py * vc.width + px] = ULLONG_MAX;
-            }
-        }
-    }
-    if (!failed) {
-        // tell the compute warps there is no more work
-        const uint32_t s = it % kStages;
-        if (acquire(s)) {
-            if (lane == 0) {
-                *sm.meta(s) = make_uint4(0u, 0u, kMetaEnd, 0u);
-                mbar_arrive(sm.full(s));
-            }
-            it++;
-        } else {
-            failed = true;
-        }
-    }
-    if (failed && lane == 0) {
-        // copies still in flight land before the CTA leaves (bounded waits)
-        for (uint32_t s = 0; s < kStages; s++) {
-            const uint32_t last_use = it > s ? (it - 1u - s) / kStages : 0xffffffffu;
-            if (last_use != 0xffffffffu) mbar_wait_bounded(sm.full(s), last_use & 1u);
-        }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(sm.bar()));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
 }
 
-// ---- compute warps ----
-// Per batch every lane walks the entries for its own pixel: the depth skip,
-// the cluster-space direction (once per object), and the conservative slab
-// test.  The pairs that survive are compacted by warp ballot into the warp's
-// ring; whenever it holds 32, all 32 lanes take one pair each and run the
-// exact entry test and the voxel DDA (vis_pair), folding the result into the
-// pixel's word with a shared-memory atomicMin.  The ring is drained at the end
-// of each batch.  The minimum over a pixel's pairs does not depend on the
-// order they are evaluated in (every word is distinct), so the buffer is the
-// same bits as one DDA per pair in entry order.  A warp whose pixels are all
-// nearer than the rest of the tile's (depth-sorted) entries skips them.
-template <bool kCount, bool kMulti>
-__device__ void tile_compute(const TileJob& J0, const TileJob* __restrict__ jobs, const TileSm& sm,
-                             tgx_dev_status* __restrict__ status)
+// One bulk copy of n contiguous entries into the stage, completing on the
+// CTA's mbarrier (expecting `extra` bytes more than it copies under the
+// lost-copy test).  Thread 0 only.
+__device__ __forceinline__ void stage_entries(const TileSm& sm, const TileEntry* src, uint32_t n, uint32_t extra)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(sm.bar()), "r"(n * (uint32_t)sizeof(TileEntry) + extra) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(sm.stage())), "l"(src), "r"(n * (uint32_t)sizeof(TileEntry)), "r"(sm.bar())
+                 : "memory");
+}
+
+// Tile `slot` (in the job's heavy-first order) of one job: every pixel's
+// nearest packed word over the entries binned to the tile.  `phase` is the
+// parity of the CTA's bulk-copy mbarrier, carried across tiles.  Returns
+// false (the same in every thread) when a batch's copy did not complete in
+// time: the status word then holds TGX_ERR_TIMEOUT, the CTA has issued no
+// further copy, has waited once more (bounded) for the one in flight and has
+// written its pixels' words so far; it must not stage another tile.
+//
+// The tile's entries (record fields and bitmask, contiguous and sorted near
+// to far by depth bucket) arrive kBatch at a time by one cp.async.bulk; the
+// first copy is issued before the pixels' rays are set up, so the two
+// overlap.  Per batch every lane walks the entries for its own pixel: the
+// depth skip, the cluster-space direction (once per object), and the
+// conservative slab test.  The pairs that survive are compacted by warp
+// ballot into the warp's ring; whenever it holds 32, all 32 lanes take one
+// pair each and run the exact entry test and the voxel DDA (vis_pair),
+// folding the result into the pixel's word with a shared-memory atomicMin.
+// The ring is drained at the end of each batch.  The minimum over a pixel's
+// pairs does not depend on the order they are evaluated in (every word is
+// distinct), so the buffer is the same bits as one DDA per pair in order.
+template <bool kCount = false>
+__device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const TileSm& sm, uint32_t& phase,
+                                         tgx_dev_status* __restrict__ status)
 {
     uint32_t work[W_COUNT];
     if (kCount) {
 #pragma unroll
         for (int i = 0; i < W_COUNT; i++) work[i] = 0u;
     }
+    // the CTA's previous tile is done with the shared state (its generic reads of the stage
+    // ordered before the bulk copy that overwrites it)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    const uint32_t tile = J.tile_order[slot];
+    // bins overflowed this frame: gather every record whose tile rectangle holds the tile (slow, exact)
+    const bool scan_all = J.counters[C_OVERFLOW] != 0u;
+    const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
+    const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
+    if (threadIdx.x == 0) {
+        if (!scan_all && end > begin) stage_entries(sm, J.entries + begin, min(kBatch, end - begin), J.extra_tx);
+        uint32_t v = 0;
+        while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
+        sm.view() = v;
+    }
+    sm.best()[threadIdx.x] = ULLONG_MAX;
+    __syncthreads();
+    const uint32_t view = sm.view();
+    const ViewConst& vc = J.views[view];
+    const uint32_t lt = tile - vc.tile_base;
+    const uint32_t tx = lt % vc.tiles_x, ty = lt / vc.tiles_x;
+    const uint32_t px = tx * vc.tile_w + threadIdx.x % vc.tile_w;
+    const uint32_t py = ty * vc.tile_h + threadIdx.x / vc.tile_w;
+    const bool valid = px < vc.width && py < vc.height;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t* const q = sm.queue(warp);
     float* const qf = (float*)q;
-    unsigned long long* const best_p = sm.best() + threadIdx.x;
-    uint32_t tile = 0, view = 0, j = 0, px = 0, py = 0;
-    bool valid = false, skip = false;
-    uint32_t best_d24 = 0xffffffu, cur_obj = 0xffffffffu;
-    float dws[3] = {0.0f, 0.0f, 0.0f};
-    float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
-    for (uint32_t it = 0;; it++) {
-        const uint32_t s = it % kStages;
-        if (!__all_sync(0xffffffffu, mbar_wait_bounded(sm.full(s), (it / kStages) & 1u))) {
-            if (lane == 0) { dev_error(status, TGX_ERR_TIMEOUT, 5, sm.meta(s)->x); *sm.abort_flag() = 1u; }
-            break;
-        }
-        const uint4 meta = *sm.meta(s);
-        if (meta.z & kMetaEnd) break;
-        const TileJob& J = job_of<kMulti>(J0, jobs, meta.w);
-        const ViewConst& vc = J.views[meta.y];
-        if (meta.z & kMetaFirst) {
-            tile = meta.x; view = meta.y; j = meta.w;
-            const uint32_t lt = tile - vc.tile_base;
-            px = (lt % vc.tiles_x) * vc.tile_w + threadIdx.x % vc.tile_w;
-            py = (lt / vc.tiles_x) * vc.tile_h + threadIdx.x / vc.tile_w;
-            valid = px < vc.width && py < vc.height;
-            // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
-            const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
-            const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)vc.height));
+    const float far_plane = vc.far_plane;
+    const TileEntry* const E = sm.stage();
+
+    // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
+    const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
+    const float fy = xsub(1.0f, xdiv(xadd((float)py, 0.5f), (float)vc.height));
+    float dws[3];
 #pragma unroll
-            for (int i = 0; i < 3; i++) {
-                const float a = xadd(xmul(vc.bl[i], xsub(1.0f, fy)), xmul(vc.tl[i], fy));
-                const float b = xadd(xmul(vc.br[i], xsub(1.0f, fy)), xmul(vc.tr[i], fy));
-                dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
-            }
-            *best_p = ULLONG_MAX;
-            best_d24 = 0xffffffu;
-            cur_obj = 0xffffffffu;
-            skip = false;
-        }
-        const uint32_t n = meta.z & 0xffffu;
-        const TileEntry* E = sm.stage(s);
-        if (!skip && n > 0u) {
-            if (kCount && valid) work[W_BATCHES]++;
-            uint32_t qh = 0, qn = 0;   // the warp's ring (warp-uniform)
-            for (uint32_t k = 0;;) {
-                if (k < n) {
-                    bool live = false, sure = false;
-                    if (valid) {
-                        if (best_d24 < E[k].d24_lb) {   // cannot produce a smaller word
-                            if (kCount) work[W_DEPTH_SKIPS]++;
-                        } else {
-                            if (kCount) work[W_PAIRS]++;
-                            const uint32_t obj = E[k].object_idx;
-                            if (obj != cur_obj) {
-                                // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
-                                // object's shared linear part (see k_object_setup)
-                                if (kCount) work[W_DIR_SETUPS]++;
-                                cur_obj = obj;
-                                const float* L = J.inv_rot + 9u * obj;
-                                const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
-                                const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
-                                const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
-                                const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
-                                dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
-                                ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
-                                iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
-                                iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
-                            }
-                            const int sc = slab_class(E[k].ox, E[k].oy, E[k].oz, dx, dy, dz, ix, iy, iz);
-                            live = sc != kMiss;
-                            sure = sc == kHit;
-                            if (kCount) work[sc == kMiss ? W_SLAB_MISSES : sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
-                        }
-                    }
-                    const uint32_t m = __ballot_sync(0xffffffffu, live);
-                    if (live) {
-                        const uint32_t e = (qh + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1u);
-                        qf[0 * kQueue + e] = dx; qf[1 * kQueue + e] = dy; qf[2 * kQueue + e] = dz;
-                        qf[3 * kQueue + e] = ix; qf[4 * kQueue + e] = iy; qf[5 * kQueue + e] = iz;
-                        q[6 * kQueue + e] = lane | (k << 5) | ((uint32_t)sure << 11);
-                    }
-                    qn += __popc(m);
-                    k++;
-                    if (qn < 32u && k < n) continue;
-                }
-                if (qn == 0u) break;   // k == n and nothing pending
-                // one pair per lane: the exact test and the DDA; the word goes to its pixel
-                const uint32_t take = min(qn, 32u);
-                __syncwarp();
-                if (lane < take) {
-                    const uint32_t e = (qh + lane) & (kQueue - 1u);
-                    const uint32_t pk = q[6 * kQueue + e];
-                    const TileEntry& te = E[(pk >> 5) & (kStageEntries - 1u)];
-                    const unsigned long long w = vis_pair<kCount>(
-                        te.ox, te.oy, te.oz, qf[0 * kQueue + e], qf[1 * kQueue + e], qf[2 * kQueue + e],
-                        qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u, te.bits,
-                        te.cluster_pointer, vc.far_plane, &J.counters[C_DDA_OVERRUN], work);
-                    if (w != ULLONG_MAX) atomicMin(sm.best() + ((warp << 5) | (pk & 31u)), w);
-                }
-                qh = (qh + take) & (kQueue - 1u);
-                qn -= take;
-                __syncwarp();
-                best_d24 = (uint32_t)(*best_p >> 40);
-            }
-            // the later entries of this tile (bucket-sorted) are no nearer than this batch's last bucket
-            if (!(meta.z & kMetaUnsorted)) {
-                const uint32_t lo = bucket_lo(depth_bucket(E[n - 1].d24_lb));
-                skip = __all_sync(0xffffffffu, !valid || best_d24 < lo);
-            }
-        }
-        if (meta.z & kMetaLast) {
-            if (valid) J.outs[view][(size_t)py * vc.width + px] = *best_p;
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(sm.empty(s));
+    for (int i = 0; i < 3; i++) {
+        const float a = xadd(xmul(vc.bl[i], xsub(1.0f, fy)), xmul(vc.tl[i], fy));
+        const float b = xadd(xmul(vc.br[i], xsub(1.0f, fy)), xmul(vc.tr[i], fy));
+        dws[i] = xadd(xmul(a, xsub(1.0f, fx)), xmul(b, fx));
     }
+
+    uint32_t best_d24 = 0xffffffu;
+    uint32_t cur_obj = 0xffffffffu;
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f, ix = 0.0f, iy = 0.0f, iz = 0.0f;
+    bool lost = false;      // a wait for a batch's copy ran out (the same in every lane of a warp)
+    uint32_t qh = 0;        // the warp's ring: first pending entry (warp-uniform)
+    for (uint32_t base = begin; base < end;) {
+        uint32_t n;
+        if (!scan_all) {
+            n = min(kBatch, end - base);
+            if (base != begin) {
+                // the previous batch is fully consumed; after a lost copy nobody stages another
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                if (__syncthreads_or(lost)) break;
+                if (threadIdx.x == 0) stage_entries(sm, J.entries + base, n, 0u);
+            }
+            base += n;
+            lost = __any_sync(0xffffffffu, !mbar_wait_bounded(sm.bar(), phase));
+            phase ^= 1u;
+            if (lost) continue;
+        } else {
+            // keep the records of this view whose tile rectangle holds this tile, copied into the stage
+            __syncthreads();
+            if (threadIdx.x == 0) sm.n() = 0;
+            __syncthreads();
+            const uint32_t m = min(kBatch, end - base);
+            for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+                const uint32_t r = base + k;
+                const uint2 qr = J.rects[r];
+                if (J.records[r].view == view && tx >= (qr.x & 0xffffu) && tx <= (qr.y & 0xffffu) &&
+                    ty >= (qr.x >> 16) && ty <= (qr.y >> 16)) {
+                    const VisRecord& rec = J.records[r];
+                    TileEntry& te = sm.stage()[atomicAdd(&sm.n(), 1u)];
+                    te.ox = rec.ox; te.oy = rec.oy; te.oz = rec.oz;
+                    te.cluster_pointer = rec.cluster_pointer;
+                    te.object_idx = rec.object_idx;
+                    te.d24_lb = rec.d24_lb;
+#pragma unroll
+                    for (int w = 0; w < 16; w++) te.bits[w] = J.bits[(uint64_t)rec.cluster_idx * 16u + w];
+                }
+            }
+            base += m;
+            __syncthreads();
+            n = sm.n();
+            if (n == 0) continue;
+        }
+        if (kCount && valid) work[W_BATCHES]++;
+        // produce live pairs entry by entry; drain the ring 32 at a time, and what is left at the end
+        uint32_t qn = 0;     // pending entries (warp-uniform)
+        for (uint32_t k = 0;;) {
+            if (k < n) {
+                bool live = false, sure = false;
+                if (valid) {
+                    if (best_d24 < E[k].d24_lb) {   // cannot produce a smaller word
+                        if (kCount) work[W_DEPTH_SKIPS]++;
+                    } else {
+                        if (kCount) work[W_PAIRS]++;
+                        const uint32_t obj = E[k].object_idx;
+                        if (obj != cur_obj) {
+                            // normalize((ws2ms * v4(dir, 0)).xyz) (visibility.frag:69) with the
+                            // object's shared linear part (see k_object_setup)
+                            if (kCount) work[W_DIR_SETUPS]++;
+                            cur_obj = obj;
+                            const float* L = J.inv_rot + 9u * obj;
+                            const float ux = xadd(xadd(xmul(dws[0], L[0]), xmul(dws[1], L[1])), xmul(dws[2], L[2]));
+                            const float uy = xadd(xadd(xmul(dws[0], L[3]), xmul(dws[1], L[4])), xmul(dws[2], L[5]));
+                            const float uz = xadd(xadd(xmul(dws[0], L[6]), xmul(dws[1], L[7])), xmul(dws[2], L[8]));
+                            const float mag = xsqrt(xadd(xadd(xmul(ux, ux), xmul(uy, uy)), xmul(uz, uz)));
+                            dx = xdiv(ux, mag); dy = xdiv(uy, mag); dz = xdiv(uz, mag);
+                            ix = dx != 0.0f ? __frcp_rn(dx) : 0.0f;
+                            iy = dy != 0.0f ? __frcp_rn(dy) : 0.0f;
+                            iz = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                        }
+                        const int sc = slab_class(E[k].ox, E[k].oy, E[k].oz, dx, dy, dz, ix, iy, iz);
+                        live = sc != kMiss;
+                        sure = sc == kHit;
+                        if (kCount) work[sc == kMiss ? W_SLAB_MISSES : sc == kHit ? W_SURE_HITS : W_EXACT_TESTS]++;
+                    }
+                }
+                const uint32_t m = __ballot_sync(0xffffffffu, live);
+                if (live) {
+                    const uint32_t e = (qh + qn + __popc(m & ((1u << lane) - 1u))) & (kQueue - 1u);
+                    qf[0 * kQueue + e] = dx; qf[1 * kQueue + e] = dy; qf[2 * kQueue + e] = dz;
+                    qf[3 * kQueue + e] = ix; qf[4 * kQueue + e] = iy; qf[5 * kQueue + e] = iz;
+                    q[6 * kQueue + e] = lane | (k << 5) | ((uint32_t)sure << 11);
+                }
+                qn += __popc(m);
+                k++;
+                if (qn < 32u && k < n) continue;
+            }
+            if (qn == 0u) break;   // k == n and nothing pending
+            // one pair per lane: the exact test and the DDA; the word goes to its pixel
+            const uint32_t take = min(qn, 32u);
+            __syncwarp();
+            if (lane < take) {
+                const uint32_t e = (qh + lane) & (kQueue - 1u);
+                const uint32_t pk = q[6 * kQueue + e];
+                const TileEntry& te = E[(pk >> 5) & 63u];
+                const unsigned long long w = vis_pair<kCount>(
+                    te.ox, te.oy, te.oz, qf[0 * kQueue + e], qf[1 * kQueue + e], qf[2 * kQueue + e],
+                    qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u, te.bits,
+                    te.cluster_pointer, far_plane, &J.counters[C_DDA_OVERRUN], work);
+                if (w != ULLONG_MAX) atomicMin(sm.best() + ((warp << 5) | (pk & 31u)), w);
+            }
+            qh = (qh + take) & (kQueue - 1u);
+            qn -= take;
+            __syncwarp();
+            best_d24 = (uint32_t)(sm.best()[threadIdx.x] >> 40);
+        }
+        // every pixel already nearer than the rest of the (bucket-sorted) entries: the tile is done
+        if (!scan_all && base < end) {
+            const uint32_t lo = bucket_lo(depth_bucket(E[n - 1].d24_lb));
+            if (__syncthreads_and(!valid || best_d24 < lo)) break;
+        }
+    }
+    const unsigned long long best = sm.best()[threadIdx.x];
+    if (__syncthreads_or(lost)) {
+        // a batch's copy did not complete: report it, give the copy still in
+        // flight one more bounded wait so it does not land after the CTA is
+        // gone, and write the words found so far
+        if (threadIdx.x == 0) {
+            dev_error(status, TGX_ERR_TIMEOUT, 5, tile);
+            mbar_wait_bounded(sm.bar(), phase ^ 1u);
+        }
+        __syncthreads();
+        if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
+        return false;
+    }
+    if (valid) J.outs[view][(size_t)py * vc.width + px] = best;
     if (kCount) {
         // per warp: sum the lanes' counters, one 64-bit atomic each
-        const TileJob& J = job_of<kMulti>(J0, jobs, j);
 #pragma unroll
         for (int i = 0; i < W_COUNT; i++) {
             unsigned long long v = work[i];
@@ -1088,34 +1007,55 @@ __device__ void tile_compute(const TileJob& J0, const TileJob* __restrict__ jobs
             if (lane == 0u && v) atomicAdd(&J.work[i], v);
         }
     }
+    return true;
 }
 
-// One launch of the tile stage: kCompute pixel threads (the tile) plus the
-// producer warp per CTA, as many CTAs as fit on the GPU.  The single-job form
-// takes its job by value and its tiles from counters[C_TILE_QUEUE] (zeroed
-// with the frame's counters); the multi-job form takes a job table whose
-// tiles form one queue, heavy-first within each job.
-template <int kCompute, int kMinBlocks, bool kCount, bool kMulti>
-__global__ void __launch_bounds__(kCompute + 32, kMinBlocks) k_vis_tiles(TileJob J0, const TileJob* __restrict__ jobs,
-                                                                         uint32_t n_jobs, uint32_t total,
-                                                                         uint32_t* __restrict__ queue,
-                                                                         tgx_dev_status* __restrict__ status)
+// Instantiated per block size (= tile pixels) so the register budget can be
+// bounded for the occupancy each size needs.  One CTA per tile of one job.
+template <int kThreads, int kMinBlocks, bool kCount = false>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
 {
-    extern __shared__ __align__(128) unsigned char tile_dyn_smem[];
-    const uint32_t n_compute = blockDim.x - 32u;
-    const TileSm sm{tile_dyn_smem, n_compute};
-    if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < kStages; s++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(sm.full(s)));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(sm.empty(s)), "r"(n_compute / 32u));
-        }
-        *sm.abort_flag() = 0u;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
+    const TileSm sm = tile_sm();
+    tile_smem_init(sm);
     pdl_wait();
-    if (threadIdx.x >= n_compute) tile_producer<kMulti>(J0, jobs, n_jobs, total, kMulti ? queue : &J0.counters[C_TILE_QUEUE], sm, status);
-    else tile_compute<kCount, kMulti>(J0, jobs, sm, status);
+    uint32_t phase = 0;
+    vis_tile<kCount>(J, blockIdx.x, sm, phase, status);
+}
+
+// Persistent form over several jobs (scenes, each with its views): CTAs take
+// tiles from one work queue in job order, each job's tiles heavy-first, until
+// all jobs' tiles are done.
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles_queue(const TileJob* __restrict__ jobs,
+                                                                          uint32_t n_jobs, uint32_t total,
+                                                                          uint32_t* __restrict__ queue,
+                                                                          tgx_dev_status* __restrict__ status)
+{
+    const TileSm sm = tile_sm();
+    __shared__ TileJob s_job;
+    __shared__ uint32_t s_slot, s_jobidx;
+    tile_smem_init(sm);
+    if (threadIdx.x == 0) s_jobidx = 0xffffffffu;
+    uint32_t phase = 0;
+    for (;;) {
+        __syncthreads();   // the previous tile is done with s_job
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(queue, 1u);
+            s_slot = 0xffffffffu;
+            if (item < total) {
+                uint32_t lo = 0, hi = n_jobs - 1;   // the last job whose first item is <= item
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
+                }
+                if (lo != s_jobidx) { s_job = jobs[lo]; s_jobidx = lo; }
+                s_slot = item - s_job.first;
+            }
+        }
+        __syncthreads();
+        if (s_slot == 0xffffffffu) break;
+        if (!vis_tile(s_job, s_slot, sm, phase, status)) break;   // its shared staging is not reusable
+    }
 }
 
 }  // namespace
@@ -1248,9 +1188,6 @@ static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long
     return J;
 }
 
-static tgx_status vis_launch_tiles(tgx_ctx* c, const TileJob& J, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total,
-                                   uint32_t* d_queue, bool count, bool pdl);
-
 // The launches of one frame (n_views views of scene s, view table d_vc / d_outs
 // on the device): all of them, or the part up to the tile scan, or the rest.
 static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs,
@@ -1287,72 +1224,63 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     if (phase == VIS_NO_TILES) return TGX_OK;
     TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
     if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
+    const uint32_t threads = c->tile_w * c->tile_h, smem = tile_smem_bytes(threads);
     if (c->vis_count_work) {
         // the counting variant (tgx_vis_count_work): same results, plus the work counters
         TGX_TRY(devbuf_reserve(c->vis_work, W_COUNT * sizeof(unsigned long long)));
         J.work = (unsigned long long*)c->vis_work.ptr;
         TGX_CUDA(cudaMemsetAsync(J.work, 0, W_COUNT * sizeof(unsigned long long), c->stream));
-        return vis_launch_tiles(c, J, nullptr, 1, n_tiles, nullptr, true, false);
+        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 20, true>), J, c->d_status);
+        else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<128, 10, true>), J, c->d_status);
+        else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<256, 5, true>), J, c->d_status);
+        else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<512, 2, true>), J, c->d_status);
+        return TGX_OK;
     }
-    return vis_launch_tiles(c, J, nullptr, 1, n_tiles, nullptr, false, true);
+    if (threads == 64) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 20>), J, c->d_status);
+    else if (threads == 128) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<128, 10>), J, c->d_status);
+    else if (threads == 256) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<256, 5>), J, c->d_status);
+    else TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<512, 2>), J, c->d_status);
+    return TGX_OK;
 }
 
-// Resident CTAs per SM of the tile kernel for `compute` pixel threads (an
-// occupancy query: call it outside stream capture).
-template <int kCompute, int kMinBlocks>
-static uint32_t vis_tile_per_sm()
+// Once per context, with its device current: the persistent tile kernel's
+// resident CTAs for the context's tile size (an occupancy query, so it is made
+// outside any stream capture).
+template <int kThreads, int kMinBlocks>
+static uint32_t vis_queue_per_sm()
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles<kCompute, kMinBlocks, false, false>,
-                                                      kCompute + 32, tile_smem_bytes(kCompute)) != cudaSuccess ||
-        per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vis_tiles_queue<kThreads, kMinBlocks>, kThreads,
+                                                      tile_smem_bytes(kThreads)) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
     return (uint32_t)per_sm;
 }
 
-uint32_t vis_tile_ctas_per_sm(uint32_t compute)
-{
-    if (compute == 64) return vis_tile_per_sm<64, 13>();
-    if (compute == 128) return vis_tile_per_sm<128, 8>();
-    if (compute == 256) return vis_tile_per_sm<256, 4>();
-    return vis_tile_per_sm<512, 1>();
-}
-
-// Once per context, with its device current: the tile kernel's resident CTAs
-// per SM for the context's tile size.
 tgx_status vis_prepare_device(tgx_ctx* c)
 {
-    c->vis_tile_ctas = (uint32_t)c->num_sms * vis_tile_ctas_per_sm(c->tile_w * c->tile_h);
+    const uint32_t threads = c->tile_w * c->tile_h;
+    const uint32_t per_sm = threads == 64 ? vis_queue_per_sm<64, 20>() : threads == 128 ? vis_queue_per_sm<128, 10>()
+                          : threads == 256 ? vis_queue_per_sm<256, 5>() : vis_queue_per_sm<512, 2>();
+    c->vis_tile_ctas = (uint32_t)c->num_sms * per_sm;
     return TGX_OK;
 }
 
-// One launch of the tile stage: the single job J (by value, its tiles from its
-// counters' queue) or the n_jobs of the device table d_jobs (their `total`
-// tiles from d_queue, zeroed here).  Persistent: at most as many CTAs as fit.
-static tgx_status vis_launch_tiles(tgx_ctx* c, const TileJob& J, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total,
-                                   uint32_t* d_queue, bool count, bool pdl)
+// The tile stage of several jobs as one persistent launch over a work queue
+// (d_jobs: the jobs' TileJob records with their first queue items; d_queue
+// zeroed here).
+static tgx_status vis_launch_queue(tgx_ctx* c, const TileJob* d_jobs, uint32_t n_jobs, uint32_t total, uint32_t* d_queue)
 {
-    const uint32_t compute = c->tile_w * c->tile_h;
+    TGX_CUDA(cudaMemsetAsync(d_queue, 0, 4, c->stream));
+    const uint32_t threads = c->tile_w * c->tile_h, smem = tile_smem_bytes(threads);
     const uint32_t grid = std::max(1u, std::min(c->vis_tile_ctas, total));
-    const uint32_t threads = compute + 32, smem = tile_smem_bytes(compute);
-    const bool multi = d_jobs != nullptr;
-    if (multi) TGX_CUDA(cudaMemsetAsync(d_queue, 0, 4, c->stream));
-#define TILE_ARGS J, d_jobs, n_jobs, total, d_queue, c->d_status
-#define TILE_VARIANT(C, B)                                                                                       \
-    do {                                                                                                         \
-        if (multi) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, true>), TILE_ARGS); \
-        else if (count) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, true, false>), TILE_ARGS); \
-        else if (pdl) TGX_LAUNCH_PDL(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, false>), TILE_ARGS); \
-        else TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles<C, B, false, false>), TILE_ARGS);     \
-    } while (0)
-    if (compute == 64) TILE_VARIANT(64, 13);
-    else if (compute == 128) TILE_VARIANT(128, 8);
-    else if (compute == 256) TILE_VARIANT(256, 4);
-    else TILE_VARIANT(512, 1);
-#undef TILE_VARIANT
-#undef TILE_ARGS
+#define QUEUE_ARGS d_jobs, n_jobs, total, d_queue, c->d_status
+    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
+    else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
+    else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
+    else TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<512, 2>), QUEUE_ARGS);
+#undef QUEUE_ARGS
     return TGX_OK;
 }
 
@@ -1629,7 +1557,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     c->stream = main_stream;
     for (uint32_t j = 0; j < n_jobs && st == TGX_OK; j++)
         if (cudaStreamWaitEvent(main_stream, done[j], 0) != cudaSuccess) st = TGX_ERR_CUDA;
-    if (st == TGX_OK) st = vis_launch_tiles(c, TileJob{}, d_jobs, n_jobs, total_tiles, d_queue, false, false);
+    if (st == TGX_OK) st = vis_launch_queue(c, d_jobs, n_jobs, total_tiles, d_queue);
 captured:
     const cudaError_t ce = cudaStreamEndCapture(c->stream, &g->graph);
     release();
@@ -1907,7 +1835,6 @@ __global__ void __launch_bounds__(128) k_vis_noalloc_setup(ViewConst vc, unsigne
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mutex;
 void* g_na_ptr[kNaMaxDevices] = {};
-uint32_t g_na_ctas[kNaMaxDevices] = {};   // resident tile CTAs on the device (16x16 tiles)
 
 // Device address of the scratch on the current device, looked up once per device.
 tgx_status na_scratch(int device, unsigned char** out)
@@ -1924,12 +1851,6 @@ tgx_status na_scratch(int device, unsigned char** out)
             tgx_set_error("tgx_vis_render_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return TGX_ERR_CUDA;
         }
-        int sms = 0;
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) {
-            tgx_set_error("tgx_vis_render_noalloc: no multiprocessor count for device %d", device);
-            return TGX_ERR_CUDA;
-        }
-        g_na_ctas[device] = (uint32_t)sms * vis_tile_ctas_per_sm(kNaTile * kNaTile);
         g_na_ptr[device] = p;
     }
     *out = (unsigned char*)g_na_ptr[device];
@@ -2037,11 +1958,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
-    {
-        const uint32_t grid = std::max(1u, std::min(g_na_ctas[device], n_tiles));
-        k_vis_tiles<256, 4, false, false><<<grid, kNaTile * kNaTile + 32, tile_smem_bytes(kNaTile * kNaTile), st>>>(
-            J, nullptr, 1u, n_tiles, nullptr, status);
-    }
+    k_vis_tiles<256, 5><<<n_tiles, kNaTile * kNaTile, tile_smem_bytes(kNaTile * kNaTile), st>>>(J, status);
     if (const cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         tgx_set_error("tgx_vis_render_noalloc: launch of k_vis_tiles failed: %s", cudaGetErrorString(le));
         return TGX_ERR_CUDA;
