@@ -37,7 +37,7 @@ def test_cfg1_bit_exact(ctx, oracle):
     assert (g != EMPTY).sum() > 10000
 
 
-@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("seed", range(16))
 def test_fuzz_scenes_bit_exact(ctx, oracle, seed):
     s = permute_clusters(fuzz_scene(seed, n_objects=6, box=40.0, max_cpa=4), seed)
     rng = np.random.default_rng(100 + seed)

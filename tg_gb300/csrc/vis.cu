@@ -622,11 +622,51 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
 // 6. per-tile ray/cluster evaluation
 // ---------------------------------------------------------------------------
 
+// gmax(gmax(q0, q1), q2) of the near-plane quotients q_i = (p_i - o_i) / d_i
+// (p_i = lo_i for d_i > 0, hi_i for d_i < 0; F32_MIN when d_i == 0), each an
+// exactly rounded division, as the slab test and the voxel entry of
+// visibility.frag compute them.  The maximum is located first with the
+// correctly rounded reciprocals r_i (RN(n * RN(1/d)) is within 2^-23 + 2^-24
+// relative of the exact quotient); when the largest approximation beats the
+// next by more than 4e-6 of their magnitudes, only that axis is divided,
+// since its exact quotient is then surely the largest and the maximum of
+// distinct values does not depend on the comparison order.  Otherwise (near
+// ties, values near underflow or overflow) all three are divided.
+__device__ __forceinline__ float max_near_quot(float ox, float oy, float oz, float dx, float dy, float dz, float rx,
+                                               float ry, float rz, float lox, float loy, float loz, float hix,
+                                               float hiy, float hiz)
+{
+    // an axis counts when d > 0 or d < 0 (not for 0 or NaN), as in the shader's test
+    const bool hx = dx > 0.0f || dx < 0.0f, hy = dy > 0.0f || dy < 0.0f, hz = dz > 0.0f || dz < 0.0f;
+    const float nx = dx > 0.0f ? xsub(lox, ox) : xsub(hix, ox);
+    const float ny = dy > 0.0f ? xsub(loy, oy) : xsub(hiy, oy);
+    const float nz = dz > 0.0f ? xsub(loz, oz) : xsub(hiz, oz);
+    const float ninf = __int_as_float(0xff800000);
+    const float ax = hx ? xmul(nx, rx) : ninf;
+    const float ay = hy ? xmul(ny, ry) : ninf;
+    const float az = hz ? xmul(nz, rz) : ninf;
+    // the largest approximation and the next one
+    float top, next, num, den;
+    if (ax >= ay && ax >= az) { top = ax; next = fmaxf(ay, az); num = nx; den = dx; }
+    else if (ay >= az)        { top = ay; next = fmaxf(ax, az); num = ny; den = dy; }
+    else                      { top = az; next = fmaxf(ax, ay); num = nz; den = dz; }
+    const bool normal_top = fabsf(top) <= 1e30f && (top == 0.0f || fabsf(top) >= 1e-30f);
+    const bool normal_next = next == ninf || (fabsf(next) <= 1e30f && (next == 0.0f || fabsf(next) >= 1e-30f));
+    const bool no_nan = ax == ax && ay == ay && az == az;
+    if (no_nan && normal_top && normal_next && (next == ninf || next < top - 4e-6f * (fabsf(top) + fabsf(next))))
+        return xdiv(num, den);
+    const float qx = hx ? xdiv(nx, dx) : F32_MIN_TG;
+    const float qy = hy ? xdiv(ny, dy) : F32_MIN_TG;
+    const float qz = hz ? xdiv(nz, dz) : F32_MIN_TG;
+    return gmax(gmax(qx, qy), qz);
+}
+
 // One (pixel, cluster) fragment of visibility.frag:78-207 given the cluster-space
 // ray (o, d), the correctly rounded reciprocals (ix, iy, iz) of its non-zero
 // direction components and the cluster's 16 bit words.  Returns the packed
 // word or ~0.  The DDA's per-axis steps 1/|d| are |ix| etc. exactly: a
-// correctly rounded 1/(-d) is the negated 1/d.
+// correctly rounded 1/(-d) is the negated 1/d.  The first voxel is tested
+// before the DDA's start distances are computed: a hit there never reads them.
 template <bool kCount = false>
 __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float oz, float dx, float dy, float dz,
                                                        float ix, float iy, float iz, bool sure_hit,
@@ -637,10 +677,7 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     if (sure_hit) {
         // the box test surely passes: only the entry distance is needed, and of
         // each axis only the near-plane quotient can be ray_aabb's minimum
-        const float nx = dx > 0.0f ? xdiv(xsub(0.0f, ox), dx) : dx < 0.0f ? xdiv(xsub(8.0f, ox), dx) : F32_MIN_TG;
-        const float ny = dy > 0.0f ? xdiv(xsub(0.0f, oy), dy) : dy < 0.0f ? xdiv(xsub(8.0f, oy), dy) : F32_MIN_TG;
-        const float nz = dz > 0.0f ? xdiv(xsub(0.0f, oz), dz) : dz < 0.0f ? xdiv(xsub(8.0f, oz), dz) : F32_MIN_TG;
-        enter = gmax(gmax(nx, ny), nz);
+        enter = max_near_quot(ox, oy, oz, dx, dy, dz, ix, iy, iz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f);
     } else {
         float exit_;
         if (!ray_aabb(ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, 0.0f, 8.0f, 8.0f, 8.0f, enter, exit_)) return ULLONG_MAX;
@@ -657,41 +694,46 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     int x = (int)gmin(gmax(floorf(hx), 0.0f), 7.0f);
     int y = (int)gmin(gmax(floorf(hy), 0.0f), 7.0f);
     int z = (int)gmin(gmax(floorf(hz), 0.0f), 7.0f);
-    int sx = 0, sy = 0, sz = 0;
-    float tmx = F32_MAX_TG, tmy = F32_MAX_TG, tmz = F32_MAX_TG;
-    float tdx = F32_MAX_TG, tdy = F32_MAX_TG, tdz = F32_MAX_TG;
-    if (dx > 0.0f) { sx = 1; tmx = xadd(enter, xdiv(xsub((float)(x + 1), hx), dx)); tdx = ix; }
-    else if (dx < 0.0f) { sx = -1; tmx = xadd(enter, xdiv(xsub(hx, (float)x), -dx)); tdx = -ix; }
-    if (dy > 0.0f) { sy = 1; tmy = xadd(enter, xdiv(xsub((float)(y + 1), hy), dy)); tdy = iy; }
-    else if (dy < 0.0f) { sy = -1; tmy = xadd(enter, xdiv(xsub(hy, (float)y), -dy)); tdy = -iy; }
-    if (dz > 0.0f) { sz = 1; tmz = xadd(enter, xdiv(xsub((float)(z + 1), hz), dz)); tdz = iz; }
-    else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = -iz; }
-    for (uint32_t step = 0; step < kMaxDdaSteps; step++) {
-        const uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
-        if (kCount) work[W_DDA_STEPS]++;
-        if (w[rvi >> 5] & (1u << (rvi & 31u))) {
-            if (kCount) work[W_HITS]++;
-            // entry distance of the voxel box (visibility.frag:155): only the near-plane
-            // quotient of each axis can be the maximum, since (vmin-o)/d <= (vmax-o)/d for d>0
-            const float nx = dx > 0.0f ? xdiv(xsub((float)x, ox), dx) : dx < 0.0f ? xdiv(xsub((float)(x + 1), ox), dx) : F32_MIN_TG;
-            const float ny = dy > 0.0f ? xdiv(xsub((float)y, oy), dy) : dy < 0.0f ? xdiv(xsub((float)(y + 1), oy), dy) : F32_MIN_TG;
-            const float nz = dz > 0.0f ? xdiv(xsub((float)z, oz), dz) : dz < 0.0f ? xdiv(xsub((float)(z + 1), oz), dz) : F32_MIN_TG;
-            const float ve = gmax(gmax(nx, ny), nz);
-            const float depth = gmax(0.0f, xdiv(ve, far_plane));
-            if (!(depth <= 1.0f)) return ULLONG_MAX;
-            const unsigned long long d24 = __float2uint_rz(xmul(depth, 16777215.0f));   // < 2^24
-            return (d24 << 40) | ((unsigned long long)cluster_pointer << 9) | (unsigned long long)rvi;
-        }
-        if (tmx < tmy) {
-            if (tmx < tmz) { tmx = xadd(tmx, tdx); x += sx; if (x < 0 || x >= 8) return ULLONG_MAX; }
-            else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
-        } else {
-            if (tmy < tmz) { tmy = xadd(tmy, tdy); y += sy; if (y < 0 || y >= 8) return ULLONG_MAX; }
-            else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
+    uint32_t rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
+    if (kCount) work[W_DDA_STEPS]++;
+    bool hit = (w[rvi >> 5] >> (rvi & 31u)) & 1u;
+    if (!hit) {
+        int sx = 0, sy = 0, sz = 0;
+        float tmx = F32_MAX_TG, tmy = F32_MAX_TG, tmz = F32_MAX_TG;
+        float tdx = F32_MAX_TG, tdy = F32_MAX_TG, tdz = F32_MAX_TG;
+        if (dx > 0.0f) { sx = 1; tmx = xadd(enter, xdiv(xsub((float)(x + 1), hx), dx)); tdx = ix; }
+        else if (dx < 0.0f) { sx = -1; tmx = xadd(enter, xdiv(xsub(hx, (float)x), -dx)); tdx = -ix; }
+        if (dy > 0.0f) { sy = 1; tmy = xadd(enter, xdiv(xsub((float)(y + 1), hy), dy)); tdy = iy; }
+        else if (dy < 0.0f) { sy = -1; tmy = xadd(enter, xdiv(xsub(hy, (float)y), -dy)); tdy = -iy; }
+        if (dz > 0.0f) { sz = 1; tmz = xadd(enter, xdiv(xsub((float)(z + 1), hz), dz)); tdz = iz; }
+        else if (dz < 0.0f) { sz = -1; tmz = xadd(enter, xdiv(xsub(hz, (float)z), -dz)); tdz = -iz; }
+        for (uint32_t step = 1;; step++) {
+            if (step >= kMaxDdaSteps) {
+                atomicAdd(overrun, 1u);
+                return ULLONG_MAX;
+            }
+            if (tmx < tmy) {
+                if (tmx < tmz) { tmx = xadd(tmx, tdx); x += sx; if (x < 0 || x >= 8) return ULLONG_MAX; }
+                else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
+            } else {
+                if (tmy < tmz) { tmy = xadd(tmy, tdy); y += sy; if (y < 0 || y >= 8) return ULLONG_MAX; }
+                else           { tmz = xadd(tmz, tdz); z += sz; if (z < 0 || z >= 8) return ULLONG_MAX; }
+            }
+            rvi = 64u * (uint32_t)z + 8u * (uint32_t)y + (uint32_t)x;
+            if (kCount) work[W_DDA_STEPS]++;
+            if ((w[rvi >> 5] >> (rvi & 31u)) & 1u) break;
         }
     }
-    atomicAdd(overrun, 1u);
-    return ULLONG_MAX;
+    if (kCount) work[W_HITS]++;
+    // entry distance of the voxel box (visibility.frag:155): only the near-plane
+    // quotient of each axis can be the maximum, since (vmin-o)/d <= (vmax-o)/d for d>0
+    const float fx0 = (float)x, fy0 = (float)y, fz0 = (float)z;
+    const float ve = max_near_quot(ox, oy, oz, dx, dy, dz, ix, iy, iz, fx0, fy0, fz0, (float)(x + 1), (float)(y + 1),
+                                   (float)(z + 1));
+    const float depth = gmax(0.0f, xdiv(ve, far_plane));
+    if (!(depth <= 1.0f)) return ULLONG_MAX;
+    const unsigned long long d24 = __float2uint_rz(xmul(depth, 16777215.0f));   // < 2^24
+    return (d24 << 40) | ((unsigned long long)cluster_pointer << 9) | (unsigned long long)rvi;
 }
 
 // Conservative classification of the exact box test of vis_pair: kMiss or
