@@ -281,6 +281,144 @@ def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, box, width: int, hei
     return res
 
 
+def camera_path(frame: int, seed: int = 11):
+    """A seeded camera path through the 512-object scene: from near the box
+    centre the camera moves 2 voxels per frame along a random direction while
+    its yaw turns 0.2 degree per frame and its pitch sways by 0.05 rad."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    pos = rng.uniform(-20.0, 20.0, 3) + 2.0 * frame * d
+    yaw = float(np.pi) + 0.0035 * frame
+    pitch = 0.05 * float(np.sin(frame / 25.0))
+    return pos, pitch, yaw
+
+
+def compare_cache_vs_plain_moving(ctx, sc, svo, scene, stream, box, move_objects: bool, width: int, height: int,
+                                  warm: int = 60, scored: int = 8):
+    """Learned-cache GI against plain GI with the camera moving every frame
+    (camera_path) and, with move_objects, 8 objects moving 1.5 voxels per frame
+    (tgx_scene_set_objects + tgx_svo_update before every frame).  Each of the
+    last `scored` frames of a run is scored against its own 256-spp plain
+    2-bounce render.  Cached GI runs warm + scored frames per spp setting from
+    a fresh cache, training online every frame along the path; plain GI
+    renders the scored frames.  Frame times are CUDA-event times of the GI
+    call alone, training included (the visibility pass and the SVO update are
+    the same for both and not counted).  The speed-up compares the lowest spp
+    whose mean relMSE over the scored frames is <= 0.01."""
+    import torch
+    import tg_gb300 as tg
+
+    rng = np.random.default_rng(5)
+    movers = rng.choice(len(scene.objects), 8, replace=False)
+    vel = rng.normal(size=(8, 3)).astype(np.float32)
+    vel *= 1.5 / np.linalg.norm(vel, axis=1, keepdims=True)
+    base_objs = scene.objects.copy()
+    n_frames = warm + scored
+    views = []
+    for f in range(n_frames):
+        pos, pitch, yaw = camera_path(f)
+        views.append(tg.make_view(tuple(float(x) for x in pos), pitch, yaw, float(np.pi / 3), width, height, 0.1,
+                                  4096.0))
+    vis = torch.empty(width * height, dtype=torch.int64, device="cuda")
+    out = torch.empty(width * height * 3, dtype=torch.float32, device="cuda")
+
+    def pose(f):
+        if not move_objects:
+            return
+        objs = base_objs.copy()
+        objs["translation"][movers] += f * vel
+        sc.set_objects(0, objs)
+        svo.update(sc)
+
+    def gi_timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1)
+
+    refs, masks = {}, {}
+    with torch.cuda.stream(stream):
+        for f in range(warm, n_frames):
+            pose(f)
+            ctx.vis_render(sc, views[f], [vis])
+            ctx.gi_render(sc, svo, views[f], vis, tg.gi_params(spp=256, bounces=2, seed=1234, frame=f), out)
+            ctx.sync()
+            refs[f] = out.cpu().numpy()
+            masks[f] = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
+        plain = {}
+        for spp in (8, 10, 12, 14, 16, 20):
+            ms, err = [], []
+            for f in range(warm, n_frames):
+                pose(f)
+                ctx.vis_render(sc, views[f], [vis])
+                ms.append(gi_timed(lambda: ctx.gi_render(sc, svo, views[f], vis,
+                                                         tg.gi_params(spp=spp, bounces=2, seed=2, frame=f), out)))
+                err.append(rel_mse(out.cpu().numpy(), refs[f], masks[f]))
+            plain[spp] = {"frame_ms": round(float(np.mean(ms)), 3), "relmse": float(np.mean(err)),
+                          "relmse_max": float(np.max(err))}
+        cp = tg.cache_gi_params(box[0], box[1], **CACHE_VARIANTS["configured_training"])
+        cached = {}
+        for spp in (2, 3, 4, 5, 6):
+            cache = tg.Cache(ctx, seed=7)
+            ms, err = [], []
+            for f in range(n_frames):
+                pose(f)
+                ctx.vis_render(sc, views[f], [vis])
+                t = gi_timed(lambda: ctx.gi_render_cached(sc, svo, cache, views[f], vis,
+                                                          tg.gi_params(spp=spp, bounces=2, seed=2, frame=f), cp, out))
+                if f >= warm:
+                    ms.append(t)
+                    err.append(rel_mse(out.cpu().numpy(), refs[f], masks[f]))
+            cache.close()
+            cached[spp] = {"frame_ms": round(float(np.mean(ms)), 3), "relmse": float(np.mean(err)),
+                           "relmse_max": float(np.max(err))}
+        if move_objects:
+            sc.set_objects(0, base_objs)
+            svo.update(sc)
+        ctx.sync()
+
+    def best(d):
+        ok = [(v["frame_ms"], k) for k, v in d.items() if v["relmse"] <= 0.01]
+        return min(ok) if ok else None
+
+    res = {"camera": "2 voxels and 0.2 degree of yaw per frame (seeded path)",
+           "objects_moving": "8 objects, 1.5 voxels per frame, tgx_svo_update every frame" if move_objects else "none",
+           "warmup_frames": warm, "scored_frames": scored, "judge": "plain 2-bounce GI, 256 spp, per frame",
+           "plain": plain, "cached_configured_training": cached, "device_status": int(ctx.device_error().code)}
+    bp, bc = best(plain), best(cached)
+    if bp:
+        res["plain_at_target"] = {"spp": bp[1], "frame_ms": bp[0]}
+    if bc:
+        res["cached_at_target"] = {"spp": bc[1], "frame_ms": bc[0]}
+    if bp and bc:
+        res["speedup_at_equal_relmse"] = round(bp[0] / bc[0], 3)
+    return res
+
+
+def cache_study_heldout(local: int, stream, box):
+    """The static 1080p study on a 512-object scene the estimator was not tuned
+    on: the same generator with seed 2 (other sizes, poses, noise and LUTs)."""
+    import torch
+    import tg_gb300 as tg
+
+    scene = tg.generate_scene(1, 512, 2, 16, 2, **SCENE_KW)
+    view = make_view()
+    ctx = tg.Context(local, tile=(8, 8))
+    sc = ctx.upload(scene)
+    vis = torch.empty(W * H, dtype=torch.int64, device="cuda")
+    ctx.vis_render(sc, view, [vis])
+    svo = ctx.svo_build(sc, (-2048.0, -2048.0, -2048.0), 12)
+    ctx.sync()
+    res = compare_cache_vs_plain(ctx, sc, svo, view, vis, torch.cuda.ExternalStream(ctx.stream), box, W, H)
+    svo.close()
+    sc.close()
+    ctx.close()
+    return res
+
+
 def cache_study_config1(local: int, stream_of):
     """The learned-cache comparison on the config-1 scene (1 object of 4x4x4
     Bernoulli(0.3) clusters at (0,0,64)) at 1920x1080, SVO 256^3 around it."""
@@ -744,10 +882,15 @@ def main() -> None:
         ctx.sync()
         cache_report = None
         if not args.no_gi_cache:
+            box = ((-1100.0,) * 3, (1100.0,) * 3)
             cache_report = {
                 "config1_scene": cache_study_config1(local, stream),
-                "512_object_scene": compare_cache_vs_plain(
-                    ctx, sc, svo, view, out, stream, ((-1100.0,) * 3, (1100.0,) * 3), W, H),
+                "512_object_scene": compare_cache_vs_plain(ctx, sc, svo, view, out, stream, box, W, H),
+                "512_object_scene_seed2": cache_study_heldout(local, stream, box),
+                "512_object_scene_moving_camera": compare_cache_vs_plain_moving(
+                    ctx, sc, svo, scene, stream, box, False, W, H),
+                "512_object_scene_moving_camera_and_objects": compare_cache_vs_plain_moving(
+                    ctx, sc, svo, scene, stream, box, True, W, H),
             }
         svo.close()
         build_ms = []
