@@ -178,12 +178,14 @@ def rel_mse(x, r, mask):
 
 PLAIN_SPP = (1, 2, 4, 8, 10, 12, 13, 14, 16, 20, 24, 32)
 CACHED_SPP = (1, 2, 3, 4, 5, 6, 8, 12, 16)
-# The configured training budget (65,536 bounce samples per frame from 16-spp SVO paths, 4 Adam steps, lr 1e-2)
-# and a lighter one; both with the pixel-point network (131,072 training pixels, shrinkage weight up to 1).
+# The configured training budget (65,536 bounce samples per frame from 16-spp SVO paths, lr 1e-2, in 16 Adam
+# steps of 4,096) and a lighter one (16,384 samples from 8-spp paths, 8 steps); both with the pixel-point network
+# (131,072 training pixels, shrinkage weight up to 1).  16 steps rather than 4 keep the networks current when
+# the camera moves (moving-camera study: 3 spp reaches relMSE 0.0098 instead of 0.012).
 CACHE_VARIANTS = {
-    "configured_training": dict(n_train=65536, train_spp=16, train_steps=4, lr=1e-2, primary_weight=1.0,
+    "configured_training": dict(n_train=65536, train_spp=16, train_steps=16, lr=1e-2, primary_weight=1.0,
                                 n_train_primary=131072),
-    "light_training": dict(n_train=16384, train_spp=8, train_steps=4, lr=1e-2, primary_weight=1.0,
+    "light_training": dict(n_train=16384, train_spp=8, train_steps=8, lr=1e-2, primary_weight=1.0,
                            n_train_primary=131072),
 }
 

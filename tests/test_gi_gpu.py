@@ -317,37 +317,38 @@ def test_gi_benchmark_frame_bands_bit_exact(ctx, oracle, bench_scene, bounces, s
 
 
 def test_cached_gi_keeps_its_gain_under_camera_and_object_motion(ctx):
-    """The camera moves every frame (and two objects with it, through
-    tgx_svo_update): cached GI, trained online along the path, still beats
+    """The camera moves every frame, and so do two objects (tgx_svo_update):
+    cached GI, trained online along the path, still has a lower error than
     plain GI of the same spp on the last frames, each scored against its own
-    256-spp plain render."""
+    256-spp plain render.  A value-noise scene like the benchmark's, smaller."""
     import torch
-    s = fuzz_scene(23, n_objects=6, box=30.0, max_cpa=4)
-    s.objects["lut_idx"] = 0
-    mn = [-128.0, -128.0, -128.0]
+    s = tg.generate_scene(1, 48, 2, 8, seed=3, noise_period=32.0, noise_threshold=0.5,
+                          box_min=(-160.0,) * 3, box_max=(160.0,) * 3, n_luts=8)
+    mn = [-256.0] * 3
     sc = ctx.upload(s)
-    svo = ctx.svo_build(sc, mn, 8)
+    svo = ctx.svo_build(sc, mn, 9)
     base = s.objects.copy()
     vel = np.zeros((len(base), 3), np.float32)
-    vel[:2] = (0.4, -0.2, 0.3)
-    box = ((-40.0,) * 3, (40.0,) * 3)
-    cp = tg.cache_gi_params(*box, n_train=8192, train_spp=8, train_steps=4, lr=1e-2, primary_weight=1.0,
-                            n_train_primary=4096)
+    vel[:2] = (0.6, -0.3, 0.45)
+    box = ((-220.0,) * 3, (220.0,) * 3)
+    cp = tg.cache_gi_params(*box, n_train=16384, train_spp=16, train_steps=16, lr=1e-2, primary_weight=1.0,
+                            n_train_primary=32768)
     cache = tg.Cache(ctx, seed=2)
-    vis = torch.empty(96 * 64, dtype=torch.int64, device="cuda")
-    out = torch.empty(96 * 64 * 3, dtype=torch.float32, device="cuda")
+    w, h = 256, 144
+    vis = torch.empty(w * h, dtype=torch.int64, device="cuda")
+    out = torch.empty(w * h * 3, dtype=torch.float32, device="cuda")
     ref = torch.empty_like(out)
     errs_cached, errs_plain = [], []
-    for f in range(44):
+    for f in range(64):
         objs = base.copy()
         objs["translation"] += f * vel
         sc.set_objects(0, objs)
         svo.update(sc)
-        view = tg.make_view((0.3 * f - 6.0, 5.0, -70.0 + 0.2 * f), 0.1, float(np.pi) + 0.004 * f, 1.1, 96, 64,
-                            0.1, 300.0)
+        view = tg.make_view((0.8 * f - 25.0, 3.0, -10.0 + 0.5 * f), 0.05, float(np.pi) + 0.004 * f, 1.0, w, h,
+                            0.1, 600.0)
         ctx.vis_render(sc, view, [vis])
         ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=f), cp, out)
-        if f >= 40:
+        if f >= 60:
             ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=9, frame=f), ref)
             ctx.sync()
             hit = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
@@ -358,6 +359,8 @@ def test_cached_gi_keeps_its_gain_under_camera_and_object_motion(ctx):
             ctx.sync()
             x = out.cpu().numpy().reshape(-1, 3)[hit]
             errs_plain.append(float(np.mean((x - r) ** 2 / (r ** 2 + 1e-2))))
+            assert hit.sum() > 5000
     assert ctx.device_error().code == 0
     cache.close(); svo.close(); sc.close()
-    assert np.mean(errs_cached) < 0.8 * np.mean(errs_plain), (errs_cached, errs_plain)
+    print("relMSE cached", errs_cached, "plain", errs_plain)
+    assert np.mean(errs_cached) < 0.7 * np.mean(errs_plain), (errs_cached, errs_plain)
