@@ -364,3 +364,37 @@ def test_cached_gi_keeps_its_gain_under_camera_and_object_motion(ctx):
     cache.close(); svo.close(); sc.close()
     print("relMSE cached", errs_cached, "plain", errs_plain)
     assert np.mean(errs_cached) < 0.7 * np.mean(errs_plain), (errs_cached, errs_plain)
+
+
+def test_cached_gi_reaches_the_target_error_on_a_held_out_scene(ctx):
+    """The shrinkage weight was tuned on the benchmark's 512-object scene
+    (seed 1).  On the same generator with seed 2 (other sizes, poses, noise
+    and LUTs), at 1920x1080 with the configured training budget, 4-spp cached
+    2-bounce GI after 60 online frames is within relMSE 0.01 of a 256-spp
+    plain render (measured 0.0084; plain GI needs 14 spp for it)."""
+    import torch
+    s = tg.generate_scene(1, 512, 2, 16, seed=2, noise_period=64.0, noise_threshold=0.5,
+                          box_min=(-1024.0,) * 3, box_max=(1024.0,) * 3, n_luts=32)
+    view = tg.make_view((0.0, 0.0, 0.0), 0.0, float(np.pi), float(np.pi / 3), 1920, 1080, 0.1, 4096.0)
+    sc = ctx.upload(s)
+    svo = ctx.svo_build(sc, (-2048.0,) * 3, 12)
+    vis = torch.empty(1920 * 1080, dtype=torch.int64, device="cuda")
+    ctx.vis_render(sc, view, [vis])
+    ref = torch.empty(1920 * 1080 * 3, dtype=torch.float32, device="cuda")
+    out = torch.empty_like(ref)
+    ctx.gi_render(sc, svo, view, vis, tg.gi_params(spp=256, bounces=2, seed=1234), ref)
+    cp = tg.cache_gi_params((-1100.0,) * 3, (1100.0,) * 3, n_train=65536, train_spp=16, train_steps=16, lr=1e-2,
+                            primary_weight=1.0, n_train_primary=131072)
+    cache = tg.Cache(ctx, seed=7)
+    for f in range(60):
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=1, bounces=2, seed=2, frame=f), cp, out)
+    ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=100), cp, out)
+    ctx.sync()
+    assert ctx.device_error().code == 0
+    hit = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
+    r = ref.cpu().numpy().reshape(-1, 3)[hit]
+    x = out.cpu().numpy().reshape(-1, 3)[hit]
+    err = float(np.mean((x - r) ** 2 / (r ** 2 + 1e-2)))
+    cache.close(); svo.close(); sc.close()
+    print("held-out scene, cached 4 spp relMSE", err)
+    assert err <= 0.01, err
