@@ -158,6 +158,27 @@ def run_reference(args, rank: int) -> None:
             steps.append(r)
         cb = r
     value = statistics.mean(s["value"] for s in steps)
+    rooflines = {}
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    if "gi_trace_work" in gi_report:
+        tw = gi_report["gi_trace_work"]
+        tbytes = 4 * tw["dda_steps"] + 48 * tw["rays"]
+        tach = tbytes / (tw["k_trace_queue_ms"] * 1e-3) / 1e9
+        rooflines["k_trace_queue"] = {
+            "bound": "hbm", "achieved": tach, "peak": hbm_peak, "unit": "GB/s", "frac": tach / hbm_peak,
+            "algorithmic_bytes": tbytes, "traffic": None,
+            "bytes_model": "4 B of occupancy per DDA step + 24 B ray read + 24 B hit written per ray, counted by "
+                           "the kernel (tgx_gi_get_work); the SVO working set is L2-resident, so the limiter is "
+                           "latency and divergent issue, not DRAM",
+            "dda_steps_per_s": tw["dda_steps"] / (tw["k_trace_queue_ms"] * 1e-3)}
+    if "mlp" in gi_report:
+        mi, mt = gi_report["mlp"]["inference"], gi_report["mlp"]["training_step"]
+        rooflines["k_mlp_forward_tc"] = {"bound": "tensor", "achieved": mi["tflops"], "peak": bf16, "unit": "TFLOP/s",
+                                         "frac": mi["tflops"] / bf16, "traffic": None,
+                                         "note": "peak of measured (bf16_tflops, burst)"}
+        rooflines["k_mlp_train_tc"] = {"bound": "tensor", "achieved": mt["tflops"], "peak": bf16, "unit": "TFLOP/s",
+                                       "frac": mt["tflops"] / bf16, "traffic": None,
+                                       "note": "training step incl. Adam; peak of measured (bf16_tflops, burst)"}
     line = {
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": W * H / (value * 1e9) * 1e3, "higher_is_better": True,
@@ -398,6 +419,53 @@ def compare_cache_vs_plain_moving(ctx, sc, svo, scene, stream, box, move_objects
     if bp and bc:
         res["speedup_at_equal_relmse"] = round(bp[0] / bc[0], 3)
     return res
+
+
+def bench_mlp(ctx, stream):
+    """The cache network's kernels alone: inference of 2^20 queries and one
+    training step (forward, backward, weight gradients and Adam) on 65,536
+    samples, the configured per-frame training set, timed with CUDA events
+    over 20 repetitions after 3 warm-up ones."""
+    import torch
+    import tg_gb300 as tg
+
+    rng = np.random.default_rng(3)
+
+    def inputs(n):
+        x = np.concatenate([rng.uniform(0, 1, (n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3))], axis=1)
+        x[:, 3:6] /= np.linalg.norm(x[:, 3:6], axis=1, keepdims=True)
+        x[:, 6:9] /= np.linalg.norm(x[:, 6:9], axis=1, keepdims=True)
+        t = (0.3 + 0.2 * np.sin(4 * x[:, :3]) + 0.1 * x[:, 3:6] ** 2).astype(np.float32)
+        return torch.from_numpy(x.astype(np.float32)).cuda(), torch.from_numpy(t).cuda()
+
+    cache = tg.Cache(ctx, seed=1)
+    xq, _ = inputs(1 << 20)
+    yq = torch.empty((1 << 20, 3), dtype=torch.float32, device="cuda")
+    xt, tt = inputs(65536)
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        ctx.sync()
+        return e0.elapsed_time(e1) / reps
+
+    with torch.cuda.stream(stream):
+        infer_ms = timed(lambda: cache.infer(xq, yq))
+        train_ms = timed(lambda: cache.train_step(xt, tt, 1e-2))
+    cache.close()
+    fwd_flop = 2 * (216 * 64 + 3 * 64 * 64 + 64 * 3)          # 52,608 per query
+    train_flop = 2 * fwd_flop + 2 * (3 * 64 * 64 + 64 * 3)   # forward, weight gradients, deltas: 130,176 per sample
+    return {"inference": {"queries": 1 << 20, "ms": infer_ms, "flop_per_query": fwd_flop,
+                          "tflops": (1 << 20) * fwd_flop / (infer_ms * 1e-3) / 1e12},
+            "training_step": {"samples": 65536, "ms": train_ms, "flop_per_sample": train_flop,
+                              "tflops": 65536 * train_flop / (train_ms * 1e-3) / 1e12,
+                              "includes": "k_mlp_train_tc + k_mlp_adam"}}
 
 
 def cache_study_heldout(local: int, stream, box):
@@ -939,6 +1007,17 @@ def main() -> None:
             g1.record(stream)
             ctx.sync()
         gi_ms = g0.elapsed_time(g1) / gi_frames
+        # one traced frame: the traversal kernel's time and its own step and ray counts
+        ctx.sync()
+        ctx.trace_reset()
+        ctx.trace(True)
+        with torch.cuda.stream(stream):
+            ctx.gi_render(sc, svo, view, out, params, rgb)
+        ctx.sync()
+        gi_trace = ctx.trace_read()
+        ctx.trace(False)
+        gi_work = ctx.gi_work()
+        mlp_report = bench_mlp(ctx, stream)
         err = ctx.device_error()
         gi_report = {
             "svo_build_ms": statistics.median(build_ms),
@@ -953,6 +1032,10 @@ def main() -> None:
             "gi_trace_autotune_ms": trace_tuning,
             "gi_bounce_rays_per_s": hits * 4 / (gi_ms * 1e-3),
             "gi_device_status": int(err.code),
+            "gi_trace_work": {"dda_steps": int(gi_work.dda_steps), "rays": int(gi_work.rays),
+                              "k_trace_queue_ms": gi_trace["k_trace_queue"][0] / max(gi_trace["k_trace_queue"][1], 1),
+                              "frame": "the 1-bounce 4-spp frame above, counted by the traversal kernel"},
+            "mlp": mlp_report,
         }
         if cache_report is not None:
             gi_report["gi_cache_vs_plain"] = cache_report
@@ -1029,6 +1112,7 @@ def main() -> None:
                      "algorithmic_bytes": algo_bytes,
                      "note": "peak of measured (MEASURED_PEAKS.json hbm_gbs)" if pk.exists() else "peak of fallback",
                      **({"limiter": limiter} if limiter else {})},
+        "rooflines_secondary": rooflines,
         "clocks": clk,
         "hit_pixels": hits,
         "vis_work": vis_work,

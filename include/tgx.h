@@ -541,6 +541,19 @@ tgx_status  tgx_gi_render_cached(tgx_ctx* ctx, const tgx_scene* scene, const tgx
                                  const tgx_view* view, const uint64_t* d_visbuf, const tgx_gi_params* params,
                                  const tgx_cache_gi_params* cache_params, float* d_rgb);
 
+/* SVO traversal work of the last tgx_gi_render / tgx_gi_render_cached call on
+ * this context, counted by the traversal kernel itself (every ray it traced:
+ * bounce, shadow and training rays; one step = one hierarchical-DDA iteration,
+ * with the bottom-up start counted like the descent it replaces).  No
+ * counterpart in the reference, which has no GI pass.  Blocking. */
+typedef struct tgx_gi_work
+{
+    uint64_t dda_steps;
+    uint64_t rays;
+} tgx_gi_work;
+
+tgx_status  tgx_gi_get_work(tgx_ctx* ctx, tgx_gi_work* out_work);
+
 /* ---- synthetic scenes (the reference's CPU noise loop, tgvk_raytracer.c:870-978) ---- */
 
 typedef struct tgx_gen_params

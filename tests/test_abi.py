@@ -118,6 +118,7 @@ int main(void)
     printf("tgx_device_error %zu\n", sizeof(tgx_device_error));
     printf("tgx_vis_stats %zu\n", sizeof(tgx_vis_stats));
     printf("tgx_vis_work %zu\n", sizeof(tgx_vis_work));
+    printf("tgx_gi_work %zu\n", sizeof(tgx_gi_work));
     printf("tgx_svo_info %zu\n", sizeof(tgx_svo_info));
     printf("tgx_gi_params %zu\n", sizeof(tgx_gi_params));
     printf("tgx_cache_gi_params %zu\n", sizeof(tgx_cache_gi_params));
@@ -153,6 +154,7 @@ def test_header_compiles_as_c99_and_layouts_match_the_binding(tmp_path):
     assert sizes["tgx_device_error"] == C.sizeof(tg.DeviceError)
     assert sizes["tgx_vis_stats"] == C.sizeof(tg.VisStats)
     assert sizes["tgx_vis_work"] == C.sizeof(tg.VisWork)
+    assert sizes["tgx_gi_work"] == C.sizeof(tg.GiWork)
     assert sizes["tgx_svo_info"] == C.sizeof(tg.SvoInfo)
     assert sizes["tgx_gi_params"] == tg.GI_PARAMS_DTYPE.itemsize
     assert sizes["tgx_cache_gi_params"] == tg.CACHE_GI_DTYPE.itemsize

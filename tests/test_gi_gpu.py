@@ -98,6 +98,8 @@ def test_gi_bit_exact_vs_oracle(ctx, oracle, bounces, spp):
     visb = vis.cpu().numpy().view(np.uint64)
     ref = gi_render(oracle, osvo, s, view, params, visb)
     assert np.array_equal(g.view(np.uint32), ref.view(np.uint32)), np.abs(g - ref).max()
+    work = ctx.gi_work()   # the traversal's own counts of this frame
+    assert 0 < work.rays and work.rays <= work.dda_steps <= 256 * work.rays
     assert (visb != np.uint64(tg.VIS_EMPTY)).sum() > 200
     svo.close()
     sc.close()

@@ -134,6 +134,11 @@ class VisStats(C.Structure):
                 ("dda_overruns", C.c_uint32)]
 
 
+class GiWork(C.Structure):
+    """tgx_gi_work: the last GI call's SVO traversal work."""
+    _fields_ = [("dda_steps", C.c_uint64), ("rays", C.c_uint64)]
+
+
 class VisWork(C.Structure):
     """tgx_vis_work: the visibility tile kernel's own work counts."""
     _fields_ = [(n, C.c_uint64) for n in ("pairs", "depth_skips", "dir_setups", "slab_misses", "sure_hits",
@@ -164,7 +169,7 @@ EXPORTS = [
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
     "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait", "tgx_vis_count_work",
-    "tgx_vis_get_work",
+    "tgx_vis_get_work", "tgx_gi_get_work",
 ]
 
 
@@ -211,6 +216,7 @@ def _load() -> C.CDLL:
         "tgx_vis_get_stats": (i32, [vp, C.POINTER(VisStats)]),
         "tgx_vis_count_work": (i32, [vp, i32]),
         "tgx_vis_get_work": (i32, [vp, C.POINTER(VisWork)]),
+        "tgx_gi_get_work": (i32, [vp, C.POINTER(GiWork)]),
         "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "tgx_cache_n_params": (u32, []),
         "tgx_gi_render_cached": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -499,6 +505,12 @@ class Context:
     def vis_count_work(self, enable: bool) -> None:
         """tgx_vis_count_work: later renders run the tile kernel's counting variant."""
         check(lib.tgx_vis_count_work(self.handle, int(enable)), "tgx_vis_count_work")
+
+    def gi_work(self) -> GiWork:
+        """tgx_gi_get_work: the last GI call's traversal steps and rays (blocking)."""
+        w = GiWork()
+        check(lib.tgx_gi_get_work(self.handle, C.byref(w)), "tgx_gi_get_work")
+        return w
 
     def vis_work(self) -> VisWork:
         """tgx_vis_get_work: the last counted render's work totals (blocking)."""

@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
                                                                   uint32_t mul_b, const uint32_t* __restrict__ n_dev,
                                                                   uint32_t max_steps, uint32_t steps_per_round,
                                                                   uint32_t* __restrict__ queue,
-                                                                  uint32_t* __restrict__ exhausted)
+                                                                  uint32_t* __restrict__ exhausted,
+                                                                  unsigned long long* __restrict__ work)
 {
     __shared__ uint32_t occ_off[16];
     __shared__ RayState ring[kTraceWarps][kRing];
@@ -283,6 +284,7 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
     bool have = false;
     uint32_t head = 0, count = 0;   // the warp's ring (warp-uniform)
     bool drained = false;           // the ray queue is exhausted (warp-uniform)
+    uint32_t done_steps = 0, done_rays = 0;   // this lane's finished rays and their DDA steps
     for (;;) {
         const uint32_t need_mask = __ballot_sync(0xffffffffu, !have);
         const uint32_t n_need = (uint32_t)__popc(need_mask);
@@ -298,8 +300,13 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
             if (it < n_tot) {
                 const Ray ray = it < n_a ? ra[it] : rb[it - n_a];
                 const int res = svo_trace_begin(s, occ_off, ray.o, ray.d, max_steps, rs);
-                if (res == kTraceRunning) running = true;
-                else write_hit(it < n_a ? &ha[it] : &hb[it - n_a], res, rs);
+                if (res == kTraceRunning) {
+                    running = true;
+                } else {
+                    write_hit(it < n_a ? &ha[it] : &hb[it - n_a], res, rs);
+                    done_steps += rs.steps;
+                    done_rays++;
+                }
             }
             const uint32_t run_mask = __ballot_sync(0xffffffffu, running);
             if (running) {
@@ -330,9 +337,22 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
             if (res != kTraceRunning) {
                 if (res < 0) atomicAdd(exhausted, 1u);
                 write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);
+                done_steps += r.steps;
+                done_rays++;
                 have = false;
             }
         }
+    }
+    // the frame's traversal work: one pair of 64-bit atomics per warp
+    unsigned long long ws = done_steps, wr = done_rays;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ws += __shfl_down_sync(0xffffffffu, ws, o);
+        wr += __shfl_down_sync(0xffffffffu, wr, o);
+    }
+    if (lane == 0 && wr) {
+        atomicAdd(&work[0], ws);
+        atomicAdd(&work[1], wr);
     }
 }
 
@@ -837,13 +857,21 @@ uint32_t stride_grid(tgx_ctx* c, uint64_t items, uint32_t block)
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((items + block - 1) / block, (uint64_t)c->num_sms * 16));
 }
 
+// The frame's traversal work counters (DDA steps, rays) sit after the 32
+// first words of the frame's counters, which every GI call zeroes.
+__host__ __device__ inline unsigned long long* trace_work(uint32_t* counters)
+{
+    return reinterpret_cast<unsigned long long*>(counters + 32);
+}
+
+// queue = &counters[CC_QUEUE] of the frame's counters
 tgx_status trace_lists(tgx_ctx* c, const SvoDev& s, const Ray* ra, RayHit* ha, uint32_t mul_a, const Ray* rb,
                        RayHit* hb, uint32_t mul_b, const uint32_t* n_dev, uint32_t max_steps, uint32_t* queue,
                        uint32_t* exhausted)
 {
     TGX_CUDA(cudaMemsetAsync(queue, 0, 4, c->stream));
     TGX_LAUNCH(c, TR_GI_TRACE, trace_grid(c), 128, 0, k_trace_queue, s, ra, ha, mul_a, rb, hb, mul_b, n_dev, max_steps,
-               c->trace_steps_per_round, queue, exhausted);
+               c->trace_steps_per_round, queue, exhausted, trace_work(queue - CC_QUEUE));
     return TGX_OK;
 }
 
@@ -1055,5 +1083,19 @@ extern "C" tgx_status tgx_gi_render_cached(tgx_ctx* c, const tgx_scene* sc, cons
         if (pper) { nets[m] = pnet; ns[m] = pper; xs[m] = ptx + 9ull * pper * k; ts[m] = ptt + 3ull * pper * k; m++; }
         TGX_TRY(cache_train_pair(c, nets, ns, xs, ts, m, cp->lr));
     }
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_gi_get_work(tgx_ctx* c, tgx_gi_work* out)
+{
+    if (!c || !out) return TGX_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    if (!c->gi_scratch.ptr) return TGX_OK;
+    unsigned long long h[2];
+    TGX_CUDA(cudaMemcpyAsync(h, trace_work((uint32_t*)c->gi_scratch.ptr), sizeof(h), cudaMemcpyDeviceToHost,
+                             c->stream));
+    TGX_CUDA(cudaStreamSynchronize(c->stream));
+    out->dda_steps = h[0];
+    out->rays = h[1];
     return TGX_OK;
 }
