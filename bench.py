@@ -158,27 +158,6 @@ def run_reference(args, rank: int) -> None:
             steps.append(r)
         cb = r
     value = statistics.mean(s["value"] for s in steps)
-    rooflines = {}
-    bf16 = peaks.get("bf16_tflops", 1900.0)
-    if "gi_trace_work" in gi_report:
-        tw = gi_report["gi_trace_work"]
-        tbytes = 4 * tw["dda_steps"] + 48 * tw["rays"]
-        tach = tbytes / (tw["k_trace_queue_ms"] * 1e-3) / 1e9
-        rooflines["k_trace_queue"] = {
-            "bound": "hbm", "achieved": tach, "peak": hbm_peak, "unit": "GB/s", "frac": tach / hbm_peak,
-            "algorithmic_bytes": tbytes, "traffic": None,
-            "bytes_model": "4 B of occupancy per DDA step + 24 B ray read + 24 B hit written per ray, counted by "
-                           "the kernel (tgx_gi_get_work); the SVO working set is L2-resident, so the limiter is "
-                           "latency and divergent issue, not DRAM",
-            "dda_steps_per_s": tw["dda_steps"] / (tw["k_trace_queue_ms"] * 1e-3)}
-    if "mlp" in gi_report:
-        mi, mt = gi_report["mlp"]["inference"], gi_report["mlp"]["training_step"]
-        rooflines["k_mlp_forward_tc"] = {"bound": "tensor", "achieved": mi["tflops"], "peak": bf16, "unit": "TFLOP/s",
-                                         "frac": mi["tflops"] / bf16, "traffic": None,
-                                         "note": "peak of measured (bf16_tflops, burst)"}
-        rooflines["k_mlp_train_tc"] = {"bound": "tensor", "achieved": mt["tflops"], "peak": bf16, "unit": "TFLOP/s",
-                                       "frac": mt["tflops"] / bf16, "traffic": None,
-                                       "note": "training step incl. Adam; peak of measured (bf16_tflops, burst)"}
     line = {
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": W * H / (value * 1e9) * 1e3, "higher_is_better": True,
@@ -523,40 +502,66 @@ def look_at_view(pos, target, w, h, far):
     return tg.make_view(tuple(float(x) for x in pos), pitch, yaw, float(np.pi / 3), w, h, 0.1, far)
 
 
-def bench_batched(local: int, frames: int = 10):
-    """Config 3: one batched frame of 64 views of the config-1 object (resolutions
-    drawn from 320x240 .. 3840x2160, cameras on a sphere around it, seed 3) plus
-    16 scenes of 32-4096 objects (log-uniform; clusters per axis U[2,8]), one view
-    each, captured once as a CUDA graph (tgx_frame_graph) and replayed."""
+def bench_batched(local: int, frames: int = 10, tune: bool = True):
+    """Config 3: one batched frame of 64 views of the 512-object scene
+    (resolutions drawn uniformly from 320x240 .. 3840x2160, camera poses
+    uniform in the scene box with random yaw and pitch, seed 3) plus 16
+    scenes of 32-4096 objects (log-uniform; clusters per axis U[2,16], value
+    noise as the 512-object scene), one view each, captured once as a CUDA
+    graph (tgx_frame_graph: every job's sorting passes on their own branch,
+    all tiles in one persistent work-queue launch) and replayed.  The scenes
+    are generated in device memory (tgx_generate_scene_device).  The tile
+    shape, depth buckets, batch and drain are tuned on this very frame."""
     import torch
     import tg_gb300 as tg
+    from tg_gb300.autotune import DEFAULTS, tune_workload
 
     rng = np.random.default_rng(3)
-    ctx = tg.Context(local, tile=(8, 16))
-    jobs, keep = [], []
-    obj = ctx.upload(tg.generate_scene(0, 1, 4, 4, seed=0, bernoulli_p=0.3, translation=(0.0, 0.0, 64.0)))
-    keep.append(obj)
-    views, outs = [], []
+    views = []
     for _ in range(64):
         w, h = RESOLUTIONS[rng.integers(len(RESOLUTIONS))]
-        u = rng.normal(size=3)
-        pos = np.array([0.0, 0.0, 64.0]) + u / np.linalg.norm(u) * rng.uniform(40.0, 160.0)
-        views.append(look_at_view(pos, (0.0, 0.0, 64.0), w, h, 400.0))
-        outs.append(torch.empty(w * h, dtype=torch.int64, device="cuda"))
-    jobs.append((obj, np.concatenate(views), outs))
+        pos = tuple(float(x) for x in rng.uniform(-900.0, 900.0, 3))
+        views.append(tg.make_view(pos, float(rng.uniform(-0.4, 0.4)), float(rng.uniform(0, 2 * np.pi)),
+                                  float(np.pi / 3), int(w), int(h), 0.1, 4096.0))
     n_objects = np.exp(rng.uniform(np.log(32), np.log(4096), 16)).astype(int)
+    side = []
     for k, n in enumerate(n_objects):
-        half = 64.0 * float(n) ** (1.0 / 3.0)
-        sc = ctx.upload(tg.generate_scene(1, int(n), 2, 8, seed=100 + k, noise_period=64.0, noise_threshold=0.5,
-                                          box_min=(-half,) * 3, box_max=(half,) * 3, n_luts=1))
-        keep.append(sc)
+        half = 1024.0 * (float(n) / 512.0) ** (1.0 / 3.0)
         w, h = RESOLUTIONS[rng.integers(len(RESOLUTIONS))]
-        v = tg.make_view((0.0, 0.0, 0.0), 0.0, float(rng.uniform(0, 2 * np.pi)), float(np.pi / 3), w, h, 0.1,
-                         4.0 * half)
-        jobs.append((sc, v, [torch.empty(w * h, dtype=torch.int64, device="cuda")]))
+        v = tg.make_view((0.0, 0.0, 0.0), 0.0, float(rng.uniform(0, 2 * np.pi)), float(np.pi / 3), int(w), int(h),
+                         0.1, 4.0 * half)
+        side.append((int(n), half, v))
+
+    def make_frame(ctx):
+        keep = [ctx.generate_scene(*SCENE_ARGS, **SCENE_KW)]
+        jobs = [(keep[0], np.concatenate(views),
+                 [torch.empty(int(v["width"][0]) * int(v["height"][0]), dtype=torch.int64, device="cuda")
+                  for v in views])]
+        for k, (n, half, v) in enumerate(side):
+            sc = ctx.generate_scene(1, n, 2, 16, 100 + k, noise_period=64.0, noise_threshold=0.5,
+                                    box_min=(-half,) * 3, box_max=(half,) * 3, n_luts=1)
+            keep.append(sc)
+            jobs.append((sc, v, [torch.empty(int(v["width"][0]) * int(v["height"][0]), dtype=torch.int64,
+                                             device="cuda")]))
+        graph = ctx.frame_graph(jobs)
+
+        def close():
+            graph.close()
+            for sc in keep:
+                sc.close()
+        make_frame.jobs, make_frame.graph = jobs, graph
+        return graph.launch, close
+
+    if tune:
+        cfg, tuning = tune_workload(make_frame, local, frames=3)
+    else:
+        cfg, tuning = {"tile": (8, 8), **DEFAULTS}, {}
+    ctx = tg.Context(local, tile=cfg["tile"])
+    ctx.set_vis_tuning(cfg["depth_buckets"], cfg["batch"], cfg["drain"])
+    launch, close = make_frame(ctx)
+    jobs, graph = make_frame.jobs, make_frame.graph
     pixels = sum(int(o.numel()) for _, _, os_ in jobs for o in os_)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    graph = ctx.frame_graph(jobs)
 
     def timed(fn):
         for _ in range(3):
@@ -578,14 +583,16 @@ def bench_batched(local: int, frames: int = 10):
         ms_graph = timed(graph.launch)
         ms_sep = timed(separate)
     err = ctx.device_error()
-    res = {"views": 64 + 16, "scenes": 17, "pixels": pixels, "objects": [1] + [int(n) for n in n_objects],
+    res = {"workload": "64 views of the 512-object scene at random poses and resolutions 320x240..3840x2160 "
+                       "(seed 3) + 16 scenes of 32-4096 objects (clusters per axis U[2,16]), one view each",
+           "views": 64 + 16, "scenes": 17, "pixels": pixels, "objects": [512] + [int(n) for n, _, _ in side],
            "graph_kernels": graph.kernels, "graph_frame_ms": round(ms_graph, 3),
            "graph_grays_per_s": pixels / (ms_graph * 1e-3) / 1e9,
            "separate_calls_frame_ms": round(ms_sep, 3), "separate_grays_per_s": pixels / (ms_sep * 1e-3) / 1e9,
-           "device_status": int(err.code)}
-    graph.close()
-    for sc in keep:
-        sc.close()
+           "tuned": {"tile": f"{cfg['tile'][0]}x{cfg['tile'][1]}", "depth_buckets": cfg["depth_buckets"],
+                     "batch": cfg["batch"], "drain": cfg["drain"]},
+           "autotune_ms": tuning, "device_status": int(err.code)}
+    close()
     ctx.close()
     return res
 
@@ -822,11 +829,14 @@ def main() -> None:
     view = make_view()
     if args.tile == "auto":
         from tg_gb300.autotune import tune_visibility
-        tile, tuning = tune_visibility(scene, view, device=local, use_cache=False)
+        vis_cfg, tuning = tune_visibility(scene, view, device=local, use_cache=False)
     else:
-        tile = tuple(int(x) for x in args.tile.lower().split("x"))
+        vis_cfg = {"tile": tuple(int(x) for x in args.tile.lower().split("x")), "depth_buckets": 16, "batch": 48,
+                   "drain": 32}
         tuning = {}
+    tile = vis_cfg["tile"]
     ctx = tg.Context(local, tile=tile)
+    ctx.set_vis_tuning(vis_cfg["depth_buckets"], vis_cfg["batch"], vis_cfg["drain"])
     sc = ctx.upload(scene)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = torch.empty(W * H, dtype=torch.int64, device="cuda")
@@ -1086,14 +1096,35 @@ def main() -> None:
                 "pairs_per_s": work["pairs"] / (ms * 1e-3), "dda_steps_per_s": work["dda_steps"] / (ms * 1e-3),
                 "rates_over": "ms_per_step (the whole frame)"}
 
+    rooflines = {}
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    if "gi_trace_work" in gi_report:
+        tw = gi_report["gi_trace_work"]
+        tbytes = 4 * tw["dda_steps"] + 48 * tw["rays"]
+        tach = tbytes / (tw["k_trace_queue_ms"] * 1e-3) / 1e9
+        rooflines["k_trace_queue"] = {
+            "bound": "hbm", "achieved": tach, "peak": hbm_peak, "unit": "GB/s", "frac": tach / hbm_peak,
+            "algorithmic_bytes": tbytes, "traffic": None,
+            "bytes_model": "4 B of occupancy per DDA step + 24 B ray read + 24 B hit written per ray, counted by "
+                           "the kernel (tgx_gi_get_work); the SVO working set is L2-resident, so the limiter is "
+                           "latency and divergent issue, not DRAM",
+            "dda_steps_per_s": tw["dda_steps"] / (tw["k_trace_queue_ms"] * 1e-3)}
+    if "mlp" in gi_report:
+        mi, mt = gi_report["mlp"]["inference"], gi_report["mlp"]["training_step"]
+        rooflines["k_mlp_forward_tc"] = {"bound": "tensor", "achieved": mi["tflops"], "peak": bf16, "unit": "TFLOP/s",
+                                         "frac": mi["tflops"] / bf16, "traffic": None,
+                                         "note": "peak of measured (bf16_tflops, burst)"}
+        rooflines["k_mlp_train_tc"] = {"bound": "tensor", "achieved": mt["tflops"], "peak": bf16, "unit": "TFLOP/s",
+                                       "frac": mt["tflops"] / bf16, "traffic": None,
+                                       "note": "training step incl. Adam; peak of measured (bf16_tflops, burst)"}
     line = {
         "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": CONFIG,
         "parallelism": "replicas" if world > 1 else "single-gpu",
-        "tuning": {"tile": f"{tile[0]}x{tile[1]}",
-                   "autotune_ms": {f"{t[0]}x{t[1]}": round(v, 4) for t, v in tuning.items()}},
+        "tuning": {"tile": f"{tile[0]}x{tile[1]}", "depth_buckets": vis_cfg["depth_buckets"],
+                   "batch": vis_cfg["batch"], "drain": vis_cfg["drain"], "autotune_ms": tuning},
         "e2e": {"value": rays * world / (e2e_blocking * 1e-3) / 1e9, "unit": "Grays/s", "h2d_bytes_per_step": 96 + 8,
                 "d2h_bytes_per_step": 8 * rays, "ms_per_step": e2e_blocking,
                 "path": "tgx_vis_render_host, one blocking call per frame: views from the host, the visibility "

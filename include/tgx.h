@@ -279,6 +279,17 @@ typedef struct tgx_vis_stats
 
 tgx_status  tgx_vis_get_stats(tgx_ctx* ctx, tgx_vis_stats* out_stats);
 
+/* Tuning of the visibility pass on this context (0 keeps a default):
+ *   depth_buckets  8, 16 (default) or 32 depth buckets per screen tile: a
+ *                  tile's clusters are sorted into them near to far, so a
+ *                  tile can stop once every pixel is nearer than what is left;
+ *   batch          clusters staged per shared-memory batch, 1..48 (48);
+ *   drain          (pixel, cluster) pairs a warp collects before its lanes
+ *                  run their DDAs, 1..32 (32).
+ * The result never depends on them (bit for bit); tg_gb300/autotune.py picks
+ * them per workload.  No counterpart in the reference. */
+tgx_status  tgx_set_vis_tuning(tgx_ctx* ctx, uint32_t depth_buckets, uint32_t batch, uint32_t drain);
+
 /* Work done by the visibility tile kernel, counted by the kernel itself.  No
  * counterpart in the reference (its GPU work is counted by nobody).  After
  * tgx_vis_count_work(ctx, 1) every tgx_vis_render on the context runs a

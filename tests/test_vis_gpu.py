@@ -257,3 +257,24 @@ def test_work_counting_variant_gives_the_same_buffer_and_consistent_counts(oracl
     assert n_hit <= w["hits"] <= w["ddas"] <= w["dda_steps"] <= 22 * w["ddas"]
     assert 0 < w["dir_setups"] <= w["pairs"] + w["depth_skips"]
     assert w["batches"] > 0
+
+
+@pytest.mark.parametrize("buckets,batch,drain", [(8, 16, 16), (32, 48, 24), (16, 1, 1), (8, 7, 32), (32, 32, 8)])
+def test_tuning_settings_change_no_result(oracle, buckets, batch, drain):
+    """tgx_set_vis_tuning: depth buckets, staged batch size and pairs per DDA
+    round only reschedule the pass; every setting gives the oracle's buffer.
+    The scene puts many clusters on each tile (several batches per tile)."""
+    s = fuzz_scene(71, n_objects=10, box=25.0, max_cpa=5)
+    v = tg.make_view((0.0, 2.0, -60.0), 0.05, float(np.pi), 1.0, 150, 110, 0.1, 256.0)
+    ref = oracle.vis_render(s, v, mode=1)
+    for tile in ((8, 8), (16, 16)):
+        with tg.Context(0, tile=tile) as c:
+            c.set_vis_tuning(buckets, batch, drain)
+            (g,) = render(c, s, v)
+            st = c.vis_stats()
+        assert_same(g, ref)
+    assert st.bin_entries > 4 * st.tiles
+    with tg.Context(0) as c:
+        for bad in ((12, 0, 0), (0, 49, 0), (0, 0, 33)):
+            with pytest.raises(tg.TgxError):
+                c.set_vis_tuning(*bad)

@@ -169,7 +169,7 @@ EXPORTS = [
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
     "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait", "tgx_vis_count_work",
-    "tgx_vis_get_work", "tgx_gi_get_work",
+    "tgx_vis_get_work", "tgx_gi_get_work", "tgx_set_vis_tuning",
 ]
 
 
@@ -217,6 +217,7 @@ def _load() -> C.CDLL:
         "tgx_vis_count_work": (i32, [vp, i32]),
         "tgx_vis_get_work": (i32, [vp, C.POINTER(VisWork)]),
         "tgx_gi_get_work": (i32, [vp, C.POINTER(GiWork)]),
+        "tgx_set_vis_tuning": (i32, [vp, u32, u32, u32]),
         "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "tgx_cache_n_params": (u32, []),
         "tgx_gi_render_cached": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -501,6 +502,11 @@ class Context:
         st = VisStats()
         check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
         return st
+
+    def set_vis_tuning(self, depth_buckets: int = 0, batch: int = 0, drain: int = 0) -> None:
+        """tgx_set_vis_tuning: depth buckets per tile (8/16/32), clusters per staged batch (1..48) and pairs per
+        DDA round (1..32); 0 keeps the default.  Results do not depend on them."""
+        check(lib.tgx_set_vis_tuning(self.handle, depth_buckets, batch, drain), "tgx_set_vis_tuning")
 
     def vis_count_work(self, enable: bool) -> None:
         """tgx_vis_count_work: later renders run the tile kernel's counting variant."""

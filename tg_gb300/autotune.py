@@ -1,15 +1,23 @@
-"""Autotuners: the visibility pass's screen-tile shape, and the SVO
+"""Autotuners: the visibility pass's tile shape and tuning, and the SVO
 traversal's DDA steps per ray-queue round.
 
-The tile shape sets the CTA size of k_vis_tiles (one thread per pixel) and
-the binning granularity.  The tuner renders a few frames of the caller's own
-scene and views with each candidate shape, times them with CUDA events on
-the library stream (tgx_trace_*), and keeps the fastest.
+Visibility: four settings change the speed of a frame but never a result
+(tested bit for bit):
+  - the tile shape: the CTA size of k_vis_tiles (one thread per pixel) and
+    the binning granularity;
+  - the depth buckets per tile (8, 16, 32): how finely a tile's clusters are
+    sorted near to far, so a tile stops once all its pixels are nearer;
+  - the batch: clusters staged per shared-memory batch (16, 32, 48);
+  - the drain: (pixel, cluster) pairs a warp gathers by ballot before its
+    lanes run their DDAs (16, 24, 32), i.e. rays per warp round.
+The tuner runs the caller's own frame (one scene and its views, or a whole
+batched frame graph) with each candidate, times it with CUDA events on the
+library stream and keeps the fastest: first over the tile shapes with the
+other settings at their defaults, then one setting at a time (coordinate
+descent).
 
-The traversal's steps per round set how long a lane of the persistent
-k_trace_queue runs its ray before the warp refills finished lanes from the
-ray queue (fewer: lanes idle less; more: refills cost less).  The tuner times
-a few GI frames of the caller's frame per candidate and keeps the fastest.
+Traversal: how long a lane of the persistent k_trace_queue runs its ray
+before the warp refills finished lanes from the ray queue.
 
 Results are cached per (GPU, workload) in a JSON file next to this module.
 """
@@ -22,6 +30,10 @@ from pathlib import Path
 import numpy as np
 
 CANDIDATES = ((8, 8), (16, 8), (8, 16), (16, 16), (32, 8))
+DEPTH_BUCKETS = (8, 16, 32)
+BATCHES = (16, 32, 48)
+DRAINS = (16, 24, 32)
+DEFAULTS = {"depth_buckets": 16, "batch": 48, "drain": 32}
 CACHE = Path(__file__).resolve().parent / "_tuning.json"
 
 
@@ -30,46 +42,103 @@ def _key(gpu: str, views: np.ndarray, n_clusters: int) -> str:
     return f"{gpu}|{sizes}|{int(np.log2(max(n_clusters, 1)))}"
 
 
-def tune_visibility(scene, views, candidates=CANDIDATES, frames: int = 5, device: int = 0, use_cache: bool = True):
-    """Returns (best_tile, {tile: ms per frame})."""
+def _read_cache() -> dict:
+    if CACHE.exists():
+        try:
+            return json.loads(CACHE.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def _write_cache(cache: dict) -> None:
+    try:
+        tmp = CACHE.with_suffix(".tmp")
+        tmp.write_text(json.dumps(cache, indent=1))
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def _label(cfg: dict) -> str:
+    t = cfg["tile"]
+    return f"{t[0]}x{t[1]}/b{cfg['depth_buckets']}/n{cfg['batch']}/d{cfg['drain']}"
+
+
+def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES, depth_buckets=DEPTH_BUCKETS,
+                  batches=BATCHES, drains=DRAINS):
+    """Coordinate search over the visibility settings for one workload.
+
+    make_frame(ctx) sets up the workload on a fresh context and returns
+    (render, close): render() issues one whole frame on the context's stream,
+    close() frees what make_frame made.  Returns (best config dict, {label:
+    ms per frame})."""
+    import torch
+    import tg_gb300 as tg
+
+    times = {}
+
+    def run(cfg):
+        lab = _label(cfg)
+        if lab in times:
+            return times[lab]
+        with tg.Context(device, tile=cfg["tile"]) as ctx:
+            ctx.set_vis_tuning(cfg["depth_buckets"], cfg["batch"], cfg["drain"])
+            render, close = make_frame(ctx)
+            stream = torch.cuda.ExternalStream(ctx.stream)
+            for _ in range(2):
+                render()
+            ctx.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(frames):
+                render()
+            e1.record(stream)
+            ctx.sync()
+            err = ctx.device_error()
+            if err.code:
+                raise RuntimeError(f"tuning frame failed: device status {err.code} at {err.where}")
+            close()
+        times[lab] = round(e0.elapsed_time(e1) / frames, 4)
+        return times[lab]
+
+    best = {"tile": tiles[0], **DEFAULTS}
+    for t in tiles:
+        cand = {**best, "tile": t}
+        if run(cand) < run(best):
+            best = cand
+    for name, values in (("depth_buckets", depth_buckets), ("batch", batches), ("drain", drains)):
+        for v in values:
+            cand = {**best, name: v}
+            if run(cand) < run(best):
+                best = cand
+    return best, times
+
+
+def tune_visibility(scene, views, frames: int = 5, device: int = 0, use_cache: bool = True, **space):
+    """The visibility settings for rendering `views` of `scene` (a HostScene)
+    with tgx_vis_render.  Returns (best config dict, {label: ms per frame})."""
     import torch
     import tg_gb300 as tg
 
     views = np.ascontiguousarray(views, dtype=tg.VIEW_DTYPE)
     gpu = torch.cuda.get_device_name(device)
-    key = _key(gpu, views, scene.n_clusters)
-    cache = {}
-    if use_cache and CACHE.exists():
-        try:
-            cache = json.loads(CACHE.read_text())
-        except ValueError:
-            cache = {}
-        if key in cache:
-            e = cache[key]
-            return tuple(e["best"]), {tuple(map(int, k.split("x"))): v for k, v in e["ms"].items()}
+    key = "vis2|" + _key(gpu, views, scene.n_clusters)
+    cache = _read_cache() if use_cache else {}
+    if key in cache:
+        e = cache[key]
+        return {**e["best"], "tile": tuple(e["best"]["tile"])}, e["ms"]
     outs = [torch.empty(int(v["width"]) * int(v["height"]), dtype=torch.int64, device=f"cuda:{device}") for v in views]
-    results = {}
-    for tile in candidates:
-        with tg.Context(device, tile=tile) as ctx:
-            sc = ctx.upload(scene)
-            for _ in range(2):
-                ctx.vis_render(sc, views, outs)
-            ctx.sync()
-            ctx.trace_reset()
-            ctx.trace(True)
-            for _ in range(frames):
-                ctx.vis_render(sc, views, outs)
-            tr = ctx.trace_read()
-            ctx.trace(False)
-            sc.close()
-        results[tile] = sum(ms for ms, _ in tr.values()) / frames
-    best = min(results, key=results.get)
+
+    def make_frame(ctx):
+        sc = ctx.upload(scene)
+        return (lambda: ctx.vis_render(sc, views, outs)), sc.close
+
+    best, times = tune_workload(make_frame, device, frames, **space)
     if use_cache:
-        cache[key] = {"best": list(best), "ms": {f"{t[0]}x{t[1]}": v for t, v in results.items()}}
-        tmp = CACHE.with_suffix(".tmp")
-        tmp.write_text(json.dumps(cache, indent=1))
-        os.replace(tmp, CACHE)
-    return best, results
+        cache[key] = {"best": {**best, "tile": list(best["tile"])}, "ms": times}
+        _write_cache(cache)
+    return best, times
 
 
 TRACE_CANDIDATES = (2, 4, 8, 16)

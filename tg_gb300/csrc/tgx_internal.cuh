@@ -133,6 +133,9 @@ struct tgx_ctx
     DevBuf vis_work;       // work counters of the tile kernel's counting variant
     uint32_t vis_tile_ctas = 0;        // resident CTAs of the persistent (batched-frame) tile kernel
     bool   vis_count_work = false;
+    uint32_t vis_bshift = 1;           // depth buckets per tile: 32 >> vis_bshift
+    uint32_t vis_batch = 48;           // entries per staged batch of the tile kernel
+    uint32_t vis_drain = 32;           // live pairs a warp collects before running their DDAs
     uint32_t vis_last_tiles = 0;
     uint64_t vis_last_pairs = 0;
     void*  h_vis_counters = nullptr;   // pinned copy of the last frame's counters

@@ -48,7 +48,7 @@ namespace {
 
 constexpr uint32_t kCluster = 8;
 constexpr uint32_t kMaxDdaSteps = 64;      // the 8^3 DDA needs at most 22
-constexpr uint32_t kBuckets = 16;          // depth buckets per tile
+constexpr uint32_t kMaxBuckets = 32;       // depth buckets per tile at the finest setting (half an octave each)
 
 struct alignas(16) VisRecord
 {
@@ -83,11 +83,23 @@ enum Work { W_PAIRS = 0, W_DEPTH_SKIPS, W_DIR_SETUPS, W_SLAB_MISSES, W_SURE_HITS
 constexpr uint32_t kOrderClasses = 32;     // tiles are launched heaviest class (log2 of bin count) first
 
 // bucket of a depth key: one per power of two of the 24-bit depth, keys < 512 share bucket 0
-__device__ __forceinline__ uint32_t depth_bucket(uint32_t key)
+// Depth buckets of a tile's entries: key = the 24-bit depth field's lower
+// bound.  Keys below 512 share the first bucket; above, every half octave of
+// the key is a fine bucket (0..31), and a frame uses 32 >> bshift buckets
+// (bshift 0, 1 or 2: 32, 16 or 8 buckets, i.e. half, one or two octaves each).
+__device__ __forceinline__ uint32_t depth_bucket(uint32_t key, uint32_t bshift)
 {
-    return key < 512u ? 0u : min(kBuckets - 1u, (31u - (uint32_t)__clz(key)) - 8u);
+    if (key < 512u) return 0u;
+    const uint32_t l = 31u - (uint32_t)__clz(key);   // 9..23
+    const uint32_t fine = 2u * (l - 8u) + ((key >> (l - 1u)) & 1u);
+    return fine >> bshift;
 }
-__device__ __forceinline__ uint32_t bucket_lo(uint32_t b) { return b == 0u ? 0u : (1u << (b + 8u)); }
+// the smallest key of bucket b
+__device__ __forceinline__ uint32_t bucket_lo(uint32_t b, uint32_t bshift)
+{
+    const uint32_t f = b << bshift;
+    return f == 0u ? 0u : (f & 1u) ? (3u << ((f >> 1) + 7u)) : (1u << ((f >> 1) + 8u));
+}
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
 {
@@ -258,7 +270,8 @@ __global__ void __launch_bounds__(256) k_vis_count(VisRecord* __restrict__ recor
                                                   const uint32_t* __restrict__ counters, uint32_t record_capacity,
                                                   const tgx_object* __restrict__ objects,
                                                   const ViewConst* __restrict__ views,
-                                                  uint32_t* __restrict__ bucket_cnt, uint32_t n_tiles)
+                                                  uint32_t* __restrict__ bucket_cnt, uint32_t n_tiles,
+                                                  uint32_t bshift)
 {
     pdl_wait();
     pdl_trigger();
@@ -292,7 +305,7 @@ __global__ void __launch_bounds__(256) k_vis_count(VisRecord* __restrict__ recor
         const uint2 r = rects[i];
         const uint32_t view = records[i].view;
         const ViewConst& vc = views[view];
-        const uint32_t b = depth_bucket(records[i].d24_lb);
+        const uint32_t b = depth_bucket(records[i].d24_lb, bshift);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
         for (uint32_t k = lane; k < cnt; k += 16) {
@@ -312,6 +325,7 @@ constexpr uint32_t kScanTiles = 256;   // tiles per CTA of the prefix and finali
 
 __device__ __forceinline__ uint32_t tile_class(uint32_t total) { return total ? 32u - __clz(total) : 0u; }
 
+template <uint32_t kBuckets>
 __global__ void __launch_bounds__(kScanTiles) k_vis_prefix(uint32_t* __restrict__ bucket_cnt,
                                                           uint32_t* __restrict__ bucket_off,
                                                           uint32_t* __restrict__ tile_total, uint32_t n_tiles,
@@ -579,7 +593,7 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
                                                      const uint32_t* __restrict__ bucket_off,
                                                      uint32_t* __restrict__ cursor, TileEntry* __restrict__ entries,
                                                      const uint32_t* __restrict__ bits,
-                                                     uint32_t n_tiles, uint32_t bin_capacity,
+                                                     uint32_t n_tiles, uint32_t bin_capacity, uint32_t bshift,
                                                      tgx_dev_status* __restrict__ status)
 {
     pdl_wait();
@@ -598,7 +612,7 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
         else if (lane >= 8u && lane < kEntryWords) word = bits[(uint64_t)rw[3] * 16u + (lane - 8u)];
         const VisRecord& rec = records[i];
         const ViewConst& vc = views[rec.view];
-        const uint32_t b = depth_bucket(rec.d24_lb);
+        const uint32_t b = depth_bucket(rec.d24_lb, bshift);
         const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
         const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
         for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
@@ -778,6 +792,9 @@ struct TileJob
     uint32_t n_views, n_tiles;
     uint32_t first;              // the job's first item in a multi-job work queue
     unsigned long long* work;    // W_COUNT work counters (counting variant of the tile kernel only)
+    uint32_t bshift;             // depth buckets: 32 >> bshift
+    uint32_t batch;              // entries per staged batch (1..kBatch)
+    uint32_t drain;              // live pairs a warp collects before its lanes run their DDAs (1..32)
     uint32_t extra_tx;           // bytes the first batch's barrier expects beyond its copies: 0, or 64
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
 };
@@ -880,7 +897,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
     const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
     if (threadIdx.x == 0) {
-        if (!scan_all && end > begin) stage_entries(sm, J.entries + begin, min(kBatch, end - begin), J.extra_tx);
+        if (!scan_all && end > begin) stage_entries(sm, J.entries + begin, min(J.batch, end - begin), J.extra_tx);
         uint32_t v = 0;
         while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
         sm.view() = v;
@@ -899,6 +916,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     float* const qf = (float*)q;
     const float far_plane = vc.far_plane;
     const TileEntry* const E = sm.stage();
+    const uint32_t drain = J.drain;
 
     // pixel ray in world space (visibility.frag:29-33,68; mix per GLSL 8.3)
     const float fx = xdiv(xadd((float)px, 0.5f), (float)vc.width);
@@ -919,7 +937,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     for (uint32_t base = begin; base < end;) {
         uint32_t n;
         if (!scan_all) {
-            n = min(kBatch, end - base);
+            n = min(J.batch, end - base);
             if (base != begin) {
                 // the previous batch is fully consumed; after a lost copy nobody stages another
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -935,7 +953,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
             __syncthreads();
             if (threadIdx.x == 0) sm.n() = 0;
             __syncthreads();
-            const uint32_t m = min(kBatch, end - base);
+            const uint32_t m = min(J.batch, end - base);
             for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
                 const uint32_t r = base + k;
                 const uint2 qr = J.rects[r];
@@ -998,7 +1016,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
                 }
                 qn += __popc(m);
                 k++;
-                if (qn < 32u && k < n) continue;
+                if (qn < drain && k < n) continue;
             }
             if (qn == 0u) break;   // k == n and nothing pending
             // one pair per lane: the exact test and the DDA; the word goes to its pixel
@@ -1021,7 +1039,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
         }
         // every pixel already nearer than the rest of the (bucket-sorted) entries: the tile is done
         if (!scan_all && base < end) {
-            const uint32_t lo = bucket_lo(depth_bucket(E[n - 1].d24_lb));
+            const uint32_t lo = bucket_lo(depth_bucket(E[n - 1].d24_lb, J.bshift), J.bshift);
             if (__syncthreads_and(!valid || best_d24 < lo)) break;
         }
     }
@@ -1190,17 +1208,18 @@ struct VisScratch
 };
 
 // bytes of the tile-sized part of the scratch
+// (the bucket arrays are sized for the finest setting, kMaxBuckets per tile)
 static size_t vis_tile_bytes(uint32_t n_tiles)
 {
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
-    return (size_t)n_tiles * kBuckets * 4 * 2 + (size_t)n_tiles * 4 + (size_t)n_scan_ctas * (1 + kOrderClasses) * 4;
+    return (size_t)n_tiles * kMaxBuckets * 4 * 2 + (size_t)n_tiles * 4 + (size_t)n_scan_ctas * (1 + kOrderClasses) * 4;
 }
 
 static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_off, uint32_t n_tiles)
 {
     w.bucket_cnt = tile_cnt;
-    w.bucket_off = w.bucket_cnt + (size_t)n_tiles * kBuckets;
-    w.tile_total = w.bucket_off + (size_t)n_tiles * kBuckets;
+    w.bucket_off = w.bucket_cnt + (size_t)n_tiles * kMaxBuckets;
+    w.tile_total = w.bucket_off + (size_t)n_tiles * kMaxBuckets;
     w.cta_aux = w.tile_total + n_tiles;
     w.tile_off = tile_off;
     w.tile_order = w.tile_off + (n_tiles + 1);
@@ -1208,10 +1227,13 @@ static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_of
 
 enum VisPhase { VIS_ALL = 0, VIS_TO_SCAN = 1, VIS_FROM_BINS = 2, VIS_NO_TILES = 3 };
 
-static TileJob tile_job(const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs, uint32_t n_views,
-                        uint32_t n_tiles, const VisScratch& w)
+static TileJob tile_job(const tgx_ctx* c, const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs,
+                        uint32_t n_views, uint32_t n_tiles, const VisScratch& w)
 {
     TileJob J;
+    J.bshift = c->vis_bshift;
+    J.batch = c->vis_batch;
+    J.drain = c->vis_drain;
     J.records = w.records;
     J.rects = w.rects;
     J.entries = w.entries;
@@ -1238,17 +1260,26 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
     const uint32_t warp_grid = (uint32_t)c->num_sms * 8;
+    const uint32_t bshift = c->vis_bshift;
     if (phase != VIS_FROM_BINS) {
         TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
         const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
         TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
                    s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-                   w.records, w.rects, w.rec_cap, w.counters, w.bucket_cnt, n_tiles * kBuckets, c->d_status);
+                   w.records, w.rects, w.rec_cap, w.counters, w.bucket_cnt, n_tiles * (kMaxBuckets >> bshift),
+                   c->d_status);
         // each later pass is a programmatic dependent of the one before
         TGX_LAUNCH_PDL(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, w.rec_cap,
-                       s->d_objects, d_vc, w.bucket_cnt, n_tiles);
-        TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix, w.bucket_cnt, w.bucket_off,
-                       w.tile_total, n_tiles, w.cta_aux);
+                       s->d_objects, d_vc, w.bucket_cnt, n_tiles, bshift);
+        if (bshift == 0)
+            TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix<32>, w.bucket_cnt, w.bucket_off,
+                           w.tile_total, n_tiles, w.cta_aux);
+        else if (bshift == 1)
+            TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix<16>, w.bucket_cnt, w.bucket_off,
+                           w.tile_total, n_tiles, w.cta_aux);
+        else
+            TGX_LAUNCH_PDL(c, TR_VIS_PREFIX, n_scan_ctas, kScanTiles, 0, k_vis_prefix<8>, w.bucket_cnt, w.bucket_off,
+                           w.tile_total, n_tiles, w.cta_aux);
         if (n_scan_ctas <= kDirectGroups) {
             TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize_direct, w.tile_total, n_tiles,
                            w.cta_aux, w.tile_off, w.tile_order, w.bin_capacity, w.counters);
@@ -1262,9 +1293,9 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     if (phase == VIS_TO_SCAN) return TGX_OK;
     TGX_LAUNCH_PDL(c, TR_VIS_BIN, warp_grid, 256, 0, k_vis_bin_fill,
                    w.records, w.rects, w.counters, d_vc, w.tile_off, w.bucket_off, w.bucket_cnt, w.entries,
-                   s->d_bits, n_tiles, w.bin_capacity, c->d_status);
+                   s->d_bits, n_tiles, w.bin_capacity, bshift, c->d_status);
     if (phase == VIS_NO_TILES) return TGX_OK;
-    TileJob J = tile_job(s, d_vc, d_outs, n_views, n_tiles, w);
+    TileJob J = tile_job(c, s, d_vc, d_outs, n_views, n_tiles, w);
     if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
     const uint32_t threads = c->tile_w * c->tile_h, smem = tile_smem_bytes(threads);
     if (c->vis_count_work) {
@@ -1537,7 +1568,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
         const ViewConst* d_vc = (const ViewConst*)(base + job.table_off);
         unsigned long long* const* d_outs = (unsigned long long* const*)(base + job.table_off + job.ptr_off);
-        tjobs[j] = tile_job(job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, w);
+        tjobs[j] = tile_job(c, job.scene, d_vc, d_outs, (uint32_t)job.views.size(), job.n_tiles, w);
         tjobs[j].first = j ? tjobs[j - 1].first + g->jobs[j - 1].n_tiles : 0u;
     }
     TileJob* d_jobs = (TileJob*)(base + jobs_off);
@@ -1780,6 +1811,21 @@ extern "C" tgx_status tgx_vis_get_stats(tgx_ctx* c, tgx_vis_stats* out)
     return TGX_OK;
 }
 
+extern "C" tgx_status tgx_set_vis_tuning(tgx_ctx* c, uint32_t depth_buckets, uint32_t batch, uint32_t drain)
+{
+    if (!c) return TGX_ERR_INVALID_ARGUMENT;
+    const uint32_t nb = depth_buckets ? depth_buckets : 16u, bt = batch ? batch : kBatch, dr = drain ? drain : 32u;
+    if ((nb != 8 && nb != 16 && nb != 32) || bt > kBatch || dr > 32) {
+        tgx_set_error("tgx_set_vis_tuning: depth buckets %u (8, 16 or 32), batch %u (1..%u), drain %u (1..32)", nb, bt,
+                      kBatch, dr);
+        return TGX_ERR_INVALID_ARGUMENT;
+    }
+    c->vis_bshift = nb == 32 ? 0u : nb == 16 ? 1u : 2u;
+    c->vis_batch = bt;
+    c->vis_drain = dr;
+    return TGX_OK;
+}
+
 extern "C" tgx_status tgx_vis_count_work(tgx_ctx* c, int enable)
 {
     if (!c) return TGX_ERR_INVALID_ARGUMENT;
@@ -1827,8 +1873,9 @@ constexpr size_t kNaInvRot = kNaViews + na_align(sizeof(ViewConst) + 16);
 constexpr size_t kNaRecords = kNaInvRot + na_align((size_t)kNaMaxObjects * 9 * 4);
 constexpr size_t kNaRects = kNaRecords + na_align((size_t)kNaMaxClusterPointers * sizeof(VisRecord));
 constexpr size_t kNaBucketCnt = kNaRects + na_align((size_t)kNaMaxClusterPointers * 8);
-constexpr size_t kNaBucketOff = kNaBucketCnt + na_align((size_t)kNaMaxTiles * kBuckets * 4);
-constexpr size_t kNaTileTotal = kNaBucketOff + na_align((size_t)kNaMaxTiles * kBuckets * 4);
+constexpr uint32_t kNaBuckets = 16;          // depth buckets per tile (bucket shift 1)
+constexpr size_t kNaBucketOff = kNaBucketCnt + na_align((size_t)kNaMaxTiles * kNaBuckets * 4);
+constexpr size_t kNaTileTotal = kNaBucketOff + na_align((size_t)kNaMaxTiles * kNaBuckets * 4);
 constexpr size_t kNaScanAux = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
 constexpr size_t kNaTileOff = kNaScanAux + na_align(((size_t)kNaMaxTiles / kScanTiles + 1) * (1 + kOrderClasses) * 4);
 constexpr size_t kNaTileOrder = kNaTileOff + na_align(((size_t)kNaMaxTiles + 1) * 4);
@@ -1970,11 +2017,11 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
               counters, status, d_objects, n_objects, inv_rot);
     NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
               d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
-              kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kBuckets, status);
+              kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kNaBuckets, status);
     NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, kNaMaxClusterPointers, d_objects, d_vc, bucket_cnt,
-              n_tiles);
+              n_tiles, 1u);
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
-    NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
+    NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix<kNaBuckets>, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
     if (n_scan_ctas <= kDirectGroups) {
         NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize_direct, tile_total, n_tiles, cta_aux, tile_off, tile_order,
                   kNaBins, counters);
@@ -1983,7 +2030,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
         NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
     }
     NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, entries,
-              d_voxel_bits, n_tiles, kNaBins, status);
+              d_voxel_bits, n_tiles, kNaBins, 1u, status);
     TileJob J;
     J.records = records;
     J.rects = rects;
@@ -2000,6 +2047,9 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
+    J.bshift = 1;
+    J.batch = kBatch;
+    J.drain = 32;
     k_vis_tiles<256, 5><<<n_tiles, kNaTile * kNaTile, tile_smem_bytes(kNaTile * kNaTile), st>>>(J, status);
     if (const cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         tgx_set_error("tgx_vis_render_noalloc: launch of k_vis_tiles failed: %s", cudaGetErrorString(le));
