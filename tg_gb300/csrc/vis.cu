@@ -19,7 +19,7 @@
 //                           first); then per group: tile offsets and order.
 //                           Up to 512 groups, k_vis_finalize_direct does both:
 //                           each CTA reads all groups' sums and histograms.
-//   5. k_vis_bin_fill       a warp per record: writes it, with its cluster's
+//   5. k_vis_bin_fill       a half-warp per record: writes it, with its cluster's
 //                           64-byte bitmask, as a 96-byte entry into each of its
 //                           (tile, bucket) bins, so every tile's entries are
 //                           contiguous and run near to far.
@@ -581,8 +581,9 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
 }
 
 // ---------------------------------------------------------------------------
-// 5. bin fill: a warp per record; its lanes take the record's tiles' slots
-//    (32 at a time), then 24 lanes write the 96-byte entry into each slot
+// 5. bin fill: a half-warp per record; its lanes take the record's tiles'
+//    slots (16 at a time), then 12 lanes write the 96-byte entry into each
+//    slot with 8-byte stores
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restrict__ records,
@@ -599,34 +600,52 @@ __global__ void __launch_bounds__(256) k_vis_bin_fill(const VisRecord* __restric
     pdl_wait();
     pdl_trigger();
     if (counters[C_OVERFLOW]) return;   // the tile kernel scans all records instead
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 15u;
+    const uint32_t src0 = threadIdx.x & 16u;   // this half-warp's first lane in the warp
     const uint32_t n = counters[C_RECORDS];
-    uint32_t* const ew = reinterpret_cast<uint32_t*>(entries);
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
-        const uint2 r = rects[i];
-        const uint32_t* rw = reinterpret_cast<const uint32_t*>(records + i);
-        // entry word `lane`: ox oy oz pointer object lb 0 0 | 16 bitmask words
-        uint32_t word = 0u;
-        if (lane < 3u) word = rw[lane];
-        else if (lane < 6u) word = rw[lane + 1u];
-        else if (lane >= 8u && lane < kEntryWords) word = bits[(uint64_t)rw[3] * 16u + (lane - 8u)];
-        const VisRecord& rec = records[i];
-        const ViewConst& vc = views[rec.view];
-        const uint32_t b = depth_bucket(rec.d24_lb, bshift);
-        const uint32_t tx0 = r.x & 0xffffu, ty0 = r.x >> 16, tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
-        const uint32_t w = tx1 - tx0 + 1, cnt = w * (ty1 - ty0 + 1);
-        for (uint32_t k0 = 0; k0 < cnt; k0 += 32u) {
+    uint2* const ew = reinterpret_cast<uint2*>(entries);
+    const uint32_t stride = (gridDim.x * blockDim.x) >> 4;
+    // every half-warp runs the same number of iterations, so the shuffles see full warps
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t it = 0; it < rounds; it++) {
+        const uint32_t i = ((blockIdx.x * blockDim.x + threadIdx.x) >> 4) + it * stride;
+        const bool have = i < n;
+        // entry words 2 lane, 2 lane + 1: ox oy | oz pointer | object lb | 0 0 | bitmask (16 words)
+        uint2 word = make_uint2(0u, 0u);
+        uint32_t cnt = 0, w = 1, tx0 = 0, ty0 = 0, b = 0, tile_base = 0, tiles_x = 0;
+        if (have) {
+            const uint32_t* rw = reinterpret_cast<const uint32_t*>(records + i);
+            if (lane == 0) word = make_uint2(rw[0], rw[1]);
+            else if (lane == 1) word = make_uint2(rw[2], rw[4]);
+            else if (lane == 2) word = make_uint2(rw[5], rw[6]);
+            else if (lane >= 4 && lane < 12) {
+                const uint2* bw = reinterpret_cast<const uint2*>(bits + (uint64_t)rw[3] * 16u);
+                word = bw[lane - 4];
+            }
+            const uint2 r = rects[i];
+            const VisRecord& rec = records[i];
+            const ViewConst& vc = views[rec.view];
+            b = depth_bucket(rec.d24_lb, bshift);
+            tx0 = r.x & 0xffffu; ty0 = r.x >> 16;
+            const uint32_t tx1 = r.y & 0xffffu, ty1 = r.y >> 16;
+            w = tx1 - tx0 + 1;
+            cnt = w * (ty1 - ty0 + 1);
+            tile_base = vc.tile_base;
+            tiles_x = vc.tiles_x;
+        }
+        // the longer record of the warp's two sets the trip count
+        const uint32_t cnt_max = max(cnt, __shfl_xor_sync(0xffffffffu, cnt, 16));
+        for (uint32_t k0 = 0; k0 < cnt_max; k0 += 16u) {
             uint32_t pos = 0xffffffffu;
             const uint32_t k = k0 + lane;
             if (k < cnt) {
-                const uint32_t t = vc.tile_base + (ty0 + k / w) * vc.tiles_x + tx0 + k % w;
+                const uint32_t t = tile_base + (ty0 + k / w) * tiles_x + tx0 + k % w;
                 pos = tile_off[t] + bucket_off[b * n_tiles + t] + atomicAdd(&cursor[b * n_tiles + t], 1u);
                 if (pos >= bin_capacity) { dev_error(status, TGX_ERR_DEVICE_FAULT, 3, pos); pos = 0xffffffffu; }
             }
-            const uint32_t m = min(32u, cnt - k0);
-            for (uint32_t q = 0; q < m; q++) {
-                const uint32_t pq = __shfl_sync(0xffffffffu, pos, q);
-                if (pq != 0xffffffffu && lane < kEntryWords) ew[(uint64_t)pq * kEntryWords + lane] = word;
+            for (uint32_t q = 0; q < 16u; q++) {
+                const uint32_t pq = __shfl_sync(0xffffffffu, pos, src0 + q);
+                if (pq != 0xffffffffu && lane < 12u) ew[(uint64_t)pq * 12u + lane] = word;
             }
         }
     }
