@@ -352,6 +352,63 @@ __global__ void __launch_bounds__(256) k_svo_pair_fill(const SvoPair* __restrict
 // (cluster, block) pairs; every set voxel goes into the CTA's shared image of
 // the block (and the material codes' maximum into its shared material grid),
 // then the block is written out whole, coalesced, with no global atomics.
+// A pair's cluster-space transform and its voxel range in the block: the
+// trimmed range of tg__construct_leaf_node (tg_sparse_voxel_octree.c:180-226).
+struct PairBox
+{
+    dv3 pmin, pext;
+    float cs2ws[16];
+    uint32_t x0, y0, z0, x1, y1, z1;
+    uint32_t ci, rel;
+    const tgx_object* od;
+};
+
+__device__ __forceinline__ void pair_box(const tgx_object* __restrict__ objects,
+                                         const uint32_t* __restrict__ cluster_pointers,
+                                         const uint32_t* __restrict__ c2o, const SvoPair& pr, float mnx, float mny,
+                                         float mnz, uint32_t B, PairBox& pb)
+{
+    const uint32_t cp = pr.cluster_pointer;
+    pb.ci = cluster_pointers[cp];
+    pb.od = &objects[c2o[pb.ci]];
+    pb.rel = cp - pb.od->first_cluster_pointer;
+    const uint32_t bx = pr.block % B, by = (pr.block / B) % B, bz = pr.block / (B * B);
+    // block box: same values the recursion produces (exact powers of two)
+    pb.pmin = dv3{xadd(mnx, (float)(bx * kBlockSide)), xadd(mny, (float)(by * kBlockSide)),
+                  xadd(mnz, (float)(bz * kBlockSide))};
+    const dv3 pmax = dv3{xadd(pb.pmin.x, 32.0f), xadd(pb.pmin.y, 32.0f), xadd(pb.pmin.z, 32.0f)};
+    pb.pext = sub3(pmax, pb.pmin);
+    svo_cs2ws(*pb.od, pb.rel, pb.cs2ws);
+    dv3 cw[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        cw[k] = mulv4p(pb.cs2ws, (k & 1) ? 8.0f : 0.0f, (k & 2) ? 8.0f : 0.0f, (k & 4) ? 8.0f : 0.0f);
+    // :180-194 -- note corner 2 twice, corner 3 never
+    auto vmin = [](dv3 p, dv3 q) { return dv3{p.x < q.x ? p.x : q.x, p.y < q.y ? p.y : q.y, p.z < q.z ? p.z : q.z}; };
+    auto vmax = [](dv3 p, dv3 q) { return dv3{p.x > q.x ? p.x : q.x, p.y > q.y ? p.y : q.y, p.z > q.z ? p.z : q.z}; };
+    const dv3 min_c = vmin(vmin(vmin(cw[0], cw[1]), vmin(cw[2], cw[2])), vmin(vmin(cw[4], cw[6]), vmin(cw[5], cw[7])));
+    const dv3 max_c = vmax(vmax(vmax(cw[0], cw[1]), vmax(cw[2], cw[2])), vmax(vmax(cw[4], cw[6]), vmax(cw[5], cw[7])));
+    const dv3 fmin_c = dv3{floorf(min_c.x), floorf(min_c.y), floorf(min_c.z)};
+    const dv3 cmax_c = dv3{ceilf(max_c.x), ceilf(max_c.y), ceilf(max_c.z)};
+    const dv3 tmin = vmax(pb.pmin, fmin_c);
+    const dv3 tmax = vmin(pmax, cmax_c);
+    pb.x0 = trim_u32(xsub(tmin.x, pb.pmin.x)); pb.y0 = trim_u32(xsub(tmin.y, pb.pmin.y)); pb.z0 = trim_u32(xsub(tmin.z, pb.pmin.z));
+    pb.x1 = trim_u32(xsub(tmax.x, pb.pmin.x)); pb.y1 = trim_u32(xsub(tmax.y, pb.pmin.y)); pb.z1 = trim_u32(xsub(tmax.z, pb.pmin.z));
+}
+
+__device__ __forceinline__ uint32_t pair_voxels(const PairBox& b)
+{
+    return (b.x0 >= b.x1 || b.y0 >= b.y1 || b.z0 >= b.z1) ? 0u : (b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+}
+
+// One CTA per block slot.  The block's pairs are taken 32 at a time: their
+// trimmed voxel counts are measured first (a lane per pair) and sorted by a
+// warp bitonic sort, then warp w voxelises the chunk's pairs of rank w and
+// 31 - w (the heaviest with the lightest), so the warps' shares of voxels are
+// close and the CTA's final barrier waits less.  Within a pair, lanes walk
+// its voxels; each voxel is the reference's corner lerp and bit fetch.  The
+// block image and the material codes are merged with atomicOr / a 16-bit max
+// in shared memory, so the order of the pairs changes no bit.
 template <bool kMat>
 __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
@@ -359,8 +416,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const uint32_t* __restrict__ off, uint32_t* __restrict__ pool, const uint8_t* __restrict__ material,
     uint16_t* __restrict__ mat_pool, float mnx, float mny, float mnz, uint32_t B)
 {
+    constexpr uint32_t kOrderCap = 32 * kWarpsPerVoxCta * 2;   // pairs ordered per round
     extern __shared__ __align__(16) uint32_t s_blk[];   // 1024 bit words, then 16384 words of u16 codes
     __shared__ uint32_t s_cw[kWarpsPerVoxCta][16];       // each warp's current cluster bits
+    __shared__ uint16_t s_order[kOrderCap];              // per chunk of 32: pair offsets, heaviest first
     uint32_t* img = s_blk;
     uint32_t* smat = s_blk + kBlockWords;
     const uint32_t slot = blockIdx.x;
@@ -370,92 +429,107 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const uint32_t words = kBlockWords + (kMat ? 16384u : 0u);
     for (uint32_t k = threadIdx.x; k < words / 4u; k += blockDim.x)
         reinterpret_cast<uint4*>(s_blk)[k] = make_uint4(0u, 0u, 0u, 0u);
-    __syncthreads();
-    for (uint32_t pi = pb + wid; pi < pe; pi += kWarpsPerVoxCta) {
-        const SvoPair pr = sorted[pi];
-        const uint32_t cp = pr.cluster_pointer;
-        const uint32_t ci = cluster_pointers[cp];
-        const tgx_object& od = objects[c2o[ci]];
-        const uint32_t rel = cp - od.first_cluster_pointer;
-        const uint32_t bx = pr.block % B, by = (pr.block / B) % B, bz = pr.block / (B * B);
-        // block box: same values the recursion produces (exact powers of two)
-        const dv3 pmin = dv3{xadd(mnx, (float)(bx * kBlockSide)), xadd(mny, (float)(by * kBlockSide)),
-                             xadd(mnz, (float)(bz * kBlockSide))};
-        const dv3 pmax = dv3{xadd(pmin.x, 32.0f), xadd(pmin.y, 32.0f), xadd(pmin.z, 32.0f)};
-        const dv3 pext = sub3(pmax, pmin);
-
-        float cs2ws[16], ws2cs[16];
-        svo_cs2ws(od, rel, cs2ws);
-        dv3 cw[8];
+    for (uint32_t r0 = pb; r0 < pe; r0 += kOrderCap) {
+        const uint32_t np = min(kOrderCap, pe - r0);
+        const uint32_t n_chunks = (np + 31u) / 32u;
+        __syncthreads();   // the previous round's order is consumed (and the image is cleared)
+        for (uint32_t ch = wid; ch < n_chunks; ch += kWarpsPerVoxCta) {
+            const uint32_t i = ch * 32u + lane;
+            // key: voxel count (pairs past the end sort last); value: pair offset in the round
+            int32_t key = -1;
+            uint32_t idx = i;
+            if (i < np) {
+                PairBox bx;
+                pair_box(objects, cluster_pointers, c2o, sorted[r0 + i], mnx, mny, mnz, B, bx);
+                key = (int32_t)pair_voxels(bx);
+            }
+            // ascending bitonic sort over the warp's 32 lanes
 #pragma unroll
-        for (int k = 0; k < 8; k++)
-            cw[k] = mulv4p(cs2ws, (k & 1) ? 8.0f : 0.0f, (k & 2) ? 8.0f : 0.0f, (k & 4) ? 8.0f : 0.0f);
-        // :180-194 -- note corner 2 twice, corner 3 never
-        auto vmin = [](dv3 p, dv3 q) { return dv3{p.x < q.x ? p.x : q.x, p.y < q.y ? p.y : q.y, p.z < q.z ? p.z : q.z}; };
-        auto vmax = [](dv3 p, dv3 q) { return dv3{p.x > q.x ? p.x : q.x, p.y > q.y ? p.y : q.y, p.z > q.z ? p.z : q.z}; };
-        const dv3 min_c = vmin(vmin(vmin(cw[0], cw[1]), vmin(cw[2], cw[2])), vmin(vmin(cw[4], cw[6]), vmin(cw[5], cw[7])));
-        const dv3 max_c = vmax(vmax(vmax(cw[0], cw[1]), vmax(cw[2], cw[2])), vmax(vmax(cw[4], cw[6]), vmax(cw[5], cw[7])));
-        const dv3 fmin_c = dv3{floorf(min_c.x), floorf(min_c.y), floorf(min_c.z)};
-        const dv3 cmax_c = dv3{ceilf(max_c.x), ceilf(max_c.y), ceilf(max_c.z)};
-        dm4_inverse(cs2ws, ws2cs);
-        dv3 bc[8];
+            for (uint32_t k = 2; k <= 32; k <<= 1) {
 #pragma unroll
-        for (int k = 0; k < 8; k++)
-            bc[k] = mulv4p(ws2cs, (k & 1) ? pmax.x : pmin.x, (k & 2) ? pmax.y : pmin.y, (k & 4) ? pmax.z : pmin.z);
-        const dv3 tmin = vmax(pmin, fmin_c);
-        const dv3 tmax = vmin(pmax, cmax_c);
-        const uint32_t x0 = trim_u32(xsub(tmin.x, pmin.x)), y0 = trim_u32(xsub(tmin.y, pmin.y)), z0 = trim_u32(xsub(tmin.z, pmin.z));
-        const uint32_t x1 = trim_u32(xsub(tmax.x, pmin.x)), y1 = trim_u32(xsub(tmax.y, pmin.y)), z1 = trim_u32(xsub(tmax.z, pmin.z));
-        if (x0 >= x1 || y0 >= y1 || z0 >= z1) continue;
-
-        const uint32_t nx = x1 - x0, ny = y1 - y0, nz = z1 - z0;
-        const uint32_t total = nx * ny * nz;
-        // the block side is exactly 32 unless min is so large that min + extent rounds
-        const bool p32 = pext.x == 32.0f && pext.y == 32.0f && pext.z == 32.0f;
-        // the cluster's 16 bit words, one shared-memory lookup per voxel
-        __syncwarp();
-        if (lane < 16) s_cw[wid][lane] = bits[(uint64_t)ci * 16u + lane];
-        __syncwarp();
-        // t -> (ix, iy, iz) without integer division: t < 2^15 and nx, ny <= 32,
-        // so (t + 0.5) / n lies at least 0.5 / n from an integer while the
-        // float product's error stays below 2^15 / n * 2^-23; truncation is exact
-        const float rnx = 1.0f / (float)nx, rny = 1.0f / (float)ny;
-        for (uint32_t t = lane; t < total; t += 32) {
-            const uint32_t q1 = (uint32_t)(((float)t + 0.5f) * rnx);
-            const uint32_t q2 = (uint32_t)(((float)q1 + 0.5f) * rny);
-            const uint32_t ix = x0 + (t - q1 * nx), iy = y0 + (q1 - q2 * ny), iz = z0 + q2;
-            // (i + 0.5) / 32 is an exact scaling: the reciprocal multiply gives the same bits
-            const float tz = p32 ? xmul(xadd((float)iz, 0.5f), 0.03125f) : xdiv(xadd((float)iz, 0.5f), pext.z);
-            const float omtz = xsub(1.0f, tz);
-            const float ty = p32 ? xmul(xadd((float)iy, 0.5f), 0.03125f) : xdiv(xadd((float)iy, 0.5f), pext.y);
-            const float omty = xsub(1.0f, ty);
-            const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
-            const float omtx = xsub(1.0f, tx);
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    const int32_t ok = __shfl_xor_sync(0xffffffffu, key, j);
+                    const uint32_t oi = __shfl_xor_sync(0xffffffffu, idx, j);
+                    const bool lower = (lane & j) == 0u, asc = (lane & k) == 0u;
+                    const bool take = (asc == lower) ? (ok < key) : (ok > key);
+                    if (take) { key = ok; idx = oi; }
+                }
+            }
+            // descending rank 31 - lane
+            s_order[ch * 32u + (31u - lane)] = (uint16_t)(key >= 0 ? idx : 0xffffu);
+        }
+        __syncthreads();
+        for (uint32_t ch = 0; ch < n_chunks; ch++) {
+#pragma unroll 1
+            for (uint32_t h = 0; h < 2; h++) {
+                const uint32_t r = h == 0 ? wid : 31u - wid;
+                const uint32_t k = s_order[ch * 32u + r];
+                if (k == 0xffffu) continue;
+                PairBox bx;
+                pair_box(objects, cluster_pointers, c2o, sorted[r0 + k], mnx, mny, mnz, B, bx);
+                const uint32_t total = pair_voxels(bx);
+                if (total == 0u) continue;
+                const uint32_t x0 = bx.x0, y0 = bx.y0, z0 = bx.z0;
+                const uint32_t nx = bx.x1 - x0, ny = bx.y1 - y0;
+                const dv3 pext = bx.pext;
+                const uint32_t ci = bx.ci;
+                const uint32_t lut = bx.od->lut_idx;
+                float ws2cs[16];
+                dm4_inverse(bx.cs2ws, ws2cs);
+                const dv3 pmax = dv3{xadd(bx.pmin.x, 32.0f), xadd(bx.pmin.y, 32.0f), xadd(bx.pmin.z, 32.0f)};
+                dv3 bc[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    bc[q] = mulv4p(ws2cs, (q & 1) ? pmax.x : bx.pmin.x, (q & 2) ? pmax.y : bx.pmin.y,
+                                   (q & 4) ? pmax.z : bx.pmin.z);
+                // the block side is exactly 32 unless min is so large that min + extent rounds
+                const bool p32 = pext.x == 32.0f && pext.y == 32.0f && pext.z == 32.0f;
+                // the cluster's 16 bit words, one shared-memory lookup per voxel
+                __syncwarp();
+                if (lane < 16) s_cw[wid][lane] = bits[(uint64_t)ci * 16u + lane];
+                __syncwarp();
+                // t -> (ix, iy, iz) without integer division: t < 2^15 and nx, ny <= 32,
+                // so (t + 0.5) / n lies at least 0.5 / n from an integer while the
+                // float product's error stays below 2^15 / n * 2^-23; truncation is exact
+                const float rnx = 1.0f / (float)nx, rny = 1.0f / (float)ny;
+                for (uint32_t t = lane; t < total; t += 32) {
+                    const uint32_t q1 = (uint32_t)(((float)t + 0.5f) * rnx);
+                    const uint32_t q2 = (uint32_t)(((float)q1 + 0.5f) * rny);
+                    const uint32_t ix = x0 + (t - q1 * nx), iy = y0 + (q1 - q2 * ny), iz = z0 + q2;
+                    // (i + 0.5) / 32 is an exact scaling: the reciprocal multiply gives the same bits
+                    const float tz = p32 ? xmul(xadd((float)iz, 0.5f), 0.03125f) : xdiv(xadd((float)iz, 0.5f), pext.z);
+                    const float omtz = xsub(1.0f, tz);
+                    const float ty = p32 ? xmul(xadd((float)iy, 0.5f), 0.03125f) : xdiv(xadd((float)iy, 0.5f), pext.y);
+                    const float omty = xsub(1.0f, ty);
+                    const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
+                    const float omtx = xsub(1.0f, tx);
 #define LZ(i, j, comp) xadd(xmul(omtz, bc[i].comp), xmul(tz, bc[j].comp))
-            const float pz0x = LZ(0, 4, x), pz0y = LZ(0, 4, y), pz0z = LZ(0, 4, z);
-            const float pz1x = LZ(1, 5, x), pz1y = LZ(1, 5, y), pz1z = LZ(1, 5, z);
-            const float pz2x = LZ(2, 6, x), pz2y = LZ(2, 6, y), pz2z = LZ(2, 6, z);
-            const float pz3x = LZ(3, 7, x), pz3y = LZ(3, 7, y), pz3z = LZ(3, 7, z);
+                    const float pz0x = LZ(0, 4, x), pz0y = LZ(0, 4, y), pz0z = LZ(0, 4, z);
+                    const float pz1x = LZ(1, 5, x), pz1y = LZ(1, 5, y), pz1z = LZ(1, 5, z);
+                    const float pz2x = LZ(2, 6, x), pz2y = LZ(2, 6, y), pz2z = LZ(2, 6, z);
+                    const float pz3x = LZ(3, 7, x), pz3y = LZ(3, 7, y), pz3z = LZ(3, 7, z);
 #undef LZ
-            const float py0x = xadd(xmul(omty, pz0x), xmul(ty, pz2x));
-            const float py0y = xadd(xmul(omty, pz0y), xmul(ty, pz2y));
-            const float py0z = xadd(xmul(omty, pz0z), xmul(ty, pz2z));
-            const float py1x = xadd(xmul(omty, pz1x), xmul(ty, pz3x));
-            const float py1y = xadd(xmul(omty, pz1y), xmul(ty, pz3y));
-            const float py1z = xadd(xmul(omty, pz1z), xmul(ty, pz3z));
-            const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
-            if (cx < 0.0f || cx >= 8.0f) continue;
-            const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
-            if (cy < 0.0f || cy >= 8.0f) continue;
-            const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
-            if (cz < 0.0f || cz >= 8.0f) continue;
-            const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
-            const uint32_t word = s_cw[wid][rvi >> 5];
-            if (word & (1u << (rvi & 31u))) {
-                const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy)),
-                                                    (float)ix);
-                atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
-                if (kMat) smem_max_u16(smat, bvi, ((od.lut_idx << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
+                    const float py0x = xadd(xmul(omty, pz0x), xmul(ty, pz2x));
+                    const float py0y = xadd(xmul(omty, pz0y), xmul(ty, pz2y));
+                    const float py0z = xadd(xmul(omty, pz0z), xmul(ty, pz2z));
+                    const float py1x = xadd(xmul(omty, pz1x), xmul(ty, pz3x));
+                    const float py1y = xadd(xmul(omty, pz1y), xmul(ty, pz3y));
+                    const float py1z = xadd(xmul(omty, pz1z), xmul(ty, pz3z));
+                    const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
+                    if (cx < 0.0f || cx >= 8.0f) continue;
+                    const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
+                    if (cy < 0.0f || cy >= 8.0f) continue;
+                    const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
+                    if (cz < 0.0f || cz >= 8.0f) continue;
+                    const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
+                    const uint32_t word = s_cw[wid][rvi >> 5];
+                    if (word & (1u << (rvi & 31u))) {
+                        const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz),
+                                                                 xmul(pext.x, (float)iy)), (float)ix);
+                        atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
+                        if (kMat) smem_max_u16(smat, bvi, ((lut << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
+                    }
+                }
             }
         }
     }
