@@ -372,8 +372,9 @@ def test_cached_gi_reaches_the_target_error_on_a_held_out_scene(ctx):
     """The shrinkage weight was tuned on the benchmark's 512-object scene
     (seed 1).  On the same generator with seed 2 (other sizes, poses, noise
     and LUTs), at 1920x1080 with the configured training budget, 4-spp cached
-    2-bounce GI after 60 online frames is within relMSE 0.01 of a 256-spp
-    plain render (measured 0.0084; plain GI needs 14 spp for it)."""
+    2-bounce GI, scored as the benchmark scores it (60 online frames at 1 spp,
+    then four at 4 spp), is within relMSE 0.01 of a 256-spp plain render
+    (measured 0.0084; plain GI needs 14 spp for it)."""
     import torch
     s = tg.generate_scene(1, 512, 2, 16, seed=2, noise_period=64.0, noise_threshold=0.5,
                           box_min=(-1024.0,) * 3, box_max=(1024.0,) * 3, n_luts=32)
@@ -388,9 +389,12 @@ def test_cached_gi_reaches_the_target_error_on_a_held_out_scene(ctx):
     cp = tg.cache_gi_params((-1100.0,) * 3, (1100.0,) * 3, n_train=65536, train_spp=16, train_steps=16, lr=1e-2,
                             primary_weight=1.0, n_train_primary=131072)
     cache = tg.Cache(ctx, seed=7)
+    # as the benchmark scores it: 60 online frames at 1 spp, then 4 frames at 4 spp, the last one scored
     for f in range(60):
         ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=1, bounces=2, seed=2, frame=f), cp, out)
-    ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=100), cp, out)
+    for f in range(4):
+        ctx.gi_render_cached(sc, svo, cache, view, vis, tg.gi_params(spp=4, bounces=2, seed=2, frame=100 + f), cp,
+                             out)
     ctx.sync()
     assert ctx.device_error().code == 0
     hit = vis.cpu().numpy().view(np.uint64) != np.uint64(tg.VIS_EMPTY)
