@@ -279,6 +279,16 @@ typedef struct tgx_vis_stats
 
 tgx_status  tgx_vis_get_stats(tgx_ctx* ctx, tgx_vis_stats* out_stats);
 
+/* A device-memory budget for the scene stores of this context (uploaded or
+ * generated): an upload or generation that would take the live stores past
+ * `bytes` fails with TGX_ERR_OUT_OF_MEMORY and a message, frees what it had
+ * allocated, and leaves the context usable, like a real allocation failure.
+ * 0 removes the limit (the default).  For an engine that runs under a fixed
+ * memory budget; the reference only asserts that an allocation succeeded
+ * (tg_memory.c:61).  tgx_get_memory reports the budget and the bytes held. */
+tgx_status  tgx_set_memory_budget(tgx_ctx* ctx, uint64_t bytes);
+tgx_status  tgx_get_memory(tgx_ctx* ctx, uint64_t* out_budget, uint64_t* out_scene_bytes);
+
 /* Tuning of the visibility pass on this context (0 keeps a default):
  *   depth_buckets  8, 16 (default) or 32 depth buckets per screen tile: a
  *                  tile's clusters are sorted into them near to far, so a

@@ -278,3 +278,33 @@ def test_tuning_settings_change_no_result(oracle, buckets, batch, drain):
         for bad in ((12, 0, 0), (0, 49, 0), (0, 0, 33)):
             with pytest.raises(tg.TgxError):
                 c.set_vis_tuning(*bad)
+
+
+def test_scene_upload_fails_cleanly_past_the_memory_budget(oracle):
+    """Allocation failure made on the host: with a budget too small for the
+    scene store the upload fails with TGX_ERR_OUT_OF_MEMORY partway through
+    its allocations, frees what it took, and the context stays usable: the
+    same upload under a larger budget renders the oracle's buffer, and the
+    budget accounting returns to zero when the scene is destroyed."""
+    s, v = cfg1_scene(), cfg1_view(64, 48)
+    need = 96 + 64 * 4 * 2 + 64 * 64 + 9 * 4   # object, pointers, map, bits, rotation
+    with tg.Context(0) as c:
+        c.set_memory_budget(64 * 8 + 96)    # room for the objects and the pointers, not the bits
+        with pytest.raises(tg.TgxError) as e:
+            c.upload(s)
+        assert e.value.status == 2
+        assert c.memory() == (64 * 8 + 96, 0)
+        c.set_memory_budget(1 << 20)
+        (g,) = render(c, s, v)
+        assert c.memory() == (1 << 20, 0)
+        sc = c.upload(s)
+        held = c.memory()[1]
+        assert held >= need
+        c.set_memory_budget(held + 100)
+        with pytest.raises(tg.TgxError):
+            c.upload(s)                    # a second copy does not fit
+        assert c.memory()[1] == held
+        sc.close()
+        assert c.memory()[1] == 0
+        c.set_memory_budget(0)
+    assert_same(g, oracle.vis_render(s, v, mode=1))

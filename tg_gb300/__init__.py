@@ -169,7 +169,7 @@ EXPORTS = [
     "tgx_frame_graph_kernels", "tgx_frame_graph_destroy", "tgx_svo_build_flags", "tgx_generate_scene_device",
     "tgx_scene_counts", "tgx_scene_download", "tgx_shade", "tgx_svo_update", "tgx_scene_set_objects",
     "tgx_set_trace_steps", "tgx_vis_render_host_async", "tgx_vis_host_wait", "tgx_vis_count_work",
-    "tgx_vis_get_work", "tgx_gi_get_work", "tgx_set_vis_tuning",
+    "tgx_vis_get_work", "tgx_gi_get_work", "tgx_set_vis_tuning", "tgx_set_memory_budget", "tgx_get_memory",
 ]
 
 
@@ -218,6 +218,8 @@ def _load() -> C.CDLL:
         "tgx_vis_get_work": (i32, [vp, C.POINTER(VisWork)]),
         "tgx_gi_get_work": (i32, [vp, C.POINTER(GiWork)]),
         "tgx_set_vis_tuning": (i32, [vp, u32, u32, u32]),
+        "tgx_set_memory_budget": (i32, [vp, u64]),
+        "tgx_get_memory": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "tgx_gi_render": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "tgx_cache_n_params": (u32, []),
         "tgx_gi_render_cached": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -502,6 +504,16 @@ class Context:
         st = VisStats()
         check(lib.tgx_vis_get_stats(self.handle, C.byref(st)), "tgx_vis_get_stats")
         return st
+
+    def set_memory_budget(self, nbytes: int) -> None:
+        """tgx_set_memory_budget: cap on the bytes of this context's scene stores (0: none)."""
+        check(lib.tgx_set_memory_budget(self.handle, nbytes), "tgx_set_memory_budget")
+
+    def memory(self) -> tuple[int, int]:
+        """tgx_get_memory: (budget, bytes held by live scene stores)."""
+        b, u = C.c_uint64(), C.c_uint64()
+        check(lib.tgx_get_memory(self.handle, C.byref(b), C.byref(u)), "tgx_get_memory")
+        return b.value, u.value
 
     def set_vis_tuning(self, depth_buckets: int = 0, batch: int = 0, drain: int = 0) -> None:
         """tgx_set_vis_tuning: depth buckets per tile (8/16/32), clusters per staged batch (1..48) and pairs per

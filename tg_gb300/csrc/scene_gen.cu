@@ -131,13 +131,13 @@ extern "C" tgx_status tgx_generate_scene_device(tgx_ctx* c, const tgx_gen_params
     s->n_cluster_pointers = s->n_clusters = (uint32_t)total;
     s->n_luts = n_luts;
     cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_objects, objects.size() * sizeof(tgx_object));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_cluster_pointers, total * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_c2o, total * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_bits, total * 64);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_material, total * 512);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_luts, luts.size() * sizeof(tgx_material));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_inv_rot, (size_t)p->n_objects * 9 * sizeof(float));
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_objects, objects.size() * sizeof(tgx_object));
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_cluster_pointers, total * 4);
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_c2o, total * 4);
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_bits, total * 64);
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_material, total * 512);
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_luts, luts.size() * sizeof(tgx_material));
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_inv_rot, (size_t)p->n_objects * 9 * sizeof(float));
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->d_objects, objects.data(), objects.size() * sizeof(tgx_object), cudaMemcpyHostToDevice,
                             c->stream);
@@ -147,6 +147,7 @@ extern "C" tgx_status tgx_generate_scene_device(tgx_ctx* c, const tgx_gen_params
         cudaGetLastError();
         tgx_set_error("tgx_generate_scene_device: %s", cudaGetErrorString(e));
         cudaStreamSynchronize(c->stream);
+        c->mem_scenes -= s->bytes;
         scene_release(s);
         return e == cudaErrorMemoryAllocation ? TGX_ERR_OUT_OF_MEMORY : TGX_ERR_CUDA;
     }
@@ -166,6 +167,7 @@ extern "C" tgx_status tgx_generate_scene_device(tgx_ctx* c, const tgx_gen_params
     if (st == TGX_OK) st = scene_finish(c, s);
     if (st != TGX_OK) {
         cudaStreamSynchronize(c->stream);
+        c->mem_scenes -= s->bytes;
         scene_release(s);
         return st;
     }

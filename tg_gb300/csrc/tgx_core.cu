@@ -7,6 +7,8 @@
 
 #include "tgx_internal.cuh"
 
+#include <algorithm>
+
 #include <cstdarg>
 #include <cstdlib>
 #include <new>
@@ -336,6 +338,34 @@ tgx_status scene_finish(tgx_ctx* c, tgx_scene* s)
     return TGX_OK;
 }
 
+// A scene-store array: refused (as an allocation failure, nothing allocated)
+// when it would take the context's live scene stores past its budget.
+cudaError_t scene_malloc(tgx_ctx* c, tgx_scene* s, void** p, size_t bytes)
+{
+    if (c->mem_budget && c->mem_scenes + bytes > c->mem_budget) return cudaErrorMemoryAllocation;
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) {
+        c->mem_scenes += bytes;
+        s->bytes += bytes;
+    }
+    return e;
+}
+
+extern "C" tgx_status tgx_set_memory_budget(tgx_ctx* c, uint64_t bytes)
+{
+    if (!c) return TGX_ERR_INVALID_ARGUMENT;
+    c->mem_budget = bytes;
+    return TGX_OK;
+}
+
+extern "C" tgx_status tgx_get_memory(tgx_ctx* c, uint64_t* out_budget, uint64_t* out_scene_bytes)
+{
+    if (!c) return TGX_ERR_INVALID_ARGUMENT;
+    if (out_budget) *out_budget = c->mem_budget;
+    if (out_scene_bytes) *out_scene_bytes = c->mem_scenes;
+    return TGX_OK;
+}
+
 extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_scene** out)
 {
     if (!c || !d || !out) { tgx_set_error("tgx_scene_upload: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
@@ -384,7 +414,7 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
     s->n_luts = d->luts ? d->n_luts : 0;
     cudaError_t e = cudaSuccess;
 #define ALLOC_COPY(dst, src, bytes)                                                                 \
-    if (e == cudaSuccess) e = cudaMalloc((void**)&(dst), (bytes));                                  \
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&(dst), (bytes));                          \
     if (e == cudaSuccess) e = cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, c->stream);
     ALLOC_COPY(s->d_objects, d->objects, (size_t)d->n_objects * sizeof(tgx_object));
     ALLOC_COPY(s->d_cluster_pointers, d->cluster_pointers, (size_t)d->n_cluster_pointers * 4);
@@ -393,15 +423,22 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
     if (d->material_idx) { ALLOC_COPY(s->d_material, d->material_idx, (size_t)d->n_clusters * 512); }
     if (d->luts) { ALLOC_COPY(s->d_luts, d->luts, (size_t)d->n_luts * 256 * sizeof(tgx_material)); }
 #undef ALLOC_COPY
-    if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_inv_rot, (size_t)d->n_objects * 9 * sizeof(float));
+    if (e == cudaSuccess) e = scene_malloc(c, s, (void**)&s->d_inv_rot, (size_t)d->n_objects * 9 * sizeof(float));
     if (e != cudaSuccess) {
-        tgx_set_error("tgx_scene_upload: %s", cudaGetErrorString(e));
+        if (e == cudaErrorMemoryAllocation && c->mem_budget)
+            tgx_set_error("tgx_scene_upload: out of device memory or past the context's budget of %llu bytes",
+                          (unsigned long long)c->mem_budget);
+        else
+            tgx_set_error("tgx_scene_upload: %s", cudaGetErrorString(e));
+        cudaGetLastError();
         cudaStreamSynchronize(c->stream);
+        c->mem_scenes -= s->bytes;
         scene_free(s);
         return e == cudaErrorMemoryAllocation ? TGX_ERR_OUT_OF_MEMORY : TGX_ERR_CUDA;
     }
     const tgx_status st = scene_finish(c, s);
     if (st != TGX_OK) {
+        c->mem_scenes -= s->bytes;
         scene_free(s);
         return st;
     }
@@ -411,7 +448,10 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
 
 extern "C" void tgx_scene_destroy(tgx_ctx* c, tgx_scene* s)
 {
-    if (c) cudaStreamSynchronize(c->stream);
+    if (c) {
+        cudaStreamSynchronize(c->stream);
+        if (s) c->mem_scenes -= std::min(c->mem_scenes, s->bytes);
+    }
     scene_free(s);
 }
 

@@ -131,6 +131,8 @@ struct tgx_ctx
     DevBuf svo_scratch;    // SVO update: dirty-block marks
     DevBuf svo_sort;       // SVO build: pairs grouped by block slot, per-slot counts and offsets
     DevBuf vis_work;       // work counters of the tile kernel's counting variant
+    uint64_t mem_budget = 0;           // bytes the context's scene stores may hold (0: no limit)
+    uint64_t mem_scenes = 0;           // bytes its live scene stores hold
     uint32_t vis_tile_ctas = 0;        // resident CTAs of the persistent (batched-frame) tile kernel
     bool   vis_count_work = false;
     uint32_t vis_bshift = 1;           // depth buckets per tile: 32 >> vis_bshift
@@ -157,6 +159,7 @@ struct tgx_ctx
 struct tgx_scene
 {
     uint32_t    n_objects = 0, n_cluster_pointers = 0, n_clusters = 0, n_luts = 0;
+    uint64_t    bytes = 0;                 // device bytes of the store, counted against the context's budget
     tgx_object* d_objects = nullptr;
     float*      d_inv_rot = nullptr;       // per object: 3x3 linear part of inverse(rotation), row-major
     uint32_t*   d_cluster_pointers = nullptr;
@@ -416,5 +419,7 @@ tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, ui
                                float* d_rgb);
 
 tgx_status vis_prepare_device(tgx_ctx* c);
+// cudaMalloc of one scene-store array, counted against the context's budget
+cudaError_t scene_malloc(tgx_ctx* c, tgx_scene* s, void** p, size_t bytes);
 tgx_status vis_render_device(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
                              uint64_t* const* d_visbuf);
