@@ -788,8 +788,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gi", action="store_true", help="skip the SVO build and GI measurements")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched many-view frame (config 3)")
-    ap.add_argument("--large", action="store_true",
-                    help="also run the 2^24-cluster config 5 (about 30 GB of device memory and a minute of setup)")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 2^24-cluster config 5 (about 77 GB of device memory, some 10 s)")
     ap.add_argument("--no-gi-cache", action="store_true",
                     help="skip the learned-cache vs plain 2-bounce GI comparison at equal relMSE")
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
@@ -1051,7 +1051,7 @@ def main() -> None:
             gi_report["gi_cache_vs_plain"] = cache_report
         svo.close()
     batched = None if args.no_batched else bench_batched(local)
-    large = bench_large(local) if args.large else None
+    large = None if args.no_large else bench_large(local)
     rays = W * H
     value = rays * world / (ms * 1e-3) / 1e9
 
