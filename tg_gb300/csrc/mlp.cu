@@ -55,11 +55,14 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 // Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
 // ---------------------------------------------------------------------------
 //
-// A CTA of 256 threads holds two independent groups of 4 warps that share the
-// weights in shared memory.  Each group works through tiles of 128 queries:
+// A CTA of 384 threads holds three independent groups of 4 warps that share
+// the weights in shared memory.  Each group works through tiles of 128 queries:
 // thread t of the group owns query t of its tile, which is row t of every
-// GEMM and TMEM lane t.  While one group waits for its MMAs the other encodes
-// or drains its accumulators, so the tensor core and the CUDA cores overlap.
+// GEMM and TMEM lane t.  While one group waits for its MMAs the others encode
+// or drain their accumulators, so the tensor core and the CUDA cores overlap.
+// A group's layer-0 feature tile (56 KB) also holds, in its first 16 KB, the
+// A operand of layers 1-4, which is written only once layer 0's MMAs have
+// completed; that is what leaves room for a third group.
 // Operands use the canonical no-swizzle K-major layout: 8 x 8 BF16 core
 // matrices (8 rows of 16 contiguous bytes), K-adjacent core matrices LBO
 // bytes apart and row-group-adjacent ones SBO bytes apart.  Per layer one
@@ -73,18 +76,22 @@ namespace tc {
 constexpr int M = 128;                      // queries per tile
 constexpr int KG0 = NEP / 8;                // 28 K core-matrix columns of layer 0
 constexpr int KGH = NH / 8;                 // 8 of the hidden layers
-constexpr int THREADS = 256;                // two groups of 128
+constexpr int NG = 3;                       // query groups per CTA
+constexpr int THREADS = 128 * NG;           // three groups of 128
 // byte offsets in dynamic shared memory (all 1024-aligned)
 constexpr int W0 = 0;                                   // [28 kg][8 ng][128 B]
 constexpr int W1 = W0 + KG0 * 8 * 128;                  // [8 kg][8 ng][128 B] x 3
 constexpr int W4 = W1 + 3 * KGH * 8 * 128;              // [8 kg][2 ng][128 B] (16 rows, 3 real)
 constexpr int GROUP = W4 + KGH * 2 * 128;               // per group:
-constexpr int A0 = 0;                                   //   [28 kg][16 mg][128 B]
-constexpr int A1 = A0 + KG0 * 16 * 128;                 //   [8 kg][16 mg][128 B]
-constexpr int GROUP_BYTES = A1 + KGH * 16 * 128;
-constexpr int BAR = GROUP + 2 * GROUP_BYTES;            // 2 mbarriers, TMEM address
+constexpr int A0 = 0;                                   //   [28 kg][16 mg][128 B] layer 0's A operand
+constexpr int A1 = A0;                                  //   [8 kg][16 mg][128 B] layers 1-4's A operand, in
+                                                        //   A0's first 16 KB: written only after layer 0's
+                                                        //   MMAs completed, and A0 again only after layer 4's
+constexpr int GROUP_BYTES = KG0 * 16 * 128;
+constexpr int BAR = GROUP + NG * GROUP_BYTES;           // NG mbarriers, TMEM address
 constexpr int SMEM = BAR + 64;
-constexpr uint32_t TMEM_COLS = 128;                     // 64 per group
+static_assert(SMEM <= 232448, "shared memory per CTA");
+constexpr uint32_t TMEM_COLS = 256;                     // 64 per group, allocated as a power of two
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
 __host__ __device__ constexpr uint32_t idesc(uint32_t n)
@@ -215,8 +222,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
     stage_weights(sm + W1 + 2 * KGH * 8 * 128, wimg + B_W3, SH, NH, NH, KGH);
     stage_weights(sm + W4, wimg + B_W4, SH, 8, 16, KGH);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&bars[0])));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&bars[1])));
+        for (int q = 0; q < NG; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&bars[q])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -238,17 +244,17 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
     // its HBM latency hides behind the current tile's layers
     float xn[NI];
     {
-        const uint32_t row = (blockIdx.x * 2 + g) * M + gt;
+        const uint32_t row = (blockIdx.x * NG + g) * M + gt;
 #pragma unroll
         for (int i = 0; i < NI; i++) xn[i] = row < n ? __ldg(&x[(uint64_t)row * NI + i]) : 0.0f;
     }
-    for (uint32_t tile = blockIdx.x * 2 + g; tile < tiles && ok; tile += gridDim.x * 2) {
+    for (uint32_t tile = blockIdx.x * NG + g; tile < tiles && ok; tile += gridDim.x * NG) {
         const uint32_t row = tile * M + gt;
         float xc[NI];
 #pragma unroll
         for (int i = 0; i < NI; i++) xc[i] = xn[i];
         {
-            const uint32_t next = (tile + gridDim.x * 2) * M + gt;
+            const uint32_t next = (tile + gridDim.x * NG) * M + gt;
 #pragma unroll
             for (int i = 0; i < NI; i++) xn[i] = next < n ? __ldg(&x[(uint64_t)next * NI + i]) : 0.0f;
         }
@@ -823,7 +829,7 @@ static tgx_status cache_forward(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, u
         attr = true;
     }
     const uint32_t tiles = (n + tc::M - 1) / tc::M;
-    const uint32_t grid = std::max(1u, std::min<uint32_t>((tiles + 1) / 2, (uint32_t)c->num_sms));
+    const uint32_t grid = std::max(1u, std::min<uint32_t>((tiles + tc::NG - 1) / tc::NG, (uint32_t)c->num_sms));
     TGX_LAUNCH(c, TR_MLP, grid, tc::THREADS, tc::SMEM, k_mlp_forward_tc, k->img, n, d_n, d_x, d_rgb, c->d_status);
     return TGX_OK;
 }
