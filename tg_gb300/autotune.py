@@ -12,9 +12,10 @@ Visibility: four settings change the speed of a frame but never a result
     lanes run their DDAs (16, 24, 32), i.e. rays per warp round.
 The tuner runs the caller's own frame (one scene and its views, or a whole
 batched frame graph) with each candidate, times it with CUDA events on the
-library stream and keeps the fastest: first over the tile shapes with the
-other settings at their defaults, then one setting at a time (coordinate
-descent).
+library stream (best of three runs) and keeps the fastest, moving away from
+the current choice only for a gain above 1 %: first over the tile shapes
+with the other settings at their defaults, then one setting at a time
+(coordinate descent).
 
 Traversal: how long a lane of the persistent k_trace_queue runs its ray
 before the warp refills finished lanes from the ray queue.
@@ -66,13 +67,16 @@ def _label(cfg: dict) -> str:
 
 
 def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES, depth_buckets=DEPTH_BUCKETS,
-                  batches=BATCHES, drains=DRAINS):
+                  batches=BATCHES, drains=DRAINS, reps: int = 3, margin: float = 0.01):
     """Coordinate search over the visibility settings for one workload.
 
     make_frame(ctx) sets up the workload on a fresh context and returns
     (render, close): render() issues one whole frame on the context's stream,
-    close() frees what make_frame made.  Returns (best config dict, {label:
-    ms per frame})."""
+    close() frees what make_frame made.  Each candidate is timed `reps` times
+    over `frames` frames and keeps its best time; a candidate replaces the
+    current choice only when it is faster by more than `margin` (run-to-run
+    noise would otherwise pick settings at random).  Returns (best config
+    dict, {label: ms per frame})."""
     import torch
     import tg_gb300 as tg
 
@@ -89,28 +93,35 @@ def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES
             for _ in range(2):
                 render()
             ctx.sync()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(frames):
-                render()
-            e1.record(stream)
-            ctx.sync()
+            best_ms = None
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(frames):
+                    render()
+                e1.record(stream)
+                ctx.sync()
+                ms = e0.elapsed_time(e1) / frames
+                best_ms = ms if best_ms is None else min(best_ms, ms)
             err = ctx.device_error()
             if err.code:
                 raise RuntimeError(f"tuning frame failed: device status {err.code} at {err.where}")
             close()
-        times[lab] = round(e0.elapsed_time(e1) / frames, 4)
+        times[lab] = round(best_ms, 4)
         return times[lab]
+
+    def better(cand, cur):
+        return run(cand) < run(cur) * (1.0 - margin)
 
     best = {"tile": tiles[0], **DEFAULTS}
     for t in tiles:
         cand = {**best, "tile": t}
-        if run(cand) < run(best):
+        if better(cand, best):
             best = cand
     for name, values in (("depth_buckets", depth_buckets), ("batch", batches), ("drain", drains)):
         for v in values:
             cand = {**best, name: v}
-            if run(cand) < run(best):
+            if better(cand, best):
                 best = cand
     return best, times
 
