@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_au
 __global__ void __launch_bounds__(kScanTiles) k_vis_finalize(const uint32_t* __restrict__ tile_total, uint32_t n_tiles,
                                                             const uint32_t* __restrict__ cta_aux,
                                                             uint32_t* __restrict__ tile_off,
-                                                            uint32_t* __restrict__ tile_order)
+                                                            uint4* __restrict__ slot_info)
 {
     __shared__ uint32_t cur[kOrderClasses];
     __shared__ uint32_t wsum[kScanTiles / 32];
@@ -486,8 +486,9 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize(const uint32_t* __r
     uint32_t before = cta_aux[blockIdx.x];
     for (uint32_t w = 0; w < wid; w++) before += wsum[w];
     if (valid) {
-        tile_off[t] = before + incl - x;
-        tile_order[atomicAdd(&cur[tile_class(x)], 1u)] = t;
+        const uint32_t off = before + incl - x;
+        tile_off[t] = off;
+        slot_info[atomicAdd(&cur[tile_class(x)], 1u)] = make_uint4(t, off, x, 0u);
     }
 }
 
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
                                                                    uint32_t n_tiles,
                                                                    const uint32_t* __restrict__ cta_aux,
                                                                    uint32_t* __restrict__ tile_off,
-                                                                   uint32_t* __restrict__ tile_order,
+                                                                   uint4* __restrict__ slot_info,
                                                                    uint32_t bin_capacity,
                                                                    uint32_t* __restrict__ counters)
 {
@@ -575,8 +576,9 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
     }
     for (uint32_t w = 0; w < wid; w++) base += wsum[w];
     if (valid) {
-        tile_off[t] = base + incl - x;
-        tile_order[atomicAdd(&cur[tile_class(x)], 1u)] = t;
+        const uint32_t off = base + incl - x;
+        tile_off[t] = off;
+        slot_info[atomicAdd(&cur[tile_class(x)], 1u)] = make_uint4(t, off, x, 0u);
     }
 }
 
@@ -802,7 +804,7 @@ struct TileJob
     const uint2* rects;
     const TileEntry* entries;
     const uint32_t* tile_off;
-    const uint32_t* tile_order;
+    const uint4* slot_info;      // per launch slot (heavy first): tile, first entry, entry count
     const ViewConst* views;
     const uint32_t* bits;
     const float* inv_rot;
@@ -910,11 +912,12 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     // ordered before the bulk copy that overwrites it)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    const uint32_t tile = J.tile_order[slot];
+    const uint4 si = J.slot_info[slot];   // one load: the tile and its entry range
+    const uint32_t tile = si.x;
     // bins overflowed this frame: gather every record whose tile rectangle holds the tile (slow, exact)
     const bool scan_all = J.counters[C_OVERFLOW] != 0u;
-    const uint32_t begin = scan_all ? 0u : J.tile_off[tile];
-    const uint32_t end = scan_all ? J.counters[C_RECORDS] : J.tile_off[tile + 1];
+    const uint32_t begin = scan_all ? 0u : si.y;
+    const uint32_t end = scan_all ? J.counters[C_RECORDS] : si.y + si.z;
     if (threadIdx.x == 0) {
         if (!scan_all && end > begin) stage_entries(sm, J.entries + begin, min(J.batch, end - begin), J.extra_tx);
         uint32_t v = 0;
@@ -1221,7 +1224,7 @@ struct VisScratch
     uint32_t* tile_total;
     uint32_t* cta_aux;
     uint32_t* tile_off;
-    uint32_t* tile_order;
+    uint4* slot_info;
     TileEntry* entries;
     uint32_t bin_capacity;     // entries
 };
@@ -1234,6 +1237,12 @@ static size_t vis_tile_bytes(uint32_t n_tiles)
     return (size_t)n_tiles * kMaxBuckets * 4 * 2 + (size_t)n_tiles * 4 + (size_t)n_scan_ctas * (1 + kOrderClasses) * 4;
 }
 
+// bytes of the tile offsets (n_tiles + 1 words, padded to 16 bytes) and the slot records
+static size_t vis_off_bytes(uint32_t n_tiles)
+{
+    return (size_t)((n_tiles + 4u) & ~3u) * 4 + (size_t)n_tiles * sizeof(uint4);
+}
+
 static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_off, uint32_t n_tiles)
 {
     w.bucket_cnt = tile_cnt;
@@ -1241,7 +1250,7 @@ static void vis_carve_tiles(VisScratch& w, uint32_t* tile_cnt, uint32_t* tile_of
     w.tile_total = w.bucket_off + (size_t)n_tiles * kMaxBuckets;
     w.cta_aux = w.tile_total + n_tiles;
     w.tile_off = tile_off;
-    w.tile_order = w.tile_off + (n_tiles + 1);
+    w.slot_info = reinterpret_cast<uint4*>(w.tile_off + ((n_tiles + 4u) & ~3u));
 }
 
 enum VisPhase { VIS_ALL = 0, VIS_TO_SCAN = 1, VIS_FROM_BINS = 2, VIS_NO_TILES = 3 };
@@ -1257,7 +1266,7 @@ static TileJob tile_job(const tgx_ctx* c, const tgx_scene* s, const ViewConst* d
     J.rects = w.rects;
     J.entries = w.entries;
     J.tile_off = w.tile_off;
-    J.tile_order = w.tile_order;
+    J.slot_info = w.slot_info;
     J.views = d_vc;
     J.bits = s->d_bits;
     J.inv_rot = s->d_inv_rot;
@@ -1301,12 +1310,12 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
                            w.tile_total, n_tiles, w.cta_aux);
         if (n_scan_ctas <= kDirectGroups) {
             TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize_direct, w.tile_total, n_tiles,
-                           w.cta_aux, w.tile_off, w.tile_order, w.bin_capacity, w.counters);
+                           w.cta_aux, w.tile_off, w.slot_info, w.bin_capacity, w.counters);
         } else {
             TGX_LAUNCH_PDL(c, TR_VIS_SCAN, 1, 1024, 0, k_vis_scan, w.cta_aux, n_tiles, w.tile_off, w.bin_capacity,
                            w.counters);
             TGX_LAUNCH_PDL(c, TR_VIS_SCAN, n_scan_ctas, kScanTiles, 0, k_vis_finalize, w.tile_total, n_tiles,
-                           w.cta_aux, w.tile_off, w.tile_order);
+                           w.cta_aux, w.tile_off, w.slot_info);
         }
     }
     if (phase == VIS_TO_SCAN) return TGX_OK;
@@ -1444,7 +1453,7 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     TGX_TRY(devbuf_reserve(c->vis_records, (size_t)w.rec_cap * (sizeof(VisRecord) + sizeof(uint2))));
     TGX_TRY(devbuf_reserve(c->vis_counters, C_COUNT * sizeof(uint32_t)));
     TGX_TRY(devbuf_reserve(c->vis_tile_cnt, vis_tile_bytes(n_tiles)));
-    TGX_TRY(devbuf_reserve(c->vis_tile_off, (size_t)(n_tiles + 1) * 4 * 2));
+    TGX_TRY(devbuf_reserve(c->vis_tile_off, vis_off_bytes(n_tiles)));
     w.records = (VisRecord*)c->vis_records.ptr;
     w.rects = (uint2*)(w.records + w.rec_cap);
     w.counters = (uint32_t*)c->vis_counters.ptr;
@@ -1522,7 +1531,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
     std::vector<std::vector<unsigned char>> tables(n_jobs);
     auto job_bytes = [&](const tgx_frame_graph::Job& job) {
         return al((size_t)job.rec_cap * (sizeof(VisRecord) + sizeof(uint2))) + 256 + al(vis_tile_bytes(job.n_tiles)) +
-               al((size_t)(job.n_tiles + 1) * 4 * 2) + al((size_t)job.bin_cap * sizeof(TileEntry));
+               al(vis_off_bytes(job.n_tiles)) + al((size_t)job.bin_cap * sizeof(TileEntry));
     };
     for (uint32_t j = 0; j < n_jobs; j++) {
         const tgx_vis_job& jb = jobs[j];
@@ -1581,7 +1590,7 @@ extern "C" tgx_status tgx_frame_graph_create(tgx_ctx* c, const tgx_vis_job* jobs
         uint32_t* tile_cnt = (uint32_t*)p;
         p += al(vis_tile_bytes(job.n_tiles));
         uint32_t* tile_off = (uint32_t*)p;
-        p += al((size_t)(job.n_tiles + 1) * 4 * 2);
+        p += al(vis_off_bytes(job.n_tiles));
         w.entries = (TileEntry*)p;
         w.bin_capacity = (uint32_t)job.bin_cap;
         vis_carve_tiles(w, tile_cnt, tile_off, job.n_tiles);
@@ -1897,8 +1906,8 @@ constexpr size_t kNaBucketOff = kNaBucketCnt + na_align((size_t)kNaMaxTiles * kN
 constexpr size_t kNaTileTotal = kNaBucketOff + na_align((size_t)kNaMaxTiles * kNaBuckets * 4);
 constexpr size_t kNaScanAux = kNaTileTotal + na_align((size_t)kNaMaxTiles * 4);
 constexpr size_t kNaTileOff = kNaScanAux + na_align(((size_t)kNaMaxTiles / kScanTiles + 1) * (1 + kOrderClasses) * 4);
-constexpr size_t kNaTileOrder = kNaTileOff + na_align(((size_t)kNaMaxTiles + 1) * 4);
-constexpr size_t kNaBinsOff = kNaTileOrder + na_align((size_t)kNaMaxTiles * 4);
+constexpr size_t kNaSlotInfo = kNaTileOff + na_align(((size_t)kNaMaxTiles + 4) * 4);
+constexpr size_t kNaBinsOff = kNaSlotInfo + na_align((size_t)kNaMaxTiles * 16);
 constexpr size_t kNaBytes = kNaBinsOff + na_align((size_t)kNaBins * sizeof(TileEntry));   // about 51 MiB
 
 // The scratch.  In host code this name is only a host-side stand-in: its
@@ -2024,7 +2033,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     uint32_t* tile_total = (uint32_t*)(base + kNaTileTotal);
     uint32_t* cta_aux = (uint32_t*)(base + kNaScanAux);
     uint32_t* tile_off = (uint32_t*)(base + kNaTileOff);
-    uint32_t* tile_order = (uint32_t*)(base + kNaTileOrder);
+    uint4* slot_info = (uint4*)(base + kNaSlotInfo);
     TileEntry* entries = (TileEntry*)(base + kNaBinsOff);
 
     int sms = 0;
@@ -2042,11 +2051,11 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
     NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_prefix<kNaBuckets>, bucket_cnt, bucket_off, tile_total, n_tiles, cta_aux);
     if (n_scan_ctas <= kDirectGroups) {
-        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize_direct, tile_total, n_tiles, cta_aux, tile_off, tile_order,
+        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize_direct, tile_total, n_tiles, cta_aux, tile_off, slot_info,
                   kNaBins, counters);
     } else {
         NA_LAUNCH(1, 1024, k_vis_scan, cta_aux, n_tiles, tile_off, kNaBins, counters);
-        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, tile_order);
+        NA_LAUNCH(n_scan_ctas, kScanTiles, k_vis_finalize, tile_total, n_tiles, cta_aux, tile_off, slot_info);
     }
     NA_LAUNCH(warp_grid, 256, k_vis_bin_fill, records, rects, counters, d_vc, tile_off, bucket_off, bucket_cnt, entries,
               d_voxel_bits, n_tiles, kNaBins, 1u, status);
@@ -2055,7 +2064,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.rects = rects;
     J.entries = entries;
     J.tile_off = tile_off;
-    J.tile_order = tile_order;
+    J.slot_info = slot_info;
     J.views = d_vc;
     J.bits = d_voxel_bits;
     J.inv_rot = inv_rot;
