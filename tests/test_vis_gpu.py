@@ -64,6 +64,29 @@ def test_axis_aligned_rays_and_zero_direction_components(ctx, oracle):
     assert_same(g, oracle.vis_render(s, v, mode=0))
 
 
+@pytest.mark.parametrize("view_i", range(3))
+def test_diagonal_rays_from_lattice_points(ctx, oracle, view_i):
+    # an axis-aligned 4x4x4-cluster object on the integer lattice, seen from
+    # lattice points along diagonals: rays cross voxel edges at (nearly) equal
+    # distances, so the hit voxel's entry axis is a near tie and the exact
+    # three-axis maximum decides; power-of-two and other far planes
+    rng = np.random.default_rng(7)
+    objs = np.zeros(1, tg.OBJECT_DTYPE)
+    objs["n_cluster_pointers_per_dim"] = (4, 4, 4)
+    objs["translation"] = (0.0, 0.0, 0.0)
+    objs["rotation"] = np.eye(4, dtype=np.float32).T.reshape(-1)
+    words = (rng.random((64, 16, 32)) < 0.06).astype(np.uint64)
+    words = (words << np.arange(32, dtype=np.uint64)).sum(axis=2).astype(np.uint32)
+    s = tg.HostScene(objs, np.arange(64, dtype=np.uint32), np.zeros(64, np.uint32), words)
+    pos, pitch, yaw, far = [((-24.0, 0.0, -24.0), 0.0, float(-3 * np.pi / 4), 128.0),
+                            ((-24.0, -24.0, -24.0), 0.6154797, float(-3 * np.pi / 4), 100.0),
+                            ((20.0, 8.0, -20.0), 0.0, float(3 * np.pi / 4), 4096.0)][view_i]
+    v = tg.make_view(pos, pitch, yaw, 1.0, 160, 120, 0.1, far)
+    (g,) = render(ctx, s, v)
+    assert_same(g, oracle.vis_render(s, v, mode=0))
+    assert (g != EMPTY).sum() > 100
+
+
 def test_multi_view_batch_equals_single_views(ctx, oracle):
     s = fuzz_scene(21, n_objects=5, box=40.0)
     views = np.concatenate([

@@ -308,9 +308,24 @@ __global__ void k_object_setup(const tgx_object* __restrict__ objs, uint32_t n, 
         for (int c = 0; c < 3; c++) inv_rot[9 * i + 3 * r + c] = DM(inv, r, c);
 }
 
+// per cluster pointer p: c2o[cluster_pointers[p]], with bit 31 set when that
+// cluster has no set voxel (such a cluster never writes a visibility word)
+__global__ void k_scene_cp_obj(const uint32_t* __restrict__ cluster_pointers, const uint32_t* __restrict__ c2o,
+                               const uint32_t* __restrict__ bits, uint32_t n, uint32_t* __restrict__ out)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t ci = cluster_pointers[p];
+    const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
+    const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
+    const bool empty = !(a.x | a.y | a.z | a.w | b.x | b.y | b.z | b.w | c.x | c.y | c.z | c.w | d.x | d.y | d.z | d.w);
+    out[p] = c2o[ci] | (empty ? 0x80000000u : 0u);
+}
+
 void scene_release(tgx_scene* s)
 {
     if (!s) return;
+    cudaFree(s->d_cp_obj);
     cudaFree(s->d_objects);
     cudaFree(s->d_inv_rot);
     cudaFree(s->d_cluster_pointers);
@@ -325,6 +340,19 @@ static void scene_free(tgx_scene* s) { scene_release(s); }
 // per-object inverse rotations of a scene whose arrays are on the device; synchronous
 tgx_status scene_finish(tgx_ctx* c, tgx_scene* s)
 {
+    if (!s->d_cp_obj) {
+        // the cull's per-pointer table, once per scene (its inputs never change)
+        const cudaError_t e = scene_malloc(c, s, (void**)&s->d_cp_obj, (size_t)s->n_cluster_pointers * 4);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            tgx_set_error("scene setup: out of device memory or past the context's budget (%u-word pointer table)",
+                          s->n_cluster_pointers);
+            return e == cudaErrorMemoryAllocation ? TGX_ERR_OUT_OF_MEMORY : TGX_ERR_CUDA;
+        }
+        k_scene_cp_obj<<<(s->n_cluster_pointers + 255) / 256, 256, 0, c->stream>>>(
+            s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, s->d_cp_obj);
+        if (cudaGetLastError() == cudaSuccess) c->launches++;
+    }
     trace_begin(c, TR_OBJECT_SETUP);
     k_object_setup<<<(s->n_objects + 127) / 128, 128, 0, c->stream>>>(s->d_objects, s->n_objects, s->d_inv_rot);
     cudaError_t le = cudaGetLastError();
@@ -377,6 +405,10 @@ extern "C" tgx_status tgx_scene_upload(tgx_ctx* c, const tgx_scene_desc* d, tgx_
     }
     if (d->n_clusters > (1u << TGX_CLUSTER_IDX_BITS) || d->n_cluster_pointers > (1u << TGX_CLUSTER_IDX_BITS)) {
         tgx_set_error("tgx_scene_upload: more than 2^31 clusters");
+        return TGX_ERR_CAPACITY;
+    }
+    if (d->n_objects >= 0x80000000u) {   // the cull's pointer table keeps an object index in 31 bits
+        tgx_set_error("tgx_scene_upload: 2^31 or more objects");
         return TGX_ERR_CAPACITY;
     }
     // Host-side validation of the data model (the reference only asserts).

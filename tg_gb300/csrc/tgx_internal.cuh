@@ -165,6 +165,8 @@ struct tgx_scene
     uint32_t*   d_cluster_pointers = nullptr;
     uint32_t*   d_c2o = nullptr;
     uint32_t*   d_bits = nullptr;
+    uint32_t*   d_cp_obj = nullptr;        // per cluster pointer: its object, bit 31 set when its cluster is empty
+                                           // (built once: pointers, owners and bits never change after upload)
     uint8_t*    d_material = nullptr;
     tgx_material* d_luts = nullptr;
 };

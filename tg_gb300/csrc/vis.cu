@@ -118,10 +118,15 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
 // 1. per-cluster setup
 // ---------------------------------------------------------------------------
 
+// kPacked: the scene's per-pointer table gives each pointer's object and
+// whether its cluster is empty (one load beside the pointer's own, instead of
+// the chain pointer -> owner -> bitmask); without it (the entry point that
+// allocates nothing) the owner and the bitmask are read.
+template <bool kPacked>
 __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
-    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, uint32_t n_cp,
-    const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
+    const uint32_t* __restrict__ c2o, const uint32_t* __restrict__ bits, const uint32_t* __restrict__ cp_obj,
+    uint32_t n_cp, const ViewConst* __restrict__ views, uint32_t n_views, VisRecord* __restrict__ records,
     uint2* __restrict__ rects, uint32_t record_capacity, uint32_t* __restrict__ counters,
     uint32_t* __restrict__ zero, uint32_t n_zero, tgx_dev_status* __restrict__ status)
 {
@@ -138,9 +143,10 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
     if (v < n_views) {
         const ViewConst& vc = views[v];
         const uint32_t ci = cluster_pointers[cp];
-        {
+        const uint32_t po = kPacked ? cp_obj[cp] : 0u;
+        if (!kPacked || !(po >> 31)) {   // bit 31: the cluster has no set voxel
             bool oi_cull = false;
-            const uint32_t oi = c2o[ci];
+            const uint32_t oi = kPacked ? po : c2o[ci];
             const tgx_object& od = objects[oi];
             const uint32_t nx = od.n_cluster_pointers_per_dim[0], ny = od.n_cluster_pointers_per_dim[1];
             const uint32_t rel = cp - od.first_cluster_pointer;
@@ -179,7 +185,7 @@ __global__ void __launch_bounds__(256, 4) k_vis_cluster_setup(
                 if (out) oi_cull = true;
             }
 
-            if (!oi_cull) {
+            if (!kPacked && !oi_cull) {
                 // a cluster without set bits never writes (its DDA finds nothing)
                 const uint4* w = reinterpret_cast<const uint4*>(bits + (uint64_t)ci * 16u);
                 const uint4 a = w[0], b = w[1], c = w[2], d = w[3];
@@ -702,11 +708,22 @@ __device__ __forceinline__ float max_near_quot(float ox, float oy, float oz, flo
 // word or ~0.  The DDA's per-axis steps 1/|d| are |ix| etc. exactly: a
 // correctly rounded 1/(-d) is the negated 1/d.  The first voxel is tested
 // before the DDA's start distances are computed: a hit there never reads them.
+// 2^-k when f = 2^k with 2^-k a normal float, else 0.  For such f,
+// RN(v * 2^-k) equals RN(v / f) for every v: both round the same exact real
+// once (zeros, infinities and subnormal results included; a NaN stays a NaN).
+__device__ __forceinline__ float pow2_reciprocal(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = b >> 23;   // sign 0 and biased exponent
+    return (b & 0x7fffffu) == 0u && e >= 1u && e <= 253u ? __uint_as_float((254u - e) << 23) : 0.0f;
+}
+
 template <bool kCount = false>
 __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float oz, float dx, float dy, float dz,
                                                        float ix, float iy, float iz, bool sure_hit,
                                                        const uint32_t* __restrict__ w, uint32_t cluster_pointer,
-                                                       float far_plane, uint32_t* overrun, uint32_t* work = nullptr)
+                                                       float far_plane, float far_rcp, uint32_t* overrun,
+                                                       uint32_t* work = nullptr)
 {
     float enter;
     if (sure_hit) {
@@ -765,7 +782,8 @@ __device__ __forceinline__ unsigned long long vis_pair(float ox, float oy, float
     const float fx0 = (float)x, fy0 = (float)y, fz0 = (float)z;
     const float ve = max_near_quot(ox, oy, oz, dx, dy, dz, ix, iy, iz, fx0, fy0, fz0, (float)(x + 1), (float)(y + 1),
                                    (float)(z + 1));
-    const float depth = gmax(0.0f, xdiv(ve, far_plane));
+    // a power-of-two far plane (far_rcp != 0) divides by one exact product
+    const float depth = gmax(0.0f, far_rcp != 0.0f ? xmul(ve, far_rcp) : xdiv(ve, far_plane));
     if (!(depth <= 1.0f)) return ULLONG_MAX;
     const unsigned long long d24 = __float2uint_rz(xmul(depth, 16777215.0f));   // < 2^24
     return (d24 << 40) | ((unsigned long long)cluster_pointer << 9) | (unsigned long long)rvi;
@@ -918,6 +936,17 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     const bool scan_all = J.counters[C_OVERFLOW] != 0u;
     const uint32_t begin = scan_all ? 0u : si.y;
     const uint32_t end = scan_all ? J.counters[C_RECORDS] : si.y + si.z;
+    if (!scan_all && si.z == 0u) {
+        // no entry: the tile is only cleared (no ray set-up, no barrier; the same in every thread)
+        uint32_t v = 0;
+        while (v + 1 < J.n_views && J.views[v + 1].tile_base <= tile) v++;
+        const ViewConst& vc = J.views[v];
+        const uint32_t lt = tile - vc.tile_base;
+        const uint32_t px = (lt % vc.tiles_x) * vc.tile_w + threadIdx.x % vc.tile_w;
+        const uint32_t py = (lt / vc.tiles_x) * vc.tile_h + threadIdx.x / vc.tile_w;
+        if (px < vc.width && py < vc.height) J.outs[v][(size_t)py * vc.width + px] = ULLONG_MAX;
+        return true;
+    }
     if (threadIdx.x == 0) {
         if (!scan_all && end > begin) stage_entries(sm, J.entries + begin, min(J.batch, end - begin), J.extra_tx);
         uint32_t v = 0;
@@ -936,7 +965,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t* const q = sm.queue(warp);
     float* const qf = (float*)q;
-    const float far_plane = vc.far_plane;
+    const float far_plane = vc.far_plane, far_rcp = pow2_reciprocal(far_plane);
     const TileEntry* const E = sm.stage();
     const uint32_t drain = J.drain;
 
@@ -1051,7 +1080,7 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
                 const unsigned long long w = vis_pair<kCount>(
                     te.ox, te.oy, te.oz, qf[0 * kQueue + e], qf[1 * kQueue + e], qf[2 * kQueue + e],
                     qf[3 * kQueue + e], qf[4 * kQueue + e], qf[5 * kQueue + e], (pk >> 11) != 0u, te.bits,
-                    te.cluster_pointer, far_plane, &J.counters[C_DDA_OVERRUN], work);
+                    te.cluster_pointer, far_plane, far_rcp, &J.counters[C_DDA_OVERRUN], work);
                 if (w != ULLONG_MAX) atomicMin(sm.best() + ((warp << 5) | (pk & 31u)), w);
             }
             qh = (qh + take) & (kQueue - 1u);
@@ -1292,10 +1321,10 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
     if (phase != VIS_FROM_BINS) {
         TGX_CUDA(cudaMemsetAsync(w.counters, 0, C_COUNT * sizeof(uint32_t), c->stream));
         const uint32_t setup_blocks = (uint32_t)((n_pairs + 255) / 256);
-        TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup,
-                   s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->n_cluster_pointers, d_vc, n_views,
-                   w.records, w.rects, w.rec_cap, w.counters, w.bucket_cnt, n_tiles * (kMaxBuckets >> bshift),
-                   c->d_status);
+        TGX_LAUNCH(c, TR_VIS_SETUP, setup_blocks, 256, 0, k_vis_cluster_setup<true>,
+                   s->d_objects, s->d_cluster_pointers, s->d_c2o, s->d_bits, s->d_cp_obj, s->n_cluster_pointers,
+                   d_vc, n_views, w.records, w.rects, w.rec_cap, w.counters, w.bucket_cnt,
+                   n_tiles * (kMaxBuckets >> bshift), c->d_status);
         // each later pass is a programmatic dependent of the one before
         TGX_LAUNCH_PDL(c, TR_VIS_COUNT, warp_grid, 256, 0, k_vis_count, w.records, w.rects, w.counters, w.rec_cap,
                        s->d_objects, d_vc, w.bucket_cnt, n_tiles, bshift);
@@ -1331,13 +1360,13 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
         TGX_TRY(devbuf_reserve(c->vis_work, W_COUNT * sizeof(unsigned long long)));
         J.work = (unsigned long long*)c->vis_work.ptr;
         TGX_CUDA(cudaMemsetAsync(J.work, 0, W_COUNT * sizeof(unsigned long long), c->stream));
-        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 20, true>), J, c->d_status);
+        if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 16, true>), J, c->d_status);
         else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<128, 10, true>), J, c->d_status);
         else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<256, 5, true>), J, c->d_status);
         else TGX_LAUNCH(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<512, 2, true>), J, c->d_status);
         return TGX_OK;
     }
-    if (threads == 64) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 20>), J, c->d_status);
+    if (threads == 64) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<64, 16>), J, c->d_status);
     else if (threads == 128) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<128, 10>), J, c->d_status);
     else if (threads == 256) TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<256, 5>), J, c->d_status);
     else TGX_LAUNCH_PDL(c, TR_VIS_TILES, n_tiles, threads, smem, (k_vis_tiles<512, 2>), J, c->d_status);
@@ -1362,7 +1391,7 @@ static uint32_t vis_queue_per_sm()
 tgx_status vis_prepare_device(tgx_ctx* c)
 {
     const uint32_t threads = c->tile_w * c->tile_h;
-    const uint32_t per_sm = threads == 64 ? vis_queue_per_sm<64, 20>() : threads == 128 ? vis_queue_per_sm<128, 10>()
+    const uint32_t per_sm = threads == 64 ? vis_queue_per_sm<64, 16>() : threads == 128 ? vis_queue_per_sm<128, 10>()
                           : threads == 256 ? vis_queue_per_sm<256, 5>() : vis_queue_per_sm<512, 2>();
     c->vis_tile_ctas = (uint32_t)c->num_sms * per_sm;
     return TGX_OK;
@@ -1377,7 +1406,7 @@ static tgx_status vis_launch_queue(tgx_ctx* c, const TileJob* d_jobs, uint32_t n
     const uint32_t threads = c->tile_w * c->tile_h, smem = tile_smem_bytes(threads);
     const uint32_t grid = std::max(1u, std::min(c->vis_tile_ctas, total));
 #define QUEUE_ARGS d_jobs, n_jobs, total, d_queue, c->d_status
-    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<64, 20>), QUEUE_ARGS);
+    if (threads == 64) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<64, 16>), QUEUE_ARGS);
     else if (threads == 128) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<128, 10>), QUEUE_ARGS);
     else if (threads == 256) TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<256, 5>), QUEUE_ARGS);
     else TGX_LAUNCH(c, TR_VIS_TILES, grid, threads, smem, (k_vis_tiles_queue<512, 2>), QUEUE_ARGS);
@@ -2043,9 +2072,9 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     // everything else is written before it is read
     NA_LAUNCH((n_objects + 127) / 128, 128, k_vis_noalloc_setup, vc, (unsigned long long*)d_visbuf, d_vc, d_outs,
               counters, status, d_objects, n_objects, inv_rot);
-    NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup, d_objects, d_cluster_pointers,
-              d_cluster_idx_to_object_idx, d_voxel_bits, n_cluster_pointers, d_vc, 1u, records, rects,
-              kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kNaBuckets, status);
+    NA_LAUNCH((n_cluster_pointers + 255) / 256, 256, k_vis_cluster_setup<false>, d_objects, d_cluster_pointers,
+              d_cluster_idx_to_object_idx, d_voxel_bits, (const uint32_t*)nullptr, n_cluster_pointers, d_vc, 1u,
+              records, rects, kNaMaxClusterPointers, counters, bucket_cnt, n_tiles * kNaBuckets, status);
     NA_LAUNCH(warp_grid, 256, k_vis_count, records, rects, counters, kNaMaxClusterPointers, d_objects, d_vc, bucket_cnt,
               n_tiles, 1u);
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
