@@ -236,18 +236,24 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const uint32_t* oc
         const int32_t cur0 = prev + (a2 ? r.st[2] : a1 ? r.st[1] : r.st[0]);
         int32_t cs[3] = {am == 0 ? cur0 : r.c[0], am == 1 ? cur0 : r.c[1], am == 2 ? cur0 : r.c[2]};
         if (!occ && (cur0 < 0 || cur0 >= (1 << (s.L - g)))) return 0;
-        // ascend to the level whose parent the step stayed in
-        uint32_t li_u = r.li, g_u = g;
-        int32_t cur = cur0;
-        while (li_u < s.NL - 1) {
-            const uint32_t gp = svo_level_log2(s.L, li_u + 1);
-            const uint32_t shift = gp - g_u;
-            if ((prev >> shift) == (cur >> shift)) break;
-            prev >>= shift; cur >>= shift;
-            cs[0] >>= shift; cs[1] >>= shift; cs[2] >>= shift;
-            li_u++;
-            g_u = gp;
+        // ascend to the level whose parent the step stayed in: the lowest level
+        // li_u >= li whose parent (log2 size gp) holds both the old and the new
+        // cell, i.e. gp > g + the highest bit in which their coordinates differ,
+        // or the root level.  The same level the one-level-at-a-time climb
+        // finds (checked exhaustively for L = 7..14), without a loop whose trip
+        // count differs between the lanes of a warp.  Only taken for a step
+        // that stays inside the cube (prev, cur0 >= 0).
+        uint32_t li_u = r.li;
+        const uint32_t diff = (uint32_t)(prev ^ cur0);
+        if (diff) {
+            const uint32_t need = g + 32u - (uint32_t)__clz((int)diff);   // the parent's log2 size must reach this
+            uint32_t lp = need <= 2u ? 1u : need == 3u ? 2u : (need + 2u) >> 1;   // first level that large
+            if (need > s.L - 1u) lp = s.NL;                                       // none below the root
+            li_u = min(s.NL - 1u, max(r.li, lp - 1u));
         }
+        const uint32_t g_u = svo_level_log2(s.L, li_u);
+        const uint32_t up = g_u - g;
+        cs[0] >>= up; cs[1] >>= up; cs[2] >>= up;
         // keep one candidate; entering a 32^3 block loads its slot
         const uint32_t tv_c = occ && g == 5u
             ? __ldg(&s.table[((uint64_t)r.c[2] * s.B + (uint64_t)r.c[1]) * s.B + (uint64_t)r.c[0]]) : r.tv;
