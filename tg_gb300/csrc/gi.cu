@@ -268,12 +268,16 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
                                                                   unsigned long long* __restrict__ work)
 {
     __shared__ uint32_t occ_off[16];
+    __shared__ LevelDesc lv[16];
+    __shared__ uint8_t first_level[kFirstLevelSize];
     __shared__ RayState ring[kTraceWarps][kRing];
     __shared__ uint32_t ring_item[kTraceWarps][kRing];
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int i = 0; i < 16; i++) occ_off[i] = s.occ_off[i];
     }
+    __syncthreads();
+    svo_level_tables(s.L, s.NL, s.B, s.occ, s.pool, s.sub, occ_off, lv, first_level);
     __syncthreads();
     const uint32_t n = *n_dev;
     const uint32_t n_a = n * mul_a, n_tot = n_a + n * mul_b;
@@ -333,7 +337,7 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
         __syncwarp();
         if (!__any_sync(0xffffffffu, have) && drained && count == 0) break;
         if (have) {
-            const int res = svo_trace_run(s, occ_off, r, max_steps, steps_per_round);
+            const int res = svo_trace_run(s, lv, first_level, r, max_steps, steps_per_round);
             if (res != kTraceRunning) {
                 if (res < 0) atomicAdd(exhausted, 1u);
                 write_hit(item < n_a ? &ha[item] : &hb[item - n_a], res, r);

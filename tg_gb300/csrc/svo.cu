@@ -1039,6 +1039,16 @@ __global__ void __launch_bounds__(128) k_svo_trace(SvoDev s, uint32_t n, const f
                                                   float* __restrict__ out_t, int32_t* __restrict__ out_voxel,
                                                   uint32_t* __restrict__ n_exhausted)
 {
+    __shared__ uint32_t occ_off[16];
+    __shared__ LevelDesc lv[16];
+    __shared__ uint8_t first_level[kFirstLevelSize];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) occ_off[k] = s.occ_off[k];
+    }
+    __syncthreads();
+    svo_level_tables(s.L, s.NL, s.B, s.occ, s.pool, s.sub, occ_off, lv, first_level);
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float oi[3] = {o[3 * i], o[3 * i + 1], o[3 * i + 2]};
@@ -1046,7 +1056,7 @@ __global__ void __launch_bounds__(128) k_svo_trace(SvoDev s, uint32_t n, const f
     float t;
     int32_t c[3], ax;
     uint32_t steps;
-    const int r = svo_trace(s, oi, di, max_steps, t, c, ax, steps);
+    const int r = svo_trace(s, lv, first_level, oi, di, max_steps, t, c, ax, steps);
     if (r == 1) {
         out_t[i] = t;
         out_voxel[3 * i] = c[0] + (int32_t)s.mn[0];

@@ -88,6 +88,60 @@ struct RayState
 
 constexpr int kTraceRunning = -2;
 
+// One traversal level, for the step loop: where its occupancy bits are and
+// how a cell's coordinates index them, so a step looks them up instead of
+// deriving them from the level's log2 size each time.  Built per launch in
+// shared memory (svo_level_tables).
+struct LevelDesc
+{
+    const uint32_t* base;   // occupancy words: the pyramid level (g >= 5), or those of block slot 1 (g < 5)
+    uint32_t stride;        // words per block slot (g < 5; the cell's words are base + (tv - 1) * stride), else 0
+    uint32_t m, mk;         // cells per axis of the indexed array, and the coordinate mask (all ones above g = 5)
+    uint32_t g;             // log2 of the cell size
+    uint32_t g_child;       // log2 of the cell size one level down (li - 1; 0 at li = 0)
+    uint32_t pad;
+};
+constexpr uint32_t kFirstLevelSize = 48;   // first_level[need]: need = g + the bit length of a coordinate step
+
+// Fills lv[0 .. 15] and first_level[0 .. kFirstLevelSize) for SVO s, threads
+// 0 .. kFirstLevelSize - 1 of the block; occ_off: the pyramid level offsets
+// (a copy in shared memory, or s.occ_off); the caller synchronises.
+// first_level[k] is the first traversal level whose cells have log2 size >= k,
+// or NL when none below the root does (k > L - 1).
+__device__ __forceinline__ void svo_level_tables(const uint32_t L, const uint32_t NL, const uint32_t B,
+                                                 const uint32_t* occ, const uint32_t* pool, const uint32_t* sub,
+                                                 const uint32_t* occ_off, LevelDesc* lv, uint8_t* first_level)
+{
+    const uint32_t i = threadIdx.x;
+    if (i < 16u) {
+        LevelDesc d = {};
+        if (i < NL) {
+            const uint32_t g = svo_level_log2(L, i);
+            d.g = g;
+            d.g_child = svo_level_log2(L, i ? i - 1u : 0u);
+            if (g >= 5u) {
+                d.base = occ + occ_off[(g - 5u) & 15u];
+                d.stride = 0u;
+                d.m = B >> (g - 5u);
+                d.mk = 0xffffffffu;
+            } else {
+                d.base = g == 0u ? pool : sub + (g == 3u ? 16u : 0u);
+                d.stride = g == 0u ? 1024u : 32u;
+                d.m = 32u >> g;
+                d.mk = d.m - 1u;
+            }
+        }
+        lv[i] = d;
+    }
+    if (i < kFirstLevelSize) {
+        uint32_t f = NL;
+        if (i <= L - 1u)
+            for (uint32_t li = 0; li < NL; li++)
+                if (svo_level_log2(L, li) >= i) { f = li; break; }
+        first_level[i] = (uint8_t)f;
+    }
+}
+
 // Occupancy bit of cell c (grid coordinates at log2 size g); tv is the slot +
 // 1 of the 32^3 block holding c, needed below the block level (g < 5).
 __device__ __forceinline__ bool svo_occupied(const SvoDev& s, const uint32_t* occ_off, uint32_t g, const int32_t c[3],
@@ -193,25 +247,22 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* 
 // does one occupancy load and computes both the descent into the child cell
 // and the step to the neighbour cell, then keeps one, so the lanes of a warp
 // stay on one instruction stream whichever way their rays go.
-__device__ __forceinline__ int svo_trace_run(const SvoDev& s, const uint32_t* occ_off, RayState& r,
-                                             uint32_t max_steps, uint32_t n)
+__device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* lv, const uint8_t* first_level,
+                                             RayState& r, uint32_t max_steps, uint32_t n)
 {
     for (uint32_t k = 0; k < n; k++) {
         if (r.steps >= max_steps) return -1;
         r.steps++;
+        const LevelDesc& ld = lv[r.li & 15u];
         const uint32_t g = r.g;
         // occupancy of the current cell
-        const bool sub = g < 5u;
-        const uint32_t m = sub ? (32u >> g) : (s.B >> (g - 5u));
-        const uint32_t mk = sub ? m - 1u : 0xffffffffu;
+        const uint32_t m = ld.m, mk = ld.mk;
         const uint32_t v = (((uint32_t)r.c[2] & mk) * m + ((uint32_t)r.c[1] & mk)) * m + ((uint32_t)r.c[0] & mk);
-        const uint32_t* base = !sub ? s.occ + occ_off[(g - 5u) & 15u]
-                             : g == 0 ? s.pool + (uint64_t)(r.tv - 1u) * 1024u
-                                      : s.sub + (uint64_t)(r.tv - 1u) * 32u + (g == 3 ? 16u : 0u);
+        const uint32_t* base = ld.base + (uint64_t)(r.tv - 1u) * ld.stride;
         const bool occ = (__ldg(&base[v >> 5]) >> (v & 31u)) & 1u;
         if (occ && r.li == 0) return 1;
         // candidate 1: descend, the child cell by point location
-        const uint32_t g_c = svo_level_log2(s.L, r.li ? r.li - 1u : 0u);
+        const uint32_t g_c = ld.g_child;
         const uint32_t sh_c = g - g_c;
         const float isz = __int_as_float((int)((127u - g_c) << 23));
         int32_t cd[3];
@@ -247,11 +298,10 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const uint32_t* oc
         const uint32_t diff = (uint32_t)(prev ^ cur0);
         if (diff) {
             const uint32_t need = g + 32u - (uint32_t)__clz((int)diff);   // the parent's log2 size must reach this
-            uint32_t lp = need <= 2u ? 1u : need == 3u ? 2u : (need + 2u) >> 1;   // first level that large
-            if (need > s.L - 1u) lp = s.NL;                                       // none below the root
+            const uint32_t lp = first_level[min(need, kFirstLevelSize - 1u)];   // first level that large, or NL
             li_u = min(s.NL - 1u, max(r.li, lp - 1u));
         }
-        const uint32_t g_u = svo_level_log2(s.L, li_u);
+        const uint32_t g_u = lv[li_u & 15u].g;
         const uint32_t up = g_u - g;
         cs[0] >>= up; cs[1] >>= up; cs[2] >>= up;
         // keep one candidate; entering a 32^3 block loads its slot
@@ -269,13 +319,14 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const uint32_t* oc
 }
 
 // Whole-ray form.  Returns 1 on hit (t, grid voxel c, face axis or -1), 0 on
-// miss, -1 when max_steps ran out.
-static __device__ int svo_trace(const SvoDev& s, const float o[3], const float d[3], uint32_t max_steps, float& out_t,
-                                int32_t out_c[3], int32_t& out_axis, uint32_t& out_steps)
+// miss, -1 when max_steps ran out.  lv, first_level: svo_level_tables.
+static __device__ int svo_trace(const SvoDev& s, const LevelDesc* lv, const uint8_t* first_level, const float o[3],
+                                const float d[3], uint32_t max_steps, float& out_t, int32_t out_c[3],
+                                int32_t& out_axis, uint32_t& out_steps)
 {
     RayState r;
     int res = svo_trace_begin(s, s.occ_off, o, d, max_steps, r);
-    if (res == kTraceRunning) res = svo_trace_run(s, s.occ_off, r, max_steps, 0xffffffffu);
+    if (res == kTraceRunning) res = svo_trace_run(s, lv, first_level, r, max_steps, 0xffffffffu);
     out_steps = r.steps;
     if (res == 1) {
         out_t = r.t;
