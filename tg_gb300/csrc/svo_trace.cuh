@@ -82,7 +82,7 @@ struct RayState
     float t;
     int32_t c[3];
     int32_t last_axis;
-    uint32_t li, g, steps;    // level, log2 of its cell size, steps used
+    uint32_t li, steps;       // level (its cell size: svo_level_log2), steps used
     uint32_t tv;              // slot + 1 of the 32^3 block the sub-block levels (g < 5) are inside
 };
 
@@ -92,14 +92,17 @@ constexpr int kTraceRunning = -2;
 // how a cell's coordinates index them, so a step looks them up instead of
 // deriving them from the level's log2 size each time.  Built per launch in
 // shared memory (svo_level_tables).
-struct LevelDesc
+struct alignas(16) LevelDesc
 {
     const uint32_t* base;   // occupancy words: the pyramid level (g >= 5), or those of block slot 1 (g < 5)
     uint32_t stride;        // words per block slot (g < 5; the cell's words are base + (tv - 1) * stride), else 0
-    uint32_t m, mk;         // cells per axis of the indexed array, and the coordinate mask (all ones above g = 5)
+    uint32_t m;             // cells per axis of the indexed array
+    uint32_t mk;            // coordinate mask (all ones above g = 5)
     uint32_t g;             // log2 of the cell size
-    uint32_t g_child;       // log2 of the cell size one level down (li - 1; 0 at li = 0)
-    uint32_t pad;
+    uint32_t sh_c;          // g minus the log2 cell size one level down (0 at li = 0)
+    float inv_child;        // 2^-(log2 cell size one level down), exact
+    float size;             // 2^g, exact
+    uint32_t pad[3];
 };
 constexpr uint32_t kFirstLevelSize = 48;   // first_level[need]: need = g + the bit length of a coordinate step
 
@@ -117,8 +120,11 @@ __device__ __forceinline__ void svo_level_tables(const uint32_t L, const uint32_
         LevelDesc d = {};
         if (i < NL) {
             const uint32_t g = svo_level_log2(L, i);
+            const uint32_t g_c = svo_level_log2(L, i ? i - 1u : 0u);
             d.g = g;
-            d.g_child = svo_level_log2(L, i ? i - 1u : 0u);
+            d.sh_c = g - g_c;
+            d.inv_child = __int_as_float((int)((127u - g_c) << 23));
+            d.size = (float)(1u << g);
             if (g >= 5u) {
                 d.base = occ + occ_off[(g - 5u) & 15u];
                 d.stride = 0u;
@@ -200,11 +206,11 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* 
     if (!(r.t < t1)) return 0;
     r.last_axis = t0 > 0.0f ? entry_axis : -1;
     r.li = s.NL - 1;
-    r.g = s.L - 1u;
     r.tv = 0;
     if (max_steps < s.NL) {   // the budget could run out inside the descent: run it
-        const float isz = __int_as_float((int)((127u - r.g) << 23));
-        const int32_t hi = (1 << (s.L - r.g)) - 1;
+        const uint32_t g_root = s.L - 1u;
+        const float isz = __int_as_float((int)((127u - g_root) << 23));
+        const int32_t hi = (1 << (s.L - g_root)) - 1;
 #pragma unroll
         for (int a = 0; a < 3; a++) r.c[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], 0, hi);
         return kTraceRunning;
@@ -226,17 +232,16 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* 
     if (e < 0) {   // the descent reaches the voxel: NL iterations, a hit
         r.steps = s.NL;
         r.li = 0;
-        r.g = 0;
         r.tv = tv;
         r.c[0] = cv[0]; r.c[1] = cv[1]; r.c[2] = cv[2];
         return 1;
     }
     r.li = (uint32_t)e;
-    r.g = svo_level_log2(s.L, (uint32_t)e);
-    r.tv = r.g < 5u ? tv : 0u;
+    const uint32_t ge = svo_level_log2(s.L, (uint32_t)e);
+    r.tv = ge < 5u ? tv : 0u;
     r.steps = s.NL - 1u - (uint32_t)e;
 #pragma unroll
-    for (int a = 0; a < 3; a++) r.c[a] = cv[a] >> r.g;
+    for (int a = 0; a < 3; a++) r.c[a] = cv[a] >> ge;
     return kTraceRunning;
 }
 
@@ -254,7 +259,7 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
         if (r.steps >= max_steps) return -1;
         r.steps++;
         const LevelDesc& ld = lv[r.li & 15u];
-        const uint32_t g = r.g;
+        const uint32_t g = ld.g;
         // occupancy of the current cell
         const uint32_t m = ld.m, mk = ld.mk;
         const uint32_t v = (((uint32_t)r.c[2] & mk) * m + ((uint32_t)r.c[1] & mk)) * m + ((uint32_t)r.c[0] & mk);
@@ -262,9 +267,8 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
         const bool occ = (__ldg(&base[v >> 5]) >> (v & 31u)) & 1u;
         if (occ && r.li == 0) return 1;
         // candidate 1: descend, the child cell by point location
-        const uint32_t g_c = ld.g_child;
-        const uint32_t sh_c = g - g_c;
-        const float isz = __int_as_float((int)((127u - g_c) << 23));
+        const uint32_t sh_c = ld.sh_c;
+        const float isz = ld.inv_child;
         int32_t cd[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -272,7 +276,7 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
             cd[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), isz, r.st[a], lo, hi);
         }
         // candidate 2: step through the nearest face
-        const float size = (float)(1u << g);
+        const float size = ld.size;
         float tn[3];
 #pragma unroll
         for (int a = 0; a < 3; a++)
@@ -301,8 +305,7 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
             const uint32_t lp = first_level[min(need, kFirstLevelSize - 1u)];   // first level that large, or NL
             li_u = min(s.NL - 1u, max(r.li, lp - 1u));
         }
-        const uint32_t g_u = lv[li_u & 15u].g;
-        const uint32_t up = g_u - g;
+        const uint32_t up = lv[li_u & 15u].g - g;
         cs[0] >>= up; cs[1] >>= up; cs[2] >>= up;
         // keep one candidate; entering a 32^3 block loads its slot
         const uint32_t tv_c = occ && g == 5u
@@ -311,7 +314,6 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
         r.t = occ ? r.t : (tam > r.t ? tam : r.t);
         r.last_axis = occ ? r.last_axis : am;
         r.li = occ ? r.li - 1u : li_u;
-        r.g = occ ? g_c : g_u;
 #pragma unroll
         for (int a = 0; a < 3; a++) r.c[a] = occ ? cd[a] : cs[a];
     }
