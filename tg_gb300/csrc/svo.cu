@@ -403,12 +403,14 @@ __device__ __forceinline__ uint32_t pair_voxels(const PairBox& b)
 
 // One CTA per block slot.  The block's pairs are taken 32 at a time: their
 // trimmed voxel counts are measured first (a lane per pair) and sorted by a
-// warp bitonic sort, then warp w voxelises the chunk's pairs of rank w and
-// 31 - w (the heaviest with the lightest), so the warps' shares of voxels are
-// close and the CTA's final barrier waits less.  Within a pair, lanes walk
-// its voxels; each voxel is the reference's corner lerp and bit fetch.  The
-// block image and the material codes are merged with atomicOr / a 16-bit max
-// in shared memory, so the order of the pairs changes no bit.
+// warp bitonic sort, heaviest first; the warps then take pairs in that order
+// from a shared counter, the next one whenever they finish one, so the CTA's
+// final barrier waits little.  Within a pair, a lane takes a row (iy, iz) of
+// the trimmed box: the reference's z- and y-lerps once per row, the x-lerp,
+// the [0, 8)^3 test and the bit fetch per voxel, the cluster's bit words and
+// material bytes from shared memory.  The block image and the material codes
+// are merged with atomicOr / a 16-bit max in shared memory, so the order of
+// the pairs changes no bit.
 template <bool kMat>
 __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     const tgx_object* __restrict__ objects, const uint32_t* __restrict__ cluster_pointers,
@@ -419,7 +421,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
     constexpr uint32_t kOrderCap = 32 * kWarpsPerVoxCta * 2;   // pairs ordered per round
     extern __shared__ __align__(16) uint32_t s_blk[];   // 1024 bit words, then 16384 words of u16 codes
     __shared__ uint32_t s_cw[kWarpsPerVoxCta][16];       // each warp's current cluster bits
+    __shared__ uint4 s_cm[kMat ? kWarpsPerVoxCta : 1][32];  // and its 512 material bytes
     __shared__ uint16_t s_order[kOrderCap];              // per chunk of 32: pair offsets, heaviest first
+    __shared__ uint32_t s_next;                          // the next entry of s_order to take
     uint32_t* img = s_blk;
     uint32_t* smat = s_blk + kBlockWords;
     const uint32_t slot = blockIdx.x;
@@ -458,12 +462,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
             // descending rank 31 - lane
             s_order[ch * 32u + (31u - lane)] = (uint16_t)(key >= 0 ? idx : 0xffffu);
         }
+        if (threadIdx.x == 0) s_next = 0u;
         __syncthreads();
-        for (uint32_t ch = 0; ch < n_chunks; ch++) {
-#pragma unroll 1
-            for (uint32_t h = 0; h < 2; h++) {
-                const uint32_t r = h == 0 ? wid : 31u - wid;
-                const uint32_t k = s_order[ch * 32u + r];
+        // warps take the round's pairs heaviest first (each chunk of 32 is sorted), the
+        // next one whenever they finish one, so the block's warps end close together
+        for (;;) {
+            uint32_t item = 0;
+            if (lane == 0) item = atomicAdd(&s_next, 1u);
+            item = __shfl_sync(0xffffffffu, item, 0);
+            if (item >= n_chunks * 32u) break;
+            {
+                const uint32_t k = s_order[item];
                 if (k == 0xffffu) continue;
                 PairBox bx;
                 pair_box(objects, cluster_pointers, c2o, sorted[r0 + k], mnx, mny, mnz, B, bx);
@@ -487,22 +496,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
                 // the cluster's 16 bit words, one shared-memory lookup per voxel
                 __syncwarp();
                 if (lane < 16) s_cw[wid][lane] = bits[(uint64_t)ci * 16u + lane];
+                if (kMat) s_cm[wid][lane] = reinterpret_cast<const uint4*>(material + (uint64_t)ci * 512u)[lane];
                 __syncwarp();
-                // t -> (ix, iy, iz) without integer division: t < 2^15 and nx, ny <= 32,
-                // so (t + 0.5) / n lies at least 0.5 / n from an integer while the
-                // float product's error stays below 2^15 / n * 2^-23; truncation is exact
-                const float rnx = 1.0f / (float)nx, rny = 1.0f / (float)ny;
-                for (uint32_t t = lane; t < total; t += 32) {
-                    const uint32_t q1 = (uint32_t)(((float)t + 0.5f) * rnx);
-                    const uint32_t q2 = (uint32_t)(((float)q1 + 0.5f) * rny);
-                    const uint32_t ix = x0 + (t - q1 * nx), iy = y0 + (q1 - q2 * ny), iz = z0 + q2;
+                // a lane per row (iy, iz) of the trim box: the z- and y-lerps of
+                // tg__construct_leaf_node depend on the row only, so they are evaluated
+                // once per row and the x-lerp per voxel; the same operations on the same
+                // values as per voxel.  row -> (iy, iz) without integer division: row <
+                // 2^10 and ny <= 32, so (row + 0.5) / ny lies at least 0.5 / ny from an
+                // integer while the float product's error stays far below that
+                const uint32_t nz = bx.z1 - z0, rows = ny * nz;
+                const float rny = 1.0f / (float)ny;
+                for (uint32_t row = lane; row < rows; row += 32) {
+                    const uint32_t q = (uint32_t)(((float)row + 0.5f) * rny);
+                    const uint32_t iy = y0 + (row - q * ny), iz = z0 + q;
                     // (i + 0.5) / 32 is an exact scaling: the reciprocal multiply gives the same bits
                     const float tz = p32 ? xmul(xadd((float)iz, 0.5f), 0.03125f) : xdiv(xadd((float)iz, 0.5f), pext.z);
                     const float omtz = xsub(1.0f, tz);
                     const float ty = p32 ? xmul(xadd((float)iy, 0.5f), 0.03125f) : xdiv(xadd((float)iy, 0.5f), pext.y);
                     const float omty = xsub(1.0f, ty);
-                    const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
-                    const float omtx = xsub(1.0f, tx);
 #define LZ(i, j, comp) xadd(xmul(omtz, bc[i].comp), xmul(tz, bc[j].comp))
                     const float pz0x = LZ(0, 4, x), pz0y = LZ(0, 4, y), pz0z = LZ(0, 4, z);
                     const float pz1x = LZ(1, 5, x), pz1y = LZ(1, 5, y), pz1z = LZ(1, 5, z);
@@ -515,19 +526,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
                     const float py1x = xadd(xmul(omty, pz1x), xmul(ty, pz3x));
                     const float py1y = xadd(xmul(omty, pz1y), xmul(ty, pz3y));
                     const float py1z = xadd(xmul(omty, pz1z), xmul(ty, pz3z));
-                    const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
-                    if (cx < 0.0f || cx >= 8.0f) continue;
-                    const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
-                    if (cy < 0.0f || cy >= 8.0f) continue;
-                    const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
-                    if (cz < 0.0f || cz >= 8.0f) continue;
-                    const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
-                    const uint32_t word = s_cw[wid][rvi >> 5];
-                    if (word & (1u << (rvi & 31u))) {
-                        const uint32_t bvi = (uint32_t)xadd(xadd(xmul(xmul(pext.x, pext.y), (float)iz),
-                                                                 xmul(pext.x, (float)iy)), (float)ix);
-                        atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
-                        if (kMat) smem_max_u16(smat, bvi, ((lut << 8) | material[(uint64_t)ci * 512u + rvi]) + 1u);
+                    // the row's first voxel index (an exact small-integer float expression)
+                    const float row_base = xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy));
+                    for (uint32_t ix = x0; ix < x0 + nx; ix++) {
+                        const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
+                        const float omtx = xsub(1.0f, tx);
+                        const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
+                        if (cx < 0.0f || cx >= 8.0f) continue;
+                        const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
+                        if (cy < 0.0f || cy >= 8.0f) continue;
+                        const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
+                        if (cz < 0.0f || cz >= 8.0f) continue;
+                        const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
+                        const uint32_t word = s_cw[wid][rvi >> 5];
+                        if (word & (1u << (rvi & 31u))) {
+                            const uint32_t bvi = (uint32_t)xadd(row_base, (float)ix);
+                            atomicOr(&img[bvi >> 5], 1u << (bvi & 31u));
+                            if (kMat)
+                                smem_max_u16(smat, bvi,
+                                             ((lut << 8) | reinterpret_cast<const uint8_t*>(s_cm[wid])[rvi]) + 1u);
+                        }
                     }
                 }
             }
