@@ -290,15 +290,16 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
             phase ^= 1u;
             fence_after();
             if (l < 4) {
-                float v[16];
-#pragma unroll 1
-                for (int q = 0; q < 4; q++) {
-                    ld16(lanes + q * 16, v);
+                // the 64 accumulator columns in one TMEM round trip
+                {
+                    float v[64];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) ld16(lanes + q * 16, v + 16 * q);
                     ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.0f);
-                    put8(ga + A1, 2 * q, (int)gt, v);
-                    put8(ga + A1, 2 * q + 1, (int)gt, v + 8);
+                    for (int j = 0; j < 64; j++) v[j] = fmaxf(v[j], 0.0f);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) put8(ga + A1, q, (int)gt, v + 8 * q);
                 }
                 fence_async_smem();
             } else {
@@ -491,23 +492,23 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
                 commit(b);
             }
             if (!(ok = sync_mma(50 + l, tile))) break;
-            float v[16];
             if (l < 4) {
+                // the 64 accumulator columns in one TMEM round trip
                 unsigned char* h = sm + tt::H + l * tt::TILE64;
+                float v[64];
+#pragma unroll
+                for (int q = 0; q < 4; q++) ld16(lanes + tt::ACC + q * 16, v + 16 * q);
+                ld_wait();
                 mask[l][0] = mask[l][1] = 0u;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    ld16(lanes + tt::ACC + q * 16, v);
-                    ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        v[j] = fmaxf(v[j], 0.0f);
-                        if (v[j] > 0.0f) mask[l][q >> 1] |= 1u << ((q & 1) * 16 + j);
-                    }
-                    put8(h, 2 * q, (int)t, v);
-                    put8(h, 2 * q + 1, (int)t, v + 8);
+                for (int j = 0; j < 64; j++) {
+                    v[j] = fmaxf(v[j], 0.0f);
+                    if (v[j] > 0.0f) mask[l][j >> 5] |= 1u << (j & 31);
                 }
+#pragma unroll
+                for (int q = 0; q < 8; q++) put8(h, q, (int)t, v + 8 * q);
             } else {
+                float v[16];
                 ld16(lanes + tt::ACC, v);
                 ld_wait();
                 y[0] = v[0]; y[1] = v[1]; y[2] = v[2];
@@ -567,17 +568,14 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
             // mask with relu'(z) of the layer's input and store the next delta into the other tile
             const int ml = 3 - s;                           // h_{ml+1} = input of W_{4-s}
             unsigned char* dout = sm + ((s & 1) ? tt::DB : tt::DA);
-            float v[16];
+            float v[64];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                ld16(lanes + tt::ACC + q * 16, v);
-                ld_wait();
-                const uint32_t m = mask[ml][q >> 1] >> ((q & 1) * 16);
+            for (int q = 0; q < 4; q++) ld16(lanes + tt::ACC + q * 16, v + 16 * q);
+            ld_wait();
 #pragma unroll
-                for (int j = 0; j < 16; j++) v[j] = ((m >> j) & 1u) && valid ? v[j] : 0.0f;
-                put8(dout, 2 * q, (int)t, v);
-                put8(dout, 2 * q + 1, (int)t, v + 8);
-            }
+            for (int j = 0; j < 64; j++) v[j] = ((mask[ml][j >> 5] >> (j & 31)) & 1u) && valid ? v[j] : 0.0f;
+#pragma unroll
+            for (int q = 0; q < 8; q++) put8(dout, q, (int)t, v + 8 * q);
         }
         acc_g = 1u;
     }
