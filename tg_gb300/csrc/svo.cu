@@ -528,15 +528,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerVoxCta) k_svo_voxelize(
                     const float py1z = xadd(xmul(omty, pz1z), xmul(ty, pz3z));
                     // the row's first voxel index (an exact small-integer float expression)
                     const float row_base = xadd(xmul(xmul(pext.x, pext.y), (float)iz), xmul(pext.x, (float)iy));
-                    for (uint32_t ix = x0; ix < x0 + nx; ix++) {
-                        const float tx = p32 ? xmul(xadd((float)ix, 0.5f), 0.03125f) : xdiv(xadd((float)ix, 0.5f), pext.x);
+                    // with a 32-voxel side, tx = (ix + 0.5) / 32 is a multiple of 2^-6 below 1, so
+                    // adding 1/32 per voxel is exact: the same bits as the product
+                    float tx32 = xmul(xadd((float)x0, 0.5f), 0.03125f);
+                    for (uint32_t ix = x0; ix < x0 + nx; ix++, tx32 = xadd(tx32, 0.03125f)) {
+                        const float tx = p32 ? tx32 : xdiv(xadd((float)ix, 0.5f), pext.x);
                         const float omtx = xsub(1.0f, tx);
                         const float cx = xadd(xmul(omtx, py0x), xmul(tx, py1x));
-                        if (cx < 0.0f || cx >= 8.0f) continue;
                         const float cy = xadd(xmul(omtx, py0y), xmul(tx, py1y));
-                        if (cy < 0.0f || cy >= 8.0f) continue;
                         const float cz = xadd(xmul(omtx, py0z), xmul(tx, py1z));
-                        if (cz < 0.0f || cz >= 8.0f) continue;
+                        // one test for the three components (a NaN passes, as in the per-axis form)
+                        if (cx < 0.0f || cx >= 8.0f || cy < 0.0f || cy >= 8.0f || cz < 0.0f || cz >= 8.0f) continue;
                         const uint32_t rvi = 64u * (uint32_t)cz + 8u * (uint32_t)cy + (uint32_t)cx;
                         const uint32_t word = s_cw[wid][rvi >> 5];
                         if (word & (1u << (rvi & 31u))) {
