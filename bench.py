@@ -711,7 +711,9 @@ def run_case(case: str, variant: str, spp: int, local: int) -> None:
 
     svo-build     two 4096^3 SVO builds of the 512-object scene (profile the second)
     train-step    cache training steps of 32,768 synthetic samples (3 warm-up, 20 timed)
-    cached-frame  60 warm-up cached-GI frames, then one more (profile the last)"""
+    cached-frame  60 warm-up cached-GI frames, then one more (profile the last)
+    gi-frame      three plain 1-bounce 4-spp GI frames of the bench view, 8 traversal steps
+                  per round (two k_trace_queue launches each: bounce rays, then sun rays)"""
     import torch
     import tg_gb300 as tg
 
@@ -731,6 +733,22 @@ def run_case(case: str, variant: str, spp: int, local: int) -> None:
             res["blocks"], res["pairs"] = int(info.n_blocks), int(info.n_pairs)
             if k == 0:
                 svo.close()
+    elif case == "gi-frame":
+        sc = ctx.upload(make_scene())
+        view = make_view()
+        vis = torch.empty(W * H, dtype=torch.int64, device="cuda")
+        ctx.vis_render(sc, view, [vis])
+        svo = ctx.svo_build(sc, (-2048.0, -2048.0, -2048.0), 12)
+        rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+        ctx.set_trace_steps(8)
+        params = tg.gi_params(spp=4, bounces=1, seed=2, max_steps=256)
+        n0 = ctx.launches()
+        for _ in range(3):
+            ctx.gi_render(sc, svo, view, vis, params, rgb)
+        ctx.sync()
+        res["frame_launches"] = (ctx.launches() - n0) // 3
+        gw = ctx.gi_work()
+        res["gi_work_last_frame"] = {"dda_steps": int(gw.dda_steps), "rays": int(gw.rays)}
     elif case == "train-step":
         n = 32768
         rng = np.random.default_rng(3)
@@ -795,7 +813,7 @@ def main() -> None:
     ap.add_argument("--tile", default="auto", help="WxH screen tile, or 'auto' to run the autotuner")
     ap.add_argument("--launch", choices=["graph", "calls"], default="graph",
                     help="time the frame as one CUDA graph replay (tgx_frame_graph) or as separate launches")
-    ap.add_argument("--case", choices=["svo-build", "train-step", "cached-frame"],
+    ap.add_argument("--case", choices=["svo-build", "train-step", "cached-frame", "gi-frame"],
                     help="run only one small workload for a profiler (see run_case) and exit")
     ap.add_argument("--case-variant", default="configured_training", choices=sorted(CACHE_VARIANTS))
     ap.add_argument("--case-spp", type=int, default=3)

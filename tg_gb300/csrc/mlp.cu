@@ -585,25 +585,30 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     fence_after();
     float* P = partial + (uint64_t)cta * N_PARAMS;
     {
-        float v[16];
 #pragma unroll 1
-        for (int blk = 0; blk < 6; blk++) {
-            const uint32_t col = blk == 0 ? tt::G0A : blk == 1 ? tt::G0B : blk == 2 ? tt::G1 : blk == 3 ? tt::G2
-                               : blk == 4 ? tt::G3 : tt::G4;
+        for (int blk = 0; blk < 5; blk++) {
+            const uint32_t col = blk == 0 ? tt::G0A : blk == 1 ? tt::G0B : blk == 2 ? tt::G1 : blk == 3 ? tt::G2 : tt::G3;
             const int i = (blk == 1 ? 128 : 0) + (int)t;                  // layer input (TMEM row)
             const int ni = blk < 2 ? NE : NH;
-            const int off = blk < 2 ? OFF_W0 : blk == 2 ? OFF_W1 : blk == 3 ? OFF_W2 : blk == 4 ? OFF_W3 : OFF_W4;
-            const int nq = blk == 5 ? 1 : 4;
-#pragma unroll 1
-            for (int q = 0; q < nq; q++) {
-                ld16(lanes + col + q * 16, v);
-                ld_wait();
-                if (i < ni) {
-                    const int no = blk == 5 ? NO : 16;
+            const int off = blk < 2 ? OFF_W0 : blk == 2 ? OFF_W1 : blk == 3 ? OFF_W2 : OFF_W3;
+            // the block's 64 columns in one TMEM round trip
+            float v[64];
 #pragma unroll
-                    for (int j = 0; j < 16; j++)
-                        if (j < no) P[off + (q * 16 + j) * ni + i] = ok && acc_g ? v[j] : 0.0f;
-                }
+            for (int q = 0; q < 4; q++) ld16(lanes + col + q * 16, v + 16 * q);
+            ld_wait();
+            if (i < ni) {
+#pragma unroll
+                for (int j = 0; j < 64; j++) P[off + j * ni + i] = ok && acc_g ? v[j] : 0.0f;
+            }
+        }
+        {   // dW4^T: 3 real columns
+            float v[16];
+            ld16(lanes + tt::G4, v);
+            ld_wait();
+            const int i = (int)t;
+            if (i < NH) {
+#pragma unroll
+                for (int j = 0; j < NO; j++) P[OFF_W4 + j * NH + i] = ok && acc_g ? v[j] : 0.0f;
             }
         }
     }
@@ -627,6 +632,16 @@ __device__ __forceinline__ float sum_slices(const float* __restrict__ partial, u
 {
     float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     uint32_t c = 0;
+    // 32 loads in flight, then the same additions in the same order as the 8-wide loop below
+    for (; c + 32 <= n_parts; c += 32) {
+        float x[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) x[j] = partial[(uint64_t)(c + j) * N_PARAMS + p];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[j] += x[8 * q + j];
+    }
     for (; c + 8 <= n_parts; c += 8) {
         float x[8];
 #pragma unroll
