@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(32 * kTraceWarps) k_trace_queue(SvoDev s, cons
             RayState rs;
             if (it < n_tot) {
                 const Ray ray = it < n_a ? ra[it] : rb[it - n_a];
-                const int res = svo_trace_begin(s, occ_off, ray.o, ray.d, max_steps, rs);
+                const int res = svo_trace_begin(s, occ_off, lv, ray.o, ray.d, max_steps, rs);
                 if (res == kTraceRunning) {
                     running = true;
                 } else {

@@ -174,8 +174,8 @@ __device__ __forceinline__ bool svo_occupied(const SvoDev& s, const uint32_t* oc
 // one.  The descent's iterations are counted into r.steps as if they had
 // run, so every result and the step budget stay those of the top-down walk.
 // occ_off: the pyramid level offsets (shared memory in the persistent kernel).
-__device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* occ_off, const float o[3],
-                                               const float d[3], uint32_t max_steps, RayState& r)
+__device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* occ_off, const LevelDesc* lv,
+                                               const float o[3], const float d[3], uint32_t max_steps, RayState& r)
 {
     const float E = (float)(1u << s.L);
 #pragma unroll
@@ -220,15 +220,23 @@ __device__ __forceinline__ int svo_trace_begin(const SvoDev& s, const uint32_t* 
 #pragma unroll
     for (int a = 0; a < 3; a++) cv[a] = svo_cell_at(xadd(r.og[a], xmul(r.t, r.d[a])), 1.0f, r.st[a], 0, vhi);
     const uint32_t tv = __ldg(&s.table[((uint64_t)(cv[2] >> 5) * s.B + (uint64_t)(cv[1] >> 5)) * s.B + (uint64_t)(cv[0] >> 5)]);
-    // coarsest empty level holding the point (-1: the voxel itself is set)
-    int32_t e = -1;
-    for (uint32_t li = 0; li < s.NL; li++) {
-        const uint32_t g = svo_level_log2(s.L, li);
-        const int32_t c[3] = {cv[0] >> g, cv[1] >> g, cv[2] >> g};
-        const bool occ = g < 5u && tv == 0u ? false : svo_occupied(s, occ_off, g, c, tv);
-        if (occ) break;
-        e = (int32_t)li;
+    // coarsest empty level holding the point (-1: the voxel itself is set): the
+    // levels below the lowest occupied one.  All levels' bits are loaded at once
+    // (at most 8 levels for L <= 14) rather than one level per dependent step.
+    uint32_t occ_mask = 0;
+#pragma unroll
+    for (uint32_t li = 0; li < 8u; li++) {
+        if (li >= s.NL) break;   // the same in every lane
+        const LevelDesc& ld = lv[li];
+        const uint32_t g = ld.g;
+        if (g < 5u && tv == 0u) continue;   // below an unallocated block: empty
+        const uint32_t m = ld.m, mk = ld.mk;
+        const uint32_t v = ((((uint32_t)cv[2] >> g) & mk) * m + (((uint32_t)cv[1] >> g) & mk)) * m +
+                           (((uint32_t)cv[0] >> g) & mk);
+        const uint32_t* base = ld.base + (uint64_t)(tv - 1u) * ld.stride;
+        if ((__ldg(&base[v >> 5]) >> (v & 31u)) & 1u) occ_mask |= 1u << li;
     }
+    const int32_t e = occ_mask ? __ffs((int)occ_mask) - 2 : (int32_t)s.NL - 1;
     if (e < 0) {   // the descent reaches the voxel: NL iterations, a hit
         r.steps = s.NL;
         r.li = 0;
@@ -327,7 +335,7 @@ static __device__ int svo_trace(const SvoDev& s, const LevelDesc* lv, const uint
                                 int32_t& out_axis, uint32_t& out_steps)
 {
     RayState r;
-    int res = svo_trace_begin(s, s.occ_off, o, d, max_steps, r);
+    int res = svo_trace_begin(s, s.occ_off, lv, o, d, max_steps, r);
     if (res == kTraceRunning) res = svo_trace_run(s, lv, first_level, r, max_steps, 0xffffffffu);
     out_steps = r.steps;
     if (res == 1) {
