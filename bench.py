@@ -609,17 +609,7 @@ def bench_large(local: int):
     import tg_gb300 as tg
 
     res = {}
-    ctx = tg.Context(local, tile=(8, 16))
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    free0 = torch.cuda.mem_get_info()[0]
-    # the store is generated in device memory (tgx_generate_scene_device), byte-equal to the host generator
-    t0 = time.perf_counter()
-    sc = ctx.generate_scene(0, 4096, 16, 16, seed=5, bernoulli_p=0.3, box_min=(-4096.0,) * 3,
-                            box_max=(4096.0,) * 3, n_luts=32)
-    ctx.sync()
-    res["generate_on_device_s"] = round(time.perf_counter() - t0, 2)
-    res["clusters"] = 4096 * 16 ** 3
-    res["scene_gib"] = round(res["clusters"] * (64 + 512) / 2**30, 2)
+    gen = dict(seed=5, bernoulli_p=0.3, box_min=(-4096.0,) * 3, box_max=(4096.0,) * 3, n_luts=32)
     rng = np.random.default_rng(5)
     sizes = [(3840, 2160), (2560, 1440), (1920, 1080), (1920, 1080), (1280, 720), (1280, 720), (640, 480), (320, 240)]
     views = np.concatenate([tg.make_view(tuple(rng.uniform(-2048.0, 2048.0, 3)), float(rng.uniform(-0.3, 0.3)),
@@ -627,6 +617,27 @@ def bench_large(local: int):
                             for w, h in sizes])
     outs = [torch.empty(w * h, dtype=torch.int64, device="cuda") for w, h in sizes]
     pixels = sum(w * h for w, h in sizes)
+    # the visibility settings tuned on this workload (each candidate context generates its own store)
+    from tg_gb300.autotune import tune_workload
+
+    def make_frame(c):
+        s = c.generate_scene(0, 4096, 16, 16, **gen)
+        return (lambda: c.vis_render(s, views, outs)), s.close
+
+    vis_cfg, vis_times = tune_workload(make_frame, local, frames=2)
+    res["vis_tuning"] = {"tile": f"{vis_cfg['tile'][0]}x{vis_cfg['tile'][1]}", "depth_buckets": vis_cfg["depth_buckets"],
+                         "batch": vis_cfg["batch"], "drain": vis_cfg["drain"], "autotune_ms": vis_times}
+    ctx = tg.Context(local, tile=vis_cfg["tile"])
+    ctx.set_vis_tuning(vis_cfg["depth_buckets"], vis_cfg["batch"], vis_cfg["drain"])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    free0 = torch.cuda.mem_get_info()[0]
+    # the store is generated in device memory (tgx_generate_scene_device), byte-equal to the host generator
+    t0 = time.perf_counter()
+    sc = ctx.generate_scene(0, 4096, 16, 16, **gen)
+    ctx.sync()
+    res["generate_on_device_s"] = round(time.perf_counter() - t0, 2)
+    res["clusters"] = 4096 * 16 ** 3
+    res["scene_gib"] = round(res["clusters"] * (64 + 512) / 2**30, 2)
     with torch.cuda.stream(stream):
         for _ in range(2):
             ctx.vis_render(sc, views, outs)
