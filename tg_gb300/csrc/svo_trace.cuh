@@ -303,7 +303,7 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
         // li_u >= li whose parent (log2 size gp) holds both the old and the new
         // cell, i.e. gp > g + the highest bit in which their coordinates differ,
         // or the root level.  The same level the one-level-at-a-time climb
-        // finds (checked exhaustively for L = 7..14), without a loop whose trip
+        // finds (checked exhaustively for L = 6..14), without a loop whose trip
         // count differs between the lanes of a warp.  Only taken for a step
         // that stays inside the cube (prev, cur0 >= 0).
         uint32_t li_u = r.li;
