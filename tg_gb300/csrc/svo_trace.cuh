@@ -62,10 +62,19 @@ __device__ __forceinline__ uint32_t svo_material(const SvoDev& s, int32_t cx, in
     return s.mat[(uint64_t)(tv - 1) * 32768u + v];
 }
 
+// The cell of coordinate p at cells of size 1/inv_size, a point on a cell
+// border going to the lower cell when the ray steps down, clamped to
+// [lo, hi].  For |x| < 2^30 (always, for rays inside the cube) the floor is an
+// exact integer and the clamp is done on integers; NaN and larger values take
+// the float form, whose results the integer form equals wherever both apply.
 __device__ __forceinline__ int32_t svo_cell_at(float p, float inv_size, int32_t step, int32_t lo, int32_t hi)
 {
     const float x = xmul(p, inv_size);
     float f = floorf(x);
+    if (fabsf(x) < 1073741824.0f) {
+        const int32_t c = (int32_t)f - ((step < 0 && x == f) ? 1 : 0);
+        return min(max(c, lo), hi);
+    }
     if (step < 0 && x == f) f = xsub(f, 1.0f);
     int32_t c = (int32_t)f;
     if (f < (float)lo) c = lo;
@@ -287,9 +296,12 @@ __device__ __forceinline__ int svo_trace_run(const SvoDev& s, const LevelDesc* l
         const float size = ld.size;
         float tn[3];
 #pragma unroll
-        for (int a = 0; a < 3; a++)
-            tn[a] = r.st[a] > 0 ? xmul(xsub(xmul((float)(r.c[a] + 1), size), r.og[a]), r.inv[a])
-                  : r.st[a] < 0 ? xmul(xsub(xmul((float)r.c[a], size), r.og[a]), r.inv[a]) : F32_MAX_TG;
+        for (int a = 0; a < 3; a++) {
+            // the face the ray leaves through: c + 1 going up, c going down (one product chain per axis)
+            const float face = (float)(r.c[a] + ((r.st[a] + 1) >> 1));
+            const float tf = xmul(xsub(xmul(face, size), r.og[a]), r.inv[a]);
+            tn[a] = r.st[a] != 0 ? tf : F32_MAX_TG;
+        }
         const bool a1 = tn[1] < tn[0];
         const float t01 = a1 ? tn[1] : tn[0];
         const bool a2 = tn[2] < t01;
