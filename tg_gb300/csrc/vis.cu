@@ -23,16 +23,15 @@
 //                           64-byte bitmask, as a 96-byte entry into each of its
 //                           (tile, bucket) bins, so every tile's entries are
 //                           contiguous and run near to far.
-//   6. k_vis_tiles          persistent, warp-specialised: per CTA a producer
-//      warp takes tiles from a queue (heaviest first) and bulk-copies batches
-//      of their entries into a two-stage shared-memory ring (cp.async.bulk on
-//      mbarriers); the tile's pixel warps, one thread per pixel, skip entries
-//      whose depth bound cannot beat the pixel's word, reject clear misses
-//      with a conservative reciprocal slab test, compact the surviving
-//      (pixel, cluster) pairs by warp ballot, and run the shader's exact
-//      ray/box test and DDA on full warps of pairs, keeping each pixel's
-//      minimum packed depth|pointer|voxel word (shared atomicMin); every
-//      pixel is written once (fused clear).
+//   6. k_vis_tiles          one CTA per tile (heaviest first), one thread per
+//      pixel: batches of the tile's entries arrive by one cp.async.bulk each
+//      on an mbarrier; every pixel skips entries whose depth bound cannot beat
+//      its word and rejects clear misses with a conservative reciprocal slab
+//      test; the surviving (pixel, cluster) pairs are compacted by warp ballot
+//      and run the shader's exact ray/box test and DDA on full warps, keeping
+//      each pixel's minimum packed depth|pointer|voxel word (shared
+//      atomicMin); every pixel is written once (fused clear).
+//      k_vis_tiles_queue is the persistent form over many jobs' tiles.
 //
 // Every pair evaluates the same binary32 operations in the same order as the
 // CPU oracle's transcription of visibility.frag, so the buffer is bit-exact.
