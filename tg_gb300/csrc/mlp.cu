@@ -328,8 +328,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
 // Training on tcgen05: forward, backward and weight gradients in one kernel
 // ---------------------------------------------------------------------------
 //
-// One CTA of 128 threads per SM works through tiles of 128 samples; thread t
-// owns sample t (row t of the forward and backward GEMMs, TMEM lane t).  All
+// One CTA of 128 * CS threads per SM works through tiles of 128 samples;
+// thread t owns sample t mod 128 (row t mod 128 of the forward and backward
+// GEMMs, TMEM lane t mod 128) and the 64 / CS accumulator columns of its
+// part t / 128: the CS warps of a TMEM lane quarter split each epilogue and
+// the feature encoding, so more warps hide each other's latency.  All
 // operands stay in shared memory in the core-matrix layout the forward uses
 // ([column group][row group][8 rows x 16 B]).  The backward reads the
 // forward's weight tiles, and the weight gradients read the activation and
@@ -351,7 +354,10 @@ namespace tt {
 
 using tc::KG0;
 using tc::KGH;
-constexpr int THREADS = 128;
+constexpr int CS = 2;                                 // threads per sample (column parts)
+constexpr int CW = 64 / CS;                           // accumulator columns per thread
+constexpr int THREADS = 128 * CS;
+static_assert(CW % 16 == 0 && CW <= 32, "column parts");
 constexpr int W0 = 0;                                 // [28 kg][8 ng][128 B]
 constexpr int W1 = W0 + KG0 * 8 * 128;                // [8 kg][8 ng][128 B] x 3 (W1, W2, W3)
 constexpr int W4 = W1 + 3 * KGH * 8 * 128;            // [8 kg][2 ng][128 B] (16 rows, 3 real)
@@ -410,6 +416,9 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     const uint32_t cta = blockIdx.x - (second ? jobs.j[1].first_cta : jobs.j[0].first_cta);
     const uint32_t n_ctas = second ? jobs.j[1].n_ctas : jobs.j[0].n_ctas;
     const uint32_t t = threadIdx.x, warp = t >> 5;
+    const uint32_t r = t & 127u;                 // the thread's sample row of a tile and TMEM lane
+    const uint32_t part = t >> 7;                // its accumulator columns [part * CW, part * CW + CW)
+    constexpr int CW = tt::CW;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tt::BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + tt::BAR + 16);
     stage_weights(sm + tt::W0, wimg + B_W0, S0, NH, NH, KG0);
@@ -431,7 +440,8 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lanes = tmem + ((warp * 32u) << 16);   // this warp's 32 lanes
+    const uint32_t lanes = tmem + (((warp & 3u) * 32u) << 16);   // this warp's 32 lanes
+    const uint32_t cols = part * (uint32_t)CW;                    // its first accumulator column
     const uint32_t b = saddr(bar);
     const uint32_t x0 = saddr(sm + tt::X0), hb = saddr(sm + tt::H), da = saddr(sm + tt::DA), db = saddr(sm + tt::DB);
     const uint32_t w0 = saddr(sm + tt::W0), w1 = saddr(sm + tt::W1), w4 = saddr(sm + tt::W4);
@@ -458,16 +468,16 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
         __syncthreads();
     };
     for (uint32_t tile = cta; tile < tiles && ok; tile += n_ctas) {
-        const uint32_t row = tile * 128 + t;
+        const uint32_t row = tile * 128 + r;
         const bool valid = row < n;
-#pragma unroll
-        for (int i = 0; i < NI; i++) encode_input(sm + tt::X0, i, (int)t, valid ? x[(uint64_t)row * NI + i] : 0.0f);
-        {
+        for (int i = (int)part; i < NI; i += tt::CS)
+            encode_input(sm + tt::X0, i, (int)r, valid ? x[(uint64_t)row * NI + i] : 0.0f);
+        if (part == tt::CS - 1) {
             const float z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            put8(sm + tt::X0, KG0 - 1, (int)t, z);   // features 216..223
+            put8(sm + tt::X0, KG0 - 1, (int)r, z);   // features 216..223
         }
         // ---- forward ----
-        uint32_t mask[4][2];
+        uint32_t mask[4];   // relu'(z) of the thread's columns per hidden layer
         float y[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
         for (int l = 0; l < 5 && ok; l++) {
@@ -493,21 +503,21 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
             }
             if (!(ok = sync_mma(50 + l, tile))) break;
             if (l < 4) {
-                // the 64 accumulator columns in one TMEM round trip
+                // the thread's accumulator columns in one TMEM round trip
                 unsigned char* h = sm + tt::H + l * tt::TILE64;
-                float v[64];
+                float v[CW];
 #pragma unroll
-                for (int q = 0; q < 4; q++) ld16(lanes + tt::ACC + q * 16, v + 16 * q);
+                for (int q = 0; q < CW / 16; q++) ld16(lanes + tt::ACC + cols + q * 16, v + 16 * q);
                 ld_wait();
-                mask[l][0] = mask[l][1] = 0u;
+                mask[l] = 0u;
 #pragma unroll
-                for (int j = 0; j < 64; j++) {
+                for (int j = 0; j < CW; j++) {
                     v[j] = fmaxf(v[j], 0.0f);
-                    if (v[j] > 0.0f) mask[l][j >> 5] |= 1u << (j & 31);
+                    if (v[j] > 0.0f) mask[l] |= 1u << j;
                 }
 #pragma unroll
-                for (int q = 0; q < 8; q++) put8(h, q, (int)t, v + 8 * q);
-            } else {
+                for (int q = 0; q < CW / 8; q++) put8(h, (int)(cols / 8) + q, (int)r, v + 8 * q);
+            } else if (part == 0) {
                 float v[16];
                 ld16(lanes + tt::ACC, v);
                 ld_wait();
@@ -516,7 +526,7 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
         }
         if (!ok) break;
         // ---- output delta (relative L2), into DB ----
-        {
+        if (part == 0) {
             float d[16];
 #pragma unroll
             for (int j = 0; j < 16; j++) d[j] = 0.0f;
@@ -530,8 +540,8 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
                     d[c] = 2.0f * res / den * inv;
                 }
             }
-            put8(sm + tt::DB, 0, (int)t, d);
-            put8(sm + tt::DB, 1, (int)t, d + 8);
+            put8(sm + tt::DB, 0, (int)r, d);
+            put8(sm + tt::DB, 1, (int)r, d + 8);
         }
         // ---- backward: stage s propagates through W_{4-s} and accumulates its gradient ----
 #pragma unroll
@@ -568,14 +578,14 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
             // mask with relu'(z) of the layer's input and store the next delta into the other tile
             const int ml = 3 - s;                           // h_{ml+1} = input of W_{4-s}
             unsigned char* dout = sm + ((s & 1) ? tt::DB : tt::DA);
-            float v[64];
+            float v[CW];
 #pragma unroll
-            for (int q = 0; q < 4; q++) ld16(lanes + tt::ACC + q * 16, v + 16 * q);
+            for (int q = 0; q < CW / 16; q++) ld16(lanes + tt::ACC + cols + q * 16, v + 16 * q);
             ld_wait();
 #pragma unroll
-            for (int j = 0; j < 64; j++) v[j] = ((mask[ml][j >> 5] >> (j & 31)) & 1u) && valid ? v[j] : 0.0f;
+            for (int j = 0; j < CW; j++) v[j] = ((mask[ml] >> j) & 1u) && valid ? v[j] : 0.0f;
 #pragma unroll
-            for (int q = 0; q < 8; q++) put8(dout, q, (int)t, v + 8 * q);
+            for (int q = 0; q < CW / 8; q++) put8(dout, (int)(cols / 8) + q, (int)r, v + 8 * q);
         }
         acc_g = 1u;
     }
@@ -588,24 +598,24 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
 #pragma unroll 1
         for (int blk = 0; blk < 5; blk++) {
             const uint32_t col = blk == 0 ? tt::G0A : blk == 1 ? tt::G0B : blk == 2 ? tt::G1 : blk == 3 ? tt::G2 : tt::G3;
-            const int i = (blk == 1 ? 128 : 0) + (int)t;                  // layer input (TMEM row)
+            const int i = (blk == 1 ? 128 : 0) + (int)r;                  // layer input (TMEM row)
             const int ni = blk < 2 ? NE : NH;
             const int off = blk < 2 ? OFF_W0 : blk == 2 ? OFF_W1 : blk == 3 ? OFF_W2 : OFF_W3;
-            // the block's 64 columns in one TMEM round trip
-            float v[64];
+            // the thread's columns of the block in one TMEM round trip
+            float v[CW];
 #pragma unroll
-            for (int q = 0; q < 4; q++) ld16(lanes + col + q * 16, v + 16 * q);
+            for (int q = 0; q < CW / 16; q++) ld16(lanes + col + cols + q * 16, v + 16 * q);
             ld_wait();
             if (i < ni) {
 #pragma unroll
-                for (int j = 0; j < 64; j++) P[off + j * ni + i] = ok && acc_g ? v[j] : 0.0f;
+                for (int j = 0; j < CW; j++) P[off + ((int)cols + j) * ni + i] = ok && acc_g ? v[j] : 0.0f;
             }
         }
-        {   // dW4^T: 3 real columns
+        if (part == 0) {   // dW4^T: 3 real columns
             float v[16];
             ld16(lanes + tt::G4, v);
             ld_wait();
-            const int i = (int)t;
+            const int i = (int)r;
             if (i < NH) {
 #pragma unroll
                 for (int j = 0; j < NO; j++) P[OFF_W4 + j * NH + i] = ok && acc_g ? v[j] : 0.0f;
@@ -614,7 +624,7 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if ((t & 31) == 0) atomicAdd(loss, lsum * inv);
+    if ((t & 31) == 0 && part == 0) atomicAdd(loss, lsum * inv);
     if (!ok) wait(b, phase);   // let MMAs still in flight land (bounded) before the columns are freed
     fence_before();
     __syncthreads();
