@@ -136,16 +136,29 @@ def test_pipelined_host_buffers_equal_the_oracle(ctx, oracle):
 def test_large_frame_scan_path_equals_small_frames():
     """More than 512 groups of 256 tiles (here two 2048x1088 views in 8x4 tiles,
     139,264 tiles) take the one-CTA scan + finalize; each view alone (272
-    groups) takes the direct finalize.  Both give the same buffers."""
+    groups) takes the direct finalize.  Both give the same buffers, and so
+    does the render into pinned host buffers (written by the tile kernel
+    directly), through either scan."""
+    import torch
     s = fuzz_scene(41, n_objects=12, box=50.0, max_cpa=5)
     views = [tg.make_view((0.0, 5.0, -90.0), 0.05, float(np.pi), 1.1, 2048, 1088, 0.1, 300.0),
              tg.make_view((20.0, -5.0, 80.0), -0.1, 0.2, 0.9, 2048, 1088, 0.1, 300.0)]
     with tg.Context(0, tile=(8, 4)) as c:
         together = render(c, s, np.concatenate(views))
         alone = [render(c, s, v)[0] for v in views]
-    for a, b in zip(together, alone):
+        sc = c.upload(s)
+        pinned = [torch.zeros(2048 * 1088, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+                  for _ in views]
+        c.vis_render_host(sc, np.concatenate(views), pinned)
+        one = torch.zeros(2048 * 1088, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        c.vis_render_host(sc, views[1], [one])
+        assert c.device_error().code == 0
+        sc.close()
+    for a, b, h in zip(together, alone, pinned):
         assert_same(a, b)
+        assert_same(h, b)
         assert (a != EMPTY).sum() > 10000
+    assert_same(one, alone[1])
 
 
 def test_host_buffers_and_pick(ctx, oracle):
