@@ -15,11 +15,16 @@
 //   k_mlp_train_tc  training: forward, relative-L2 output delta, backward and
 //                   the weight gradients of 128-sample tiles in one kernel;
 //                   gradients summed in TMEM over a CTA's tiles, then written
-//                   to the CTA's slice of a partial buffer.
+//                   to the CTA's slice of a partial buffer, its loss beside
+//                   them.
 //   k_mlp_adam      sums the slices in a fixed order (deterministic), then
 //                   Adam on the FP32 master weights; refreshes the BF16
-//                   image the kernels stage from.
-//   k_mlp_reduce    the same sum into the gradient, for tgx_cache_gradient.
+//                   image the kernels stage from; sums the CTAs' losses.
+//   k_mlp_reduce    the same sums into the gradient and the loss, for
+//                   tgx_cache_gradient.
+// A training step's two launches are programmatic dependents of the kernel
+// before them (the step's inputs, or the previous step's Adam), so each
+// launch overlaps the previous kernel's drain.
 
 #include "tgx_internal.cuh"
 
@@ -347,8 +352,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_mlp_forward_tc(const __nv_bf
 //             tile's rows as the rest of M; those accumulator rows are never
 //             read out.
 // At the end each CTA writes its summed gradient into its own slice of a
-// partial buffer, and k_mlp_reduce adds the slices in a fixed order, so a
-// training step is deterministic.
+// partial buffer (and its share of the loss after the n_ctas slices), and
+// k_mlp_reduce adds the slices in a fixed order, so a training step is
+// deterministic.
 
 namespace tt {
 
@@ -393,8 +399,7 @@ struct TrainJob
     const __nv_bfloat16* wimg;
     const float* x;
     const float* target;
-    float* partial;
-    float* loss;
+    float* partial;              // n_ctas gradient slices, then n_ctas losses
     uint32_t n, first_cta, n_ctas;
 };
 struct TrainJobs
@@ -411,7 +416,6 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     const float* x = second ? jobs.j[1].x : jobs.j[0].x;
     const float* target = second ? jobs.j[1].target : jobs.j[0].target;
     float* partial = second ? jobs.j[1].partial : jobs.j[0].partial;
-    float* loss = second ? jobs.j[1].loss : jobs.j[0].loss;
     const uint32_t n = second ? jobs.j[1].n : jobs.j[0].n;
     const uint32_t cta = blockIdx.x - (second ? jobs.j[1].first_cta : jobs.j[0].first_cta);
     const uint32_t n_ctas = second ? jobs.j[1].n_ctas : jobs.j[0].n_ctas;
@@ -421,6 +425,9 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     constexpr int CW = tt::CW;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tt::BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + tt::BAR + 16);
+    float* warp_loss = reinterpret_cast<float*>(sm + tt::BAR + 32);   // the 4 sample warps' loss sums
+    pdl_wait();      // the weight image and the batch come from earlier kernels of the stream
+    pdl_trigger();
     stage_weights(sm + tt::W0, wimg + B_W0, S0, NH, NH, KG0);
     stage_weights(sm + tt::W1 + 0 * KGH * 8 * 128, wimg + B_W1, SH, NH, NH, KGH);
     stage_weights(sm + tt::W1 + 1 * KGH * 8 * 128, wimg + B_W2, SH, NH, NH, KGH);
@@ -624,11 +631,13 @@ __global__ void __launch_bounds__(tt::THREADS, 1) k_mlp_train_tc(TrainJobs jobs,
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if ((t & 31) == 0 && part == 0) atomicAdd(loss, lsum * inv);
+    if ((t & 31) == 0 && part == 0) warp_loss[warp] = lsum;
     if (!ok) wait(b, phase);   // let MMAs still in flight land (bounded) before the columns are freed
     fence_before();
     __syncthreads();
     fence_after();
+    if (t == 0)   // this CTA's share of the loss, after the n_ctas gradient slices
+        partial[(uint64_t)n_ctas * N_PARAMS + cta] = (((warp_loss[0] + warp_loss[1]) + warp_loss[2]) + warp_loss[3]) * inv;
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(tt::TMEM_COLS) : "memory");
 }
@@ -667,11 +676,21 @@ __device__ __forceinline__ float sum_slices(const float* __restrict__ partial, u
     return s + tail;
 }
 
-// The slices' sum added to the gradient.
-__global__ void __launch_bounds__(256) k_mlp_reduce(const float* __restrict__ partial, uint32_t n_parts,
-                                                   float* __restrict__ g)
+// The CTAs' losses (after the n_parts gradient slices), added in CTA order.
+__device__ __forceinline__ float sum_losses(const float* __restrict__ partial, uint32_t n_parts)
 {
+    float l = 0.0f;
+    for (uint32_t c = 0; c < n_parts; c++) l += partial[(uint64_t)n_parts * N_PARAMS + c];
+    return l;
+}
+
+// The slices' sum added to the gradient; the loss.
+__global__ void __launch_bounds__(256) k_mlp_reduce(const float* __restrict__ partial, uint32_t n_parts,
+                                                   float* __restrict__ g, float* __restrict__ loss)
+{
+    pdl_wait();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) *loss = sum_losses(partial, n_parts);
     if (p >= N_PARAMS) return;
     g[p] += sum_slices(partial, n_parts, p);
 }
@@ -699,6 +718,7 @@ struct AdamJob
     float* g;
     const float* partial;
     __nv_bfloat16* img;
+    float* loss;
     uint32_t n_parts;
     float c1, c2;
 };
@@ -709,8 +729,9 @@ struct AdamJobs
 
 __global__ void __launch_bounds__(256) k_mlp_adam(AdamJobs jobs, float lr, float b1, float b2, float eps)
 {
+    pdl_wait();      // the training kernel's slices
+    pdl_trigger();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= N_PARAMS) return;
     const AdamJob& J = jobs.j[0];
     const AdamJob& K = jobs.j[1];
     const bool second = blockIdx.y != 0;
@@ -722,6 +743,8 @@ __global__ void __launch_bounds__(256) k_mlp_adam(AdamJobs jobs, float lr, float
     const uint32_t n_parts = second ? K.n_parts : J.n_parts;
     const float c1 = second ? K.c1 : J.c1, c2 = second ? K.c2 : J.c2;
     __nv_bfloat16* img = second ? K.img : J.img;
+    if (p == 0) *(second ? K.loss : J.loss) = sum_losses(partial, n_parts);
+    if (p >= N_PARAMS) return;
     const float gp = g[p] + sum_slices(partial, n_parts, p);
     g[p] = 0.0f;
     const float mp = b1 * m[p] + (1.0f - b1) * gp;
@@ -901,20 +924,18 @@ static tgx_status cache_grad_parts(tgx_ctx* c, tgx_cache* const* k, const uint32
         const uint32_t tiles = (n[i] + 127) / 128;
         const uint32_t share = total <= sms ? tiles : (uint32_t)((uint64_t)tiles * sms / total);
         const uint32_t ctas = std::max(1u, std::min(tiles, share));
-        TGX_TRY(devbuf_reserve(k[i]->scratch, (size_t)ctas * N_PARAMS * 4));
-        TGX_CUDA(cudaMemsetAsync(k[i]->loss, 0, 4, c->stream));
+        TGX_TRY(devbuf_reserve(k[i]->scratch, (size_t)ctas * (N_PARAMS + 1) * 4));
         J.wimg = k[i]->img;
         J.x = d_x[i];
         J.target = d_t[i];
         J.partial = (float*)k[i]->scratch.ptr;
-        J.loss = k[i]->loss;
         J.n = n[i];
         J.first_cta = grid;
         J.n_ctas = ctas;
         parts[i] = ctas;
         grid += ctas;
     }
-    TGX_LAUNCH(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, jobs, c->d_status);
+    TGX_LAUNCH_PDL(c, TR_MLP_FWD_BWD, grid, tt::THREADS, tt::SMEM, k_mlp_train_tc, jobs, c->d_status);
     return TGX_OK;
 }
 
@@ -923,7 +944,8 @@ static tgx_status cache_grad(tgx_ctx* c, tgx_cache* k, uint32_t n, const float* 
 {
     uint32_t parts = 0;
     TGX_TRY(cache_grad_parts(c, &k, &n, &d_x, &d_t, 1, &parts));
-    TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, (const float*)k->scratch.ptr, parts, k->g);
+    TGX_LAUNCH(c, TR_MLP_WGRAD, (N_PARAMS + 255) / 256, 256, 0, k_mlp_reduce, (const float*)k->scratch.ptr, parts, k->g,
+               k->loss);
     return TGX_OK;
 }
 
@@ -955,12 +977,13 @@ tgx_status cache_train_pair(tgx_ctx* c, tgx_cache* const* k, const uint32_t* n, 
         J.w = k[i]->w; J.m = k[i]->m; J.v = k[i]->v; J.g = k[i]->g;
         J.partial = (const float*)k[i]->scratch.ptr;
         J.img = k[i]->img;
+        J.loss = k[i]->loss;
         J.n_parts = parts[i];
         J.c1 = (float)(1.0 - pow((double)b1, (double)k[i]->step));
         J.c2 = (float)(1.0 - pow((double)b2, (double)k[i]->step));
     }
     if (n_nets < 2) jobs.j[1] = jobs.j[0];
-    TGX_LAUNCH(c, TR_MLP_ADAM, dim3((N_PARAMS + 255) / 256, n_nets), 256, 0, k_mlp_adam, jobs, lr, b1, b2, eps);
+    TGX_LAUNCH_PDL(c, TR_MLP_ADAM, dim3((N_PARAMS + 255) / 256, n_nets), 256, 0, k_mlp_adam, jobs, lr, b1, b2, eps);
     return TGX_OK;
 }
 
