@@ -423,5 +423,6 @@ tgx_status cache_infer_counted(tgx_ctx* c, tgx_cache* k, const uint32_t* d_n, ui
 tgx_status vis_prepare_device(tgx_ctx* c);
 // cudaMalloc of one scene-store array, counted against the context's budget
 cudaError_t scene_malloc(tgx_ctx* c, tgx_scene* s, void** p, size_t bytes);
+// host_out: some outputs are pinned host memory the tile kernel writes directly
 tgx_status vis_render_device(tgx_ctx* ctx, const tgx_scene* scene, const tgx_view* views, uint32_t n_views,
-                             uint64_t* const* d_visbuf);
+                             uint64_t* const* d_visbuf, bool host_out = false);

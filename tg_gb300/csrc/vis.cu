@@ -60,7 +60,8 @@ struct alignas(16) VisRecord
 };
 static_assert(sizeof(VisRecord) == 32, "record layout");
 
-enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_TILE_QUEUE = 4, C_COUNT = 8 };
+enum Counter { C_RECORDS = 0, C_ENTRIES = 1, C_DDA_OVERRUN = 2, C_OVERFLOW = 3, C_TILE_QUEUE = 4, C_NONEMPTY = 5,
+               C_COUNT = 8 };
 
 // One binned (tile, cluster) entry as the tile kernel stages it: the record's
 // fields the DDA needs and the cluster's 64-byte bitmask, so a batch of a
@@ -429,6 +430,7 @@ __global__ void __launch_bounds__(1024) k_vis_scan(uint32_t* __restrict__ cta_au
         tile_off[n_tiles] = carry;
         counters[C_ENTRIES] = carry;
         counters[C_OVERFLOW] = carry > bin_capacity ? 1u : 0u;
+        counters[C_NONEMPTY] = n_tiles - cls_tot[0];   // class 0: the tiles without entries
         uint32_t run = 0;   // heaviest class first
         for (int c = (int)kOrderClasses - 1; c >= 0; c--) {
             cls_base[c] = run;
@@ -569,6 +571,7 @@ __global__ void __launch_bounds__(kScanTiles) k_vis_finalize_direct(const uint32
             if (lane + o < 32) suffix += y;
         }
         cur[lane] = suffix - tot + before;
+        if (g == 0 && lane == 0) counters[C_NONEMPTY] = n_tiles - tot;   // class 0: the tiles without entries
     }
     __syncthreads();
     uint32_t base = 0, total = 0;
@@ -835,6 +838,8 @@ struct TileJob
     uint32_t drain;              // live pairs a warp collects before its lanes run their DDAs (1..32)
     uint32_t extra_tx;           // bytes the first batch's barrier expects beyond its copies: 0, or 64
                                  // under TGX_FLAG_TEST_LOST_COPY (its wait then runs out)
+    uint32_t interleave;         // k_vis_tiles: spread the tiles without entries evenly over the launch
+                                 // (outputs in host memory), instead of launching them last
 };
 
 // Shared memory of a tile CTA (dynamic, tile_smem_bytes(threads)):
@@ -1122,6 +1127,19 @@ __device__ __forceinline__ bool vis_tile(const TileJob& J, uint32_t slot, const 
 
 // Instantiated per block size (= tile pixels) so the register budget can be
 // bounded for the occupancy each size needs.  One CTA per tile of one job.
+// The slot (heavy-first order, the tiles without entries last) that CTA b of
+// t takes.  With interleave, the n non-empty tiles keep their order but are
+// spread over the launch, one every t / n CTAs, and the empty ones fill the
+// CTAs between: CTA b is the c(b)-th non-empty one when c(b + 1) > c(b), with
+// c(b) = floor(b n / t), else the (b - c(b))-th empty one.  Both maps are
+// bijections of [0, t).
+__device__ __forceinline__ uint32_t tile_slot(uint32_t b, uint32_t t, uint32_t n, bool interleave)
+{
+    if (!interleave || n >= t) return b;
+    const uint32_t c0 = (uint32_t)((uint64_t)b * n / t), c1 = (uint32_t)((uint64_t)(b + 1) * n / t);
+    return c1 > c0 ? c0 : n + (b - c0);
+}
+
 template <int kThreads, int kMinBlocks, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, tgx_dev_status* __restrict__ status)
 {
@@ -1129,7 +1147,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_vis_tiles(TileJob J, t
     tile_smem_init(sm);
     pdl_wait();
     uint32_t phase = 0;
-    vis_tile<kCount>(J, blockIdx.x, sm, phase, status);
+    const uint32_t slot = J.interleave ? tile_slot(blockIdx.x, J.n_tiles, J.counters[C_NONEMPTY], true) : blockIdx.x;
+    vis_tile<kCount>(J, slot, sm, phase, status);
 }
 
 // Persistent form over several jobs (scenes, each with its views): CTAs take
@@ -1305,13 +1324,15 @@ static TileJob tile_job(const tgx_ctx* c, const tgx_scene* s, const ViewConst* d
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
+    J.interleave = 0;
     return J;
 }
 
 // The launches of one frame (n_views views of scene s, view table d_vc / d_outs
 // on the device): all of them, or the part up to the tile scan, or the rest.
 static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_vc, unsigned long long* const* d_outs,
-                             uint32_t n_views, uint32_t n_tiles, const VisScratch& w, int phase = VIS_ALL)
+                             uint32_t n_views, uint32_t n_tiles, const VisScratch& w, int phase = VIS_ALL,
+                             bool interleave = false)
 {
     const uint64_t n_pairs = (uint64_t)s->n_cluster_pointers * n_views;
     const uint32_t n_scan_ctas = (n_tiles + kScanTiles - 1) / kScanTiles;
@@ -1352,6 +1373,7 @@ static tgx_status vis_launch(tgx_ctx* c, const tgx_scene* s, const ViewConst* d_
                    s->d_bits, n_tiles, w.bin_capacity, bshift, c->d_status);
     if (phase == VIS_NO_TILES) return TGX_OK;
     TileJob J = tile_job(c, s, d_vc, d_outs, n_views, n_tiles, w);
+    J.interleave = interleave ? 1u : 0u;
     if (c->flags & TGX_FLAG_TEST_LOST_COPY) J.extra_tx = 64u;
     const uint32_t threads = c->tile_w * c->tile_h, smem = tile_smem_bytes(threads);
     if (c->vis_count_work) {
@@ -1432,7 +1454,7 @@ static std::vector<unsigned char> vis_view_table(tgx_ctx* c, const tgx_view* vie
 }
 
 tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* views, uint32_t n_views,
-                             uint64_t* const* d_visbuf)
+                             uint64_t* const* d_visbuf, bool host_out)
 {
     if (!c || !s || !d_visbuf) { tgx_set_error("tgx_vis_render: NULL argument"); return TGX_ERR_INVALID_ARGUMENT; }
     TGX_TRY(check_views(views, n_views, c->tile_w, c->tile_h));
@@ -1488,9 +1510,9 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
     w.entries = (TileEntry*)c->vis_bins.ptr;
     vis_carve_tiles(w, (uint32_t*)c->vis_tile_cnt.ptr, (uint32_t*)c->vis_tile_off.ptr, n_tiles);
     if (!exact) {
-        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w));
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_ALL, host_out));
     } else {
-        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_TO_SCAN));
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_TO_SCAN, host_out));
         TGX_CUDA(cudaMemcpyAsync(c->h_vis_counters, w.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
         TGX_CUDA(cudaStreamSynchronize(c->stream));
         const uint32_t entries = ((const uint32_t*)c->h_vis_counters)[C_ENTRIES];
@@ -1500,7 +1522,7 @@ tgx_status vis_render_device(tgx_ctx* c, const tgx_scene* s, const tgx_view* vie
             w.bin_capacity = (uint32_t)std::min<size_t>(c->vis_bins.bytes / kEntry, 0xffffffffu);
             if (entries <= w.bin_capacity) TGX_CUDA(cudaMemsetAsync(w.counters + C_OVERFLOW, 0, 4, c->stream));
         }
-        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_FROM_BINS));
+        TGX_TRY(vis_launch(c, s, d_vc, d_outs, n_views, n_tiles, w, VIS_FROM_BINS, host_out));
     }
     c->vis_last_tiles = n_tiles;
     c->vis_last_pairs = n_pairs;
@@ -1759,6 +1781,14 @@ static uint64_t* mapped_host(const void* p)
     return a.type == cudaMemoryTypeHost && a.devicePointer ? (uint64_t*)a.devicePointer : nullptr;
 }
 
+// whether some output of a host-buffer render is written in host memory directly
+static bool any_mapped(const std::vector<bool>& staged)
+{
+    for (bool st : staged)
+        if (!st) return true;
+    return false;
+}
+
 // Output pointers of a host-buffer render: pinned buffers directly, the rest
 // in `stage` (device memory, `staged` entries) for a copy afterwards.
 static tgx_status host_outputs(tgx_ctx* c, const tgx_view* views, uint32_t n_views, uint64_t* const* h_visbuf,
@@ -1791,7 +1821,7 @@ extern "C" tgx_status tgx_vis_render_host(tgx_ctx* c, const tgx_scene* s, const 
     std::vector<uint64_t*> dptr;
     std::vector<bool> staged;
     TGX_TRY(host_outputs(c, views, n_views, h_visbuf, c->host_stage, dptr, staged, "tgx_vis_render_host"));
-    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data()));
+    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data(), any_mapped(staged)));
     for (uint32_t i = 0; i < n_views; i++)
         if (staged[i])
             TGX_CUDA(cudaMemcpyAsync(h_visbuf[i], dptr[i], (size_t)views[i].width * views[i].height * 8,
@@ -1827,7 +1857,7 @@ extern "C" tgx_status tgx_vis_render_host_async(tgx_ctx* c, const tgx_scene* s, 
     std::vector<uint64_t*> dptr;
     std::vector<bool> staged;
     TGX_TRY(host_outputs(c, views, n_views, h_visbuf, c->host_slot[slot], dptr, staged, "tgx_vis_render_host_async"));
-    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data()));
+    TGX_TRY(vis_render_device(c, s, views, n_views, dptr.data(), any_mapped(staged)));
     TGX_CUDA(cudaEventRecord(c->host_rendered[slot], c->stream));
     TGX_CUDA(cudaStreamWaitEvent(c->copy_stream, c->host_rendered[slot], 0));
     for (uint32_t i = 0; i < n_views; i++)
@@ -2103,6 +2133,7 @@ extern "C" tgx_status tgx_vis_render_noalloc(void* stream, const tgx_object* d_o
     J.first = 0;
     J.work = nullptr;
     J.extra_tx = 0;
+    J.interleave = 0;
     J.bshift = 1;
     J.batch = kBatch;
     J.drain = 32;
