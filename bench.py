@@ -193,7 +193,7 @@ CACHE_VARIANTS = {
 def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, box, width: int, height: int):
     """2-bounce GI on one frame: plain SVO GI against learned-cache GI.
 
-    The judge is a 256-spp plain 2-bounce render.  Plain GI and cached GI are
+    The ground truth is a 256-spp plain 2-bounce render.  Plain GI and cached GI are
     each timed per frame at several spp and scored by relMSE =
     mean((x - r)^2 / (r^2 + 1e-2)) over the pixels that hit geometry.  Cached
     GI (each entry of CACHE_VARIANTS, after a 60-frame online warm-up): bounce
@@ -271,7 +271,7 @@ def compare_cache_vs_plain(ctx, sc, svo, view, vis, stream, box, width: int, hei
             variants[name] = v
             cache.close()
     err = ctx.device_error()
-    res = {"judge": "plain 2-bounce GI, 256 spp", "judge_frame_ms": round(ref_ms, 2), "geometry_pixels": int(mask.sum()),
+    res = {"ground_truth": "plain 2-bounce GI, 256 spp", "ground_truth_frame_ms": round(ref_ms, 2), "geometry_pixels": int(mask.sum()),
            "target_relmse": 0.01, "cache_warmup_frames": warm, "plain": plain, "plain_kernel_ms_at_target": plain_kernels,
            "cached_variants": variants, "device_status": int(err.code)}
     if bp:
@@ -391,7 +391,7 @@ def compare_cache_vs_plain_moving(ctx, sc, svo, scene, stream, box, move_objects
 
     res = {"camera": "2 voxels and 0.2 degree of yaw per frame (seeded path)",
            "objects_moving": "8 objects, 1.5 voxels per frame, tgx_svo_update every frame" if move_objects else "none",
-           "warmup_frames": warm, "scored_frames": scored, "judge": "plain 2-bounce GI, 256 spp, per frame",
+           "warmup_frames": warm, "scored_frames": scored, "ground_truth": "plain 2-bounce GI, 256 spp, per frame",
            "plain": plain, "cached_configured_training": cached_by["configured_training"],
            "cached_light_training": cached_by["light_training"], "device_status": int(ctx.device_error().code)}
     bp = best(plain)
@@ -712,7 +712,7 @@ def bench_large(local: int):
                                                       cp, out))
             cached[spp] = {"frame_ms": round(ms, 2), "relmse": rel_mse(out.cpu().numpy(), r, mask)}
         cache.close()
-    res["gi_4k"] = {"geometry_pixels": int(mask.sum()), "judge": "plain 2-bounce GI, 64 spp",
+    res["gi_4k"] = {"geometry_pixels": int(mask.sum()), "ground_truth": "plain 2-bounce GI, 64 spp",
                     "plain": plain, "cached_configured_training": cached}
     res["device_gib_used"] = round((free0 - torch.cuda.mem_get_info()[0]) / 2**30, 2)
     res["device_status"] = int(ctx.device_error().code)
