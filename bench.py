@@ -114,6 +114,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest x over all ranks of the process group (the slowest
+    replica's time), or x itself without one."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_reference(budget_s: float = 12.0, scene=None, view=None):
     """The oracle (CPU transcription of visibility.frag) rendering whole frames
     of the same workload on all host threads until about budget_s seconds are
@@ -924,11 +935,7 @@ def main() -> None:
         barrier()
         launches = ctx.launches() - launches0
         ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-        ms = statistics.mean(ms_steps)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(statistics.mean(ms_steps), dist, "cuda")
 
         if graph is not None:
             graph.close()
@@ -964,7 +971,7 @@ def main() -> None:
             t0 = time.perf_counter()
             ctx.vis_render_host(sc, view, [host_out])
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        e2e_blocking = statistics.mean(e2e_ms)
+        e2e_blocking = max_over_ranks(statistics.mean(e2e_ms), dist, "cuda")
         # pipelined frame loop (throughput): the host issues frame i+1 while frame i renders into
         # its pinned host buffer; the L2 flush runs before every render on the render stream,
         # inside the clock
@@ -983,7 +990,7 @@ def main() -> None:
             ctx.vis_render_host_async(sc, view, [host_bufs[i & 1]])
             ctx.vis_host_wait(1)
         ctx.vis_host_wait(0)
-        e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+        e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist, "cuda")
         err = ctx.device_error()
         if err.code:
             raise RuntimeError(f"device status {err.code} at {err.where} ({err.detail})")
