@@ -66,26 +66,53 @@ def _label(cfg: dict) -> str:
     return f"{t[0]}x{t[1]}/b{cfg['depth_buckets']}/n{cfg['batch']}/d{cfg['drain']}"
 
 
-def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES, depth_buckets=DEPTH_BUCKETS,
-                  batches=BATCHES, drains=DRAINS, reps: int = 3, margin: float = 0.01):
-    """Coordinate search over the visibility settings for one workload.
-
-    make_frame(ctx) sets up the workload on a fresh context and returns
-    (render, close): render() issues one whole frame on the context's stream,
-    close() frees what make_frame made.  Each candidate is timed `reps` times
-    over `frames` frames and keeps its best time; a candidate replaces the
-    current choice only when it is faster by more than `margin` (run-to-run
-    noise would otherwise pick settings at random).  Returns (best config
-    dict, {label: ms per frame})."""
-    import torch
-    import tg_gb300 as tg
-
+def coordinate_search(measure, tiles=CANDIDATES, depth_buckets=DEPTH_BUCKETS, batches=BATCHES, drains=DRAINS,
+                      margin: float = 0.01):
+    """Coordinate search over the visibility settings: the tile shapes first
+    (from the defaults), then the depth buckets, the batch and the drain, one
+    at a time from the best so far.  measure(cfg) returns a frame time; each
+    distinct setting is measured once.  A candidate replaces the current
+    choice only when it is faster by more than `margin` (run-to-run noise
+    would otherwise pick settings at random).  Returns (best config dict,
+    {label: measured time})."""
     times = {}
 
     def run(cfg):
         lab = _label(cfg)
-        if lab in times:
-            return times[lab]
+        if lab not in times:
+            times[lab] = measure(cfg)
+        return times[lab]
+
+    def better(cand, cur):
+        return run(cand) < run(cur) * (1.0 - margin)
+
+    best = {"tile": tiles[0], **DEFAULTS}
+    for t in tiles:
+        cand = {**best, "tile": t}
+        if better(cand, best):
+            best = cand
+    for name, values in (("depth_buckets", depth_buckets), ("batch", batches), ("drain", drains)):
+        for v in values:
+            cand = {**best, name: v}
+            if better(cand, best):
+                best = cand
+    return best, times
+
+
+def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES, depth_buckets=DEPTH_BUCKETS,
+                  batches=BATCHES, drains=DRAINS, reps: int = 3, margin: float = 0.01):
+    """Coordinate search (coordinate_search) over the visibility settings for
+    one workload, timed on the GPU.
+
+    make_frame(ctx) sets up the workload on a fresh context and returns
+    (render, close): render() issues one whole frame on the context's stream,
+    close() frees what make_frame made.  Each candidate is timed `reps` times
+    over `frames` frames and keeps its best time.  Returns (best config dict,
+    {label: ms per frame})."""
+    import torch
+    import tg_gb300 as tg
+
+    def measure(cfg):
         with tg.Context(device, tile=cfg["tile"]) as ctx:
             ctx.set_vis_tuning(cfg["depth_buckets"], cfg["batch"], cfg["drain"])
             render, close = make_frame(ctx)
@@ -107,23 +134,9 @@ def tune_workload(make_frame, device: int = 0, frames: int = 5, tiles=CANDIDATES
             if err.code:
                 raise RuntimeError(f"tuning frame failed: device status {err.code} at {err.where}")
             close()
-        times[lab] = round(best_ms, 4)
-        return times[lab]
+        return round(best_ms, 4)
 
-    def better(cand, cur):
-        return run(cand) < run(cur) * (1.0 - margin)
-
-    best = {"tile": tiles[0], **DEFAULTS}
-    for t in tiles:
-        cand = {**best, "tile": t}
-        if better(cand, best):
-            best = cand
-    for name, values in (("depth_buckets", depth_buckets), ("batch", batches), ("drain", drains)):
-        for v in values:
-            cand = {**best, name: v}
-            if better(cand, best):
-                best = cand
-    return best, times
+    return coordinate_search(measure, tiles, depth_buckets, batches, drains, margin)
 
 
 def tune_visibility(scene, views, frames: int = 5, device: int = 0, use_cache: bool = True, **space):
