@@ -40,3 +40,26 @@ def test_malformed_and_unavailable_lines_are_skipped():
 def test_no_samples():
     r = sampler([])
     assert r == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_rel_mse_matches_its_definition_over_masked_pixels():
+    import numpy as np
+    rng = np.random.default_rng(3)
+    r = rng.uniform(0.0, 2.0, (40, 3)).astype(np.float32)
+    x = r + rng.normal(0.0, 0.1, (40, 3)).astype(np.float32)
+    mask = rng.random(40) < 0.6
+    want = np.mean([((x[i, c] - r[i, c]) ** 2) / (r[i, c] ** 2 + 1e-2)
+                    for i in range(40) if mask[i] for c in range(3)])
+    got = bench.rel_mse(x.reshape(-1), r.reshape(-1), mask)
+    assert abs(got - want) <= 1e-6 * want
+    assert bench.rel_mse(r.reshape(-1), r.reshape(-1), mask) == 0.0
+
+
+def test_camera_path_is_seeded_and_moves_two_voxels_per_frame():
+    import numpy as np
+    a = [bench.camera_path(f) for f in range(5)]
+    b = [bench.camera_path(f) for f in range(5)]
+    for (pa, ya, wa), (pb, yb, wb) in zip(a, b):
+        assert np.array_equal(pa, pb) and ya == yb and wa == wb
+    steps = [np.linalg.norm(a[f + 1][0] - a[f][0]) for f in range(4)]
+    assert np.allclose(steps, 2.0)
