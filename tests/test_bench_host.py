@@ -1,6 +1,8 @@
-"""Host-side pieces of bench.py that decide whether a run is valid, on
-canned input (no GPU): the clock sampler's reading of nvidia-smi's CSV lines
-(median SM clock under load, the maximum clock, the throttle reasons seen)."""
+"""Host-side pieces of bench.py, on canned input (no GPU): the clock
+sampler's reading of nvidia-smi's CSV lines (median SM clock under load, the
+maximum clock, the throttle reasons seen), which decides whether a run is
+valid; the relMSE that scores cached against plain GI; the seeded camera
+path of the motion study."""
 from __future__ import annotations
 
 import sys
